@@ -1,0 +1,105 @@
+"""Contracted spherical Gaussian atomic orbitals.
+
+Mirrors ``jqmc/atomic_orbital.py``: the data layout of ``AOs_sphe_data``
+(atomic_orbital.py:781-929) and the public calls ``compute_AOs``
+(atomic_orbital.py:1886) and ``compute_AOs_value_grad_lap``
+(atomic_orbital.py:3594-3640).  An AO is
+
+    phi_mu(r) = sum_p c_p N_p exp(-Z_p |r-R|^2) * sqrt((2l+1)/4pi) * S_lm(r-R)
+
+with N_p the primitive normalisation of atomic_orbital.py:2316-2323 and S_lm the
+real regular solid harmonic scaled by sqrt(4pi/(2l+1)) (atomic_orbital.py:2353-2585).
+
+The evaluation itself runs in the CUDA library (``ao_vgl`` in
+``csrc/jqmc_gpu.cu``); this module packs the basis into the shell table the
+kernels read and wraps the C-ABI call.  Unlike the reference, the batched call
+takes electron positions with a leading walker axis.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from math import factorial, pi, sqrt
+
+import numpy as np
+
+from .structure import Structure_data
+
+L_MAX = 6
+
+
+def primitive_norm(l: int, Z: float) -> float:
+    """sqrt(2^(2l+3) (l+1)! (2Z)^(l+3/2) / ((2l+2)! sqrt(pi))): the radial
+    normalisation of atomic_orbital.py:2316-2323, times the sqrt((2l+1)/4pi)
+    angular factor that multiplies the scaled solid harmonic."""
+    n2 = (2.0 ** (2 * l + 3)) * factorial(l + 1) * (2.0 * Z) ** (l + 1.5) / (factorial(2 * l + 2) * sqrt(pi))
+    return sqrt(n2) * sqrt((2 * l + 1) / (4.0 * pi))
+
+
+@dataclass(frozen=True)
+class AOs_sphe_data:
+    """Field-for-field mirror of jqmc's ``AOs_sphe_data`` (atomic_orbital.py:910-929)."""
+
+    structure_data: Structure_data = field(default_factory=Structure_data)
+    nucleus_index: tuple = ()
+    num_ao: int = 0
+    num_ao_prim: int = 0
+    orbital_indices: tuple = ()
+    exponents: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    coefficients: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    angular_momentums: tuple = ()
+    magnetic_quantum_numbers: tuple = ()
+
+    def __post_init__(self):
+        object.__setattr__(self, "exponents", np.asarray(self.exponents, dtype=np.float64))
+        object.__setattr__(self, "coefficients", np.asarray(self.coefficients, dtype=np.float64))
+
+    def sanity_check(self) -> None:
+        if len(self.nucleus_index) != self.num_ao:
+            raise ValueError("len(nucleus_index) != num_ao")
+        if len(self.angular_momentums) != self.num_ao or len(self.magnetic_quantum_numbers) != self.num_ao:
+            raise ValueError("angular_momentums / magnetic_quantum_numbers must have num_ao entries")
+        if len(self.orbital_indices) != self.num_ao_prim or len(self.exponents) != self.num_ao_prim:
+            raise ValueError("primitive arrays must have num_ao_prim entries")
+        if len(self.coefficients) != self.num_ao_prim:
+            raise ValueError("len(coefficients) != num_ao_prim")
+        for l, m in zip(self.angular_momentums, self.magnetic_quantum_numbers):
+            if not (0 <= l <= L_MAX and -l <= m <= l):
+                raise ValueError(f"(l, m)=({l}, {m}) outside the supported range l<={L_MAX}")
+        if set(self.orbital_indices) != set(range(self.num_ao)):
+            raise ValueError("every AO needs at least one primitive")
+
+    @property
+    def orb_num(self) -> int:
+        return self.num_ao
+
+    @property
+    def _atomic_center_carts_np(self) -> np.ndarray:
+        return self.structure_data.positions[np.asarray(self.nucleus_index, dtype=np.int64)]
+
+    def primitives_of(self, ao: int):
+        idx = [i for i, v in enumerate(self.orbital_indices) if v == ao]
+        return self.exponents[idx], self.coefficients[idx]
+
+    def shells(self):
+        """Group AOs into shells: consecutive AOs on one nucleus with the same l and
+        the same primitive list.  Returns a list of dicts with keys
+        ``atom, l, exps, coefs, aos (list of AO indices), ms (list of m)``.  Every
+        AO appears in exactly one shell, so evaluation per shell shares the
+        exponentials across the 2l+1 AOs of a shell."""
+        shells = []
+        for ao in range(self.num_ao):
+            e, c = self.primitives_of(ao)
+            atom = int(self.nucleus_index[ao])
+            l = int(self.angular_momentums[ao])
+            m = int(self.magnetic_quantum_numbers[ao])
+            if shells:
+                s = shells[-1]
+                if (s["atom"] == atom and s["l"] == l and len(s["exps"]) == len(e)
+                        and np.array_equal(s["exps"], e) and np.array_equal(s["coefs"], c)
+                        and m not in s["ms"] and len(s["ms"]) < 2 * l + 1):
+                    s["aos"].append(ao)
+                    s["ms"].append(m)
+                    continue
+            shells.append({"atom": atom, "l": l, "exps": e, "coefs": c, "aos": [ao], "ms": [m]})
+        return shells

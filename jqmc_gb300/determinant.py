@@ -1,0 +1,67 @@
+"""Geminal (AGP / Slater) determinant part of the wavefunction.
+
+Mirrors ``jqmc/determinant.py``: ``Geminal_data`` (determinant.py:94-141).  The
+geminal matrix is G_ij = phi_up(r_i)^T lambda_paired phi_dn(r_j), with the
+unpaired block phi_up(r_i)^T lambda_unpaired for N_up > N_dn
+(_compute_geminal_all_elements, determinant.py:1380-1402).
+
+The walker kernels hold, per walker, G^-1 and the two "ratio tables"
+T_up = lambda phi_dn G^-1 and T_dn = G^-1 phi_up^T lambda.  With them the ratio
+for moving up-electron i to r' is phi(r') . T_up[:, i] and the gradient of
+ln det for electron i is grad phi(r_i) . T_up[:, i]; both are the same numbers
+the reference obtains from the row/column rebuild of determinant.py:1430-1526
+and the traces of determinant.py:2141-2250.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .atomic_orbital import AOs_sphe_data
+from .molecular_orbital import MOs_data
+
+
+@dataclass(frozen=True)
+class Geminal_data:
+    """Field-for-field mirror of ``Geminal_data`` (determinant.py:110-120)."""
+
+    num_electron_up: int = 0
+    num_electron_dn: int = 0
+    orb_data_up_spin: AOs_sphe_data | MOs_data = field(default_factory=AOs_sphe_data)
+    orb_data_dn_spin: AOs_sphe_data | MOs_data = field(default_factory=AOs_sphe_data)
+    lambda_matrix: np.ndarray = field(default_factory=lambda: np.zeros((0, 0)))
+
+    def __post_init__(self):
+        object.__setattr__(self, "lambda_matrix", np.asarray(self.lambda_matrix, dtype=np.float64))
+
+    @property
+    def orb_num_up(self) -> int:
+        return self.orb_data_up_spin.orb_num
+
+    @property
+    def orb_num_dn(self) -> int:
+        return self.orb_data_dn_spin.orb_num
+
+    def sanity_check(self) -> None:
+        """Same checks and messages as determinant.py:122-141."""
+        if self.orb_num_up != self.orb_num_dn:
+            raise ValueError(f"The number of up and down orbitals ({self.orb_num_up}, {self.orb_num_dn}) should be the same.")
+        exp_shape = (self.orb_num_up, self.orb_num_dn + (self.num_electron_up - self.num_electron_dn))
+        if self.lambda_matrix.shape != exp_shape:
+            raise ValueError(f"dim. of lambda_matrix = {self.lambda_matrix.shape} is incompatible with {exp_shape}.")
+        if self.num_electron_up < self.num_electron_dn:
+            raise ValueError("Number of up electrons must not be smaller than dn electrons.")
+
+    def ao_basis_lambda(self):
+        """(aos_data, lambda_paired_AO, lambda_unpaired_AO) with any MO layer folded
+        into the pairing matrix: lambda_AO = C_up^T lambda C_dn."""
+        lam = self.lambda_matrix
+        lp, lu = lam[:, : self.orb_num_dn], lam[:, self.orb_num_dn:]
+        up, dn = self.orb_data_up_spin, self.orb_data_dn_spin
+        if isinstance(up, MOs_data):
+            cu = up.mo_coefficients
+            cd = dn.mo_coefficients
+            return up.aos_data, cu.T @ lp @ cd, cu.T @ lu
+        return up, lp, lu

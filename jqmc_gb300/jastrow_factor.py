@@ -1,0 +1,87 @@
+"""J1 / J2 / J3 Jastrow factor data.
+
+Mirrors ``jqmc/jastrow_factor.py``:
+  * J1 (jastrow_factor.py:561-645, value 649-726): per electron-nucleus pair
+    exp form  -(2Z)^(3/4) (1 - exp(-a (2Z)^(1/4) r)) / (2a),
+    pade form -(2Z)^(3/4) r / (2 (1 + a (2Z)^(1/4) r)), Z the effective charge;
+  * J2 (jastrow_factor.py:1111-1251): pade r/(2(1+b r)) or exp (1-exp(-b r))/(2b),
+    the same for parallel and antiparallel pairs;
+  * J3 (jastrow_factor.py:1317-1476, value 1744-1801): j_matrix (n, n+1) over an
+    AO set; last column j1 gives sum_i j1 . phi(r_i); the square block J gives
+    sum_{i<j same spin} phi_i^T J phi_j + sum_{i up, j dn} phi_i^T J phi_j.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .atomic_orbital import AOs_sphe_data
+from .structure import Structure_data
+
+
+@dataclass(frozen=True)
+class Jastrow_one_body_data:
+    jastrow_1b_param: float = 1.0
+    jastrow_1b_type: str = "exp"
+    structure_data: Structure_data = field(default_factory=Structure_data)
+    core_electrons: tuple = ()
+
+    def sanity_check(self) -> None:
+        if self.jastrow_1b_param < 0.0:
+            raise ValueError(f"jastrow_1b_param = {self.jastrow_1b_param} must be non-negative.")
+        if self.jastrow_1b_type not in ("exp", "pade"):
+            raise ValueError(f"jastrow_1b_type = '{self.jastrow_1b_type}' must be 'exp' or 'pade'.")
+        if len(self.core_electrons) != self.structure_data.natom:
+            raise ValueError("len(core_electrons) must equal the number of nuclei")
+
+    @property
+    def effective_charges(self) -> np.ndarray:
+        return np.asarray(self.structure_data.atomic_numbers, dtype=np.float64) - np.asarray(self.core_electrons, dtype=np.float64)
+
+
+@dataclass(frozen=True)
+class Jastrow_two_body_data:
+    jastrow_2b_param: float = 1.0
+    jastrow_2b_type: str = "pade"
+
+    def sanity_check(self) -> None:
+        if self.jastrow_2b_param < 0.0:
+            raise ValueError(f"jastrow_2b_param = {self.jastrow_2b_param} must be non-negative.")
+        if self.jastrow_2b_type not in ("exp", "pade"):
+            raise ValueError(f"jastrow_2b_type = '{self.jastrow_2b_type}' must be 'exp' or 'pade'.")
+
+
+@dataclass(frozen=True)
+class Jastrow_three_body_data:
+    orb_data: AOs_sphe_data = field(default_factory=AOs_sphe_data)
+    j_matrix: np.ndarray = field(default_factory=lambda: np.zeros((0, 1)))
+
+    def __post_init__(self):
+        object.__setattr__(self, "j_matrix", np.asarray(self.j_matrix, dtype=np.float64))
+
+    @property
+    def orb_num(self) -> int:
+        return self.orb_data.orb_num
+
+    def sanity_check(self) -> None:
+        if self.j_matrix.shape != (self.orb_num, self.orb_num + 1):
+            raise ValueError(f"dim. of j_matrix = {self.j_matrix.shape} is incompatible with ({self.orb_num}, {self.orb_num + 1})")
+        if not isinstance(self.orb_data, AOs_sphe_data):
+            raise NotImplementedError("the J3 basis must be a spherical AO set on the walker path")
+
+
+@dataclass(frozen=True)
+class Jastrow_data:
+    jastrow_one_body_data: Jastrow_one_body_data | None = None
+    jastrow_two_body_data: Jastrow_two_body_data | None = None
+    jastrow_three_body_data: Jastrow_three_body_data | None = None
+    jastrow_nn_data: object | None = None
+
+    def sanity_check(self) -> None:
+        if self.jastrow_nn_data is not None:
+            raise NotImplementedError("the neural-network Jastrow is not on the walker path")
+        for part in (self.jastrow_one_body_data, self.jastrow_two_body_data, self.jastrow_three_body_data):
+            if part is not None:
+                part.sanity_check()
