@@ -1,0 +1,156 @@
+/*
+ * jqmc_gpu.h -- C ABI of the GB300 (sm_103a) walker-path library libjqmc_gpu.so.
+ *
+ * All pointers named d_* are device pointers owned by the caller; host
+ * descriptors are read during the call only.  Every entry point returns 0 on
+ * success or a negative JQMC_E_* code; nothing throws across the ABI.  Calls
+ * are asynchronous on the given CUDA stream (cudaStream_t passed as void*);
+ * the library synchronises only inside jqmc_system_create/destroy.
+ *
+ * Each entry point names the reference interface (jQMC, Python/JAX) whose
+ * per-walker computation it replaces, batched over a leading walker axis.
+ */
+#ifndef JQMC_GPU_H
+#define JQMC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JQMC_OK 0
+#define JQMC_E_ARG (-1)       /* bad pointer / size / unsupported option     */
+#define JQMC_E_LIMIT (-2)     /* size above a compiled maximum               */
+#define JQMC_E_CUDA (-3)      /* a CUDA runtime call failed                  */
+#define JQMC_E_SMEM (-4)      /* shared-memory footprint too large           */
+
+#define JQMC_LMAX 6           /* highest AO angular momentum                 */
+#define JQMC_ECP_SLOTS 8      /* channels per nucleus in the ECP table       */
+#define JQMC_MAX_ELEC 256     /* N_up + N_dn                                 */
+#define JQMC_MAX_NUP 128
+#define JQMC_MAX_AO 4096
+#define JQMC_MAX_ATOM 512
+
+/* Walker status bits (per walker, OR-ed by the kernels). */
+#define JQMC_ST_SINGULAR 1    /* zero pivot while inverting G                */
+#define JQMC_ST_ZERO_RATIO 2  /* a chosen/accepted move had det ratio 0      */
+#define JQMC_ST_NAN 4         /* non-finite weight or energy                 */
+
+typedef struct jqmc_system jqmc_system; /* opaque: device copy of the tables */
+
+/* One contracted-GTO basis.  shells: nshell rows of 8 int32
+ *   {atom, l, nprim, prim0, ao0, nm, mfirst, 0}
+ * (AO ao0+k of the shell carries m = mfirst+k, k < nm; 1 <= nm <= 2l+1);
+ * prims: nprim rows of {Z, c*N_p*sqrt((2l+1)/4pi)} with N_p the primitive
+ * normalisation of jqmc/atomic_orbital.py:2316-2323. */
+typedef struct {
+  int32_t nshell, nao, nprim;
+  const int32_t* shells;
+  const double* prims;
+} jqmc_basis_desc;
+
+typedef struct {
+  int32_t natom, n_up, n_dn;
+  const double* atom_pos;        /* natom*3 (bohr)                           */
+  const double* atom_zeff;       /* natom: Coulomb charges (Z - z_core)      */
+  jqmc_basis_desc det;           /* geminal basis                            */
+  const double* lambda;          /* det.nao^2, row-major, paired block in AOs*/
+  int32_t has_j1, j1_type;       /* type 0 = exp, 1 = pade                   */
+  double j1_param;
+  const double* j1_zeff;         /* natom                                    */
+  int32_t has_j2, j2_type;       /* type 0 = pade, 1 = exp                   */
+  double j2_param;
+  int32_t has_j3;
+  jqmc_basis_desc j3;
+  const double* j3_matrix;       /* j3.nao*(j3.nao+1), row-major; last column = j1 vector */
+  int32_t ecp_flag;
+  const int32_t* ecp_maxl1;      /* natom: index of the local channel        */
+  const int32_t* ecp_chan;       /* natom*JQMC_ECP_SLOTS*2: (first term, count) per (atom, l) */
+  int32_t ecp_nterm;
+  const double* ecp_terms;       /* ecp_nterm*3: (c, n, alpha)               */
+  int32_t nv;                    /* angular quadrature: 4, 6, 12 or 18       */
+  const double* mesh_points;     /* nv*3 unit vectors                        */
+  const double* mesh_weights;    /* nv                                       */
+  double ion_ion;                /* constant ion-ion Coulomb energy          */
+} jqmc_system_desc;
+
+/* Per-walker state, all device arrays (N = n_up + n_dn, n = n_up, A = det.nao,
+ * A3 = j3.nao).  Electron-major layouts: electron e's vectors are contiguous. */
+typedef struct {
+  int32_t nwalk;
+  double* r;        /* nwalk*N*3, up electrons first                          */
+  double* G;        /* nwalk*n*n geminal matrix                               */
+  double* Ginv;     /* nwalk*n*n                                              */
+  double* Tup;      /* nwalk*n*A: row i = lambda Phi_dn G^-1 [:, i]           */
+  double* Tdn;      /* nwalk*n*A: row j = (G^-1 Phi_up^T lambda)[j, :]        */
+  double* h3;       /* nwalk*N*A3 J3 field: dJ3/dphi3(r_e) (unused if no J3)  */
+  int32_t* status;  /* nwalk JQMC_ST_* bits                                   */
+} jqmc_walkers;
+
+/* Copy the tables to the current device.  Replaces the per-call packing of
+ * AOs_sphe_data / Geminal_data / Jastrow_data / Coulomb_potential_data
+ * (jqmc/atomic_orbital.py:781-929, determinant.py:94-141,
+ * jastrow_factor.py:561-1476, coulomb_potential.py:188-598). */
+int jqmc_system_create(const jqmc_system_desc* desc, jqmc_system** out);
+int jqmc_system_destroy(jqmc_system* sys);
+
+/* Bytes of walker state per walker (sum over the jqmc_walkers arrays). */
+int64_t jqmc_walker_bytes(const jqmc_system* sys);
+
+/* AO values, gradients and Laplacians at npts points of basis 0 (geminal) or
+ * 1 (J3).  d_out: 5*nao*npts = (val, gx, gy, gz, lap), AO-major.
+ * Replaces compute_AOs_value_grad_lap (jqmc/atomic_orbital.py:3594-3640) and,
+ * through its first block, compute_AOs (atomic_orbital.py:1886). */
+int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_t npts, double* d_out, void* stream);
+
+/* Build every walker's state from its positions w->r: AO tables, G (geminal,
+ * jqmc/determinant.py:1380-1402), G^-1 by LU with partial pivoting (in place
+ * of the SVD pseudo-inverse of jqmc_mcmc.py:4249-4261 / jqmc_gfmc.py:691),
+ * T tables and the J3 field. */
+int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream);
+
+/* ln|det G| and its sign per walker from G (LU, jqmc/determinant.py:1026-1111),
+ * plus the Jastrow value J (jastrow_factor.py:2127-2178). */
+int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow, void* stream);
+
+/* K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523, fori_loop body),
+ * explicit draws: d_idraw nwalk*K*4 int32 (sel in [0,N), up index, dn index,
+ * axis), d_fdraw nwalk*K*2 double (standard normal, uniform).  Adds the number
+ * of accepted moves to d_accept[w]. */
+int jqmc_vmc_sweep(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const int32_t* d_idraw,
+                   const double* d_fdraw, double Dt, double eps_AS, int32_t* d_accept, void* stream);
+
+/* Local energy and AS weight per walker (jqmc/hamiltonians.py:225-290 with the
+ * non-local ECP on the rotated quadrature, coulomb_potential.py:1478-1712;
+ * w_L = (R_AS / max(R_AS, eps))^2, jqmc_mcmc.py:743-747).  d_angles: nwalk*3
+ * Euler angles; the rotation is R(angles) of jqmc_mcmc.py:4228-4245. */
+int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double eps_AS,
+                     double* d_eL, double* d_wL, void* stream);
+
+/* K LRDMC fixed-count projections per walker (GFMC_n, jqmc_gfmc.py:4779-5166),
+ * T-move ECP treatment.  d_draw nwalk*K*4 = (alpha, beta, gamma, u_move).
+ * d_w is multiplied by the K step weights b_x. */
+int jqmc_lrdmc_project(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const double* d_draw, double alat,
+                       double E_scf, double* d_w, void* stream);
+
+/* e_L = V_diag + V_nondiag and V_diag at the current positions with the
+ * rotation of d_draw (nwalk*4, the last step's draw): jqmc_gfmc.py:5361-5640. */
+int jqmc_lrdmc_energy(const jqmc_system* sys, const jqmc_walkers* w, const double* d_draw, double alat,
+                      double* d_eL, double* d_vdiag, void* stream);
+
+/* Stochastic reconfiguration with one comb draw zeta (jqmc_gfmc.py:2010-2090):
+ * d_chosen[k] = first j with cumsum(w/sum w)[j] >= (k + zeta)/nwalk (clamped
+ * to nwalk-1).  d_cum: caller-provided scratch of nwalk doubles that receives
+ * the cumulative normalised weights. */
+int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, double* d_cum, void* stream);
+
+/* dst walker k <- src walker d_chosen[k] for every state array (walker
+ * migration of jqmc_gfmc.py:2100-2266 on one device). */
+int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jqmc_walkers* dst,
+                       const int32_t* d_chosen, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JQMC_GPU_H */

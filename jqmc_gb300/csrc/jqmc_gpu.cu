@@ -1,0 +1,1722 @@
+// libjqmc_gpu: the jQMC walker hot path on one GB300 (sm_103a), FP64 form.
+//
+// One CTA owns one walker.  The basis / ECP tables are staged into shared
+// memory at kernel start; the per-walker ratio tables T_up, T_dn and the J3
+// field live in HBM and are read through L1.  Threads split a walker's work by
+// mesh point (kinetic lattice moves, ECP quadrature points), by electron, or by
+// AO index, and every thread walks the shell list in the same order, so the
+// AO loops are branch-uniform across a warp.
+//
+// Algebra (n = N_up = N_dn, A = number of geminal AOs, lambda the AO pairing
+// matrix, Phi the AO tables at the electrons, G = Phi_up^T lambda Phi_dn):
+//   T_up = lambda Phi_dn G^-1   (row i: up electron i),
+//   T_dn = G^-1 Phi_up^T lambda (row j: dn electron j).
+// Moving up electron i to r' multiplies det G by phi(r') . T_up[i]; moving dn
+// electron j by T_dn[j] . phi(r').  grad_i ln det = grad phi(r_i) . T_up[i] and
+// lap_i ln det = lap phi(r_i) . T_up[i] - |grad_i ln det|^2.  After a move the
+// tables are patched by rank-1 (Sherman-Morrison) updates plus one lambda
+// mat-vec; see sm_move below.
+//
+// J3 = j1 . sum_e phi3_e + sum_{pairs} phi3_a^T J phi3_b is linear in each
+// electron's J3-AO vector, so the field h_e = dJ3/dphi3_e gives
+// Delta J3 = (phi3(r') - phi3(r_e)) . h_e, grad_e J3 = grad phi3(r_e) . h_e and
+// lap_e J3 = lap phi3(r_e) . h_e.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "jqmc_gpu.h"
+#include "solid_harmonics.cuh"
+
+namespace {
+
+constexpr int kSlots = JQMC_ECP_SLOTS;
+constexpr int kRed = 64;  // doubles of reduction scratch
+
+struct Basis {
+  int nshell, nao, nprim;
+  const int* shells;
+  const double* prims;
+};
+
+struct Sys {
+  int natom, n_up, n_dn, N;
+  const double* atom_pos;
+  const double* atom_zeff;
+  Basis det;
+  const double* lam;   // A x A row-major
+  const double* lamT;  // transpose
+  int has_j1, j1_type;
+  double j1_param;
+  const double* j1_zeff;
+  int has_j2, j2_type;
+  double j2_param;
+  int has_j3;
+  Basis j3;
+  const double* j3mat;   // A3 x A3
+  const double* j3matT;  // transpose
+  const double* j3vec;   // A3
+  int ecp_flag;
+  const int* ecp_maxl1;
+  const int* ecp_chan;
+  int ecp_nterm;
+  const double* ecp_terms;
+  int nv;
+  const double* mesh_pts;
+  const double* mesh_w;
+  double ion_ion;
+};
+
+struct WS {
+  double *r, *G, *Ginv, *Tup, *Tdn, *h3;
+  int* status;
+};
+
+// Shared-memory table layout (byte offsets), identical for every walker kernel.
+struct TableLayout {
+  int off_dsh, off_dpr, off_jsh, off_jpr, off_apos, off_azeff, off_j1z, off_maxl1, off_chan, off_terms, off_mpts, off_mw;
+  int bytes;
+};
+
+__host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
+
+TableLayout table_layout(const Sys& s) {
+  TableLayout L;
+  int o = 0;
+  L.off_dsh = o; o = align16(o + s.det.nshell * 8 * 4);
+  L.off_dpr = o; o = align16(o + s.det.nprim * 2 * 8);
+  L.off_jsh = o; o = align16(o + (s.has_j3 ? s.j3.nshell : 0) * 8 * 4);
+  L.off_jpr = o; o = align16(o + (s.has_j3 ? s.j3.nprim : 0) * 2 * 8);
+  L.off_apos = o; o = align16(o + s.natom * 3 * 8);
+  L.off_azeff = o; o = align16(o + s.natom * 8);
+  L.off_j1z = o; o = align16(o + s.natom * 8);
+  L.off_maxl1 = o; o = align16(o + s.natom * 4);
+  L.off_chan = o; o = align16(o + s.natom * kSlots * 2 * 4);
+  L.off_terms = o; o = align16(o + s.ecp_nterm * 3 * 8);
+  L.off_mpts = o; o = align16(o + s.nv * 3 * 8);
+  L.off_mw = o; o = align16(o + s.nv * 8);
+  L.bytes = o;
+  return L;
+}
+
+__device__ void copy_words(void* dst, const void* src, int bytes) {
+  if (!src || bytes <= 0) return;
+  const int nw = bytes / 4;
+  const uint32_t* s = static_cast<const uint32_t*>(src);
+  uint32_t* d = static_cast<uint32_t*>(dst);
+  for (int k = threadIdx.x; k < nw; k += blockDim.x) d[k] = s[k];
+}
+
+// Copy the tables into shared memory and return a Sys whose table pointers
+// refer to the shared copies.  Ends with __syncthreads().
+__device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* smem) {
+  Sys s = g;
+  copy_words(smem + L.off_dsh, g.det.shells, g.det.nshell * 32);
+  copy_words(smem + L.off_dpr, g.det.prims, g.det.nprim * 16);
+  s.det.shells = reinterpret_cast<const int*>(smem + L.off_dsh);
+  s.det.prims = reinterpret_cast<const double*>(smem + L.off_dpr);
+  if (g.has_j3) {
+    copy_words(smem + L.off_jsh, g.j3.shells, g.j3.nshell * 32);
+    copy_words(smem + L.off_jpr, g.j3.prims, g.j3.nprim * 16);
+    s.j3.shells = reinterpret_cast<const int*>(smem + L.off_jsh);
+    s.j3.prims = reinterpret_cast<const double*>(smem + L.off_jpr);
+  }
+  copy_words(smem + L.off_apos, g.atom_pos, g.natom * 24);
+  copy_words(smem + L.off_azeff, g.atom_zeff, g.natom * 8);
+  copy_words(smem + L.off_j1z, g.j1_zeff, g.natom * 8);
+  copy_words(smem + L.off_maxl1, g.ecp_maxl1, g.natom * 4);
+  copy_words(smem + L.off_chan, g.ecp_chan, g.natom * kSlots * 8);
+  copy_words(smem + L.off_terms, g.ecp_terms, g.ecp_nterm * 24);
+  copy_words(smem + L.off_mpts, g.mesh_pts, g.nv * 24);
+  copy_words(smem + L.off_mw, g.mesh_w, g.nv * 8);
+  s.atom_pos = reinterpret_cast<const double*>(smem + L.off_apos);
+  s.atom_zeff = reinterpret_cast<const double*>(smem + L.off_azeff);
+  s.j1_zeff = reinterpret_cast<const double*>(smem + L.off_j1z);
+  s.ecp_maxl1 = reinterpret_cast<const int*>(smem + L.off_maxl1);
+  s.ecp_chan = reinterpret_cast<const int*>(smem + L.off_chan);
+  s.ecp_terms = reinterpret_cast<const double*>(smem + L.off_terms);
+  s.mesh_pts = reinterpret_cast<const double*>(smem + L.off_mpts);
+  s.mesh_w = reinterpret_cast<const double*>(smem + L.off_mw);
+  __syncthreads();
+  return s;
+}
+
+// ------------------------------------------------------------------ AO shells
+template <int L>
+__device__ __forceinline__ void sh_val(double x, double y, double z, double* S) {
+  if constexpr (L == 0) sh_l0(x, y, z, S);
+  else if constexpr (L == 1) sh_l1(x, y, z, S);
+  else if constexpr (L == 2) sh_l2(x, y, z, S);
+  else if constexpr (L == 3) sh_l3(x, y, z, S);
+  else if constexpr (L == 4) sh_l4(x, y, z, S);
+  else if constexpr (L == 5) sh_l5(x, y, z, S);
+  else sh_l6(x, y, z, S);
+}
+
+template <int L>
+__device__ __forceinline__ void sh_grad(double x, double y, double z, double* S, double* G) {
+  if constexpr (L == 0) shg_l0(x, y, z, S, G);
+  else if constexpr (L == 1) shg_l1(x, y, z, S, G);
+  else if constexpr (L == 2) shg_l2(x, y, z, S, G);
+  else if constexpr (L == 3) shg_l3(x, y, z, S, G);
+  else if constexpr (L == 4) shg_l4(x, y, z, S, G);
+  else if constexpr (L == 5) shg_l5(x, y, z, S, G);
+  else shg_l6(x, y, z, S, G);
+}
+
+template <int L, class F>
+__device__ __forceinline__ void emit_val(double dx, double dy, double dz, double rad, int ao0, int jlo, int nm, F& f) {
+  double S[2 * L + 1];
+  sh_val<L>(dx, dy, dz, S);
+#pragma unroll
+  for (int j = 0; j < 2 * L + 1; ++j) {
+    const int k = j - jlo;
+    if (k >= 0 && k < nm) f(ao0 + k, rad * S[j]);
+  }
+}
+
+// value, gradient, Laplacian of every AO of one shell:
+//   phi = rad S, grad phi = rad grad S - 2 radZ S d, lap phi = S (4 r^2 radZ2 - (4l+6) radZ)
+// (rad = sum_p cN_p e^{-Z_p r^2}, radZ = sum cN Z e, radZ2 = sum cN Z^2 e; the
+// solid harmonics are harmonic and homogeneous of degree l).
+template <int L, class F>
+__device__ __forceinline__ void emit_vgl(double dx, double dy, double dz, double r2, double rad, double radZ,
+                                         double radZ2, int ao0, int jlo, int nm, F& f) {
+  double S[2 * L + 1], G[3 * (2 * L + 1)];
+  sh_grad<L>(dx, dy, dz, S, G);
+  const double lapf = 4.0 * r2 * radZ2 - (4.0 * L + 6.0) * radZ;
+#pragma unroll
+  for (int j = 0; j < 2 * L + 1; ++j) {
+    const int k = j - jlo;
+    if (k >= 0 && k < nm) {
+      const double t = -2.0 * radZ * S[j];
+      f(ao0 + k, rad * S[j], rad * G[3 * j] + t * dx, rad * G[3 * j + 1] + t * dy, rad * G[3 * j + 2] + t * dz,
+        S[j] * lapf);
+    }
+  }
+}
+
+template <class F>
+__device__ __forceinline__ void shell_val(const Basis& b, const double* apos, int s, double px, double py, double pz,
+                                          F& f) {
+  const int* sh = b.shells + 8 * s;
+  const int atom = sh[0], l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const double dx = px - apos[3 * atom], dy = py - apos[3 * atom + 1], dz = pz - apos[3 * atom + 2];
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  double rad = 0.0;
+  for (int p = 0; p < np; ++p) {
+    const double* pr = b.prims + 2 * (p0 + p);
+    rad += pr[1] * exp(-pr[0] * r2);
+  }
+  switch (l) {
+    case 0: emit_val<0>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 1: emit_val<1>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 2: emit_val<2>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 3: emit_val<3>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 4: emit_val<4>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 5: emit_val<5>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    default: emit_val<6>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+  }
+}
+
+template <class F>
+__device__ __forceinline__ void shell_vgl(const Basis& b, const double* apos, int s, double px, double py, double pz,
+                                          F& f) {
+  const int* sh = b.shells + 8 * s;
+  const int atom = sh[0], l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const double dx = px - apos[3 * atom], dy = py - apos[3 * atom + 1], dz = pz - apos[3 * atom + 2];
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  double rad = 0.0, radZ = 0.0, radZ2 = 0.0;
+  for (int p = 0; p < np; ++p) {
+    const double* pr = b.prims + 2 * (p0 + p);
+    const double e = pr[1] * exp(-pr[0] * r2);
+    rad += e;
+    radZ += pr[0] * e;
+    radZ2 += pr[0] * pr[0] * e;
+  }
+  switch (l) {
+    case 0: emit_vgl<0>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 1: emit_vgl<1>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 2: emit_vgl<2>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 3: emit_vgl<3>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 4: emit_vgl<4>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 5: emit_vgl<5>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    default: emit_vgl<6>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+  }
+}
+
+// sum_a phi_a(p) v[a]
+__device__ double ao_dot(const Basis& b, const double* apos, double px, double py, double pz, const double* v) {
+  double acc = 0.0;
+  auto f = [&](int a, double val) { acc += val * v[a]; };
+  for (int s = 0; s < b.nshell; ++s) shell_val(b, apos, s, px, py, pz, f);
+  return acc;
+}
+
+// all AO values at one point into out[] (block-cooperative, split by shell; no sync)
+__device__ void ao_fill_block(const Basis& b, const double* apos, double px, double py, double pz, double* out) {
+  auto f = [&](int a, double val) { out[a] = val; };
+  for (int s = threadIdx.x; s < b.nshell; s += blockDim.x) shell_val(b, apos, s, px, py, pz, f);
+}
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block; every thread receives the total.  red: >= 33 doubles.
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < nw; ++k) t += red[k];
+    red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+__device__ double block_min(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = red[0];
+    for (int k = 1; k < nw; ++k) t = fmin(t, red[k]);
+    red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// out[k] = sum_a M[k*A + a] x[a] for k < n (one warp per row)
+__device__ void rows_dot(const double* M, int n, int A, const double* x, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = wid; k < n; k += nw) {
+    double acc = 0.0;
+    for (int a = lane; a < A; a += 32) acc += M[(size_t)k * A + a] * x[a];
+    acc = warp_sum(acc);
+    if (lane == 0) out[k] = acc;
+  }
+}
+
+// ------------------------------------------------------------------ physics helpers
+__device__ __forceinline__ double j1_pair(int type, double a, double Z, double d) {
+  const double c = pow(2.0 * Z, 0.25), A = pow(2.0 * Z, 0.75);
+  if (type == 0) return -A * (1.0 / (2.0 * a)) * (1.0 - exp(-a * c * d));
+  return -A * d / (2.0 * (1.0 + a * c * d));
+}
+
+__device__ __forceinline__ double j2_pair(int type, double b, double d) {
+  if (type == 0) return d / 2.0 * (1.0 / (1.0 + b * d));
+  return 1.0 / (2.0 * b) * (1.0 - exp(-b * d));
+}
+
+__device__ double j1_at(const Sys& s, double x, double y, double z) {
+  double acc = 0.0;
+  for (int a = 0; a < s.natom; ++a) {
+    const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+    acc += j1_pair(s.j1_type, s.j1_param, s.j1_zeff[a], sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  return acc;
+}
+
+// sum over electrons m != skip of the J2 pair function at distance |p - r_m|
+__device__ double j2_at(const Sys& s, const double* r, int skip, double x, double y, double z) {
+  double acc = 0.0;
+  for (int m = 0; m < s.N; ++m) {
+    if (m == skip) continue;
+    const double dx = x - r[3 * m], dy = y - r[3 * m + 1], dz = z - r[3 * m + 2];
+    acc += j2_pair(s.j2_type, s.j2_param, sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  return acc;
+}
+
+__device__ __forceinline__ double ipow(double x, double n) {
+  const int k = (int)n;
+  if ((double)k == n && k >= 0 && k <= 8) {
+    double r = 1.0;
+    for (int i = 0; i < k; ++i) r *= x;
+    return r;
+  }
+  return pow(x, n);
+}
+
+// r^-2 sum_k c_k r^{n_k} exp(-alpha_k r^2) over the terms of (atom, slot)
+__device__ double ecp_channel(const Sys& s, int atom, int slot, double d) {
+  const int* ch = s.ecp_chan + (atom * kSlots + slot) * 2;
+  double v = 0.0;
+  for (int t = 0; t < ch[1]; ++t) {
+    const double* tm = s.ecp_terms + 3 * (ch[0] + t);
+    v += tm[0] * ipow(d, tm[1]) * exp(-tm[2] * d * d);
+  }
+  return pow(d, -2.0) * v;
+}
+
+__device__ __forceinline__ double legendre(int l, double x) {
+  switch (l) {
+    case 0: return 1.0;
+    case 1: return x;
+    case 2: return 1.0 / 2.0 * (3.0 * x * x - 1);
+    case 3: return 1.0 / 2.0 * (5.0 * x * x * x - 3.0 * x);
+    case 4: return 1.0 / 8.0 * (35.0 * x * x * x * x - 30.0 * x * x + 3.0);
+    case 5: return 1.0 / 8.0 * (63.0 * x * x * x * x * x - 70 * x * x * x + 15 * x);
+    default: return 1.0 / 16.0 * (231.0 * x * x * x * x * x * x - 315.0 * x * x * x * x + 105.0 * x * x - 5);
+  }
+}
+
+// nearest nucleus (lowest index on ties), as the stable argsort of jqmc/structure.py:393-405
+__device__ int nearest_atom(const Sys& s, double x, double y, double z) {
+  int best = 0;
+  double bd = 1e300;
+  for (int a = 0; a < s.natom; ++a) {
+    const double dx = s.atom_pos[3 * a] - x, dy = s.atom_pos[3 * a + 1] - y, dz = s.atom_pos[3 * a + 2] - z;
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (d < bd) { bd = d; best = a; }
+  }
+  return best;
+}
+
+// R(alpha, beta, gamma) of jqmc_mcmc.py:4228-4245 / jqmc_gfmc.py:4721-4736
+__device__ void rotation(double a, double b, double g, double* R) {
+  const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cg = cos(g), sg = sin(g);
+  R[0] = cb * cg; R[1] = cg * sa * sb - ca * sg; R[2] = sa * sg + ca * cg * sb;
+  R[3] = cb * sg; R[4] = ca * cg + sa * sb * sg; R[5] = ca * sb * sg - cg * sa;
+  R[6] = -sb;     R[7] = cb * sa;                R[8] = ca * cb;
+}
+
+// ------------------------------------------------------------------ per-walker workspace
+struct Work {
+  Sys s;
+  int N, n, A, A3;
+  double* r;     // N*3
+  double* G;     // n*n
+  double* Gi;    // n*n
+  double* Tup;   // global, this walker
+  double* Tdn;
+  double* h3;
+  double* vA0;   // A
+  double* vA1;   // A
+  double* vA2;   // A
+  double* v30;   // A3
+  double* v31;
+  double* v32;
+  double* vn0;   // n
+  double* vn1;
+  double* vn2;
+  double* vn3;
+  double* red;   // kRed
+  double* sc;    // 32 scalars
+};
+
+struct WorkLayout {
+  int off_r, off_G, off_Gi, off_vA, off_v3, off_vn, off_red, off_sc, bytes;
+};
+
+WorkLayout work_layout(const Sys& s, int base) {
+  WorkLayout L;
+  const int A3 = s.has_j3 ? s.j3.nao : 1;
+  int o = base;
+  L.off_r = o; o = align16(o + s.N * 3 * 8);
+  L.off_G = o; o = align16(o + s.n_up * s.n_up * 8);
+  L.off_Gi = o; o = align16(o + s.n_up * s.n_up * 8);
+  L.off_vA = o; o = align16(o + 3 * s.det.nao * 8);
+  L.off_v3 = o; o = align16(o + 3 * A3 * 8);
+  L.off_vn = o; o = align16(o + 4 * s.n_up * 8);
+  L.off_red = o; o = align16(o + kRed * 8);
+  L.off_sc = o; o = align16(o + 32 * 8);
+  L.bytes = o;
+  return L;
+}
+
+__device__ Work make_work(const Sys& s, const WorkLayout& L, unsigned char* smem, const WS& ws, int w) {
+  Work k;
+  k.s = s;
+  k.N = s.N;
+  k.n = s.n_up;
+  k.A = s.det.nao;
+  k.A3 = s.has_j3 ? s.j3.nao : 1;
+  k.r = reinterpret_cast<double*>(smem + L.off_r);
+  k.G = reinterpret_cast<double*>(smem + L.off_G);
+  k.Gi = reinterpret_cast<double*>(smem + L.off_Gi);
+  k.vA0 = reinterpret_cast<double*>(smem + L.off_vA);
+  k.vA1 = k.vA0 + k.A;
+  k.vA2 = k.vA1 + k.A;
+  k.v30 = reinterpret_cast<double*>(smem + L.off_v3);
+  k.v31 = k.v30 + k.A3;
+  k.v32 = k.v31 + k.A3;
+  k.vn0 = reinterpret_cast<double*>(smem + L.off_vn);
+  k.vn1 = k.vn0 + k.n;
+  k.vn2 = k.vn1 + k.n;
+  k.vn3 = k.vn2 + k.n;
+  k.red = reinterpret_cast<double*>(smem + L.off_red);
+  k.sc = reinterpret_cast<double*>(smem + L.off_sc);
+  k.Tup = ws.Tup + (size_t)w * k.n * k.A;
+  k.Tdn = ws.Tdn + (size_t)w * k.n * k.A;
+  k.h3 = s.has_j3 ? ws.h3 + (size_t)w * k.N * k.A3 : nullptr;
+  return k;
+}
+
+__device__ void load_walker(Work& k, const WS& ws, int w) {
+  const int nn = k.n * k.n;
+  for (int t = threadIdx.x; t < k.N * 3; t += blockDim.x) k.r[t] = ws.r[(size_t)w * k.N * 3 + t];
+  for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+    k.G[t] = ws.G[(size_t)w * nn + t];
+    k.Gi[t] = ws.Ginv[(size_t)w * nn + t];
+  }
+  __syncthreads();
+}
+
+__device__ void store_walker(const Work& k, const WS& ws, int w) {
+  __syncthreads();
+  const int nn = k.n * k.n;
+  for (int t = threadIdx.x; t < k.N * 3; t += blockDim.x) ws.r[(size_t)w * k.N * 3 + t] = k.r[t];
+  for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+    ws.G[(size_t)w * nn + t] = k.G[t];
+    ws.Ginv[(size_t)w * nn + t] = k.Gi[t];
+  }
+}
+
+// Move electron e (global index, up first) to (px, py, pz) and patch G, G^-1,
+// T_up, T_dn and the J3 field.  Block-cooperative; returns the det ratio.
+//   up i:  a = T_up phi',  ratio = a_i,  w = a - e_i,  g' = a^T G (new row i),
+//          G^-1 -= G^-1[:,i] w^T / ratio,  T_up -= T_up[i] (x) w / ratio,
+//          T_dn += G^-1[:,i] (x) (lambda^T dphi - T_dn^T G^T w) / ratio
+//   dn j:  b = T_dn phi', ratio = b_j,  q = b - e_j,  c' = G b (new column j),
+//          G^-1 -= q G^-1[j,:] / ratio, T_dn -= q (x) T_dn[j] / ratio,
+//          T_up += G^-1[j,:] (x) (lambda dphi - T_up^T G q) / ratio
+// (every right-hand side uses the tables before the move).
+__device__ double sm_move(Work& k, int e, double px, double py, double pz) {
+  const Sys& s = k.s;
+  const int n = k.n, A = k.A, A3 = k.A3;
+  const bool up = e < s.n_up;
+  const int i = up ? e : e - s.n_up;
+  const double ox = k.r[3 * e], oy = k.r[3 * e + 1], oz = k.r[3 * e + 2];
+  // phi' -> vA0, phi_old -> vA1, then vA1 = dphi
+  ao_fill_block(s.det, s.atom_pos, px, py, pz, k.vA0);
+  ao_fill_block(s.det, s.atom_pos, ox, oy, oz, k.vA1);
+  if (s.has_j3) {
+    ao_fill_block(s.j3, s.atom_pos, px, py, pz, k.v30);
+    ao_fill_block(s.j3, s.atom_pos, ox, oy, oz, k.v31);
+  }
+  __syncthreads();
+  for (int a = threadIdx.x; a < A; a += blockDim.x) k.vA1[a] = k.vA0[a] - k.vA1[a];
+  if (s.has_j3)
+    for (int a = threadIdx.x; a < A3; a += blockDim.x) k.v31[a] = k.v30[a] - k.v31[a];
+  // a / b vector -> vn0
+  rows_dot(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
+  __syncthreads();
+  const double ratio = k.vn0[i];
+  const double inv = 1.0 / ratio;
+  if (up) {
+    // vn1 = w = a - e_i ; vn2 = G^T w ; vn3 = old column i of G^-1 ; new row i of G -> sc later
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      k.vn1[t] = k.vn0[t] - (t == i ? 1.0 : 0.0);
+      k.vn3[t] = k.Gi[t * n + i];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      double u = 0.0;
+      for (int t = 0; t < n; ++t) u += k.G[t * n + c] * k.vn1[t];
+      k.vn2[c] = u;
+    }
+    // x_b = (sum_a lam[a][b] dphi_a - sum_j Tdn[j][b] u_j) / ratio -> vA2
+    __syncthreads();
+    for (int b = threadIdx.x; b < A; b += blockDim.x) {
+      double dl = 0.0;
+      for (int a = 0; a < A; ++a) dl += s.lam[(size_t)a * A + b] * k.vA1[a];
+      double mw = 0.0;
+      for (int j = 0; j < n; ++j) mw += k.Tdn[(size_t)j * A + b] * k.vn2[j];
+      k.vA2[b] = (dl - mw) * inv;
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < A; b += blockDim.x) {
+      const double xb = k.vA2[b];
+      for (int j = 0; j < n; ++j) k.Tdn[(size_t)j * A + b] += k.vn3[j] * xb;
+      const double ti = k.Tup[(size_t)i * A + b];
+      for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + b] -= ti * k.vn1[t] * inv;
+    }
+    // new row i of G: g'_c = sum_t a_t G[t][c]  (uses old G; write after sync)
+    double* gnew = k.sc;  // n <= 32 handled below via vA2 reuse when larger
+    double* gn = (n <= 32) ? gnew : k.vA2;
+    __syncthreads();
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      double g = 0.0;
+      for (int t = 0; t < n; ++t) g += k.vn0[t] * k.G[t * n + c];
+      gn[c] = g;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int rr = t / n, cc = t % n;
+      k.Gi[t] -= k.vn3[rr] * k.vn1[cc] * inv;
+    }
+    for (int c = threadIdx.x; c < n; c += blockDim.x) k.G[i * n + c] = gn[c];
+  } else {
+    // vn1 = q = b - e_i ; vn2 = G q ; vn3 = old row i of G^-1
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      k.vn1[t] = k.vn0[t] - (t == i ? 1.0 : 0.0);
+      k.vn3[t] = k.Gi[i * n + t];
+    }
+    __syncthreads();
+    for (int rr = threadIdx.x; rr < n; rr += blockDim.x) {
+      double u = 0.0;
+      for (int t = 0; t < n; ++t) u += k.G[rr * n + t] * k.vn1[t];
+      k.vn2[rr] = u;
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+      double dm = 0.0;
+      for (int b = 0; b < A; ++b) dm += s.lamT[(size_t)b * A + a] * k.vA1[b];
+      double mq = 0.0;
+      for (int t = 0; t < n; ++t) mq += k.Tup[(size_t)t * A + a] * k.vn2[t];
+      k.vA2[a] = (dm - mq) * inv;
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+      const double xa = k.vA2[a];
+      for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + a] += xa * k.vn3[t];
+      const double tj = k.Tdn[(size_t)i * A + a];
+      for (int t = 0; t < n; ++t) k.Tdn[(size_t)t * A + a] -= k.vn1[t] * tj * inv;
+    }
+    double* cn = (n <= 32) ? k.sc : k.vA2;
+    __syncthreads();
+    for (int rr = threadIdx.x; rr < n; rr += blockDim.x) {
+      double c = 0.0;
+      for (int t = 0; t < n; ++t) c += k.G[rr * n + t] * k.vn0[t];
+      cn[rr] = c;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int rr = t / n, cc = t % n;
+      k.Gi[t] -= k.vn1[rr] * k.vn3[cc] * inv;
+    }
+    for (int rr = threadIdx.x; rr < n; rr += blockDim.x) k.G[rr * n + i] = cn[rr];
+  }
+  // J3 field: h_m += J dphi3 or J^T dphi3 for every other electron m
+  if (s.has_j3) {
+    __syncthreads();
+    for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+      double jd = 0.0, jtd = 0.0;
+      for (int cp = 0; cp < A3; ++cp) {
+        jd += s.j3matT[(size_t)cp * A3 + c] * k.v31[cp];   // (J d)_c
+        jtd += s.j3mat[(size_t)cp * A3 + c] * k.v31[cp];   // (J^T d)_c
+      }
+      k.v32[c] = jd;
+      k.v30[c] = jtd;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < k.N * A3; t += blockDim.x) {
+      const int m = t / A3, c = t % A3;
+      if (m == e) continue;
+      const bool mup = m < s.n_up;
+      bool useJ;  // h_m += J d  iff the pair is (phi_m^T J phi_e)
+      if (mup == up) useJ = m < e;
+      else useJ = !up;  // e dn, m up -> phi_m^T J phi_e
+      k.h3[(size_t)m * A3 + c] += useJ ? k.v32[c] : k.v30[c];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    k.r[3 * e] = px;
+    k.r[3 * e + 1] = py;
+    k.r[3 * e + 2] = pz;
+  }
+  __syncthreads();
+  return ratio;
+}
+
+// ------------------------------------------------------------------ per-step terms
+// Arrays in shared memory for the energy / projection kernels.
+struct Terms {
+  double* ke;     // N continuum kinetic energy per electron
+  double* j1o;    // N  J1 of electron e at its position
+  double* j2o;    // N  sum_{m != e} J2 pair values
+  double* c3;     // N  phi3(r_e) . h_e
+  double* ei;     // N  e-ion Coulomb per electron
+  double* eid;    // N  discretised e-ion (distance floor alat)
+  double* edist;  // N  distance to the nearest nucleus
+  int* eatom;     // N  nearest nucleus
+  double* el;     // 6N kinetic lattice elements
+  double* V;      // nv*N non-local ECP elements
+  double* R;      // 9 rotation
+};
+
+struct TermsLayout {
+  int off_ke, off_j1o, off_j2o, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, bytes;
+};
+
+TermsLayout terms_layout(const Sys& s, int base) {
+  TermsLayout L;
+  const int N = s.N;
+  int o = base;
+  L.off_ke = o; o = align16(o + N * 8);
+  L.off_j1o = o; o = align16(o + N * 8);
+  L.off_j2o = o; o = align16(o + N * 8);
+  L.off_c3 = o; o = align16(o + N * 8);
+  L.off_ei = o; o = align16(o + N * 8);
+  L.off_eid = o; o = align16(o + N * 8);
+  L.off_ed = o; o = align16(o + N * 8);
+  L.off_ea = o; o = align16(o + N * 4);
+  L.off_el = o; o = align16(o + 6 * N * 8);
+  L.off_V = o; o = align16(o + (s.nv > 0 ? s.nv : 1) * N * 8);
+  L.off_R = o; o = align16(o + 9 * 8);
+  L.bytes = o;
+  return L;
+}
+
+__device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
+  Terms t;
+  t.ke = reinterpret_cast<double*>(smem + L.off_ke);
+  t.j1o = reinterpret_cast<double*>(smem + L.off_j1o);
+  t.j2o = reinterpret_cast<double*>(smem + L.off_j2o);
+  t.c3 = reinterpret_cast<double*>(smem + L.off_c3);
+  t.ei = reinterpret_cast<double*>(smem + L.off_ei);
+  t.eid = reinterpret_cast<double*>(smem + L.off_eid);
+  t.edist = reinterpret_cast<double*>(smem + L.off_ed);
+  t.eatom = reinterpret_cast<int*>(smem + L.off_ea);
+  t.el = reinterpret_cast<double*>(smem + L.off_el);
+  t.V = reinterpret_cast<double*>(smem + L.off_V);
+  t.R = reinterpret_cast<double*>(smem + L.off_R);
+  return t;
+}
+
+// Phase A: per-electron continuum kinetic energy and the old-position values
+// the ratios need (wavefunction.py:1142-1207, jastrow_factor.py:961-1034,
+// 3435-3558, 4077-4156).
+__device__ void electron_terms(Work& k, Terms& t, double alat) {
+  const Sys& s = k.s;
+  for (int e = threadIdx.x; e < k.N; e += blockDim.x) {
+    const bool up = e < s.n_up;
+    const int i = up ? e : e - s.n_up;
+    const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
+    const double* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
+    double gx = 0, gy = 0, gz = 0, lp = 0;
+    {
+      auto f = [&](int a, double v, double ax, double ay, double az, double al) {
+        const double tv = Trow[a];
+        gx += ax * tv; gy += ay * tv; gz += az * tv; lp += al * tv;
+      };
+      for (int sh = 0; sh < s.det.nshell; ++sh) shell_vgl(s.det, s.atom_pos, sh, x, y, z, f);
+    }
+    // ln det part
+    double Gx = gx, Gy = gy, Gz = gz;
+    double L = lp - (gx * gx + gy * gy + gz * gz);
+    double c3 = 0.0;
+    if (s.has_j3) {
+      const double* h = k.h3 + (size_t)e * k.A3;
+      double hx = 0, hy = 0, hz = 0, hl = 0;
+      auto f = [&](int a, double v, double ax, double ay, double az, double al) {
+        const double hv = h[a];
+        c3 += v * hv; hx += ax * hv; hy += ay * hv; hz += az * hv; hl += al * hv;
+      };
+      for (int sh = 0; sh < s.j3.nshell; ++sh) shell_vgl(s.j3, s.atom_pos, sh, x, y, z, f);
+      Gx += hx; Gy += hy; Gz += hz; L += hl;
+    }
+    double j1o = 0.0, ei = 0.0, eid = 0.0;
+    int best = 0;
+    double bd = 1e300;
+    for (int a = 0; a < s.natom; ++a) {
+      const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+      const double d = sqrt(dx * dx + dy * dy + dz * dz);
+      if (d < bd) { bd = d; best = a; }
+      ei += -s.atom_zeff[a] / d;
+      eid += -s.atom_zeff[a] / fmax(d, alat);
+      if (s.has_j1) {
+        const double Z = s.j1_zeff[a], aa = s.j1_param;
+        const double c = pow(2.0 * Z, 0.25), AA = pow(2.0 * Z, 0.75);
+        double f1, f2;
+        if (s.j1_type == 0) {
+          const double ex = exp(-aa * c * d);
+          j1o += -AA * (1.0 / (2.0 * aa)) * (1.0 - ex);
+          f1 = -AA * c * ex / 2.0;
+          f2 = AA * aa * c * c * ex / 2.0;
+        } else {
+          const double q = 1.0 + aa * c * d;
+          j1o += -AA * d / (2.0 * q);
+          f1 = -AA / (2.0 * q * q);
+          f2 = AA * aa * c / (q * q * q);
+        }
+        Gx += f1 * dx / d; Gy += f1 * dy / d; Gz += f1 * dz / d;
+        L += f2 + 2.0 * f1 / d;
+      }
+    }
+    double j2o = 0.0;
+    if (s.has_j2) {
+      const double b = s.j2_param;
+      for (int m = 0; m < k.N; ++m) {
+        if (m == e) continue;
+        const double dx = x - k.r[3 * m], dy = y - k.r[3 * m + 1], dz = z - k.r[3 * m + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        double f1, f2;
+        if (s.j2_type == 0) {
+          const double q = 1.0 + b * d;
+          j2o += d / 2.0 * (1.0 / q);
+          f1 = 1.0 / (2.0 * q * q);
+          f2 = -b / (q * q * q);
+        } else {
+          const double ex = exp(-b * d);
+          j2o += 1.0 / (2.0 * b) * (1.0 - ex);
+          f1 = 0.5 * ex;
+          f2 = -0.5 * b * ex;
+        }
+        Gx += f1 * dx / d; Gy += f1 * dy / d; Gz += f1 * dz / d;
+        L += f2 + 2.0 * f1 / d;
+      }
+    }
+    t.ke[e] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
+    t.j1o[e] = j1o;
+    t.j2o[e] = j2o;
+    t.c3[e] = c3;
+    t.ei[e] = ei;
+    t.eid[e] = eid;
+    t.eatom[e] = best;
+    t.edist[e] = bd;
+  }
+  __syncthreads();
+}
+
+// psi(r')/psi(r) for electron e moved to p (det x Jastrow)
+__device__ double wf_ratio(const Work& k, const Terms& t, int e, double px, double py, double pz) {
+  const Sys& s = k.s;
+  const bool up = e < s.n_up;
+  const int i = up ? e : e - s.n_up;
+  const double det = ao_dot(s.det, s.atom_pos, px, py, pz, (up ? k.Tup : k.Tdn) + (size_t)i * k.A);
+  double dJ = 0.0;
+  if (s.has_j1) dJ += j1_at(s, px, py, pz) - t.j1o[e];
+  if (s.has_j2) dJ += j2_at(s, k.r, e, px, py, pz) - t.j2o[e];
+  if (s.has_j3) dJ += ao_dot(s.j3, s.atom_pos, px, py, pz, k.h3 + (size_t)e * k.A3) - t.c3[e];
+  return det * exp(dJ);
+}
+
+// Phase B: kinetic lattice elements (wavefunction.py:1740-1860) and non-local ECP
+// elements (coulomb_potential.py:1478-1712, NN = 1).  Rotation R in t.R.
+__device__ void mesh_terms(const Work& k, Terms& t, double alat, bool kinetic) {
+  const Sys& s = k.s;
+  const int N = k.N, nv = s.nv;
+  const int nkin = kinetic ? 6 * N : 0;
+  const int necp = s.ecp_flag ? nv * N : 0;
+  for (int p = threadIdx.x; p < nkin + necp; p += blockDim.x) {
+    if (p < nkin) {
+      const int e = p / 6, kk = p % 6, ax = kk >> 1;
+      const double sg = (kk & 1) ? -alat : alat;
+      const double px = k.r[3 * e] + sg * t.R[0 * 3 + ax];
+      const double py = k.r[3 * e + 1] + sg * t.R[1 * 3 + ax];
+      const double pz = k.r[3 * e + 2] + sg * t.R[2 * 3 + ax];
+      t.el[p] = -1.0 / (2.0 * alat * alat) * wf_ratio(k, t, e, px, py, pz);
+    } else {
+      const int q = p - nkin, e = q / nv, v = q % nv;
+      const int atom = t.eatom[e];
+      const int lmax = s.ecp_maxl1[atom];
+      if (lmax <= 0) { t.V[q] = 0.0; continue; }
+      const double* m = s.mesh_pts + 3 * v;
+      const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
+      const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
+      const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
+      const double Rx = s.atom_pos[3 * atom], Ry = s.atom_pos[3 * atom + 1], Rz = s.atom_pos[3 * atom + 2];
+      // rel = R - r; r' = r + rel + |rel| g ; cos = (-rel/|rel|) . (g/|g|)
+      const double relx = Rx - k.r[3 * e], rely = Ry - k.r[3 * e + 1], relz = Rz - k.r[3 * e + 2];
+      const double dist = sqrt(relx * relx + rely * rely + relz * relz);
+      const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+      const double cth = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
+      const double px = k.r[3 * e] + relx + dist * gx;
+      const double py = k.r[3 * e + 1] + rely + dist * gy;
+      const double pz = k.r[3 * e + 2] + relz + dist * gz;
+      const double ratio = wf_ratio(k, t, e, px, py, pz);
+      double vsum = 0.0;
+      for (int l = 0; l < lmax; ++l)
+        vsum += ecp_channel(s, atom, l, dist) * ((2 * l + 1) * legendre(l, cth) * s.mesh_w[v] * ratio);
+      t.V[q] = vsum;
+    }
+  }
+  __syncthreads();
+}
+
+// e-e Coulomb, block-reduced
+__device__ double coulomb_ee(const Work& k) {
+  const int N = k.N;
+  double acc = 0.0;
+  for (int p = threadIdx.x; p < N * N; p += blockDim.x) {
+    const int a = p / N, b = p % N;
+    if (b <= a) continue;
+    const double dx = k.r[3 * a] - k.r[3 * b], dy = k.r[3 * a + 1] - k.r[3 * b + 1], dz = k.r[3 * a + 2] - k.r[3 * b + 2];
+    acc += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+  }
+  return block_sum(acc, k.red);
+}
+
+// local ECP channel summed over electrons and nuclei (coulomb_potential.py:1145-1246)
+__device__ double ecp_local_sum(const Work& k) {
+  const Sys& s = k.s;
+  double acc = 0.0;
+  if (s.ecp_flag) {
+    for (int p = threadIdx.x; p < k.N * s.natom; p += blockDim.x) {
+      const int e = p / s.natom, a = p % s.natom;
+      const double dx = k.r[3 * e] - s.atom_pos[3 * a], dy = k.r[3 * e + 1] - s.atom_pos[3 * a + 1],
+                   dz = k.r[3 * e + 2] - s.atom_pos[3 * a + 2];
+      acc += ecp_channel(s, a, s.ecp_maxl1[a], sqrt(dx * dx + dy * dy + dz * dz));
+    }
+  }
+  return block_sum(acc, k.red);
+}
+
+// Phase C of the GFMC_n step: (diag, nondiag) sums (jqmc_gfmc.py:4806-5030).
+__device__ void lrdmc_sums(const Work& k, Terms& t, double alat, double* diag_out, double* nondiag_out) {
+  const Sys& s = k.s;
+  const int N = k.N;
+  double fn = 0.0, sp = 0.0, opt = 0.0;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) {
+    bool flip = false;
+    double nd = 0.0;
+    for (int kk = 0; kk < 6; ++kk) {
+      const double x = t.el[6 * e + kk];
+      fn += fmin(x, 0.0);
+      sp += fmax(x, 0.0);
+      flip = flip || (x >= 0.0);
+      nd += x + 1.0 / (4.0 * alat * alat);
+    }
+    const double zv = t.ei[e] + t.ke[e] - nd;
+    const double eu = s.ecp_flag ? t.ei[e] : t.eid[e];
+    opt += flip ? fmax(zv, eu) : zv;
+  }
+  double vfn = 0.0, vsp = 0.0;
+  if (s.ecp_flag)
+    for (int q = threadIdx.x; q < N * s.nv; q += blockDim.x) {
+      vfn += fmin(t.V[q], 0.0);
+      vsp += fmax(t.V[q], 0.0);
+    }
+  fn = block_sum(fn, k.red);
+  sp = block_sum(sp, k.red);
+  opt = block_sum(opt, k.red);
+  vfn = block_sum(vfn, k.red);
+  vsp = block_sum(vsp, k.red);
+  const double ee = coulomb_ee(k);
+  const double loc = ecp_local_sum(k);
+  const double disc = ee + s.ion_ion + opt;
+  const double dk = 3.0 / (2.0 * alat * alat) * N;
+  if (s.ecp_flag) {
+    *nondiag_out = fn + vfn;
+    *diag_out = dk + disc + loc + sp + vsp;
+  } else {
+    *nondiag_out = fn;
+    *diag_out = dk + disc + sp;
+  }
+}
+
+// ------------------------------------------------------------------ kernels
+struct KParams {
+  Sys s;
+  WS ws;
+  TableLayout tl;
+  WorkLayout wl;
+  TermsLayout ml;
+  int nwalk;
+};
+
+__global__ void k_ao_vgl(Sys s, int basis, const double* __restrict__ r, long long npts, double* __restrict__ out) {
+  const Basis& b = basis == 0 ? s.det : s.j3;
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const double x = r[3 * p], y = r[3 * p + 1], z = r[3 * p + 2];
+  const long long nao = b.nao;
+  auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
+    out[(0 * nao + a) * npts + p] = v;
+    out[(1 * nao + a) * npts + p] = gx;
+    out[(2 * nao + a) * npts + p] = gy;
+    out[(3 * nao + a) * npts + p] = gz;
+    out[(4 * nao + a) * npts + p] = lp;
+  };
+  for (int sh = 0; sh < b.nshell; ++sh) shell_vgl(b, s.atom_pos, sh, x, y, z, f);
+}
+
+// Walker initialisation: G, G^-1 (Gauss-Jordan, partial pivoting), T tables, J3 field.
+__global__ void k_walker_init(KParams P, int off_aug, int off_phi3) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work k = make_work(s, P.wl, smem, P.ws, w);
+  const int n = k.n, A = k.A, N = k.N;
+  for (int t = threadIdx.x; t < N * 3; t += blockDim.x) k.r[t] = P.ws.r[(size_t)w * N * 3 + t];
+  __syncthreads();
+  // M_up rows -> Tdn rows
+  for (int i = 0; i < n; ++i) {
+    ao_fill_block(s.det, s.atom_pos, k.r[3 * i], k.r[3 * i + 1], k.r[3 * i + 2], k.vA0);
+    __syncthreads();
+    for (int b = threadIdx.x; b < A; b += blockDim.x) {
+      double acc = 0.0;
+      for (int a = 0; a < A; ++a) acc += k.vA0[a] * s.lam[(size_t)a * A + b];
+      k.Tdn[(size_t)i * A + b] = acc;
+    }
+    __syncthreads();
+  }
+  // G columns and M_dn rows -> Tup rows
+  for (int j = 0; j < s.n_dn; ++j) {
+    const int e = s.n_up + j;
+    ao_fill_block(s.det, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.vA0);
+    __syncthreads();
+    rows_dot(k.Tdn, n, A, k.vA0, k.vn0);
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+      double acc = 0.0;
+      for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * k.vA0[b];
+      k.Tup[(size_t)j * A + a] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) k.G[i * n + j] = k.vn0[i];
+    __syncthreads();
+  }
+  // Gauss-Jordan on [G | I]
+  double* aug = reinterpret_cast<double*>(smem + off_aug);
+  const int n2 = 2 * n;
+  for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+    const int rr = t / n2, cc = t % n2;
+    aug[t] = cc < n ? k.G[rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  int* piv = reinterpret_cast<int*>(k.sc);
+  for (int c = 0; c < n; ++c) {
+    if (threadIdx.x == 0) {
+      int p = c;
+      double best = fabs(aug[c * n2 + c]);
+      for (int rr = c + 1; rr < n; ++rr) {
+        const double v = fabs(aug[rr * n2 + c]);
+        if (v > best) { best = v; p = rr; }
+      }
+      piv[0] = p;
+      if (best == 0.0) atomicOr(P.ws.status + w, JQMC_ST_SINGULAR);
+    }
+    __syncthreads();
+    const int p = piv[0];
+    if (p != c)
+      for (int cc = threadIdx.x; cc < n2; cc += blockDim.x) {
+        const double tmp = aug[c * n2 + cc];
+        aug[c * n2 + cc] = aug[p * n2 + cc];
+        aug[p * n2 + cc] = tmp;
+      }
+    __syncthreads();
+    const double pv = aug[c * n2 + c];
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < n2; cc += blockDim.x) aug[c * n2 + cc] /= pv;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+      const int rr = t / n2, cc = t % n2;
+      if (rr == c || cc == c) continue;
+      aug[t] -= aug[rr * n2 + c] * aug[c * n2 + cc];
+    }
+    __syncthreads();
+    for (int rr = threadIdx.x; rr < n; rr += blockDim.x)
+      if (rr != c) aug[rr * n2 + c] = 0.0;
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) k.Gi[t] = aug[(t / n) * n2 + n + (t % n)];
+  __syncthreads();
+  // T_up[k][a] = sum_j M_dn[j][a] G^-1[j][k] ; T_dn[k][b] = sum_i G^-1[k][i] M_up[i][b]  (in place per column)
+  for (int a = threadIdx.x; a < A; a += blockDim.x) {
+    double m[JQMC_MAX_NUP];
+    for (int j = 0; j < n; ++j) m[j] = k.Tup[(size_t)j * A + a];
+    for (int kk = 0; kk < n; ++kk) {
+      double acc = 0.0;
+      for (int j = 0; j < n; ++j) acc += m[j] * k.Gi[j * n + kk];
+      k.Tup[(size_t)kk * A + a] = acc;
+    }
+    for (int j = 0; j < n; ++j) m[j] = k.Tdn[(size_t)j * A + a];
+    for (int kk = 0; kk < n; ++kk) {
+      double acc = 0.0;
+      for (int j = 0; j < n; ++j) acc += k.Gi[kk * n + j] * m[j];
+      k.Tdn[(size_t)kk * A + a] = acc;
+    }
+  }
+  // J3 field
+  if (s.has_j3) {
+    const int A3 = k.A3;
+    double* phi3 = reinterpret_cast<double*>(smem + off_phi3);  // N*A3
+    for (int p = threadIdx.x; p < N * s.j3.nshell; p += blockDim.x) {
+      const int e = p / s.j3.nshell, sh = p % s.j3.nshell;
+      double* out = phi3 + (size_t)e * A3;
+      auto f = [&](int a, double v) { out[a] = v; };
+      shell_val(s.j3, s.atom_pos, sh, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], f);
+    }
+    __syncthreads();
+    // v30 = total up, v31 = total dn, v32 = running prefix of the current spin
+    for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+      double tu = 0.0, td = 0.0;
+      for (int e = 0; e < s.n_up; ++e) tu += phi3[(size_t)e * A3 + c];
+      for (int e = s.n_up; e < N; ++e) td += phi3[(size_t)e * A3 + c];
+      k.v30[c] = tu;
+      k.v31[c] = td;
+      k.v32[c] = 0.0;
+    }
+    __syncthreads();
+    double* h = k.h3;
+    for (int e = 0; e < N; ++e) {
+      const bool up = e < s.n_up;
+      if (e == s.n_up)
+        for (int c = threadIdx.x; c < A3; c += blockDim.x) k.v32[c] = 0.0;
+      __syncthreads();
+      const double* tot_same = up ? k.v30 : k.v31;
+      const double* pe = phi3 + (size_t)e * A3;
+      for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+        // h = j1 + J^T pfx + J (tot_same - pfx - phi_e) + (up ? J tot_dn : J^T tot_up)
+        double acc = s.j3vec[c];
+        for (int cp = 0; cp < A3; ++cp) {
+          const double Jcpc = s.j3mat[(size_t)cp * A3 + c];    // J[cp][c]
+          const double Jccp = s.j3matT[(size_t)cp * A3 + c];   // J[c][cp]
+          const double pf = k.v32[cp];
+          acc += Jcpc * pf + Jccp * (tot_same[cp] - pf - pe[cp]);
+          acc += up ? Jccp * k.v31[cp] : Jcpc * k.v30[cp];
+        }
+        h[(size_t)e * A3 + c] = acc;
+      }
+      __syncthreads();
+      for (int c = threadIdx.x; c < A3; c += blockDim.x) k.v32[c] += pe[c];
+      __syncthreads();
+    }
+  }
+  store_walker(k, P.ws, w);
+}
+
+// ln|det G|, sign (LU with partial pivoting on a copy of G) and J
+__global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work k = make_work(s, P.wl, smem, P.ws, w);
+  load_walker(k, P.ws, w);
+  const int n = k.n, N = k.N;
+  double* a = reinterpret_cast<double*>(smem + off_aug);
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) a[t] = k.G[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ld = 0.0, sg = 1.0;
+    for (int c = 0; c < n; ++c) {
+      int p = c;
+      double best = fabs(a[c * n + c]);
+      for (int rr = c + 1; rr < n; ++rr)
+        if (fabs(a[rr * n + c]) > best) { best = fabs(a[rr * n + c]); p = rr; }
+      if (p != c) {
+        sg = -sg;
+        for (int cc = 0; cc < n; ++cc) { const double tmp = a[c * n + cc]; a[c * n + cc] = a[p * n + cc]; a[p * n + cc] = tmp; }
+      }
+      const double pv = a[c * n + c];
+      if (pv < 0) sg = -sg;
+      ld += log(fabs(pv));
+      for (int rr = c + 1; rr < n; ++rr) {
+        const double f = a[rr * n + c] / pv;
+        for (int cc = c + 1; cc < n; ++cc) a[rr * n + cc] -= f * a[c * n + cc];
+      }
+    }
+    logdet[w] = ld;
+    sign[w] = sg;
+  }
+  // J = J1 + J2 + J3;  J3 = (sum_e phi3_e . h_e + j1 . sum_e phi3_e) / 2
+  double j = 0.0;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) {
+    const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
+    if (s.has_j1) j += j1_at(s, x, y, z);
+    if (s.has_j2) j += 0.5 * j2_at(s, k.r, e, x, y, z);
+    if (s.has_j3) {
+      const double* h = k.h3 + (size_t)e * k.A3;
+      double acc = 0.0;
+      auto f = [&](int aa, double v) { acc += v * (h[aa] + s.j3vec[aa]); };
+      for (int sh = 0; sh < s.j3.nshell; ++sh) shell_val(s.j3, s.atom_pos, sh, x, y, z, f);
+      j += 0.5 * acc;
+    }
+  }
+  j = block_sum(j, k.red);
+  if (threadIdx.x == 0) jas[w] = j;
+}
+
+__device__ double as_factor_block(const Work& k) {
+  const int n = k.n;
+  double F = 0.0;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) F += k.Gi[t] * k.Gi[t];
+  F = block_sum(F, k.red);
+  double mn = 1e300;
+  for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+    double acc = 0.0;
+    if (t < n) for (int c = 0; c < n; ++c) acc += k.G[t * n + c] * k.G[t * n + c];
+    else for (int rr = 0; rr < n; ++rr) acc += k.G[rr * n + (t - n)] * k.G[rr * n + (t - n)];
+    mn = fmin(mn, acc);
+  }
+  mn = block_min(mn, k.red);
+  const double SF = mn * F;
+  return SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
+}
+
+// VMC: K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523)
+__global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt,
+                            double eps_AS, int* accept, int off_cand) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work k = make_work(s, P.wl, smem, P.ws, w);
+  load_walker(k, P.ws, w);
+  const int n = k.n, A = k.A, A3 = k.A3;
+  double* cand = reinterpret_cast<double*>(smem + off_cand);  // n*n candidate G^-1
+  double* Gc = cand + n * n;                                   // n*n candidate G
+  int nacc = 0;
+  double R_old = as_factor_block(k);
+  for (int step = 0; step < K; ++step) {
+    const int* id = idraw + ((size_t)w * K + step) * 4;
+    const double* fd = fdraw + ((size_t)w * K + step) * 2;
+    // proposal (thread 0), broadcast via sc
+    if (threadIdx.x == 0) {
+      const int sel = id[0];
+      const bool is_up = sel < s.n_up;
+      const int e = is_up ? id[1] : s.n_up + id[2];
+      const double ox = k.r[3 * e], oy = k.r[3 * e + 1], oz = k.r[3 * e + 2];
+      int a0 = nearest_atom(s, ox, oy, oz);
+      double Z = s.atom_zeff[a0];
+      double dd = sqrt((ox - s.atom_pos[3 * a0]) * (ox - s.atom_pos[3 * a0]) + (oy - s.atom_pos[3 * a0 + 1]) * (oy - s.atom_pos[3 * a0 + 1]) +
+                       (oz - s.atom_pos[3 * a0 + 2]) * (oz - s.atom_pos[3 * a0 + 2]));
+      const double fl = 1.0 / (Z * Z) * (1.0 + Z * Z * dd) / (1.0 + dd);
+      const double g = fd[0] * (fl * Dt);
+      double nx = ox, ny = oy, nz = oz;
+      if (id[3] == 0) nx += g; else if (id[3] == 1) ny += g; else nz += g;
+      a0 = nearest_atom(s, nx, ny, nz);
+      Z = s.atom_zeff[a0];
+      dd = sqrt((nx - s.atom_pos[3 * a0]) * (nx - s.atom_pos[3 * a0]) + (ny - s.atom_pos[3 * a0 + 1]) * (ny - s.atom_pos[3 * a0 + 1]) +
+                (nz - s.atom_pos[3 * a0 + 2]) * (nz - s.atom_pos[3 * a0 + 2]));
+      const double fp = 1.0 / (Z * Z) * (1.0 + Z * Z * dd) / (1.0 + dd);
+      const double d2 = (nx - ox) * (nx - ox) + (ny - oy) * (ny - oy) + (nz - oz) * (nz - oz);
+      const double Tr = (fl / fp) * exp(-d2 * (1.0 / (2.0 * fp * fp * Dt * Dt) - 1.0 / (2.0 * fl * fl * Dt * Dt)));
+      k.sc[0] = e;
+      k.sc[1] = nx; k.sc[2] = ny; k.sc[3] = nz;
+      k.sc[4] = Tr;
+      double dJ = 0.0;
+      if (s.has_j1) dJ += j1_at(s, nx, ny, nz) - j1_at(s, ox, oy, oz);
+      k.sc[5] = dJ;
+    }
+    __syncthreads();
+    const int e = (int)k.sc[0];
+    const double nx = k.sc[1], ny = k.sc[2], nz = k.sc[3];
+    const bool up = e < s.n_up;
+    const int i = up ? e : e - s.n_up;
+    // J2 and J3 ratio parts
+    double dJ = 0.0;
+    if (s.has_j2)
+      for (int m = threadIdx.x; m < k.N; m += blockDim.x) {
+        if (m == e) continue;
+        const double ax = nx - k.r[3 * m], ay = ny - k.r[3 * m + 1], az = nz - k.r[3 * m + 2];
+        const double bx = k.r[3 * e] - k.r[3 * m], by = k.r[3 * e + 1] - k.r[3 * m + 1], bz = k.r[3 * e + 2] - k.r[3 * m + 2];
+        dJ += j2_pair(s.j2_type, s.j2_param, sqrt(ax * ax + ay * ay + az * az)) -
+              j2_pair(s.j2_type, s.j2_param, sqrt(bx * bx + by * by + bz * bz));
+      }
+    ao_fill_block(s.det, s.atom_pos, nx, ny, nz, k.vA0);
+    if (s.has_j3) {
+      ao_fill_block(s.j3, s.atom_pos, nx, ny, nz, k.v30);
+      ao_fill_block(s.j3, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.v31);
+    }
+    __syncthreads();
+    if (s.has_j3)
+      for (int a = threadIdx.x; a < A3; a += blockDim.x) dJ += (k.v30[a] - k.v31[a]) * k.h3[(size_t)e * A3 + a];
+    dJ = block_sum(dJ, k.red);
+    rows_dot(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
+    __syncthreads();
+    const double ratio = k.vn0[i];
+    const double inv = 1.0 / ratio;
+    // candidate G, G^-1 for the AS factor of the proposed state
+    if (up) {
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int rr = t / n, cc = t % n;
+        cand[t] = k.Gi[t] - k.Gi[rr * n + i] * (k.vn0[cc] - (cc == i ? 1.0 : 0.0)) * inv;
+        if (rr == i) {
+          double g = 0.0;
+          for (int q = 0; q < n; ++q) g += k.vn0[q] * k.G[q * n + cc];
+          Gc[t] = g;
+        } else {
+          Gc[t] = k.G[t];
+        }
+      }
+    } else {
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int rr = t / n, cc = t % n;
+        cand[t] = k.Gi[t] - (k.vn0[rr] - (rr == i ? 1.0 : 0.0)) * k.Gi[i * n + cc] * inv;
+        if (cc == i) {
+          double g = 0.0;
+          for (int q = 0; q < n; ++q) g += k.G[rr * n + q] * k.vn0[q];
+          Gc[t] = g;
+        } else {
+          Gc[t] = k.G[t];
+        }
+      }
+    }
+    __syncthreads();
+    double F = 0.0;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) F += cand[t] * cand[t];
+    F = block_sum(F, k.red);
+    double mn = 1e300;
+    for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+      double acc = 0.0;
+      if (t < n) for (int c = 0; c < n; ++c) acc += Gc[t * n + c] * Gc[t * n + c];
+      else for (int rr = 0; rr < n; ++rr) acc += Gc[rr * n + (t - n)] * Gc[rr * n + (t - n)];
+      mn = fmin(mn, acc);
+    }
+    mn = block_min(mn, k.red);
+    const double SF = mn * F;
+    const double R_new = SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
+    if (threadIdx.x == 0) {
+      const double Jr = exp(k.sc[5] + dJ);
+      const double Ras = (fmax(R_new, eps_AS) / R_new) / (fmax(R_old, eps_AS) / R_old);
+      const double Rr = pow(Ras * Jr * ratio, 2.0);
+      const double pacc = fmin(1.0, Rr * k.sc[4]);
+      k.sc[6] = (fd[1] < pacc) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (k.sc[6] != 0.0) {
+      sm_move(k, e, nx, ny, nz);
+      R_old = R_new;
+      ++nacc;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) accept[w] += nacc;
+  store_walker(k, P.ws, w);
+}
+
+// VMC local energy and weight (hamiltonians.py:225-290, jqmc_mcmc.py:725-747)
+__global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, double eps_AS, double* eL, double* wL) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Terms t = make_terms(P.ml, smem);
+  load_walker(k, P.ws, w);
+  if (threadIdx.x == 0) rotation(angles[3 * w], angles[3 * w + 1], angles[3 * w + 2], t.R);
+  __syncthreads();
+  electron_terms(k, t, 0.0);
+  mesh_terms(k, t, 0.0, false);
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < k.N; e += blockDim.x) acc += t.ke[e] + t.ei[e];
+  if (s.ecp_flag)
+    for (int q = threadIdx.x; q < k.N * s.nv; q += blockDim.x) acc += t.V[q];
+  acc = block_sum(acc, k.red);
+  const double ee = coulomb_ee(k);
+  const double loc = ecp_local_sum(k);
+  const double R = as_factor_block(k);
+  if (threadIdx.x == 0) {
+    eL[w] = acc + ee + s.ion_ion + loc;
+    const double q = R / fmax(R, eps_AS);
+    wL[w] = q * q;
+  }
+}
+
+// LRDMC GFMC_n projections; K steps fused.  K == 0 with energy outputs computes
+// e_L and V_diag at the current positions with the rotation of draw[w].
+__global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
+                        double* eL, double* vdiag) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Terms t = make_terms(P.ml, smem);
+  load_walker(k, P.ws, w);
+  const int N = k.N;
+  const int nsteps = K > 0 ? K : 1;
+  double wl = K > 0 ? wgt[w] : 1.0;
+  for (int step = 0; step < nsteps; ++step) {
+    const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * 4;
+    if (threadIdx.x == 0) rotation(d[0], d[1], d[2], t.R);
+    __syncthreads();
+    electron_terms(k, t, alat);
+    mesh_terms(k, t, alat, true);
+    double diag, nondiag;
+    lrdmc_sums(k, t, alat, &diag, &nondiag);
+    if (K == 0) {
+      if (threadIdx.x == 0) {
+        eL[w] = diag + nondiag;
+        vdiag[w] = diag;
+      }
+      break;
+    }
+    wl = wl * (1.0 / (diag - E_scf) * (-1.0 * nondiag));
+    // move choice: sequential cumsum over the normalised FN weights (thread 0)
+    if (threadIdx.x == 0) {
+      const int nk = 6 * N, ne = s.ecp_flag ? s.nv * N : 0;
+      double sum = 0.0;
+      for (int p = 0; p < nk; ++p) sum += fmin(t.el[p], 0.0);
+      for (int q = 0; q < ne; ++q) sum += fmin(t.V[q], 0.0);
+      const double u = d[3];
+      double cdf = 0.0;
+      int kk = nk + ne - 1;
+      for (int p = 0; p < nk + ne; ++p) {
+        const double x = p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0);
+        cdf += x / sum;
+        if (cdf >= u) { kk = p; break; }
+      }
+      double px, py, pz;
+      int e;
+      if (kk < nk) {
+        e = kk / 6;
+        const int sh = kk % 6, ax = sh >> 1;
+        const double sg = (sh & 1) ? -alat : alat;
+        px = k.r[3 * e] + sg * t.R[ax];
+        py = k.r[3 * e + 1] + sg * t.R[3 + ax];
+        pz = k.r[3 * e + 2] + sg * t.R[6 + ax];
+      } else {
+        const int q = kk - nk, v = q % s.nv;
+        e = q / s.nv;
+        const int atom = t.eatom[e];
+        const double* m = s.mesh_pts + 3 * v;
+        const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
+        const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
+        const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
+        const double relx = s.atom_pos[3 * atom] - k.r[3 * e], rely = s.atom_pos[3 * atom + 1] - k.r[3 * e + 1],
+                     relz = s.atom_pos[3 * atom + 2] - k.r[3 * e + 2];
+        const double dist = sqrt(relx * relx + rely * rely + relz * relz);
+        px = k.r[3 * e] + relx + dist * gx;
+        py = k.r[3 * e + 1] + rely + dist * gy;
+        pz = k.r[3 * e + 2] + relz + dist * gz;
+      }
+      k.sc[0] = e; k.sc[1] = px; k.sc[2] = py; k.sc[3] = pz;
+    }
+    __syncthreads();
+    const double ratio = sm_move(k, (int)k.sc[0], k.sc[1], k.sc[2], k.sc[3]);
+    if (threadIdx.x == 0 && ratio == 0.0) atomicOr(P.ws.status + w, JQMC_ST_ZERO_RATIO);
+  }
+  if (K > 0) {
+    if (threadIdx.x == 0) {
+      wgt[w] = wl;
+      if (!isfinite(wl)) atomicOr(P.ws.status + w, JQMC_ST_NAN);
+    }
+    store_walker(k, P.ws, w);
+  }
+}
+
+__global__ void k_branch_comb(int W, const double* __restrict__ wv, double* cum) {
+  // cumulative normalised weights, sequential as np.cumsum (one thread), then a
+  // parallel left searchsorted for the comb points (k + zeta) / W
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int j = 0; j < W; ++j) tot += wv[j];
+    double c = 0.0;
+    for (int j = 0; j < W; ++j) { c += wv[j] / tot; cum[j] = c; }
+  }
+}
+
+__global__ void k_branch_search(int W, const double* __restrict__ cum, double zeta, int* chosen) {
+  const int kq = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kq >= W) return;
+  const double z = (kq + zeta) / W;
+  int lo = 0, hi = W;  // first j with cum[j] >= z
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cum[mid] < z) lo = mid + 1; else hi = mid;
+  }
+  chosen[kq] = lo < W ? lo : W - 1;
+}
+
+__global__ void k_gather(const double* __restrict__ src, double* __restrict__ dst, long long per, const int* chosen, int W) {
+  const long long tot = per * W;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const long long w = t / per, o = t % per;
+    dst[t] = src[(long long)chosen[w] * per + o];
+  }
+}
+
+__global__ void k_gather_int(const int* __restrict__ src, int* __restrict__ dst, const int* chosen, int W) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < W) dst[t] = src[chosen[t]];
+}
+
+// ------------------------------------------------------------------ host side
+inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
+
+KParams make_params(const jqmc_system* sys, const jqmc_walkers* w);
+
+}  // namespace
+
+struct jqmc_system {
+  Sys s;
+  void* blob;
+};
+
+namespace {
+
+WS to_ws(const jqmc_walkers* w) {
+  WS x;
+  x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3; x.status = w->status;
+  return x;
+}
+
+bool walkers_ok(const jqmc_system* sys, const jqmc_walkers* w) {
+  if (!sys || !w || w->nwalk <= 0) return false;
+  if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status) return false;
+  if (sys->s.has_j3 && !w->h3) return false;
+  return true;
+}
+
+KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
+  KParams P;
+  P.s = sys->s;
+  P.ws = to_ws(w);
+  P.tl = table_layout(sys->s);
+  P.wl = work_layout(sys->s, P.tl.bytes);
+  P.ml = terms_layout(sys->s, P.wl.bytes);
+  P.nwalk = w->nwalk;
+  return P;
+}
+
+int launch_check(const void* fn, int smem) {
+  if (smem > 227 * 1024) return JQMC_E_SMEM;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return JQMC_E_CUDA;
+  return JQMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
+  if (!d || !out) return JQMC_E_ARG;
+  *out = nullptr;
+  const int M = d->natom, A = d->det.nao;
+  if (M <= 0 || M > JQMC_MAX_ATOM || d->n_up <= 0 || d->n_up > JQMC_MAX_NUP) return JQMC_E_LIMIT;
+  if (d->n_up != d->n_dn) return JQMC_E_ARG;  // the walker kernels treat closed shells
+  if (d->n_up + d->n_dn > JQMC_MAX_ELEC || A <= 0 || A > JQMC_MAX_AO) return JQMC_E_LIMIT;
+  if (!d->atom_pos || !d->atom_zeff || !d->lambda || !d->det.shells || !d->det.prims) return JQMC_E_ARG;
+  const int A3 = d->has_j3 ? d->j3.nao : 0;
+  if (d->has_j3 && (A3 <= 0 || A3 > JQMC_MAX_AO || !d->j3.shells || !d->j3.prims || !d->j3_matrix)) return JQMC_E_ARG;
+  if (d->has_j1 && !d->j1_zeff) return JQMC_E_ARG;
+  if (d->ecp_flag && (!d->ecp_maxl1 || !d->ecp_chan || !d->ecp_terms || !d->mesh_points || !d->mesh_weights)) return JQMC_E_ARG;
+  if (d->ecp_flag && !(d->nv == 4 || d->nv == 6 || d->nv == 12 || d->nv == 18)) return JQMC_E_ARG;
+  auto check_basis = [](const jqmc_basis_desc& b) {
+    for (int s = 0; s < b.nshell; ++s) {
+      const int* sh = b.shells + 8 * s;
+      if (sh[1] < 0 || sh[1] > JQMC_LMAX || sh[2] <= 0 || sh[3] < 0 || sh[3] + sh[2] > b.nprim) return false;
+      if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) return false;
+    }
+    return true;
+  };
+  if (!check_basis(d->det) || (d->has_j3 && !check_basis(d->j3))) return JQMC_E_ARG;
+  for (int s = 0; s < d->det.nshell; ++s)
+    if (d->det.shells[8 * s] < 0 || d->det.shells[8 * s] >= M) return JQMC_E_ARG;
+  if (d->has_j3)
+    for (int s = 0; s < d->j3.nshell; ++s)
+      if (d->j3.shells[8 * s] < 0 || d->j3.shells[8 * s] >= M) return JQMC_E_ARG;
+  if (d->ecp_flag)
+    for (int a = 0; a < M; ++a) {
+      if (d->ecp_maxl1[a] < 0 || d->ecp_maxl1[a] >= kSlots) return JQMC_E_ARG;
+      for (int l = 0; l < kSlots; ++l) {
+        const int* ch = d->ecp_chan + (a * kSlots + l) * 2;
+        if (ch[1] < 0 || ch[0] < 0 || ch[0] + ch[1] > d->ecp_nterm) return JQMC_E_ARG;
+      }
+    }
+
+  // one device blob for every table
+  std::vector<unsigned char> host;
+  auto put = [&host](const void* src, size_t bytes) -> size_t {
+    const size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + bytes);
+    if (bytes) memcpy(host.data() + off, src, bytes);
+    return off;
+  };
+  std::vector<double> lamT((size_t)A * A);
+  for (int a = 0; a < A; ++a)
+    for (int b = 0; b < A; ++b) lamT[(size_t)b * A + a] = d->lambda[(size_t)a * A + b];
+  std::vector<double> j3m, j3mT, j3v;
+  if (d->has_j3) {
+    j3m.resize((size_t)A3 * A3);
+    j3mT.resize((size_t)A3 * A3);
+    j3v.resize(A3);
+    for (int a = 0; a < A3; ++a) {
+      for (int b = 0; b < A3; ++b) {
+        j3m[(size_t)a * A3 + b] = d->j3_matrix[(size_t)a * (A3 + 1) + b];
+        j3mT[(size_t)b * A3 + a] = d->j3_matrix[(size_t)a * (A3 + 1) + b];
+      }
+      j3v[a] = d->j3_matrix[(size_t)a * (A3 + 1) + A3];
+    }
+  }
+  std::vector<double> zero(M, 0.0);
+  std::vector<int> zeroi(M * kSlots * 2 + M, 0);
+  const size_t o_apos = put(d->atom_pos, (size_t)M * 24);
+  const size_t o_az = put(d->atom_zeff, (size_t)M * 8);
+  const size_t o_dsh = put(d->det.shells, (size_t)d->det.nshell * 32);
+  const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
+  const size_t o_lam = put(d->lambda, (size_t)A * A * 8);
+  const size_t o_lamT = put(lamT.data(), (size_t)A * A * 8);
+  const size_t o_j1z = put(d->has_j1 ? d->j1_zeff : zero.data(), (size_t)M * 8);
+  size_t o_jsh = 0, o_jpr = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0;
+  if (d->has_j3) {
+    o_jsh = put(d->j3.shells, (size_t)d->j3.nshell * 32);
+    o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
+    o_j3m = put(j3m.data(), j3m.size() * 8);
+    o_j3mT = put(j3mT.data(), j3mT.size() * 8);
+    o_j3v = put(j3v.data(), j3v.size() * 8);
+  }
+  const size_t o_maxl1 = put(d->ecp_flag ? d->ecp_maxl1 : zeroi.data(), (size_t)M * 4);
+  const size_t o_chan = put(d->ecp_flag ? d->ecp_chan : zeroi.data(), (size_t)M * kSlots * 8);
+  const size_t o_terms = put(d->ecp_flag ? d->ecp_terms : zero.data(), (size_t)(d->ecp_flag ? d->ecp_nterm : 1) * 24);
+  const int nv = d->ecp_flag ? d->nv : 0;
+  const size_t o_mp = put(d->ecp_flag ? d->mesh_points : zero.data(), (size_t)(nv > 0 ? nv : 1) * 24);
+  const size_t o_mw = put(d->ecp_flag ? d->mesh_weights : zero.data(), (size_t)(nv > 0 ? nv : 1) * 8);
+
+  void* blob = nullptr;
+  if (cudaMalloc(&blob, host.size()) != cudaSuccess) return JQMC_E_CUDA;
+  if (cudaMemcpy(blob, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(blob);
+    return JQMC_E_CUDA;
+  }
+  auto dp = [blob](size_t off) { return reinterpret_cast<const double*>(static_cast<unsigned char*>(blob) + off); };
+  auto ip = [blob](size_t off) { return reinterpret_cast<const int*>(static_cast<unsigned char*>(blob) + off); };
+  jqmc_system* sys = new jqmc_system();
+  Sys& s = sys->s;
+  s.natom = M; s.n_up = d->n_up; s.n_dn = d->n_dn; s.N = d->n_up + d->n_dn;
+  s.atom_pos = dp(o_apos); s.atom_zeff = dp(o_az);
+  s.det.nshell = d->det.nshell; s.det.nao = A; s.det.nprim = d->det.nprim;
+  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr);
+  s.lam = dp(o_lam); s.lamT = dp(o_lamT);
+  s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_zeff = dp(o_j1z);
+  s.has_j2 = d->has_j2; s.j2_type = d->j2_type; s.j2_param = d->j2_param;
+  s.has_j3 = d->has_j3;
+  if (d->has_j3) {
+    s.j3.nshell = d->j3.nshell; s.j3.nao = A3; s.j3.nprim = d->j3.nprim;
+    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr);
+    s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v);
+  } else {
+    s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr;
+    s.j3mat = s.j3matT = s.j3vec = nullptr;
+  }
+  s.ecp_flag = d->ecp_flag;
+  s.ecp_maxl1 = ip(o_maxl1); s.ecp_chan = ip(o_chan);
+  s.ecp_nterm = d->ecp_flag ? d->ecp_nterm : 0; s.ecp_terms = dp(o_terms);
+  s.nv = nv; s.mesh_pts = dp(o_mp); s.mesh_w = dp(o_mw);
+  s.ion_ion = d->ion_ion;
+  sys->blob = blob;
+  *out = sys;
+  return JQMC_OK;
+}
+
+int jqmc_system_destroy(jqmc_system* sys) {
+  if (!sys) return JQMC_E_ARG;
+  cudaDeviceSynchronize();
+  if (sys->blob) cudaFree(sys->blob);
+  delete sys;
+  return JQMC_OK;
+}
+
+int64_t jqmc_walker_bytes(const jqmc_system* sys) {
+  if (!sys) return JQMC_E_ARG;
+  const Sys& s = sys->s;
+  const int64_t n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
+  return 8 * (N * 3 + 2 * n * n + 2 * n * A + N * A3) + 4;
+}
+
+int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_t npts, double* d_out, void* stream) {
+  if (!sys || !d_r || !d_out || npts < 0 || (basis != 0 && basis != 1)) return JQMC_E_ARG;
+  if (basis == 1 && !sys->s.has_j3) return JQMC_E_ARG;
+  if (npts == 0) return JQMC_OK;
+  const int bs = 128;
+  k_ao_vgl<<<(unsigned)((npts + bs - 1) / bs), bs, 0, S(stream)>>>(sys->s, basis, d_r, npts, d_out);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream) {
+  if (!walkers_ok(sys, w)) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const Sys& s = sys->s;
+  const int off_aug = P.wl.bytes;
+  const int off_phi3 = align16(off_aug + s.n_up * 2 * s.n_up * 8);
+  const int smem = align16(off_phi3 + (s.has_j3 ? s.N * s.j3.nao * 8 : 0));
+  int rc = launch_check((const void*)k_walker_init, smem);
+  if (rc) return rc;
+  k_walker_init<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, off_phi3);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow,
+                 void* stream) {
+  if (!walkers_ok(sys, w) || !d_logdet || !d_sign || !d_jastrow) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int off_aug = P.wl.bytes;
+  const int smem = align16(off_aug + sys->s.n_up * sys->s.n_up * 8);
+  int rc = launch_check((const void*)k_log_psi, smem);
+  if (rc) return rc;
+  k_log_psi<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, d_logdet, d_sign, d_jastrow);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_vmc_sweep(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const int32_t* d_idraw,
+                   const double* d_fdraw, double Dt, double eps_AS, int32_t* d_accept, void* stream) {
+  if (!walkers_ok(sys, w) || K < 0 || !d_idraw || !d_fdraw || !d_accept) return JQMC_E_ARG;
+  if (K == 0) return JQMC_OK;
+  KParams P = make_params(sys, w);
+  const int off_cand = P.wl.bytes;
+  const int smem = align16(off_cand + 2 * sys->s.n_up * sys->s.n_up * 8);
+  int rc = launch_check((const void*)k_vmc_sweep, smem);
+  if (rc) return rc;
+  k_vmc_sweep<<<w->nwalk, 64, smem, S(stream)>>>(P, K, d_idraw, d_fdraw, Dt, eps_AS, d_accept, off_cand);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double eps_AS,
+                     double* d_eL, double* d_wL, void* stream) {
+  if (!walkers_ok(sys, w) || !d_angles || !d_eL || !d_wL) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  int rc = launch_check((const void*)k_vmc_measure, smem);
+  if (rc) return rc;
+  k_vmc_measure<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, eps_AS, d_eL, d_wL);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_lrdmc_project(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const double* d_draw, double alat,
+                       double E_scf, double* d_w, void* stream) {
+  if (!walkers_ok(sys, w) || K < 0 || !d_draw || !d_w || !(alat > 0.0)) return JQMC_E_ARG;
+  if (K == 0) return JQMC_OK;
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  int rc = launch_check((const void*)k_lrdmc, smem);
+  if (rc) return rc;
+  k_lrdmc<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, nullptr, nullptr);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_lrdmc_energy(const jqmc_system* sys, const jqmc_walkers* w, const double* d_draw, double alat, double* d_eL,
+                      double* d_vdiag, void* stream) {
+  if (!walkers_ok(sys, w) || !d_draw || !d_eL || !d_vdiag || !(alat > 0.0)) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  int rc = launch_check((const void*)k_lrdmc, smem);
+  if (rc) return rc;
+  k_lrdmc<<<w->nwalk, 128, smem, S(stream)>>>(P, 0, d_draw, alat, 0.0, nullptr, d_eL, d_vdiag);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, double* d_cum, void* stream) {
+  if (nwalk <= 0 || !d_w || !d_chosen || !d_cum || !(zeta >= 0.0 && zeta < 1.0)) return JQMC_E_ARG;
+  k_branch_comb<<<1, 1, 0, S(stream)>>>(nwalk, d_w, d_cum);
+  k_branch_search<<<(nwalk + 127) / 128, 128, 0, S(stream)>>>(nwalk, d_cum, zeta, d_chosen);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jqmc_walkers* dst, const int32_t* d_chosen,
+                       void* stream) {
+  if (!walkers_ok(sys, src) || !walkers_ok(sys, dst) || !d_chosen || src->nwalk != dst->nwalk) return JQMC_E_ARG;
+  const Sys& s = sys->s;
+  const int W = src->nwalk;
+  const long long n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
+  const int grid = 4 * 152, bs = 256;
+  k_gather<<<grid, bs, 0, S(stream)>>>(src->r, dst->r, N * 3, d_chosen, W);
+  k_gather<<<grid, bs, 0, S(stream)>>>(src->G, dst->G, n * n, d_chosen, W);
+  k_gather<<<grid, bs, 0, S(stream)>>>(src->Ginv, dst->Ginv, n * n, d_chosen, W);
+  k_gather<<<grid, bs, 0, S(stream)>>>(src->Tup, dst->Tup, n * A, d_chosen, W);
+  k_gather<<<grid, bs, 0, S(stream)>>>(src->Tdn, dst->Tdn, n * A, d_chosen, W);
+  if (A3) k_gather<<<grid, bs, 0, S(stream)>>>(src->h3, dst->h3, N * A3, d_chosen, W);
+  k_gather_int<<<(W + 255) / 256, 256, 0, S(stream)>>>(src->status, dst->status, d_chosen, W);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+}  // extern "C"

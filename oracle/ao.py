@@ -78,7 +78,8 @@ def primitive_norm(l: int, Z):
 
 
 class AOTable:
-    """Per-AO primitive lists extracted once from an AOs_sphe_data-like object."""
+    """Per-AO primitive tables (padded to the deepest contraction) extracted once
+    from an AOs_sphe_data-like object."""
 
     def __init__(self, aos):
         self.num_ao = aos.num_ao
@@ -88,51 +89,47 @@ class AOTable:
         oi = np.asarray(aos.orbital_indices, dtype=int)
         ex = np.asarray(aos.exponents, dtype=np.float64)
         co = np.asarray(aos.coefficients, dtype=np.float64)
-        self.prims = [(ex[oi == a], co[oi == a]) for a in range(self.num_ao)]
+        kmax = int(np.max(np.bincount(oi, minlength=self.num_ao)))
+        self.Z = np.zeros((self.num_ao, kmax))
+        self.cN = np.zeros((self.num_ao, kmax))
+        for a in range(self.num_ao):
+            z, c = ex[oi == a], co[oi == a]
+            self.Z[a, : len(z)] = z
+            self.cN[a, : len(z)] = c * primitive_norm(int(self.l[a]), z)
+        self.by_l = {l: np.nonzero(self.l == l)[0] for l in np.unique(self.l)}
+
+
+def _common(tab: AOTable, r, need_grad: bool):
+    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
+    d = r[:, None, :] - tab.centers[None, :, :]                     # (P, A, 3)
+    r2 = np.sum(d * d, axis=-1)                                      # (P, A)
+    e = np.exp(-tab.Z[None, :, :] * r2[:, :, None])                  # (P, A, K)
+    pref = tab.cN[None] * e                                          # (P, A, K)
+    S = np.zeros(r2.shape)
+    gS = np.zeros(d.shape) if need_grad else None
+    for l, idx in tab.by_l.items():
+        Sl, Gl = solid_harmonics(int(l), d[:, idx])                  # (2l+1, P, n), (2l+1, P, n, 3)
+        sel = tab.m[idx] + l
+        cols = np.arange(len(idx))
+        S[:, idx] = Sl[sel, :, cols].T
+        if need_grad:
+            gS[:, idx] = np.transpose(Gl[sel, :, cols], (1, 0, 2))
+    return d, r2, pref, S, gS
 
 
 def ao_value(tab: AOTable, r: np.ndarray) -> np.ndarray:
     """AO values (num_ao, P) at points r (P, 3)."""
-    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
-    out = np.zeros((tab.num_ao, r.shape[0]))
-    cache = {}
-    for a in range(tab.num_ao):
-        d = r - tab.centers[a]
-        r2 = np.sum(d * d, axis=-1)
-        l, m = int(tab.l[a]), int(tab.m[a])
-        key = (tuple(tab.centers[a]), l)
-        if key not in cache:
-            cache[key] = solid_harmonics(l, d)[0]
-        Z, c = tab.prims[a]
-        rad = np.sum((c * primitive_norm(l, Z))[:, None] * np.exp(-Z[:, None] * r2[None, :]), axis=0)
-        out[a] = rad * cache[key][m + l]
-    return out
+    d, r2, pref, S, _ = _common(tab, r, False)
+    return (pref.sum(-1) * S).T
 
 
 def ao_vgl(tab: AOTable, r: np.ndarray):
     """(val, gx, gy, gz, lap), each (num_ao, P), following atomic_orbital.py:3560-3591."""
-    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
-    P = r.shape[0]
-    val = np.zeros((tab.num_ao, P))
-    grad = np.zeros((tab.num_ao, P, 3))
-    lap = np.zeros((tab.num_ao, P))
-    cache = {}
-    for a in range(tab.num_ao):
-        d = r - tab.centers[a]
-        r2 = np.sum(d * d, axis=-1)
-        l, m = int(tab.l[a]), int(tab.m[a])
-        key = (tuple(tab.centers[a]), l)
-        if key not in cache:
-            cache[key] = solid_harmonics(l, d)
-        S = cache[key][0][m + l]
-        gS = cache[key][1][m + l]
-        Z, c = tab.prims[a]
-        pref = (c * primitive_norm(l, Z))[:, None] * np.exp(-Z[:, None] * r2[None, :])   # (np, P)
-        ao_p = pref * S[None, :]
-        g = ao_p[..., None] * (-2.0 * Z[:, None, None] * d[None]) + pref[..., None] * gS[None]
-        gSd = np.sum(gS * d, axis=-1)
-        lp = ao_p * (4.0 * Z[:, None] ** 2 * r2[None, :] - 6.0 * Z[:, None]) - 4.0 * Z[:, None] * pref * gSd[None, :]
-        val[a] = ao_p.sum(0)
-        grad[a] = g.sum(0)
-        lap[a] = lp.sum(0)
-    return val, grad[..., 0], grad[..., 1], grad[..., 2], lap
+    d, r2, pref, S, gS = _common(tab, r, True)
+    Z = tab.Z[None]                                                  # (1, A, K)
+    ao_p = pref * S[..., None]                                       # (P, A, K)
+    g = (ao_p[..., None] * (-2.0 * Z[..., None] * d[:, :, None, :]) + pref[..., None] * gS[:, :, None, :]).sum(2)
+    gSd = np.sum(gS * d, axis=-1)                                    # (P, A)
+    lap = (ao_p * (4.0 * Z**2 * r2[..., None] - 6.0 * Z) - 4.0 * Z * pref * gSd[..., None]).sum(-1)
+    val = ao_p.sum(-1)
+    return val.T, g[..., 0].T, g[..., 1].T, g[..., 2].T, lap.T
