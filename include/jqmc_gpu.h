@@ -150,6 +150,12 @@ int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_c
 int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jqmc_walkers* dst,
                        const int32_t* d_chosen, void* stream);
 
+/* Measurement helper (no reference counterpart): launches a kernel of
+ * 8 independent FP64 FMA chains per thread (blocks x 256 threads, iters
+ * iterations) and returns in *flops the FP64 operations it performs, so that a
+ * caller timing it obtains the device's FP64 FMA throughput. */
+int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1431,6 +1431,19 @@ __global__ void k_gather_int(const int* __restrict__ src, int* __restrict__ dst,
   if (t < W) dst[t] = src[chosen[t]];
 }
 
+// FP64 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void k_probe_fp64(long long iters, double* out) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double m = 0.999999999, c = 1e-12;
+  for (long long i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.0) out[0] = s;  // keeps the chains live
+}
+
 // ------------------------------------------------------------------ host side
 inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
 
@@ -1716,6 +1729,14 @@ int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jq
   k_gather<<<grid, bs, 0, S(stream)>>>(src->Tdn, dst->Tdn, n * A, d_chosen, W);
   if (A3) k_gather<<<grid, bs, 0, S(stream)>>>(src->h3, dst->h3, N * A3, d_chosen, W);
   k_gather_int<<<(W + 255) / 256, 256, 0, S(stream)>>>(src->status, dst->status, d_chosen, W);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops, void* stream) {
+  if (iters <= 0 || blocks <= 0 || !d_sink || !flops) return JQMC_E_ARG;
+  const int bs = 256;
+  k_probe_fp64<<<blocks, bs, 0, S(stream)>>>(iters, d_sink);
+  *flops = 2.0 * 8.0 * (double)iters * (double)blocks * bs;
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 

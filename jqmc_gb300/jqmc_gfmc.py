@@ -1,0 +1,118 @@
+"""LRDMC driver with fixed projection count (GFMC_n), on one GPU.
+
+Mirrors ``GFMC_n`` of jqmc/jqmc_gfmc.py:4191-6990: the constructor arguments,
+``run(num_mcmc_steps)``, the stored per-branching observables and ``get_E``.
+One "MCMC step" is one branching cycle: ``num_mcmc_per_measurement``
+projections of every walker (one fused ``jqmc_lrdmc_project`` launch), the
+local energy at the final positions (``jqmc_lrdmc_energy``), the weighted
+averages, and the comb reconfiguration (``jqmc_branch_comb`` +
+``jqmc_walker_gather``) with the walker state rebuilt from the positions
+(``jqmc_walker_init``), as the reference recomputes G^-1 after branching.
+
+Random numbers: per projection the three Euler angles U(-2pi, 2pi) and the move
+uniform; per branching one comb offset zeta.  They are drawn on the device from
+a seeded torch generator (or passed explicitly to ``run_block``).  The JAX
+threefry stream of the reference is not reproduced.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from .engine import GpuSystem, WalkerSet, branch_comb
+from .hamiltonians import Hamiltonian_data
+from .statistics import gfmc_G_L, jackknife_energy
+from ._init_config import initial_electrons
+
+
+class GFMC_n:
+    def __init__(self, hamiltonian_data: Hamiltonian_data = None, num_walkers: int = 40, num_mcmc_per_measurement: int = 16,
+                 mcmc_seed: int = 34467, E_scf: float = 0.0, alat: float = 0.1, random_discretized_mesh: bool = True,
+                 non_local_move: str = "tmove", num_gfmc_collect_steps: int = 5, Nv: int = 6,
+                 init_r_up=None, init_r_dn=None, rebuild_after_branching: bool = True):
+        if non_local_move != "tmove":
+            raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+        hamiltonian_data.sanity_check()
+        self.hamiltonian_data = hamiltonian_data
+        self.num_walkers = num_walkers
+        self.num_mcmc_per_measurement = num_mcmc_per_measurement
+        self.E_scf = E_scf
+        self.alat = alat
+        self.random_discretized_mesh = random_discretized_mesh
+        self.num_gfmc_collect_steps = num_gfmc_collect_steps
+        self.rebuild_after_branching = rebuild_after_branching
+        self.sys = GpuSystem(hamiltonian_data, Nv=Nv)
+        if init_r_up is None:
+            st = hamiltonian_data.structure_data
+            coul = hamiltonian_data.coulomb_potential_data
+            init_r_up, init_r_dn = initial_electrons(st.positions, coul.effective_charges, self.sys.n_up, self.sys.n_dn,
+                                                     num_walkers, mcmc_seed)
+        self.walkers = WalkerSet(self.sys, init_r_up, init_r_dn)
+        self._spare = WalkerSet.empty_like(self.walkers)
+        dev = self.sys.device
+        self.gen = torch.Generator(device=dev)
+        self.gen.manual_seed(mcmc_seed)
+        self._np_rng = np.random.default_rng(mcmc_seed)
+        self._chosen = torch.empty(num_walkers, dtype=torch.int32, device=dev)
+        self._cum = torch.empty(num_walkers, dtype=torch.float64, device=dev)
+        self._e_L, self._e_L2, self._w_L = [], [], []
+        self.mcmc_counter = 0
+
+    # ------------------------------------------------------------------ draws
+    def draws(self, K: int | None = None) -> torch.Tensor:
+        K = self.num_mcmc_per_measurement if K is None else K
+        d = torch.rand((self.num_walkers, K, 4), generator=self.gen, dtype=torch.float64, device=self.sys.device)
+        if self.random_discretized_mesh:
+            d[..., :3].mul_(4.0 * math.pi).sub_(2.0 * math.pi)
+        else:
+            d[..., :3].zero_()
+        return d
+
+    # ------------------------------------------------------------------ one branching cycle
+    def run_block(self, draws: torch.Tensor, zeta: float):
+        """Projection block + energy + reconfiguration.  Returns device scalars
+        (w_sum, sum w/(Vd-E), sum w e/(Vd-E), sum w e^2/(Vd-E)) before branching."""
+        ws = self.walkers
+        w = torch.ones(self.num_walkers, dtype=torch.float64, device=self.sys.device)
+        ws.lrdmc_project(draws, self.alat, self.E_scf, w)
+        last = draws[:, -1].contiguous()
+        eL, vd = ws.lrdmc_energy(last, self.alat)
+        f = w / (vd - self.E_scf)
+        sums = torch.stack([w.sum(), f.sum(), (f * eL).sum(), (f * eL * eL).sum()])
+        branch_comb(w, zeta, self._chosen, self._cum)
+        self._spare.gather_from(ws, self._chosen)
+        self.walkers, self._spare = self._spare, self.walkers
+        if self.rebuild_after_branching:
+            self.walkers.init()
+        return sums
+
+    def run(self, num_mcmc_steps: int = 50, max_time: int = 86400) -> None:
+        for _ in range(num_mcmc_steps):
+            zeta = float(self._np_rng.random())
+            sums = self.run_block(self.draws(), zeta).cpu().numpy()
+            w_avg = sums[0] / self.num_walkers
+            self._w_L.append(w_avg)
+            self._e_L.append(sums[2] / sums[1])
+            self._e_L2.append(sums[3] / sums[1])
+            self.mcmc_counter += 1
+
+    # ------------------------------------------------------------------ observables
+    @property
+    def w_L(self) -> np.ndarray:
+        """G_L weight products over the collect window (jqmc_gfmc.py:136-152)."""
+        return gfmc_G_L(np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1), self.num_gfmc_collect_steps)
+
+    @property
+    def e_L(self) -> np.ndarray:
+        return np.asarray(self._e_L, dtype=np.float64).reshape(-1, 1)[self.num_gfmc_collect_steps:]
+
+    @property
+    def e_L2(self) -> np.ndarray:
+        return np.asarray(self._e_L2, dtype=np.float64).reshape(-1, 1)[self.num_gfmc_collect_steps:]
+
+    def get_E(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
+        e, e2, w = self.e_L[num_mcmc_warmup_steps:], self.e_L2[num_mcmc_warmup_steps:], self.w_L[num_mcmc_warmup_steps:]
+        return jackknife_energy(e, e2, w, num_mcmc_bin_blocks)

@@ -30,6 +30,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
+from ._init_config import initial_electrons
 from .atomic_orbital import AOs_sphe_data
 from .coulomb_potential import Coulomb_potential_data
 from .determinant import Geminal_data
@@ -124,22 +125,8 @@ class SyntheticSystem:
     def initial_electrons(self, num_walkers: int, seed: int = 0):
         """(W, n_up, 3), (W, n_dn, 3): electrons assigned to nuclei by valence count,
         alternating spins, displaced by N(0, 1 bohr)."""
-        rng = np.random.default_rng(seed)
-        pos = self.hamiltonian.structure_data.positions
-        owners = []
-        for atom, v in enumerate(self.valence):
-            owners += [atom] * int(round(v))
-        total = self.n_up + self.n_dn
-        while len(owners) < total:           # charged systems: extra electrons round-robin
-            owners.append(len(owners) % len(pos))
-        up_owner, dn_owner = [], []
-        for k, atom in enumerate(owners[:total]):
-            want_up = (k % 2 == 0 and len(up_owner) < self.n_up) or len(dn_owner) >= self.n_dn
-            (up_owner if want_up else dn_owner).append(atom)
-        up_owner, dn_owner = np.array(up_owner, dtype=int), np.array(dn_owner, dtype=int)
-        r_up = pos[up_owner][None] + rng.normal(size=(num_walkers, self.n_up, 3))
-        r_dn = pos[dn_owner][None] + rng.normal(size=(num_walkers, self.n_dn, 3))
-        return r_up, r_dn
+        return initial_electrons(self.hamiltonian.structure_data.positions, self.valence, self.n_up, self.n_dn,
+                                 num_walkers, seed)
 
 
 def _assemble(name, positions, atomic_numbers, z_cores, kinds, n_up, n_dn, det_recipe, j3_recipe, rng,
