@@ -150,6 +150,21 @@ int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_c
 int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jqmc_walkers* dst,
                        const int32_t* d_chosen, void* stream);
 
+/* Allocation-free form of jqmc_branch_comb.  It has no counterpart in the
+ * reference.  It is for callers that cannot allocate device memory -- for
+ * example a host code whose own pool has reserved the GPU's memory, or a
+ * driver loop that must not wait on an allocation -- so they need not find a
+ * scratch buffer: the cumulative weights go to a fixed device array of
+ * JQMC_NOALLOC_MAX_WALKERS doubles (2 MiB) that the library holds on every GPU
+ * that loads it until the process exits.  nwalk above that limit returns
+ * JQMC_E_LIMIT; no cudaMalloc/cudaFree is called.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one array, so calls that overlap on the GPU (other streams, other host
+ * threads) race: serialise them. */
+#define JQMC_NOALLOC_MAX_WALKERS 262144
+int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, void* stream);
+
 /* Measurement helper (no reference counterpart): launches a kernel of
  * 8 independent FP64 FMA chains per thread (blocks x 256 threads, iters
  * iterations) and returns in *flops the FP64 operations it performs, so that a

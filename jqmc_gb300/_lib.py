@@ -74,9 +74,10 @@ def lib():
         L.jqmc_branch_comb.argtypes = [i32, vp, f64, vp, vp, vp]
         L.jqmc_walker_gather.argtypes = [vp, C.POINTER(Walkers), C.POINTER(Walkers), vp, vp]
         L.jqmc_probe_fp64.argtypes = [i64, i32, vp, pf64, vp]
+        L.jqmc_branch_comb_noalloc.argtypes = [i32, vp, f64, vp, vp]
         for name in ("jqmc_probe_fp64", "jqmc_system_create", "jqmc_system_destroy", "jqmc_ao_vgl", "jqmc_walker_init", "jqmc_log_psi",
                      "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
-                     "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64"):
+                     "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -89,4 +90,4 @@ def check(rc: int, what: str) -> None:
 
 EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "jqmc_ao_vgl", "jqmc_walker_init",
             "jqmc_log_psi", "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
-            "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64")
+            "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc")

@@ -28,6 +28,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "jqmc_gpu.h"
@@ -1737,6 +1738,43 @@ int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops
   const int bs = 256;
   k_probe_fp64<<<blocks, bs, 0, S(stream)>>>(iters, d_sink);
   *flops = 2.0 * 8.0 * (double)iters * (double)blocks * bs;
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free branching.  Some callers cannot allocate device memory: a host
+// code whose memory pool reserved the whole GPU at start-up (cudaMalloc would
+// fail or break its accounting), or a driver loop that must not stall on the
+// device synchronisation cudaMalloc may imply.  For them the comb's
+// cumulative-weight scratch lives in this fixed device array instead of a
+// caller buffer.  Every GPU that loads the library holds the array until the
+// process exits.
+static __device__ __align__(256) double g_branch_scratch[JQMC_NOALLOC_MAX_WALKERS];
+
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[64] = {nullptr};
+
+int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, void* stream) {
+  if (nwalk <= 0 || !d_w || !d_chosen || !(zeta >= 0.0 && zeta < 1.0)) return JQMC_E_ARG;
+  if (nwalk > JQMC_NOALLOC_MAX_WALKERS) return JQMC_E_LIMIT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return JQMC_E_CUDA;
+  double* scratch = nullptr;
+  {
+    // one-time set-up per device, with that device current: the host-side
+    // symbol is only a stand-in, so the kernels get the device address
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_branch_scratch) != cudaSuccess || !p) return JQMC_E_CUDA;
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  // every scratch entry the search reads is written by the cumsum first, so
+  // nothing needs clearing between calls
+  k_branch_comb<<<1, 1, 0, S(stream)>>>(nwalk, d_w, scratch);
+  k_branch_search<<<(nwalk + 127) / 128, 128, 0, S(stream)>>>(nwalk, scratch, zeta, d_chosen);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
