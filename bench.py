@@ -227,11 +227,8 @@ def gpu_arm(a):
         dist.barrier()
     clocks = clk.stop() if clk else None
     drv.walkers.__class__.lrdmc_project = orig_project
-    ms = t0.elapsed_time(t1)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt)
+    from jqmc_gb300.replicas import max_over_ranks
+    ms = max_over_ranks(t0.elapsed_time(t1), device=dev)
     walker_steps = W * K * a.steps * world
     value = walker_steps / (ms / 1e3)
     proj_ms = [e0.elapsed_time(e1) for e0, e1 in proj_events]
@@ -251,11 +248,7 @@ def gpu_arm(a):
         dev_buf.copy_(host_draws[s], non_blocking=True)
         out = drv.run_block(dev_buf, zetas[s]).cpu()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - te0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt)
+    e2e_s = max_over_ranks(time.perf_counter() - te0, device=dev)
     e2e = {"value": W * K * a.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(out.numel() * 8)}
 
@@ -267,9 +260,8 @@ def gpu_arm(a):
     ecp_frac = float((maxl1[near] > 0).double().mean())
     flops_launch = lrdmc_step_flops(gs, ecp_frac) * W * K
     achieved = flops_launch / (proj_avg / 1e3) / 1e9
-    sink = torch.zeros(1, dtype=torch.float64, device=dev)
-    fl = _lib.C.c_double() if hasattr(_lib, "C") else None
     import ctypes
+    sink = torch.zeros(1, dtype=torch.float64, device=dev)
     fl = ctypes.c_double()
     pe0 = torch.cuda.Event(enable_timing=True)
     pe1 = torch.cuda.Event(enable_timing=True)

@@ -1,0 +1,155 @@
+"""CPU-only checks: the C ABI library and its exports, table packing, oracle
+self-consistency, statistics, and the replica reduction across gloo ranks."""
+
+import os
+import re
+import socket
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            names += re.findall(r"^\s*(?:int|int64_t)\s+(jqmc_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    from jqmc_gb300 import _lib
+    from jqmc_gb300.build import build
+    build()
+    import ctypes
+    L = ctypes.CDLL(_lib.LIB_PATH)
+    declared = _declared_symbols()
+    assert len(declared) >= 14
+    missing = [n for n in declared if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(_lib.EXPORTED) == set(declared)
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12", "chain32"])
+def test_pack_basis_covers_every_ao(name):
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.engine import pack_basis
+    from oracle.ao import primitive_norm
+    syn = synthetic.SYSTEMS[name]()
+    g = syn.hamiltonian.wavefunction_data.geminal_data
+    aos, _, _ = g.ao_basis_lambda()
+    for basis in (aos, syn.hamiltonian.wavefunction_data.jastrow_data.jastrow_three_body_data.orb_data):
+        shells, prims = pack_basis(basis)
+        covered = np.zeros(basis.num_ao, dtype=int)
+        for atom, l, npr, p0, ao0, nm, mf, _ in shells:
+            covered[ao0:ao0 + nm] += 1
+            for k in range(nm):
+                assert basis.angular_momentums[ao0 + k] == l and basis.magnetic_quantum_numbers[ao0 + k] == mf + k
+                assert basis.nucleus_index[ao0 + k] == atom
+            z, c = basis.primitives_of(ao0)
+            assert np.allclose(prims[p0:p0 + npr, 0], z)
+            assert np.allclose(prims[p0:p0 + npr, 1], c * primitive_norm(l, z), rtol=1e-14)
+        assert np.all(covered == 1)
+
+
+def test_synthetic_workload_sizes():
+    from jqmc_gb300 import synthetic
+    w, r, c = synthetic.water_like(), synthetic.ring12(), synthetic.chain32()
+    assert (w.n_up, w.n_dn) == (4, 4) and (r.n_up, r.n_dn) == (15, 15) and (c.n_up, c.n_dn) == (48, 48)
+    aw = w.hamiltonian.wavefunction_data.geminal_data.ao_basis_lambda()[0].num_ao
+    ar = r.hamiltonian.wavefunction_data.geminal_data.ao_basis_lambda()[0].num_ao
+    ac = c.hamiltonian.wavefunction_data.geminal_data.ao_basis_lambda()[0].num_ao
+    assert 35 <= aw <= 45 and 180 <= ar <= 220 and 650 <= ac <= 760
+    assert r.hamiltonian.wavefunction_data.jastrow_data.jastrow_three_body_data.orb_num == 60
+
+
+def test_oracle_sherman_morrison_stays_consistent():
+    from jqmc_gb300 import synthetic
+    from oracle import drivers as D
+    from oracle.wf import OracleSystem
+    syn = synthetic.water_like()
+    o = OracleSystem(syn.hamiltonian)
+    ru, rd = syn.initial_electrons(1, seed=4)
+    st = D.init_state(o, ru[0], rd[0])
+    rng = np.random.default_rng(1)
+    K = 60
+    idr = np.stack([rng.integers(0, 8, K), rng.integers(0, 4, K), rng.integers(0, 4, K), rng.integers(0, 3, K)], 1)
+    fdr = np.stack([rng.normal(size=K), rng.uniform(size=K)], 1)
+    acc = D.vmc_block(o, st, idr, fdr, 0.4, 0.0)
+    assert 0 < acc <= K
+    G = o.geminal(st.r_up, st.r_dn)
+    assert np.max(np.abs(st.G - G)) < 1e-10 * np.max(np.abs(G))
+    assert np.max(np.abs(st.Ginv - np.linalg.inv(G))) < 1e-8 * np.max(np.abs(st.Ginv))
+
+
+def test_oracle_branch_comb_semantics():
+    from oracle.drivers import branch_comb
+    w = np.array([1.0, 0.0, 3.0, 0.5])
+    idx = branch_comb(w, 0.2)
+    cum = np.cumsum(w / w.sum())
+    z = (np.arange(4) + 0.2) / 4
+    assert np.array_equal(idx, np.searchsorted(cum, z))
+    assert 1 not in idx   # zero-weight walkers are never chosen
+
+
+def test_jackknife_constant_energy():
+    from jqmc_gb300.statistics import gfmc_G_L, jackknife_energy
+    e = np.full((20, 3), -1.5)
+    w = np.ones((20, 3))
+    E, Es, V, Vs = jackknife_energy(e, e**2, w, 5)
+    assert abs(E + 1.5) < 1e-14 and Es < 1e-12 and abs(V) < 1e-12
+    g = gfmc_G_L(np.arange(1.0, 7.0).reshape(-1, 1), 2)
+    assert np.allclose(g[:, 0], [1 * 2, 2 * 3, 3 * 4, 4 * 5])
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _replica_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+    from jqmc_gb300 import replicas
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    t = replicas.max_over_ranks(10.0 + rank)
+    sums = torch.tensor([2.0 * (rank + 1), 1.0 + rank, -3.0 * (1.0 + rank), 9.0 * (1.0 + rank)], dtype=torch.float64)
+    w_avg, e, e2 = replicas.lrdmc_observables(sums, num_walkers_per_rank=2)
+    out.put((rank, t, w_avg, e, e2))
+    dist.destroy_process_group()
+
+
+def test_replica_reduction_gloo_world2():
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_replica_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, t, w_avg, e, e2 in res:
+        assert t == 11.0
+        assert abs(w_avg - (2.0 + 4.0) / 4) < 1e-15
+        assert abs(e - (-3.0 - 6.0) / (1.0 + 2.0)) < 1e-15
+        assert abs(e2 - (9.0 + 18.0) / 3.0) < 1e-15
+
+
+def test_engine_refuses_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300._lib import JqmcError
+    from jqmc_gb300.engine import GpuSystem
+    with pytest.raises(JqmcError):
+        GpuSystem(synthetic.water_like().hamiltonian)
