@@ -1,4 +1,4 @@
-"""Walker-path benchmark on GB300: LRDMC (GFMC_n) projections, FP64.
+"""Walker-path benchmark on GB300: LRDMC (GFMC_n) projections, mixed precision vs plain FP64.
 
 Workload (default): the 12-nucleus synthetic ring -- 6 C-like nuclei (Z_eff 4,
 semilocal ECP with l = 0, 1 non-local channels) at 2.64 bohr and 6 H at 4.69
@@ -9,8 +9,11 @@ cycle: 40 projections of every walker, the local energy, the weighted sums,
 the comb reconfiguration and the rebuild of G^-1 / T tables from positions.
 walker-steps per bench step = walkers x 40.
 
-value : walker-steps/s with the draws resident in HBM (kernel throughput).
-e2e   : the same through the public driver API (jqmc_gb300.jqmc_gfmc.GFMC_n.run_block)
+value : walker-steps/s of the mixed-precision form with the draws resident in
+        HBM; the plain FP64 form runs the same draws and is reported beside it
+        (plain_fp64, speedup_vs_plain_fp64) with the accuracy of the mixed form
+        against it (per-configuration e_L rms, difference of mean energies).
+e2e   : the mixed form through the public driver API (jqmc_gb300.jqmc_gfmc.GFMC_n.run_block)
         with the draws copied from pinned host memory each step and the step's
         sums read back to the host.
 Walker state is 8192 x 64 KB = 0.5 GB > L2 (129 MB), so no L2 flush is needed.
@@ -153,7 +156,68 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def _probe(L, fn, dev, stream, dtype):
+    import ctypes
+
+    import torch
+    sink = torch.zeros(1, dtype=dtype, device=dev)
+    fl = ctypes.c_double()
+    blocks = torch.cuda.get_device_properties(dev).multi_processor_count * 8
+    fn(2000, blocks, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn(20000, blocks, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return fl.value / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+def _time_form(drv, draws, zetas, warmup, steps, stream, world, dev):
+    """Warm up, then time `steps` branching cycles with device-resident draws.
+    Returns (ms, per-step sums (steps, 4), list of project-launch ms)."""
+    import torch
+    import torch.distributed as dist
+
+    from jqmc_gb300.replicas import max_over_ranks
+    cls = drv.walkers.__class__
+    orig = cls.lrdmc_project
+    events = []
+
+    def timed_project(self, d, alat, E_scf, w):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        orig(self, d, alat, E_scf, w)
+        e1.record(stream)
+        events.append((e0, e1))
+
+    for s in range(warmup):
+        drv.run_block(draws[s], zetas[s])
+    torch.cuda.synchronize()
+    cls.lrdmc_project = timed_project
+    try:
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        sums = [drv.run_block(draws[s], zetas[s]) for s in range(warmup, warmup + steps)]
+        t1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    finally:
+        cls.lrdmc_project = orig
+    ms = max_over_ranks(t0.elapsed_time(t1), device=dev)
+    return ms, torch.stack(sums).cpu().numpy(), [a.elapsed_time(b) for a, b in events]
+
+
 def gpu_arm(a):
+    import ctypes
+
     import torch
     import torch.distributed as dist
 
@@ -171,75 +235,61 @@ def gpu_arm(a):
     if world > 1:
         dist.init_process_group("nccl")
     from jqmc_gb300 import _lib, synthetic
+    from jqmc_gb300.engine import WalkerSet
     from jqmc_gb300.jqmc_gfmc import GFMC_n
-    from jqmc_gb300.workload import EXP_FLOPS, lrdmc_step_bytes, lrdmc_step_flops
+    from jqmc_gb300.replicas import max_over_ranks
+    from jqmc_gb300.workload import EXP_FLOPS, lrdmc_step_bytes, lrdmc_step_flops, lrdmc_step_split
 
     syn = synthetic.SYSTEMS[a.workload]()
     W, K = a.walkers, a.nproj
     r_up, r_dn = syn.initial_electrons(W, seed=1234 + rank)
-    drv = GFMC_n(syn.hamiltonian, num_walkers=W, num_mcmc_per_measurement=K, mcmc_seed=7 + rank, alat=a.alat,
-                 init_r_up=r_up, init_r_dn=r_dn)
-    gs = drv.sys
-    dev = gs.device
     stream = torch.cuda.current_stream()
-    launches = {"n": 0}
-
-    # count our kernel launches: wrap the ctypes entry points used inside a block
     L = _lib.lib()
-    per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 7 if gs.A3 else 6,
-                "jqmc_walker_init": 1}
-    # dominant-kernel timing with events on the launching (current) stream
-    proj_events = []
-    orig_project = drv.walkers.__class__.lrdmc_project
+    total = a.warmup + a.steps
+    forms = {}
+    draws_keep = None
+    for form in ("fp64", "mixed"):
+        drv = GFMC_n(syn.hamiltonian, num_walkers=W, num_mcmc_per_measurement=K, mcmc_seed=7 + rank, alat=a.alat,
+                     init_r_up=r_up, init_r_dn=r_dn, precision=form)
+        dev = drv.sys.device
+        if draws_keep is None:
+            draws_keep = [drv.draws() for _ in range(total)]
+            zetas = [float(x) for x in np.random.default_rng(99 + rank).random(total)]
+        clk = ClockSampler(torch.cuda.current_device()) if (rank == 0 and form == "mixed") else None
+        if clk:
+            time.sleep(0.4)
+        ms, sums, proj = _time_form(drv, draws_keep, zetas, a.warmup, a.steps, stream, world, dev)
+        clocks = clk.stop() if clk else None
+        forms[form] = {"drv": drv, "ms": ms, "sums": sums, "proj": proj, "clocks": clocks,
+                       "value": W * K * a.steps * world / (ms / 1e3)}
+        if form == "fp64":
+            # free the plain form's state before the mixed form allocates its own
+            del drv
+            forms["fp64"].pop("drv")
+            torch.cuda.empty_cache()
+    mixed, plain = forms["mixed"], forms["fp64"]
+    gs = mixed["drv"].sys
+    dev = gs.device
 
-    def timed_project(self, draws, alat, E_scf, w):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        orig_project(self, draws, alat, E_scf, w)
-        e1.record(stream)
-        proj_events.append((e0, e1))
+    # accuracy of the mixed form against the FP64 form
+    e_plain = plain["sums"][:, 2] / plain["sums"][:, 1]
+    e_mixed = mixed["sums"][:, 2] / mixed["sums"][:, 1]
+    ws_m = mixed["drv"].walkers
+    n_cmp = min(W, 2048)
+    r = ws_m.r[:n_cmp].cpu().numpy()
+    ref = WalkerSet(gs, r[:, : gs.n_up], r[:, gs.n_up:], precision="fp64")
+    mix = WalkerSet(gs, r[:, : gs.n_up], r[:, gs.n_up:], precision="mixed")
+    last = draws_keep[-1][:n_cmp, -1].contiguous()
+    e64, _ = ref.lrdmc_energy(last, a.alat)
+    e32, _ = mix.lrdmc_energy(last, a.alat)
+    de = (e32 - e64).cpu().numpy()
+    eL_rms = float(np.sqrt(np.mean(de**2)))
+    del ref, mix
 
-    total_steps = a.warmup + a.steps
-    draws = [drv.draws() for _ in range(total_steps)]
-    zetas = [float(x) for x in np.random.default_rng(99 + rank).random(total_steps)]
-    for s in range(a.warmup):
-        drv.run_block(draws[s], zetas[s])
-    torch.cuda.synchronize()
-
-    # ---- timed region: device-resident inputs
-    drv.walkers.__class__.lrdmc_project = timed_project
-    clk = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
-    time.sleep(0.4 if clk else 0.0)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    sums = []
-    for s in range(a.warmup, total_steps):
-        sums.append(drv.run_block(draws[s], zetas[s]))
-        launches["n"] += sum(per_call.values())
-    t1.record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    clocks = clk.stop() if clk else None
-    drv.walkers.__class__.lrdmc_project = orig_project
-    from jqmc_gb300.replicas import max_over_ranks
-    ms = max_over_ranks(t0.elapsed_time(t1), device=dev)
-    walker_steps = W * K * a.steps * world
-    value = walker_steps / (ms / 1e3)
-    proj_ms = [e0.elapsed_time(e1) for e0, e1 in proj_events]
-    proj_avg = sum(proj_ms) / len(proj_ms)
-    energies = torch.stack(sums).cpu().numpy()
-    e_mean = float(np.mean(energies[:, 2] / energies[:, 1]))
-
-    # ---- e2e: public driver API, draws from pinned host memory, sums back to host
-    host_draws = [d.cpu().pin_memory() for d in draws[: a.steps]]
-    dev_buf = torch.empty_like(draws[0])
-    h2d = host_draws[0].numel() * 8
+    # e2e through the public driver API (mixed form): draws from pinned host memory, sums to host
+    drv = mixed["drv"]
+    host_draws = [d.cpu().pin_memory() for d in draws_keep[: a.steps]]
+    dev_buf = torch.empty_like(draws_keep[0])
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -249,68 +299,78 @@ def gpu_arm(a):
         out = drv.run_block(dev_buf, zetas[s]).cpu()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - te0, device=dev)
-    e2e = {"value": W * K * a.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    e2e = {"value": W * K * a.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(host_draws[0].numel() * 8),
            "d2h_bytes_per_step": int(out.numel() * 8)}
 
-    # ---- roofline of the dominant kernel (jqmc_lrdmc_project): FP64 pipe
-    r_all = drv.walkers.r.reshape(W, -1, 3)
+    # roofline: the mixed projection kernel (FP32 part against a measured FP32 FMA peak, FP64 part
+    # against the measured FP64 peak) and the plain kernel (FP64)
+    r_all = ws_m.r.reshape(W, -1, 3)
     pos = torch.as_tensor(gs._keep["pos"], device=dev)
     near = torch.cdist(r_all, pos[None].expand(W, -1, -1)).argmin(-1)
     maxl1 = torch.as_tensor(gs._keep.get("maxl1", np.zeros(len(gs._keep["pos"]), dtype=np.int32)), device=dev)
     ecp_frac = float((maxl1[near] > 0).double().mean())
-    flops_launch = lrdmc_step_flops(gs, ecp_frac) * W * K
-    achieved = flops_launch / (proj_avg / 1e3) / 1e9
-    import ctypes
-    sink = torch.zeros(1, dtype=torch.float64, device=dev)
-    fl = ctypes.c_double()
-    pe0 = torch.cuda.Event(enable_timing=True)
-    pe1 = torch.cuda.Event(enable_timing=True)
-    blocks = torch.cuda.get_device_properties(dev).multi_processor_count * 8
-    L.jqmc_probe_fp64(2000, blocks, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(fl), ctypes.c_void_p(stream.cuda_stream))
-    torch.cuda.synchronize()
-    pe0.record(stream)
-    _lib.check(L.jqmc_probe_fp64(20000, blocks, ctypes.c_void_p(sink.data_ptr()), ctypes.byref(fl),
-                                 ctypes.c_void_p(stream.cuda_stream)), "probe")
-    pe1.record(stream)
-    torch.cuda.synchronize()
-    peak = fl.value / (pe0.elapsed_time(pe1) / 1e3) / 1e9
+    peak64 = _probe(L, L.jqmc_probe_fp64, dev, stream, torch.float64)
+    peak32 = _probe(L, L.jqmc_probe_fp32, dev, stream, torch.float32)
+    f32, f64 = lrdmc_step_split(gs, ecp_frac)
+    mix_ms = sum(mixed["proj"]) / len(mixed["proj"])
+    plain_ms = sum(plain["proj"]) / len(plain["proj"])
+    ach32 = f32 * W * K / (mix_ms / 1e3) / 1e9
+    ach64 = f64 * W * K / (mix_ms / 1e3) / 1e9
+    plain_flops = lrdmc_step_flops(gs, ecp_frac) * W * K
+    plain_ach = plain_flops / (plain_ms / 1e3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "lrdmc_project_traffic.json")
     if os.path.exists(prof):
         try:
             with open(prof) as f:
-                traffic = json.load(f).get(a.workload)
+                traffic = json.load(f).get(f"{a.workload}_mixed")
         except (OSError, ValueError):
             traffic = None
-    bytes_launch = lrdmc_step_bytes(gs) * W * K
-    if rank == 0:
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
         peaks = {}
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                peaks = json.load(f)
-        except (OSError, ValueError):
-            peaks = {}
+    bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
+    per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 7 if gs.A3 else 6,
+                "jqmc_walker_init": 1}
+    if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": mixed["ms"] / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": f"lrdmc_{a.workload}", "form": "plain FP64", "walkers": W, "projections_per_branching": K,
-                       "alat": a.alat, "electrons": gs.N, "aos": gs.A, "j3_aos": gs.A3, "nuclei": len(gs._keep["pos"]),
+            "config": {"workload": f"lrdmc_{a.workload}", "form": "mixed precision (headline) vs plain FP64", "walkers": W,
+                       "projections_per_branching": K, "alat": a.alat, "electrons": gs.N, "aos": gs.A, "j3_aos": gs.A3,
+                       "nuclei": len(gs._keep["pos"]),
                        "parallelism": "walkers (one CTA per walker)" + ("; replicas" if world > 1 else ""),
-                       "l2": f"walker state {gs.walker_bytes() * W / 2**20:.0f} MiB > L2, no flush"},
+                       "l2": f"walker state {gs.walker_bytes('mixed') * W / 2**20:.0f} MiB (mixed) / "
+                             f"{gs.walker_bytes('fp64') * W / 2**20:.0f} MiB (fp64) > L2, no flush"},
+            "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms"] / a.steps, "dtype": "f64"},
+            "speedup_vs_plain_fp64": mixed["value"] / plain["value"],
+            "accuracy": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": n_cmp,
+                         "dE_mean_Ha": float(np.mean(de)), "dE_mean_stderr_Ha": float(np.std(de) / np.sqrt(len(de))),
+                         "note": "mixed minus FP64 local energy on the same sampled configurations and rotation; "
+                                 "dE_mean is the bias the mixed form adds to <E>",
+                         "bar": "|dE_L| <= 1e-5 Ha rms per configuration; |d<E>| <= 1e-4 Ha",
+                         "timed_runs_E_Ha": {"mixed": float(np.mean(e_mixed)), "fp64": float(np.mean(e_plain)),
+                                             "note": "branching-cycle averages of the two timed runs (few cycles, not converged)"}},
             "e2e": e2e,
-            "gpu_launches": launches["n"],
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "GFLOP/s", "frac": achieved / peak,
-                         "traffic": traffic, "kernel": "k_lrdmc (jqmc_lrdmc_project)",
-                         "flop_convention": f"FMA=2, add/mul/div/sqrt=1, FP64 exp={EXP_FLOPS:g}; per launch {flops_launch:.3e} FP64 ops",
-                         "peak_source": "measured in this run by jqmc_probe_fp64 (8 independent DFMA chains per thread)",
-                         "avg_launch_ms": proj_avg, "ecp_electron_fraction": ecp_frac,
+            "gpu_launches": sum(per_call.values()) * a.steps,
+            "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,
+                         "traffic": traffic, "kernel": "k_lrdmc<float,float,double> (jqmc_lrdmc_project, mixed)",
+                         "flop_convention": f"FMA=2, add/mul/div/sqrt=1, exp={EXP_FLOPS:g}",
+                         "peak_source": "measured in this run by jqmc_probe_fp32 (8 independent FMA chains per thread)",
+                         "avg_launch_ms": mix_ms, "ecp_electron_fraction": ecp_frac,
+                         "fp64_part": {"achieved": ach64, "peak": peak64, "frac": ach64 / peak64,
+                                       "peak_source": "jqmc_probe_fp64, this run"},
                          "hbm": {"algorithmic_bytes_per_launch": bytes_launch,
-                                 "achieved_gbs": bytes_launch / (proj_avg / 1e3) / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
-                                 "peak_source": "MEASURED_PEAKS.json"}},
+                                 "achieved_gbs": bytes_launch / (mix_ms / 1e3) / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
+                                 "peak_source": "MEASURED_PEAKS.json"},
+                         "plain_fp64_kernel": {"bound": "fp64", "achieved": plain_ach, "peak": peak64, "frac": plain_ach / peak64,
+                                               "avg_launch_ms": plain_ms}},
             "cpu_baseline": cpu_base,
-            "clocks": clocks,
-            "E_mean_Ha": e_mean,
+            "clocks": mixed["clocks"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:

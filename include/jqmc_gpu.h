@@ -75,17 +75,31 @@ typedef struct {
   double ion_ion;                /* constant ion-ion Coulomb energy          */
 } jqmc_system_desc;
 
+/* Walker-table precision. */
+#define JQMC_PREC_FP64 0      /* every table and every operation in double       */
+#define JQMC_PREC_MIXED 1     /* G, G^-1, T_up, T_dn, h3 float; AO values, ratios  */
+                              /* and rank-1 updates float; AO gradients/Laplacians,*/
+                              /* energies, weights and the table rebuild double   */
+
 /* Per-walker state, all device arrays (N = n_up + n_dn, n = n_up, A = det.nao,
- * A3 = j3.nao).  Electron-major layouts: electron e's vectors are contiguous. */
+ * A3 = j3.nao).  Electron-major layouts: electron e's vectors are contiguous.
+ * Table element type: double for JQMC_PREC_FP64, float for JQMC_PREC_MIXED. */
 typedef struct {
   int32_t nwalk;
-  double* r;        /* nwalk*N*3, up electrons first                          */
-  double* G;        /* nwalk*n*n geminal matrix                               */
-  double* Ginv;     /* nwalk*n*n                                              */
-  double* Tup;      /* nwalk*n*A: row i = lambda Phi_dn G^-1 [:, i]           */
-  double* Tdn;      /* nwalk*n*A: row j = (G^-1 Phi_up^T lambda)[j, :]        */
-  double* h3;       /* nwalk*N*A3 J3 field: dJ3/dphi3(r_e) (unused if no J3)  */
-  int32_t* status;  /* nwalk JQMC_ST_* bits                                   */
+  int32_t precision;  /* JQMC_PREC_*                                             */
+  double* r;          /* nwalk*N*3, up electrons first (always double)           */
+  void* G;            /* nwalk*n*n geminal matrix                                */
+  void* Ginv;         /* nwalk*n*n                                               */
+  void* Tup;          /* nwalk*n*A: row i = lambda Phi_dn G^-1 [:, i]            */
+  void* Tdn;          /* nwalk*n*A: row j = (G^-1 Phi_up^T lambda)[j, :]         */
+  void* h3;           /* nwalk*N*A3 J3 field: dJ3/dphi3(r_e) (unused if no J3)   */
+  void* dphi;         /* nwalk*N*4*A: grad x, y, z and Laplacian of every geminal */
+                      /* AO at each electron (kept current by every move)       */
+  void* dphi3;        /* nwalk*N*5*A3: value, grad x, y, z, Laplacian of the J3  */
+                      /* AOs at each electron (unused if no J3)                  */
+  double* scratch;    /* JQMC_PREC_MIXED: nwalk*2*n*A doubles used by the FP64   */
+                      /* rebuild in jqmc_walker_init; unused for JQMC_PREC_FP64  */
+  int32_t* status;    /* nwalk JQMC_ST_* bits                                    */
 } jqmc_walkers;
 
 /* Copy the tables to the current device.  Replaces the per-call packing of
@@ -95,8 +109,9 @@ typedef struct {
 int jqmc_system_create(const jqmc_system_desc* desc, jqmc_system** out);
 int jqmc_system_destroy(jqmc_system* sys);
 
-/* Bytes of walker state per walker (sum over the jqmc_walkers arrays). */
-int64_t jqmc_walker_bytes(const jqmc_system* sys);
+/* Bytes of walker state per walker (sum over the jqmc_walkers arrays) for a
+ * JQMC_PREC_* precision. */
+int64_t jqmc_walker_bytes(const jqmc_system* sys, int32_t precision);
 
 /* AO values, gradients and Laplacians at npts points of basis 0 (geminal) or
  * 1 (J3).  d_out: 5*nao*npts = (val, gx, gy, gz, lap), AO-major.
@@ -111,26 +126,27 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
 int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream);
 
 /* ln|det G| and its sign per walker from G (LU, jqmc/determinant.py:1026-1111),
- * plus the Jastrow value J (jastrow_factor.py:2127-2178). */
+ * plus the Jastrow value J (jastrow_factor.py:2127-2178).  JQMC_PREC_FP64 only. */
 int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow, void* stream);
 
 /* K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523, fori_loop body),
  * explicit draws: d_idraw nwalk*K*4 int32 (sel in [0,N), up index, dn index,
  * axis), d_fdraw nwalk*K*2 double (standard normal, uniform).  Adds the number
- * of accepted moves to d_accept[w]. */
+ * of accepted moves to d_accept[w].  JQMC_PREC_FP64 only. */
 int jqmc_vmc_sweep(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const int32_t* d_idraw,
                    const double* d_fdraw, double Dt, double eps_AS, int32_t* d_accept, void* stream);
 
 /* Local energy and AS weight per walker (jqmc/hamiltonians.py:225-290 with the
  * non-local ECP on the rotated quadrature, coulomb_potential.py:1478-1712;
  * w_L = (R_AS / max(R_AS, eps))^2, jqmc_mcmc.py:743-747).  d_angles: nwalk*3
- * Euler angles; the rotation is R(angles) of jqmc_mcmc.py:4228-4245. */
+ * Euler angles; the rotation is R(angles) of jqmc_mcmc.py:4228-4245.
+ * JQMC_PREC_FP64 only. */
 int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double eps_AS,
                      double* d_eL, double* d_wL, void* stream);
 
 /* K LRDMC fixed-count projections per walker (GFMC_n, jqmc_gfmc.py:4779-5166),
  * T-move ECP treatment.  d_draw nwalk*K*4 = (alpha, beta, gamma, u_move).
- * d_w is multiplied by the K step weights b_x. */
+ * d_w is multiplied by the K step weights b_x.  Both precisions. */
 int jqmc_lrdmc_project(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const double* d_draw, double alat,
                        double E_scf, double* d_w, void* stream);
 
@@ -170,6 +186,9 @@ int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int3
  * iterations) and returns in *flops the FP64 operations it performs, so that a
  * caller timing it obtains the device's FP64 FMA throughput. */
 int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops, void* stream);
+
+/* The same for FP32 FMA chains (measurement helper, no reference counterpart). */
+int jqmc_probe_fp32(int64_t iters, int32_t blocks, float* d_sink, double* flops, void* stream);
 
 #ifdef __cplusplus
 }

@@ -42,7 +42,11 @@ class SystemDesc(C.Structure):
 
 
 class Walkers(C.Structure):
-    _fields_ = [("nwalk", i32), ("r", vp), ("G", vp), ("Ginv", vp), ("Tup", vp), ("Tdn", vp), ("h3", vp), ("status", vp)]
+    _fields_ = [("nwalk", i32), ("precision", i32), ("r", vp), ("G", vp), ("Ginv", vp), ("Tup", vp), ("Tdn", vp), ("h3", vp),
+                ("dphi", vp), ("dphi3", vp), ("scratch", vp), ("status", vp)]
+
+
+PREC_FP64, PREC_MIXED = 0, 1
 
 
 class JqmcError(RuntimeError):
@@ -62,7 +66,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.jqmc_system_create.argtypes = [C.POINTER(SystemDesc), C.POINTER(vp)]
         L.jqmc_system_destroy.argtypes = [vp]
-        L.jqmc_walker_bytes.argtypes = [vp]
+        L.jqmc_walker_bytes.argtypes = [vp, i32]
         L.jqmc_walker_bytes.restype = i64
         L.jqmc_ao_vgl.argtypes = [vp, i32, vp, i64, vp, vp]
         L.jqmc_walker_init.argtypes = [vp, C.POINTER(Walkers), vp]
@@ -75,9 +79,10 @@ def lib():
         L.jqmc_walker_gather.argtypes = [vp, C.POINTER(Walkers), C.POINTER(Walkers), vp, vp]
         L.jqmc_probe_fp64.argtypes = [i64, i32, vp, pf64, vp]
         L.jqmc_branch_comb_noalloc.argtypes = [i32, vp, f64, vp, vp]
+        L.jqmc_probe_fp32.argtypes = [i64, i32, vp, pf64, vp]
         for name in ("jqmc_probe_fp64", "jqmc_system_create", "jqmc_system_destroy", "jqmc_ao_vgl", "jqmc_walker_init", "jqmc_log_psi",
                      "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
-                     "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc"):
+                     "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -90,4 +95,4 @@ def check(rc: int, what: str) -> None:
 
 EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "jqmc_ao_vgl", "jqmc_walker_init",
             "jqmc_log_psi", "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
-            "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc")
+            "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32")

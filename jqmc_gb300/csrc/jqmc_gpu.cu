@@ -1,4 +1,4 @@
-// libjqmc_gpu: the jQMC walker hot path on one GB300 (sm_103a), FP64 form.
+// libjqmc_gpu: the jQMC walker hot path on one GB300 (sm_103a).
 //
 // One CTA owns one walker.  The basis / ECP tables are staged into shared
 // memory at kernel start; the per-walker ratio tables T_up, T_dn and the J3
@@ -21,6 +21,14 @@
 // electron's J3-AO vector, so the field h_e = dJ3/dphi3_e gives
 // Delta J3 = (phi3(r') - phi3(r_e)) . h_e, grad_e J3 = grad phi3(r_e) . h_e and
 // lap_e J3 = lap phi3(r_e) . h_e.
+//
+// Two forms share this code through templates:
+//   plain FP64 (JQMC_PREC_FP64): every quantity in double;
+//   mixed      (JQMC_PREC_MIXED): AO values, ratios, T tables, G^-1, the J3
+//     field and the Sherman-Morrison updates in float (exp on the SFU); the
+//     continuum kinetic energy (AO gradients/Laplacians), every energy and
+//     weight accumulation, and the rebuild of the tables from the positions
+//     (jqmc_walker_init) in double.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -39,11 +47,34 @@ namespace {
 constexpr int kSlots = JQMC_ECP_SLOTS;
 constexpr int kRed = 64;  // doubles of reduction scratch
 
+template <class R>
+struct Num;
+template <>
+struct Num<double> {
+  static __device__ __forceinline__ double ex(double x) { return exp(x); }
+  static __device__ __forceinline__ double sq(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double em1(double x) { return expm1(x); }
+};
+template <>
+struct Num<float> {
+  static __device__ __forceinline__ float ex(float x) { return __expf(x); }
+  static __device__ __forceinline__ float sq(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
+};
+
 struct Basis {
   int nshell, nao, nprim;
   const int* shells;
-  const double* prims;
+  const double* prims;   // (Z, cN) double
+  const float* primsf;   // (Z, cN) float copy
 };
+
+template <class R>
+__device__ __forceinline__ const R* prims_of(const Basis& b);
+template <>
+__device__ __forceinline__ const double* prims_of<double>(const Basis& b) { return b.prims; }
+template <>
+__device__ __forceinline__ const float* prims_of<float>(const Basis& b) { return b.primsf; }
 
 struct Sys {
   int natom, n_up, n_dn, N;
@@ -52,9 +83,11 @@ struct Sys {
   Basis det;
   const double* lam;   // A x A row-major
   const double* lamT;  // transpose
+  const float* lamf;
+  const float* lamTf;
   int has_j1, j1_type;
   double j1_param;
-  const double* j1_zeff;
+  const double* j1_cA;   // natom x 2: ((2Z)^(1/4), (2Z)^(3/4)) with Z the J1 effective charge
   int has_j2, j2_type;
   double j2_param;
   int has_j3;
@@ -62,6 +95,8 @@ struct Sys {
   const double* j3mat;   // A3 x A3
   const double* j3matT;  // transpose
   const double* j3vec;   // A3
+  const float* j3matf;
+  const float* j3matTf;
   int ecp_flag;
   const int* ecp_maxl1;
   const int* ecp_chan;
@@ -73,14 +108,43 @@ struct Sys {
   double ion_ion;
 };
 
+template <class T>
+__device__ __forceinline__ const T* lam_of(const Sys& s);
+template <>
+__device__ __forceinline__ const double* lam_of<double>(const Sys& s) { return s.lam; }
+template <>
+__device__ __forceinline__ const float* lam_of<float>(const Sys& s) { return s.lamf; }
+template <class T>
+__device__ __forceinline__ const T* lamT_of(const Sys& s);
+template <>
+__device__ __forceinline__ const double* lamT_of<double>(const Sys& s) { return s.lamT; }
+template <>
+__device__ __forceinline__ const float* lamT_of<float>(const Sys& s) { return s.lamTf; }
+template <class T>
+__device__ __forceinline__ const T* j3m_of(const Sys& s);
+template <>
+__device__ __forceinline__ const double* j3m_of<double>(const Sys& s) { return s.j3mat; }
+template <>
+__device__ __forceinline__ const float* j3m_of<float>(const Sys& s) { return s.j3matf; }
+template <class T>
+__device__ __forceinline__ const T* j3mT_of(const Sys& s);
+template <>
+__device__ __forceinline__ const double* j3mT_of<double>(const Sys& s) { return s.j3matT; }
+template <>
+__device__ __forceinline__ const float* j3mT_of<float>(const Sys& s) { return s.j3matTf; }
+
+// Device view of a jqmc_walkers descriptor (tables typed at the kernel).
 struct WS {
-  double *r, *G, *Ginv, *Tup, *Tdn, *h3;
+  double* r;
+  void *G, *Ginv, *Tup, *Tdn, *h3, *dphi, *dphi3;
+  double* scratch;
   int* status;
 };
 
 // Shared-memory table layout (byte offsets), identical for every walker kernel.
 struct TableLayout {
-  int off_dsh, off_dpr, off_jsh, off_jpr, off_apos, off_azeff, off_j1z, off_maxl1, off_chan, off_terms, off_mpts, off_mw;
+  int off_dsh, off_dpr, off_dprf, off_jsh, off_jpr, off_jprf, off_apos, off_azeff, off_j1z, off_maxl1, off_chan, off_terms,
+      off_mpts, off_mw;
   int bytes;
 };
 
@@ -89,13 +153,16 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 TableLayout table_layout(const Sys& s) {
   TableLayout L;
   int o = 0;
+  const int jsh = s.has_j3 ? s.j3.nshell : 0, jpr = s.has_j3 ? s.j3.nprim : 0;
   L.off_dsh = o; o = align16(o + s.det.nshell * 8 * 4);
   L.off_dpr = o; o = align16(o + s.det.nprim * 2 * 8);
-  L.off_jsh = o; o = align16(o + (s.has_j3 ? s.j3.nshell : 0) * 8 * 4);
-  L.off_jpr = o; o = align16(o + (s.has_j3 ? s.j3.nprim : 0) * 2 * 8);
+  L.off_dprf = o; o = align16(o + s.det.nprim * 2 * 4);
+  L.off_jsh = o; o = align16(o + jsh * 8 * 4);
+  L.off_jpr = o; o = align16(o + jpr * 2 * 8);
+  L.off_jprf = o; o = align16(o + jpr * 2 * 4);
   L.off_apos = o; o = align16(o + s.natom * 3 * 8);
   L.off_azeff = o; o = align16(o + s.natom * 8);
-  L.off_j1z = o; o = align16(o + s.natom * 8);
+  L.off_j1z = o; o = align16(o + s.natom * 16);
   L.off_maxl1 = o; o = align16(o + s.natom * 4);
   L.off_chan = o; o = align16(o + s.natom * kSlots * 2 * 4);
   L.off_terms = o; o = align16(o + s.ecp_nterm * 3 * 8);
@@ -119,17 +186,21 @@ __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* s
   Sys s = g;
   copy_words(smem + L.off_dsh, g.det.shells, g.det.nshell * 32);
   copy_words(smem + L.off_dpr, g.det.prims, g.det.nprim * 16);
+  copy_words(smem + L.off_dprf, g.det.primsf, g.det.nprim * 8);
   s.det.shells = reinterpret_cast<const int*>(smem + L.off_dsh);
   s.det.prims = reinterpret_cast<const double*>(smem + L.off_dpr);
+  s.det.primsf = reinterpret_cast<const float*>(smem + L.off_dprf);
   if (g.has_j3) {
     copy_words(smem + L.off_jsh, g.j3.shells, g.j3.nshell * 32);
     copy_words(smem + L.off_jpr, g.j3.prims, g.j3.nprim * 16);
+    copy_words(smem + L.off_jprf, g.j3.primsf, g.j3.nprim * 8);
     s.j3.shells = reinterpret_cast<const int*>(smem + L.off_jsh);
     s.j3.prims = reinterpret_cast<const double*>(smem + L.off_jpr);
+    s.j3.primsf = reinterpret_cast<const float*>(smem + L.off_jprf);
   }
   copy_words(smem + L.off_apos, g.atom_pos, g.natom * 24);
   copy_words(smem + L.off_azeff, g.atom_zeff, g.natom * 8);
-  copy_words(smem + L.off_j1z, g.j1_zeff, g.natom * 8);
+  copy_words(smem + L.off_j1z, g.j1_cA, g.natom * 16);
   copy_words(smem + L.off_maxl1, g.ecp_maxl1, g.natom * 4);
   copy_words(smem + L.off_chan, g.ecp_chan, g.natom * kSlots * 8);
   copy_words(smem + L.off_terms, g.ecp_terms, g.ecp_nterm * 24);
@@ -137,7 +208,7 @@ __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* s
   copy_words(smem + L.off_mw, g.mesh_w, g.nv * 8);
   s.atom_pos = reinterpret_cast<const double*>(smem + L.off_apos);
   s.atom_zeff = reinterpret_cast<const double*>(smem + L.off_azeff);
-  s.j1_zeff = reinterpret_cast<const double*>(smem + L.off_j1z);
+  s.j1_cA = reinterpret_cast<const double*>(smem + L.off_j1z);
   s.ecp_maxl1 = reinterpret_cast<const int*>(smem + L.off_maxl1);
   s.ecp_chan = reinterpret_cast<const int*>(smem + L.off_chan);
   s.ecp_terms = reinterpret_cast<const double*>(smem + L.off_terms);
@@ -148,8 +219,8 @@ __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* s
 }
 
 // ------------------------------------------------------------------ AO shells
-template <int L>
-__device__ __forceinline__ void sh_val(double x, double y, double z, double* S) {
+template <int L, class R>
+__device__ __forceinline__ void sh_val(R x, R y, R z, R* S) {
   if constexpr (L == 0) sh_l0(x, y, z, S);
   else if constexpr (L == 1) sh_l1(x, y, z, S);
   else if constexpr (L == 2) sh_l2(x, y, z, S);
@@ -159,8 +230,8 @@ __device__ __forceinline__ void sh_val(double x, double y, double z, double* S) 
   else sh_l6(x, y, z, S);
 }
 
-template <int L>
-__device__ __forceinline__ void sh_grad(double x, double y, double z, double* S, double* G) {
+template <int L, class R>
+__device__ __forceinline__ void sh_grad(R x, R y, R z, R* S, R* G) {
   if constexpr (L == 0) shg_l0(x, y, z, S, G);
   else if constexpr (L == 1) shg_l1(x, y, z, S, G);
   else if constexpr (L == 2) shg_l2(x, y, z, S, G);
@@ -170,10 +241,10 @@ __device__ __forceinline__ void sh_grad(double x, double y, double z, double* S,
   else shg_l6(x, y, z, S, G);
 }
 
-template <int L, class F>
-__device__ __forceinline__ void emit_val(double dx, double dy, double dz, double rad, int ao0, int jlo, int nm, F& f) {
-  double S[2 * L + 1];
-  sh_val<L>(dx, dy, dz, S);
+template <int L, class R, class F>
+__device__ __forceinline__ void emit_val(R dx, R dy, R dz, R rad, int ao0, int jlo, int nm, F& f) {
+  R S[2 * L + 1];
+  sh_val<L, R>(dx, dy, dz, S);
 #pragma unroll
   for (int j = 0; j < 2 * L + 1; ++j) {
     const int k = j - jlo;
@@ -185,88 +256,127 @@ __device__ __forceinline__ void emit_val(double dx, double dy, double dz, double
 //   phi = rad S, grad phi = rad grad S - 2 radZ S d, lap phi = S (4 r^2 radZ2 - (4l+6) radZ)
 // (rad = sum_p cN_p e^{-Z_p r^2}, radZ = sum cN Z e, radZ2 = sum cN Z^2 e; the
 // solid harmonics are harmonic and homogeneous of degree l).
-template <int L, class F>
-__device__ __forceinline__ void emit_vgl(double dx, double dy, double dz, double r2, double rad, double radZ,
-                                         double radZ2, int ao0, int jlo, int nm, F& f) {
-  double S[2 * L + 1], G[3 * (2 * L + 1)];
-  sh_grad<L>(dx, dy, dz, S, G);
-  const double lapf = 4.0 * r2 * radZ2 - (4.0 * L + 6.0) * radZ;
+template <int L, class R, class F>
+__device__ __forceinline__ void emit_vgl(R dx, R dy, R dz, R r2, R rad, R radZ, R radZ2, int ao0, int jlo, int nm, F& f) {
+  R S[2 * L + 1], G[3 * (2 * L + 1)];
+  sh_grad<L, R>(dx, dy, dz, S, G);
+  const R lapf = R(4) * r2 * radZ2 - (R(4 * L) + R(6)) * radZ;
 #pragma unroll
   for (int j = 0; j < 2 * L + 1; ++j) {
     const int k = j - jlo;
     if (k >= 0 && k < nm) {
-      const double t = -2.0 * radZ * S[j];
+      const R t = R(-2) * radZ * S[j];
       f(ao0 + k, rad * S[j], rad * G[3 * j] + t * dx, rad * G[3 * j + 1] + t * dy, rad * G[3 * j + 2] + t * dz,
         S[j] * lapf);
     }
   }
 }
 
-template <class F>
-__device__ __forceinline__ void shell_val(const Basis& b, const double* apos, int s, double px, double py, double pz,
-                                          F& f) {
+// d = p - R_atom in double (no cancellation), then rounded to R
+template <class R>
+__device__ __forceinline__ void disp(const double* apos, int atom, double px, double py, double pz, R& dx, R& dy, R& dz) {
+  dx = (R)(px - apos[3 * atom]);
+  dy = (R)(py - apos[3 * atom + 1]);
+  dz = (R)(pz - apos[3 * atom + 2]);
+}
+
+template <class R, class F>
+__device__ __forceinline__ void shell_val_d(const Basis& b, int s, R dx, R dy, R dz, F& f) {
   const int* sh = b.shells + 8 * s;
-  const int atom = sh[0], l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
-  const double dx = px - apos[3 * atom], dy = py - apos[3 * atom + 1], dz = pz - apos[3 * atom + 2];
-  const double r2 = dx * dx + dy * dy + dz * dz;
-  double rad = 0.0;
-  for (int p = 0; p < np; ++p) {
-    const double* pr = b.prims + 2 * (p0 + p);
-    rad += pr[1] * exp(-pr[0] * r2);
-  }
+  const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const R r2 = dx * dx + dy * dy + dz * dz;
+  const R* pr = prims_of<R>(b) + 2 * p0;
+  R rad = R(0);
+  for (int p = 0; p < np; ++p) rad += pr[2 * p + 1] * Num<R>::ex(-pr[2 * p] * r2);
   switch (l) {
-    case 0: emit_val<0>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    case 1: emit_val<1>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    case 2: emit_val<2>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    case 3: emit_val<3>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    case 4: emit_val<4>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    case 5: emit_val<5>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
-    default: emit_val<6>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 0: emit_val<0, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 1: emit_val<1, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 2: emit_val<2, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 3: emit_val<3, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 4: emit_val<4, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    case 5: emit_val<5, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
+    default: emit_val<6, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
   }
 }
 
-template <class F>
-__device__ __forceinline__ void shell_vgl(const Basis& b, const double* apos, int s, double px, double py, double pz,
-                                          F& f) {
+template <class R, class F>
+__device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R dz, F& f) {
   const int* sh = b.shells + 8 * s;
-  const int atom = sh[0], l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
-  const double dx = px - apos[3 * atom], dy = py - apos[3 * atom + 1], dz = pz - apos[3 * atom + 2];
-  const double r2 = dx * dx + dy * dy + dz * dz;
-  double rad = 0.0, radZ = 0.0, radZ2 = 0.0;
+  const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const R r2 = dx * dx + dy * dy + dz * dz;
+  const R* pr = prims_of<R>(b) + 2 * p0;
+  R rad = R(0), radZ = R(0), radZ2 = R(0);
   for (int p = 0; p < np; ++p) {
-    const double* pr = b.prims + 2 * (p0 + p);
-    const double e = pr[1] * exp(-pr[0] * r2);
+    const R Z = pr[2 * p];
+    const R e = pr[2 * p + 1] * Num<R>::ex(-Z * r2);
     rad += e;
-    radZ += pr[0] * e;
-    radZ2 += pr[0] * pr[0] * e;
+    radZ += Z * e;
+    radZ2 += Z * Z * e;
   }
   switch (l) {
-    case 0: emit_vgl<0>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    case 1: emit_vgl<1>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    case 2: emit_vgl<2>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    case 3: emit_vgl<3>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    case 4: emit_vgl<4>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    case 5: emit_vgl<5>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
-    default: emit_vgl<6>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 0: emit_vgl<0, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 1: emit_vgl<1, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 2: emit_vgl<2, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 3: emit_vgl<3, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 4: emit_vgl<4, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    case 5: emit_vgl<5, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+    default: emit_vgl<6, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+  }
+}
+
+// Visit every AO of a basis at point p (shells are grouped by nucleus, so the
+// displacement is recomputed only when the nucleus changes).
+template <class R, class F>
+__device__ __forceinline__ void ao_visit(const Basis& b, const double* apos, double px, double py, double pz, F& f) {
+  int last = -1;
+  R dx = R(0), dy = R(0), dz = R(0);
+  for (int s = 0; s < b.nshell; ++s) {
+    const int atom = b.shells[8 * s];
+    if (atom != last) {
+      disp<R>(apos, atom, px, py, pz, dx, dy, dz);
+      last = atom;
+    }
+    shell_val_d<R>(b, s, dx, dy, dz, f);
+  }
+}
+
+template <class R, class F>
+__device__ __forceinline__ void ao_visit_vgl(const Basis& b, const double* apos, double px, double py, double pz, F& f) {
+  int last = -1;
+  R dx = R(0), dy = R(0), dz = R(0);
+  for (int s = 0; s < b.nshell; ++s) {
+    const int atom = b.shells[8 * s];
+    if (atom != last) {
+      disp<R>(apos, atom, px, py, pz, dx, dy, dz);
+      last = atom;
+    }
+    shell_vgl_d<R>(b, s, dx, dy, dz, f);
   }
 }
 
 // sum_a phi_a(p) v[a]
-__device__ double ao_dot(const Basis& b, const double* apos, double px, double py, double pz, const double* v) {
-  double acc = 0.0;
-  auto f = [&](int a, double val) { acc += val * v[a]; };
-  for (int s = 0; s < b.nshell; ++s) shell_val(b, apos, s, px, py, pz, f);
+template <class R, class V>
+__device__ R ao_dot(const Basis& b, const double* apos, double px, double py, double pz, const V* v) {
+  R acc = R(0);
+  auto f = [&](int a, R val) { acc += val * (R)v[a]; };
+  ao_visit<R>(b, apos, px, py, pz, f);
   return acc;
 }
 
 // all AO values at one point into out[] (block-cooperative, split by shell; no sync)
-__device__ void ao_fill_block(const Basis& b, const double* apos, double px, double py, double pz, double* out) {
-  auto f = [&](int a, double val) { out[a] = val; };
-  for (int s = threadIdx.x; s < b.nshell; s += blockDim.x) shell_val(b, apos, s, px, py, pz, f);
+template <class R, class V>
+__device__ void ao_fill_block(const Basis& b, const double* apos, double px, double py, double pz, V* out) {
+  auto f = [&](int a, R val) { out[a] = (V)val; };
+  for (int s = threadIdx.x; s < b.nshell; s += blockDim.x) {
+    R dx, dy, dz;
+    disp<R>(apos, b.shells[8 * s], px, py, pz, dx, dy, dz);
+    shell_val_d<R>(b, s, dx, dy, dz, f);
+  }
 }
 
 // ------------------------------------------------------------------ reductions
-__device__ __forceinline__ double warp_sum(double v) {
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -305,10 +415,11 @@ __device__ double block_min(double v, double* red) {
 }
 
 // out[k] = sum_a M[k*A + a] x[a] for k < n (one warp per row)
-__device__ void rows_dot(const double* M, int n, int A, const double* x, double* out) {
+template <class T>
+__device__ void rows_dot(const T* M, int n, int A, const T* x, T* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = wid; k < n; k += nw) {
-    double acc = 0.0;
+    T acc = T(0);
     for (int a = lane; a < A; a += 32) acc += M[(size_t)k * A + a] * x[a];
     acc = warp_sum(acc);
     if (lane == 0) out[k] = acc;
@@ -316,33 +427,37 @@ __device__ void rows_dot(const double* M, int n, int A, const double* x, double*
 }
 
 // ------------------------------------------------------------------ physics helpers
-__device__ __forceinline__ double j1_pair(int type, double a, double Z, double d) {
-  const double c = pow(2.0 * Z, 0.25), A = pow(2.0 * Z, 0.75);
-  if (type == 0) return -A * (1.0 / (2.0 * a)) * (1.0 - exp(-a * c * d));
-  return -A * d / (2.0 * (1.0 + a * c * d));
+template <class R>
+__device__ __forceinline__ R j2_pair(int type, R b, R d) {
+  if (type == 0) return d / R(2) * (R(1) / (R(1) + b * d));
+  return R(1) / (R(2) * b) * (R(1) - Num<R>::ex(-b * d));
 }
 
-__device__ __forceinline__ double j2_pair(int type, double b, double d) {
-  if (type == 0) return d / 2.0 * (1.0 / (1.0 + b * d));
-  return 1.0 / (2.0 * b) * (1.0 - exp(-b * d));
-}
-
-__device__ double j1_at(const Sys& s, double x, double y, double z) {
-  double acc = 0.0;
-  for (int a = 0; a < s.natom; ++a) {
-    const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
-    acc += j1_pair(s.j1_type, s.j1_param, s.j1_zeff[a], sqrt(dx * dx + dy * dy + dz * dz));
+// J1 at one point: sum over nuclei
+template <class R>
+__device__ R j1_at(const Sys& s, double x, double y, double z) {
+  R acc = R(0);
+  const R a = (R)s.j1_param;
+  for (int at = 0; at < s.natom; ++at) {
+    R dx, dy, dz;
+    disp<R>(s.atom_pos, at, x, y, z, dx, dy, dz);
+    const R d = Num<R>::sq(dx * dx + dy * dy + dz * dz);
+    const R c = (R)s.j1_cA[2 * at], A = (R)s.j1_cA[2 * at + 1];
+    if (s.j1_type == 0) acc += -A * (R(1) / (R(2) * a)) * (R(1) - Num<R>::ex(-a * c * d));
+    else acc += -A * d / (R(2) * (R(1) + a * c * d));
   }
   return acc;
 }
 
 // sum over electrons m != skip of the J2 pair function at distance |p - r_m|
-__device__ double j2_at(const Sys& s, const double* r, int skip, double x, double y, double z) {
-  double acc = 0.0;
+template <class R>
+__device__ R j2_at(const Sys& s, const double* r, int skip, double x, double y, double z) {
+  R acc = R(0);
+  const R b = (R)s.j2_param;
   for (int m = 0; m < s.N; ++m) {
     if (m == skip) continue;
-    const double dx = x - r[3 * m], dy = y - r[3 * m + 1], dz = z - r[3 * m + 2];
-    acc += j2_pair(s.j2_type, s.j2_param, sqrt(dx * dx + dy * dy + dz * dz));
+    const R dx = (R)(x - r[3 * m]), dy = (R)(y - r[3 * m + 1]), dz = (R)(z - r[3 * m + 2]);
+    acc += j2_pair<R>(s.j2_type, b, Num<R>::sq(dx * dx + dy * dy + dz * dz));
   }
   return acc;
 }
@@ -365,7 +480,7 @@ __device__ double ecp_channel(const Sys& s, int atom, int slot, double d) {
     const double* tm = s.ecp_terms + 3 * (ch[0] + t);
     v += tm[0] * ipow(d, tm[1]) * exp(-tm[2] * d * d);
   }
-  return pow(d, -2.0) * v;
+  return v / (d * d);
 }
 
 __device__ __forceinline__ double legendre(int l, double x) {
@@ -400,26 +515,154 @@ __device__ void rotation(double a, double b, double g, double* R) {
   R[6] = -sb;     R[7] = cb * sa;                R[8] = ca * cb;
 }
 
+// Derivative tables of one electron at (x, y, z), computed in double and stored
+// in Tab: dp[c*A + a] = (grad x, y, z, lap)_c of geminal AO a; dp3[c*A3 + a] =
+// (value, grad x, y, z, lap)_c of J3 AO a.  Block-cooperative over shells, no sync.
+template <class Tab>
+__device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp, Tab* dp3) {
+  const int A = s.det.nao;
+  for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
+    double dx, dy, dz;
+    disp<double>(s.atom_pos, s.det.shells[8 * sh], x, y, z, dx, dy, dz);
+    auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
+      dp[a] = (Tab)gx; dp[A + a] = (Tab)gy; dp[2 * A + a] = (Tab)gz; dp[3 * A + a] = (Tab)lp;
+    };
+    shell_vgl_d<double>(s.det, sh, dx, dy, dz, f);
+  }
+  if (s.has_j3) {
+    const int A3 = s.j3.nao;
+    for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.j3.shells[8 * sh], x, y, z, dx, dy, dz);
+      auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
+        dp3[a] = (Tab)v; dp3[A3 + a] = (Tab)gx; dp3[2 * A3 + a] = (Tab)gy; dp3[3 * A3 + a] = (Tab)gz; dp3[4 * A3 + a] = (Tab)lp;
+      };
+      shell_vgl_d<double>(s.j3, sh, dx, dy, dz, f);
+    }
+  }
+}
+
+// J1 + J2 change when electron e moves to p, as sums of pair differences
+// f(r') - f(r) with r'^2 - r^2 = (2 d + s) . s (d = r_e - X, s = p - r_e), so
+// that the difference keeps the working precision of R even though J1 and J2
+// themselves are large (jastrow_factor.py:2288-2567 evaluate exp(J(r') - J(r))).
+template <class R>
+__device__ R j12_delta(const Sys& s, const double* r, int e, double px, double py, double pz) {
+  const double ex = r[3 * e], ey = r[3 * e + 1], ez = r[3 * e + 2];
+  const R sx = (R)(px - ex), sy = (R)(py - ey), sz = (R)(pz - ez);
+  R acc = R(0);
+  if (s.has_j1) {
+    const R a = (R)s.j1_param;
+    for (int at = 0; at < s.natom; ++at) {
+      R dx, dy, dz;
+      disp<R>(s.atom_pos, at, ex, ey, ez, dx, dy, dz);
+      const R r2 = dx * dx + dy * dy + dz * dz;
+      const R dr2 = (R(2) * dx + sx) * sx + (R(2) * dy + sy) * sy + (R(2) * dz + sz) * sz;
+      const R rr = Num<R>::sq(r2);
+      const R rp2 = r2 + dr2;
+      const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
+      const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
+      const R c = (R)s.j1_cA[2 * at], A = (R)s.j1_cA[2 * at + 1];
+      if (s.j1_type == 0) acc += A / (R(2) * a) * Num<R>::ex(-a * c * rr) * Num<R>::em1(-a * c * dr);
+      else acc += -A * dr / (R(2) * (R(1) + a * c * rr) * (R(1) + a * c * rp));
+    }
+  }
+  if (s.has_j2) {
+    const R b = (R)s.j2_param;
+    for (int m = 0; m < s.N; ++m) {
+      if (m == e) continue;
+      const R dx = (R)(ex - r[3 * m]), dy = (R)(ey - r[3 * m + 1]), dz = (R)(ez - r[3 * m + 2]);
+      const R r2 = dx * dx + dy * dy + dz * dz;
+      const R dr2 = (R(2) * dx + sx) * sx + (R(2) * dy + sy) * sy + (R(2) * dz + sz) * sz;
+      const R rr = Num<R>::sq(r2);
+      const R rp2 = r2 + dr2;
+      const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
+      const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
+      if (s.j2_type == 0) acc += dr / (R(2) * (R(1) + b * rr) * (R(1) + b * rp));
+      else acc += -Num<R>::ex(-b * rr) * Num<R>::em1(-b * dr) / (R(2) * b);
+    }
+  }
+  return acc;
+}
+
+// Mixed form: the same sums from cached float displacements d = r_e - X plus the
+// move vector s, so that a mesh point costs no double arithmetic.
+template <class V>
+__device__ float ao_dot_rel(const Basis& b, const float* dAe, float sx, float sy, float sz, const V* v) {
+  float acc = 0.0f;
+  auto f = [&](int a, float val) { acc += val * (float)v[a]; };
+  int last = -1;
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  for (int sh = 0; sh < b.nshell; ++sh) {
+    const int atom = b.shells[8 * sh];
+    if (atom != last) {
+      dx = dAe[3 * atom] + sx;
+      dy = dAe[3 * atom + 1] + sy;
+      dz = dAe[3 * atom + 2] + sz;
+      last = atom;
+    }
+    shell_val_d<float>(b, sh, dx, dy, dz, f);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ float pair_dr(float dx, float dy, float dz, float sx, float sy, float sz, float& rr, float& rp) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  const float dr2 = (2.f * dx + sx) * sx + (2.f * dy + sy) * sy + (2.f * dz + sz) * sz;
+  rr = sqrtf(r2);
+  const float rp2 = r2 + dr2;
+  rp = sqrtf(rp2 > 0.f ? rp2 : 0.f);
+  return (rp + rr > 0.f) ? dr2 / (rp + rr) : 0.f;
+}
+
+__device__ float j12_delta_rel(const Sys& s, const float* dAe, const float* dEe, int e, float sx, float sy, float sz) {
+  float acc = 0.0f;
+  if (s.has_j1) {
+    const float a = (float)s.j1_param;
+    for (int at = 0; at < s.natom; ++at) {
+      float rr, rp;
+      const float dr = pair_dr(dAe[3 * at], dAe[3 * at + 1], dAe[3 * at + 2], sx, sy, sz, rr, rp);
+      const float c = (float)s.j1_cA[2 * at], A = (float)s.j1_cA[2 * at + 1];
+      if (s.j1_type == 0) acc += A / (2.f * a) * __expf(-a * c * rr) * expm1f(-a * c * dr);
+      else acc += -A * dr / (2.f * (1.f + a * c * rr) * (1.f + a * c * rp));
+    }
+  }
+  if (s.has_j2) {
+    const float b = (float)s.j2_param;
+    for (int m = 0; m < s.N; ++m) {
+      if (m == e) continue;
+      float rr, rp;
+      const float dr = pair_dr(dEe[3 * m], dEe[3 * m + 1], dEe[3 * m + 2], sx, sy, sz, rr, rp);
+      if (s.j2_type == 0) acc += dr / (2.f * (1.f + b * rr) * (1.f + b * rp));
+      else acc += -__expf(-b * rr) * expm1f(-b * dr) / (2.f * b);
+    }
+  }
+  return acc;
+}
+
 // ------------------------------------------------------------------ per-walker workspace
+template <class Tab>
 struct Work {
   Sys s;
   int N, n, A, A3;
-  double* r;     // N*3
-  double* G;     // n*n
-  double* Gi;    // n*n
-  double* Tup;   // global, this walker
-  double* Tdn;
-  double* h3;
-  double* vA0;   // A
-  double* vA1;   // A
-  double* vA2;   // A
-  double* v30;   // A3
-  double* v31;
-  double* v32;
-  double* vn0;   // n
-  double* vn1;
-  double* vn2;
-  double* vn3;
+  double* r;     // N*3 (shared)
+  Tab* G;        // n*n (shared)
+  Tab* Gi;       // n*n (shared)
+  Tab* Tup;      // global, this walker
+  Tab* Tdn;
+  Tab* h3;
+  Tab* dphi;     // global: N x 4 x A  (grad x, y, z, lap of the geminal AOs at each electron)
+  Tab* dphi3;    // global: N x 5 x A3 (value, grad x, y, z, lap of the J3 AOs at each electron)
+  Tab* vA0;      // A (shared)
+  Tab* vA1;
+  Tab* vA2;
+  Tab* v30;      // A3 (shared)
+  Tab* v31;
+  Tab* v32;
+  Tab* vn0;      // n (shared)
+  Tab* vn1;
+  Tab* vn2;
+  Tab* vn3;
   double* red;   // kRed
   double* sc;    // 32 scalars
 };
@@ -428,67 +671,76 @@ struct WorkLayout {
   int off_r, off_G, off_Gi, off_vA, off_v3, off_vn, off_red, off_sc, bytes;
 };
 
-WorkLayout work_layout(const Sys& s, int base) {
+WorkLayout work_layout(const Sys& s, int base, int tab_bytes) {
   WorkLayout L;
   const int A3 = s.has_j3 ? s.j3.nao : 1;
   int o = base;
   L.off_r = o; o = align16(o + s.N * 3 * 8);
-  L.off_G = o; o = align16(o + s.n_up * s.n_up * 8);
-  L.off_Gi = o; o = align16(o + s.n_up * s.n_up * 8);
-  L.off_vA = o; o = align16(o + 3 * s.det.nao * 8);
-  L.off_v3 = o; o = align16(o + 3 * A3 * 8);
-  L.off_vn = o; o = align16(o + 4 * s.n_up * 8);
+  L.off_G = o; o = align16(o + s.n_up * s.n_up * tab_bytes);
+  L.off_Gi = o; o = align16(o + s.n_up * s.n_up * tab_bytes);
+  L.off_vA = o; o = align16(o + 3 * s.det.nao * tab_bytes);
+  L.off_v3 = o; o = align16(o + 3 * A3 * tab_bytes);
+  L.off_vn = o; o = align16(o + 4 * s.n_up * tab_bytes);
   L.off_red = o; o = align16(o + kRed * 8);
   L.off_sc = o; o = align16(o + 32 * 8);
   L.bytes = o;
   return L;
 }
 
-__device__ Work make_work(const Sys& s, const WorkLayout& L, unsigned char* smem, const WS& ws, int w) {
-  Work k;
+template <class Tab>
+__device__ Work<Tab> make_work(const Sys& s, const WorkLayout& L, unsigned char* smem, const WS& ws, int w) {
+  Work<Tab> k;
   k.s = s;
   k.N = s.N;
   k.n = s.n_up;
   k.A = s.det.nao;
   k.A3 = s.has_j3 ? s.j3.nao : 1;
   k.r = reinterpret_cast<double*>(smem + L.off_r);
-  k.G = reinterpret_cast<double*>(smem + L.off_G);
-  k.Gi = reinterpret_cast<double*>(smem + L.off_Gi);
-  k.vA0 = reinterpret_cast<double*>(smem + L.off_vA);
+  k.G = reinterpret_cast<Tab*>(smem + L.off_G);
+  k.Gi = reinterpret_cast<Tab*>(smem + L.off_Gi);
+  k.vA0 = reinterpret_cast<Tab*>(smem + L.off_vA);
   k.vA1 = k.vA0 + k.A;
   k.vA2 = k.vA1 + k.A;
-  k.v30 = reinterpret_cast<double*>(smem + L.off_v3);
+  k.v30 = reinterpret_cast<Tab*>(smem + L.off_v3);
   k.v31 = k.v30 + k.A3;
   k.v32 = k.v31 + k.A3;
-  k.vn0 = reinterpret_cast<double*>(smem + L.off_vn);
+  k.vn0 = reinterpret_cast<Tab*>(smem + L.off_vn);
   k.vn1 = k.vn0 + k.n;
   k.vn2 = k.vn1 + k.n;
   k.vn3 = k.vn2 + k.n;
   k.red = reinterpret_cast<double*>(smem + L.off_red);
   k.sc = reinterpret_cast<double*>(smem + L.off_sc);
-  k.Tup = ws.Tup + (size_t)w * k.n * k.A;
-  k.Tdn = ws.Tdn + (size_t)w * k.n * k.A;
-  k.h3 = s.has_j3 ? ws.h3 + (size_t)w * k.N * k.A3 : nullptr;
+  k.Tup = static_cast<Tab*>(ws.Tup) + (size_t)w * k.n * k.A;
+  k.Tdn = static_cast<Tab*>(ws.Tdn) + (size_t)w * k.n * k.A;
+  k.h3 = s.has_j3 ? static_cast<Tab*>(ws.h3) + (size_t)w * k.N * k.A3 : nullptr;
+  k.dphi = static_cast<Tab*>(ws.dphi) + (size_t)w * k.N * 4 * k.A;
+  k.dphi3 = s.has_j3 ? static_cast<Tab*>(ws.dphi3) + (size_t)w * k.N * 5 * k.A3 : nullptr;
   return k;
 }
 
-__device__ void load_walker(Work& k, const WS& ws, int w) {
+template <class Tab>
+__device__ void load_walker(Work<Tab>& k, const WS& ws, int w) {
   const int nn = k.n * k.n;
   for (int t = threadIdx.x; t < k.N * 3; t += blockDim.x) k.r[t] = ws.r[(size_t)w * k.N * 3 + t];
+  const Tab* G = static_cast<const Tab*>(ws.G) + (size_t)w * nn;
+  const Tab* Gi = static_cast<const Tab*>(ws.Ginv) + (size_t)w * nn;
   for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-    k.G[t] = ws.G[(size_t)w * nn + t];
-    k.Gi[t] = ws.Ginv[(size_t)w * nn + t];
+    k.G[t] = G[t];
+    k.Gi[t] = Gi[t];
   }
   __syncthreads();
 }
 
-__device__ void store_walker(const Work& k, const WS& ws, int w) {
+template <class Tab>
+__device__ void store_walker(const Work<Tab>& k, const WS& ws, int w) {
   __syncthreads();
   const int nn = k.n * k.n;
+  Tab* G = static_cast<Tab*>(ws.G) + (size_t)w * nn;
+  Tab* Gi = static_cast<Tab*>(ws.Ginv) + (size_t)w * nn;
   for (int t = threadIdx.x; t < k.N * 3; t += blockDim.x) ws.r[(size_t)w * k.N * 3 + t] = k.r[t];
   for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-    ws.G[(size_t)w * nn + t] = k.G[t];
-    ws.Ginv[(size_t)w * nn + t] = k.Gi[t];
+    G[t] = k.G[t];
+    Gi[t] = k.Gi[t];
   }
 }
 
@@ -500,63 +752,63 @@ __device__ void store_walker(const Work& k, const WS& ws, int w) {
 //   dn j:  b = T_dn phi', ratio = b_j,  q = b - e_j,  c' = G b (new column j),
 //          G^-1 -= q G^-1[j,:] / ratio, T_dn -= q (x) T_dn[j] / ratio,
 //          T_up += G^-1[j,:] (x) (lambda dphi - T_up^T G q) / ratio
-// (every right-hand side uses the tables before the move).
-__device__ double sm_move(Work& k, int e, double px, double py, double pz) {
+// (every right-hand side uses the tables before the move).  Arithmetic in Tab.
+template <class Tab>
+__device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) {
   const Sys& s = k.s;
   const int n = k.n, A = k.A, A3 = k.A3;
   const bool up = e < s.n_up;
   const int i = up ? e : e - s.n_up;
   const double ox = k.r[3 * e], oy = k.r[3 * e + 1], oz = k.r[3 * e + 2];
+  const Tab* lam = lam_of<Tab>(s);
+  const Tab* lamT = lamT_of<Tab>(s);
   // phi' -> vA0, phi_old -> vA1, then vA1 = dphi
-  ao_fill_block(s.det, s.atom_pos, px, py, pz, k.vA0);
-  ao_fill_block(s.det, s.atom_pos, ox, oy, oz, k.vA1);
+  ao_fill_block<Tab, Tab>(s.det, s.atom_pos, px, py, pz, k.vA0);
+  ao_fill_block<Tab, Tab>(s.det, s.atom_pos, ox, oy, oz, k.vA1);
   if (s.has_j3) {
-    ao_fill_block(s.j3, s.atom_pos, px, py, pz, k.v30);
-    ao_fill_block(s.j3, s.atom_pos, ox, oy, oz, k.v31);
+    ao_fill_block<Tab, Tab>(s.j3, s.atom_pos, px, py, pz, k.v30);
+    ao_fill_block<Tab, Tab>(s.j3, s.atom_pos, ox, oy, oz, k.v31);
   }
   __syncthreads();
   for (int a = threadIdx.x; a < A; a += blockDim.x) k.vA1[a] = k.vA0[a] - k.vA1[a];
   if (s.has_j3)
     for (int a = threadIdx.x; a < A3; a += blockDim.x) k.v31[a] = k.v30[a] - k.v31[a];
-  // a / b vector -> vn0
-  rows_dot(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
+  rows_dot<Tab>(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
   __syncthreads();
-  const double ratio = k.vn0[i];
-  const double inv = 1.0 / ratio;
+  const Tab ratio = k.vn0[i];
+  const Tab inv = Tab(1) / ratio;
+  Tab* scn = reinterpret_cast<Tab*>(k.sc);  // 32 doubles of scratch
+  const int scn_cap = (int)(32 * sizeof(double) / sizeof(Tab));
   if (up) {
-    // vn1 = w = a - e_i ; vn2 = G^T w ; vn3 = old column i of G^-1 ; new row i of G -> sc later
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      k.vn1[t] = k.vn0[t] - (t == i ? 1.0 : 0.0);
+      k.vn1[t] = k.vn0[t] - (t == i ? Tab(1) : Tab(0));
       k.vn3[t] = k.Gi[t * n + i];
     }
     __syncthreads();
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      double u = 0.0;
+      Tab u = Tab(0);
       for (int t = 0; t < n; ++t) u += k.G[t * n + c] * k.vn1[t];
       k.vn2[c] = u;
     }
-    // x_b = (sum_a lam[a][b] dphi_a - sum_j Tdn[j][b] u_j) / ratio -> vA2
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
-      double dl = 0.0;
-      for (int a = 0; a < A; ++a) dl += s.lam[(size_t)a * A + b] * k.vA1[a];
-      double mw = 0.0;
+      Tab dl = Tab(0);
+      for (int a = 0; a < A; ++a) dl += lam[(size_t)a * A + b] * k.vA1[a];
+      Tab mw = Tab(0);
       for (int j = 0; j < n; ++j) mw += k.Tdn[(size_t)j * A + b] * k.vn2[j];
       k.vA2[b] = (dl - mw) * inv;
     }
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
-      const double xb = k.vA2[b];
+      const Tab xb = k.vA2[b];
       for (int j = 0; j < n; ++j) k.Tdn[(size_t)j * A + b] += k.vn3[j] * xb;
-      const double ti = k.Tup[(size_t)i * A + b];
+      const Tab ti = k.Tup[(size_t)i * A + b];
       for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + b] -= ti * k.vn1[t] * inv;
     }
-    // new row i of G: g'_c = sum_t a_t G[t][c]  (uses old G; write after sync)
-    double* gnew = k.sc;  // n <= 32 handled below via vA2 reuse when larger
-    double* gn = (n <= 32) ? gnew : k.vA2;
+    Tab* gn = (n <= scn_cap) ? scn : k.vA2;
     __syncthreads();
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      double g = 0.0;
+      Tab g = Tab(0);
       for (int t = 0; t < n; ++t) g += k.vn0[t] * k.G[t * n + c];
       gn[c] = g;
     }
@@ -567,36 +819,35 @@ __device__ double sm_move(Work& k, int e, double px, double py, double pz) {
     }
     for (int c = threadIdx.x; c < n; c += blockDim.x) k.G[i * n + c] = gn[c];
   } else {
-    // vn1 = q = b - e_i ; vn2 = G q ; vn3 = old row i of G^-1
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      k.vn1[t] = k.vn0[t] - (t == i ? 1.0 : 0.0);
+      k.vn1[t] = k.vn0[t] - (t == i ? Tab(1) : Tab(0));
       k.vn3[t] = k.Gi[i * n + t];
     }
     __syncthreads();
     for (int rr = threadIdx.x; rr < n; rr += blockDim.x) {
-      double u = 0.0;
+      Tab u = Tab(0);
       for (int t = 0; t < n; ++t) u += k.G[rr * n + t] * k.vn1[t];
       k.vn2[rr] = u;
     }
     __syncthreads();
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
-      double dm = 0.0;
-      for (int b = 0; b < A; ++b) dm += s.lamT[(size_t)b * A + a] * k.vA1[b];
-      double mq = 0.0;
+      Tab dm = Tab(0);
+      for (int b = 0; b < A; ++b) dm += lamT[(size_t)b * A + a] * k.vA1[b];
+      Tab mq = Tab(0);
       for (int t = 0; t < n; ++t) mq += k.Tup[(size_t)t * A + a] * k.vn2[t];
       k.vA2[a] = (dm - mq) * inv;
     }
     __syncthreads();
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
-      const double xa = k.vA2[a];
+      const Tab xa = k.vA2[a];
       for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + a] += xa * k.vn3[t];
-      const double tj = k.Tdn[(size_t)i * A + a];
+      const Tab tj = k.Tdn[(size_t)i * A + a];
       for (int t = 0; t < n; ++t) k.Tdn[(size_t)t * A + a] -= k.vn1[t] * tj * inv;
     }
-    double* cn = (n <= 32) ? k.sc : k.vA2;
+    Tab* cn = (n <= scn_cap) ? scn : k.vA2;
     __syncthreads();
     for (int rr = threadIdx.x; rr < n; rr += blockDim.x) {
-      double c = 0.0;
+      Tab c = Tab(0);
       for (int t = 0; t < n; ++t) c += k.G[rr * n + t] * k.vn0[t];
       cn[rr] = c;
     }
@@ -609,12 +860,14 @@ __device__ double sm_move(Work& k, int e, double px, double py, double pz) {
   }
   // J3 field: h_m += J dphi3 or J^T dphi3 for every other electron m
   if (s.has_j3) {
+    const Tab* J = j3m_of<Tab>(s);
+    const Tab* JT = j3mT_of<Tab>(s);
     __syncthreads();
     for (int c = threadIdx.x; c < A3; c += blockDim.x) {
-      double jd = 0.0, jtd = 0.0;
+      Tab jd = Tab(0), jtd = Tab(0);
       for (int cp = 0; cp < A3; ++cp) {
-        jd += s.j3matT[(size_t)cp * A3 + c] * k.v31[cp];   // (J d)_c
-        jtd += s.j3mat[(size_t)cp * A3 + c] * k.v31[cp];   // (J^T d)_c
+        jd += JT[(size_t)cp * A3 + c] * k.v31[cp];   // (J d)_c
+        jtd += J[(size_t)cp * A3 + c] * k.v31[cp];   // (J^T d)_c
       }
       k.v32[c] = jd;
       k.v30[c] = jtd;
@@ -630,6 +883,7 @@ __device__ double sm_move(Work& k, int e, double px, double py, double pz) {
       k.h3[(size_t)m * A3 + c] += useJ ? k.v32[c] : k.v30[c];
     }
   }
+  fill_dtables<Tab>(s, px, py, pz, k.dphi + (size_t)e * 4 * A, s.has_j3 ? k.dphi3 + (size_t)e * 5 * A3 : nullptr);
   __syncthreads();
   if (threadIdx.x == 0) {
     k.r[3 * e] = px;
@@ -637,44 +891,47 @@ __device__ double sm_move(Work& k, int e, double px, double py, double pz) {
     k.r[3 * e + 2] = pz;
   }
   __syncthreads();
-  return ratio;
+  return (double)ratio;
 }
 
 // ------------------------------------------------------------------ per-step terms
 // Arrays in shared memory for the energy / projection kernels.
 struct Terms {
   double* ke;     // N continuum kinetic energy per electron
-  double* j1o;    // N  J1 of electron e at its position
-  double* j2o;    // N  sum_{m != e} J2 pair values
   double* c3;     // N  phi3(r_e) . h_e
   double* ei;     // N  e-ion Coulomb per electron
   double* eid;    // N  discretised e-ion (distance floor alat)
   double* edist;  // N  distance to the nearest nucleus
+  double* vl;     // N*kSlots non-local channel values V_l(edist) at the nearest nucleus
   int* eatom;     // N  nearest nucleus
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
   double* R;      // 9 rotation
+  float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
+  float* dE;      // mixed form: N*N*3      float(r_e - r_m)
 };
 
 struct TermsLayout {
-  int off_ke, off_j1o, off_j2o, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_vl, off_ea, off_el, off_V, off_R, off_dA, off_dE, bytes;
 };
 
-TermsLayout terms_layout(const Sys& s, int base) {
+// rel: reserve the float displacement caches of the mixed form
+TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   TermsLayout L;
   const int N = s.N;
   int o = base;
   L.off_ke = o; o = align16(o + N * 8);
-  L.off_j1o = o; o = align16(o + N * 8);
-  L.off_j2o = o; o = align16(o + N * 8);
   L.off_c3 = o; o = align16(o + N * 8);
   L.off_ei = o; o = align16(o + N * 8);
   L.off_eid = o; o = align16(o + N * 8);
   L.off_ed = o; o = align16(o + N * 8);
+  L.off_vl = o; o = align16(o + N * kSlots * 8);
   L.off_ea = o; o = align16(o + N * 4);
   L.off_el = o; o = align16(o + 6 * N * 8);
   L.off_V = o; o = align16(o + (s.nv > 0 ? s.nv : 1) * N * 8);
   L.off_R = o; o = align16(o + 9 * 8);
+  L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
+  L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
   L.bytes = o;
   return L;
 }
@@ -682,130 +939,165 @@ TermsLayout terms_layout(const Sys& s, int base) {
 __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
   Terms t;
   t.ke = reinterpret_cast<double*>(smem + L.off_ke);
-  t.j1o = reinterpret_cast<double*>(smem + L.off_j1o);
-  t.j2o = reinterpret_cast<double*>(smem + L.off_j2o);
   t.c3 = reinterpret_cast<double*>(smem + L.off_c3);
   t.ei = reinterpret_cast<double*>(smem + L.off_ei);
   t.eid = reinterpret_cast<double*>(smem + L.off_eid);
   t.edist = reinterpret_cast<double*>(smem + L.off_ed);
+  t.vl = reinterpret_cast<double*>(smem + L.off_vl);
   t.eatom = reinterpret_cast<int*>(smem + L.off_ea);
   t.el = reinterpret_cast<double*>(smem + L.off_el);
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
+  t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
+  t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
   return t;
 }
 
 // Phase A: per-electron continuum kinetic energy and the old-position values
 // the ratios need (wavefunction.py:1142-1207, jastrow_factor.py:961-1034,
-// 3435-3558, 4077-4156).
-__device__ void electron_terms(Work& k, Terms& t, double alat) {
+// 3435-3558, 4077-4156).  One warp per electron: the cached AO derivative tables
+// are dotted with the electron's T row and J3 field in double; J1/J2 in double.
+template <class Tab>
+__device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   const Sys& s = k.s;
-  for (int e = threadIdx.x; e < k.N; e += blockDim.x) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int A = k.A, A3 = k.A3;
+  if (t.dA) {
+    const int M = s.natom, N = k.N;
+    for (int p = threadIdx.x; p < N * (M + N); p += blockDim.x) {
+      const int e = p / (M + N), q = p % (M + N);
+      const double* X = q < M ? s.atom_pos + 3 * q : k.r + 3 * (q - M);
+      float* out = q < M ? t.dA + (size_t)(e * M + q) * 3 : t.dE + (size_t)(e * N + q - M) * 3;
+      out[0] = (float)(k.r[3 * e] - X[0]);
+      out[1] = (float)(k.r[3 * e + 1] - X[1]);
+      out[2] = (float)(k.r[3 * e + 2] - X[2]);
+    }
+  }
+  for (int e = wid; e < k.N; e += nw) {
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
     const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
-    const double* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
+    const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
+    const Tab* dp = k.dphi + (size_t)e * 4 * A;
     double gx = 0, gy = 0, gz = 0, lp = 0;
-    {
-      auto f = [&](int a, double v, double ax, double ay, double az, double al) {
-        const double tv = Trow[a];
-        gx += ax * tv; gy += ay * tv; gz += az * tv; lp += al * tv;
-      };
-      for (int sh = 0; sh < s.det.nshell; ++sh) shell_vgl(s.det, s.atom_pos, sh, x, y, z, f);
+    for (int a = lane; a < A; a += 32) {
+      const double tv = (double)Trow[a];
+      gx += (double)dp[a] * tv;
+      gy += (double)dp[A + a] * tv;
+      gz += (double)dp[2 * A + a] * tv;
+      lp += (double)dp[3 * A + a] * tv;
     }
-    // ln det part
-    double Gx = gx, Gy = gy, Gz = gz;
-    double L = lp - (gx * gx + gy * gy + gz * gz);
-    double c3 = 0.0;
+    double c3 = 0, hx = 0, hy = 0, hz = 0, hl = 0;
     if (s.has_j3) {
-      const double* h = k.h3 + (size_t)e * k.A3;
-      double hx = 0, hy = 0, hz = 0, hl = 0;
-      auto f = [&](int a, double v, double ax, double ay, double az, double al) {
-        const double hv = h[a];
-        c3 += v * hv; hx += ax * hv; hy += ay * hv; hz += az * hv; hl += al * hv;
-      };
-      for (int sh = 0; sh < s.j3.nshell; ++sh) shell_vgl(s.j3, s.atom_pos, sh, x, y, z, f);
-      Gx += hx; Gy += hy; Gz += hz; L += hl;
+      const Tab* h = k.h3 + (size_t)e * A3;
+      const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
+      for (int a = lane; a < A3; a += 32) {
+        const double hv = (double)h[a];
+        c3 += (double)q[a] * hv;
+        hx += (double)q[A3 + a] * hv;
+        hy += (double)q[2 * A3 + a] * hv;
+        hz += (double)q[3 * A3 + a] * hv;
+        hl += (double)q[4 * A3 + a] * hv;
+      }
     }
-    double j1o = 0.0, ei = 0.0, eid = 0.0;
-    int best = 0;
-    double bd = 1e300;
-    for (int a = 0; a < s.natom; ++a) {
-      const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
-      const double d = sqrt(dx * dx + dy * dy + dz * dz);
-      if (d < bd) { bd = d; best = a; }
-      ei += -s.atom_zeff[a] / d;
-      eid += -s.atom_zeff[a] / fmax(d, alat);
-      if (s.has_j1) {
-        const double Z = s.j1_zeff[a], aa = s.j1_param;
-        const double c = pow(2.0 * Z, 0.25), AA = pow(2.0 * Z, 0.75);
+    double jx = 0, jy = 0, jz = 0, jl = 0;
+    if (s.has_j1)
+      for (int a = lane; a < s.natom; a += 32) {
+        const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        const double aa = s.j1_param, c = s.j1_cA[2 * a], AA = s.j1_cA[2 * a + 1];
         double f1, f2;
         if (s.j1_type == 0) {
           const double ex = exp(-aa * c * d);
-          j1o += -AA * (1.0 / (2.0 * aa)) * (1.0 - ex);
           f1 = -AA * c * ex / 2.0;
           f2 = AA * aa * c * c * ex / 2.0;
         } else {
           const double q = 1.0 + aa * c * d;
-          j1o += -AA * d / (2.0 * q);
           f1 = -AA / (2.0 * q * q);
           f2 = AA * aa * c / (q * q * q);
         }
-        Gx += f1 * dx / d; Gy += f1 * dy / d; Gz += f1 * dz / d;
-        L += f2 + 2.0 * f1 / d;
+        jx += f1 * dx / d; jy += f1 * dy / d; jz += f1 * dz / d;
+        jl += f2 + 2.0 * f1 / d;
       }
-    }
-    double j2o = 0.0;
     if (s.has_j2) {
       const double b = s.j2_param;
-      for (int m = 0; m < k.N; ++m) {
+      for (int m = lane; m < k.N; m += 32) {
         if (m == e) continue;
         const double dx = x - k.r[3 * m], dy = y - k.r[3 * m + 1], dz = z - k.r[3 * m + 2];
         const double d = sqrt(dx * dx + dy * dy + dz * dz);
         double f1, f2;
         if (s.j2_type == 0) {
           const double q = 1.0 + b * d;
-          j2o += d / 2.0 * (1.0 / q);
           f1 = 1.0 / (2.0 * q * q);
           f2 = -b / (q * q * q);
         } else {
           const double ex = exp(-b * d);
-          j2o += 1.0 / (2.0 * b) * (1.0 - ex);
           f1 = 0.5 * ex;
           f2 = -0.5 * b * ex;
         }
-        Gx += f1 * dx / d; Gy += f1 * dy / d; Gz += f1 * dz / d;
-        L += f2 + 2.0 * f1 / d;
+        jx += f1 * dx / d; jy += f1 * dy / d; jz += f1 * dz / d;
+        jl += f2 + 2.0 * f1 / d;
       }
     }
-    t.ke[e] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
-    t.j1o[e] = j1o;
-    t.j2o[e] = j2o;
-    t.c3[e] = c3;
-    t.ei[e] = ei;
-    t.eid[e] = eid;
-    t.eatom[e] = best;
-    t.edist[e] = bd;
+    gx = warp_sum(gx); gy = warp_sum(gy); gz = warp_sum(gz); lp = warp_sum(lp);
+    c3 = warp_sum(c3); hx = warp_sum(hx); hy = warp_sum(hy); hz = warp_sum(hz); hl = warp_sum(hl);
+    jx = warp_sum(jx); jy = warp_sum(jy); jz = warp_sum(jz); jl = warp_sum(jl);
+    if (lane == 0) {
+      const double Gx = gx + hx + jx, Gy = gy + hy + jy, Gz = gz + hz + jz;
+      const double L = lp - (gx * gx + gy * gy + gz * gz) + hl + jl;
+      double ei = 0.0, eid = 0.0, bd = 1e300;
+      int best = 0;
+      for (int a = 0; a < s.natom; ++a) {
+        const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        if (d < bd) { bd = d; best = a; }
+        ei += -s.atom_zeff[a] / d;
+        eid += -s.atom_zeff[a] / fmax(d, alat);
+      }
+      t.ke[e] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
+      t.c3[e] = c3;
+      t.ei[e] = ei;
+      t.eid[e] = eid;
+      t.eatom[e] = best;
+      t.edist[e] = bd;
+      if (s.ecp_flag) {
+        const int lmax = s.ecp_maxl1[best];
+        for (int l = 0; l < kSlots; ++l) t.vl[e * kSlots + l] = l < lmax ? ecp_channel(s, best, l, bd) : 0.0;
+      }
+    }
   }
   __syncthreads();
 }
 
-// psi(r')/psi(r) for electron e moved to p (det x Jastrow)
-__device__ double wf_ratio(const Work& k, const Terms& t, int e, double px, double py, double pz) {
+// psi(r')/psi(r) for electron e moved by (sx, sy, sz) (det x Jastrow), arithmetic in R
+template <class R, class Tab>
+__device__ R wf_ratio(const Work<Tab>& k, const Terms& t, int e, double sx, double sy, double sz) {
   const Sys& s = k.s;
   const bool up = e < s.n_up;
   const int i = up ? e : e - s.n_up;
-  const double det = ao_dot(s.det, s.atom_pos, px, py, pz, (up ? k.Tup : k.Tdn) + (size_t)i * k.A);
-  double dJ = 0.0;
-  if (s.has_j1) dJ += j1_at(s, px, py, pz) - t.j1o[e];
-  if (s.has_j2) dJ += j2_at(s, k.r, e, px, py, pz) - t.j2o[e];
-  if (s.has_j3) dJ += ao_dot(s.j3, s.atom_pos, px, py, pz, k.h3 + (size_t)e * k.A3) - t.c3[e];
-  return det * exp(dJ);
+  const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
+  if constexpr (sizeof(R) == sizeof(float)) {
+    if (t.dA) {
+      const float fx = (float)sx, fy = (float)sy, fz = (float)sz;
+      const float* dAe = t.dA + (size_t)e * s.natom * 3;
+      const float* dEe = t.dE + (size_t)e * k.N * 3;
+      const float det = ao_dot_rel<Tab>(s.det, dAe, fx, fy, fz, Trow);
+      float dJ = j12_delta_rel(s, dAe, dEe, e, fx, fy, fz);
+      if (s.has_j3) dJ += ao_dot_rel<Tab>(s.j3, dAe, fx, fy, fz, k.h3 + (size_t)e * k.A3) - (float)t.c3[e];
+      return det * __expf(dJ);
+    }
+  }
+  const double px = k.r[3 * e] + sx, py = k.r[3 * e + 1] + sy, pz = k.r[3 * e + 2] + sz;
+  const R det = ao_dot<R, Tab>(s.det, s.atom_pos, px, py, pz, Trow);
+  R dJ = j12_delta<R>(s, k.r, e, px, py, pz);
+  if (s.has_j3) dJ += ao_dot<R, Tab>(s.j3, s.atom_pos, px, py, pz, k.h3 + (size_t)e * k.A3) - (R)t.c3[e];
+  return det * Num<R>::ex(dJ);
 }
 
 // Phase B: kinetic lattice elements (wavefunction.py:1740-1860) and non-local ECP
 // elements (coulomb_potential.py:1478-1712, NN = 1).  Rotation R in t.R.
-__device__ void mesh_terms(const Work& k, Terms& t, double alat, bool kinetic) {
+template <class R, class Tab>
+__device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
   const Sys& s = k.s;
   const int N = k.N, nv = s.nv;
   const int nkin = kinetic ? 6 * N : 0;
@@ -814,10 +1106,8 @@ __device__ void mesh_terms(const Work& k, Terms& t, double alat, bool kinetic) {
     if (p < nkin) {
       const int e = p / 6, kk = p % 6, ax = kk >> 1;
       const double sg = (kk & 1) ? -alat : alat;
-      const double px = k.r[3 * e] + sg * t.R[0 * 3 + ax];
-      const double py = k.r[3 * e + 1] + sg * t.R[1 * 3 + ax];
-      const double pz = k.r[3 * e + 2] + sg * t.R[2 * 3 + ax];
-      t.el[p] = -1.0 / (2.0 * alat * alat) * wf_ratio(k, t, e, px, py, pz);
+      t.el[p] = -1.0 / (2.0 * alat * alat) *
+                (double)wf_ratio<R, Tab>(k, t, e, sg * t.R[0 * 3 + ax], sg * t.R[1 * 3 + ax], sg * t.R[2 * 3 + ax]);
     } else {
       const int q = p - nkin, e = q / nv, v = q % nv;
       const int atom = t.eatom[e];
@@ -833,13 +1123,9 @@ __device__ void mesh_terms(const Work& k, Terms& t, double alat, bool kinetic) {
       const double dist = sqrt(relx * relx + rely * rely + relz * relz);
       const double gn = sqrt(gx * gx + gy * gy + gz * gz);
       const double cth = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
-      const double px = k.r[3 * e] + relx + dist * gx;
-      const double py = k.r[3 * e + 1] + rely + dist * gy;
-      const double pz = k.r[3 * e + 2] + relz + dist * gz;
-      const double ratio = wf_ratio(k, t, e, px, py, pz);
+      const double ratio = (double)wf_ratio<R, Tab>(k, t, e, relx + dist * gx, rely + dist * gy, relz + dist * gz);
       double vsum = 0.0;
-      for (int l = 0; l < lmax; ++l)
-        vsum += ecp_channel(s, atom, l, dist) * ((2 * l + 1) * legendre(l, cth) * s.mesh_w[v] * ratio);
+      for (int l = 0; l < lmax; ++l) vsum += t.vl[e * kSlots + l] * ((2 * l + 1) * legendre(l, cth) * s.mesh_w[v] * ratio);
       t.V[q] = vsum;
     }
   }
@@ -847,37 +1133,34 @@ __device__ void mesh_terms(const Work& k, Terms& t, double alat, bool kinetic) {
 }
 
 // e-e Coulomb, block-reduced
-__device__ double coulomb_ee(const Work& k) {
-  const int N = k.N;
+__device__ double coulomb_ee(const double* r, int N, double* red) {
   double acc = 0.0;
   for (int p = threadIdx.x; p < N * N; p += blockDim.x) {
     const int a = p / N, b = p % N;
     if (b <= a) continue;
-    const double dx = k.r[3 * a] - k.r[3 * b], dy = k.r[3 * a + 1] - k.r[3 * b + 1], dz = k.r[3 * a + 2] - k.r[3 * b + 2];
+    const double dx = r[3 * a] - r[3 * b], dy = r[3 * a + 1] - r[3 * b + 1], dz = r[3 * a + 2] - r[3 * b + 2];
     acc += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
   }
-  return block_sum(acc, k.red);
+  return block_sum(acc, red);
 }
 
 // local ECP channel summed over electrons and nuclei (coulomb_potential.py:1145-1246)
-__device__ double ecp_local_sum(const Work& k) {
-  const Sys& s = k.s;
+__device__ double ecp_local_sum(const Sys& s, const double* r, int N, double* red) {
   double acc = 0.0;
   if (s.ecp_flag) {
-    for (int p = threadIdx.x; p < k.N * s.natom; p += blockDim.x) {
+    for (int p = threadIdx.x; p < N * s.natom; p += blockDim.x) {
       const int e = p / s.natom, a = p % s.natom;
-      const double dx = k.r[3 * e] - s.atom_pos[3 * a], dy = k.r[3 * e + 1] - s.atom_pos[3 * a + 1],
-                   dz = k.r[3 * e + 2] - s.atom_pos[3 * a + 2];
+      const double dx = r[3 * e] - s.atom_pos[3 * a], dy = r[3 * e + 1] - s.atom_pos[3 * a + 1],
+                   dz = r[3 * e + 2] - s.atom_pos[3 * a + 2];
       acc += ecp_channel(s, a, s.ecp_maxl1[a], sqrt(dx * dx + dy * dy + dz * dz));
     }
   }
-  return block_sum(acc, k.red);
+  return block_sum(acc, red);
 }
 
 // Phase C of the GFMC_n step: (diag, nondiag) sums (jqmc_gfmc.py:4806-5030).
-__device__ void lrdmc_sums(const Work& k, Terms& t, double alat, double* diag_out, double* nondiag_out) {
-  const Sys& s = k.s;
-  const int N = k.N;
+__device__ void lrdmc_sums(const Sys& s, const double* r, int N, double* red, Terms& t, double alat, double* diag_out,
+                           double* nondiag_out) {
   double fn = 0.0, sp = 0.0, opt = 0.0;
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
     bool flip = false;
@@ -899,13 +1182,13 @@ __device__ void lrdmc_sums(const Work& k, Terms& t, double alat, double* diag_ou
       vfn += fmin(t.V[q], 0.0);
       vsp += fmax(t.V[q], 0.0);
     }
-  fn = block_sum(fn, k.red);
-  sp = block_sum(sp, k.red);
-  opt = block_sum(opt, k.red);
-  vfn = block_sum(vfn, k.red);
-  vsp = block_sum(vsp, k.red);
-  const double ee = coulomb_ee(k);
-  const double loc = ecp_local_sum(k);
+  fn = block_sum(fn, red);
+  sp = block_sum(sp, red);
+  opt = block_sum(opt, red);
+  vfn = block_sum(vfn, red);
+  vsp = block_sum(vsp, red);
+  const double ee = coulomb_ee(r, N, red);
+  const double loc = ecp_local_sum(s, r, N, red);
   const double disc = ee + s.ion_ion + opt;
   const double dk = 3.0 / (2.0 * alat * alat) * N;
   if (s.ecp_flag) {
@@ -940,53 +1223,68 @@ __global__ void k_ao_vgl(Sys s, int basis, const double* __restrict__ r, long lo
     out[(3 * nao + a) * npts + p] = gz;
     out[(4 * nao + a) * npts + p] = lp;
   };
-  for (int sh = 0; sh < b.nshell; ++sh) shell_vgl(b, s.atom_pos, sh, x, y, z, f);
+  ao_visit_vgl<double>(b, s.atom_pos, x, y, z, f);
 }
 
-// Walker initialisation: G, G^-1 (Gauss-Jordan, partial pivoting), T tables, J3 field.
-__global__ void k_walker_init(KParams P, int off_aug, int off_phi3) {
+// Walker initialisation in FP64: G, G^-1 (Gauss-Jordan, partial pivoting), T
+// tables and J3 field, written in the table type Tab.  M_up / M_dn go to the
+// double scratch (for Tab == double the T buffers themselves).
+template <class Tab>
+__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int off_phi3) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work k = make_work(s, P.wl, smem, P.ws, w);
-  const int n = k.n, A = k.A, N = k.N;
-  for (int t = threadIdx.x; t < N * 3; t += blockDim.x) k.r[t] = P.ws.r[(size_t)w * N * 3 + t];
+  const int n = s.n_up, A = s.det.nao, N = s.N, A3 = s.has_j3 ? s.j3.nao : 1;
+  double* r = reinterpret_cast<double*>(smem + P.wl.off_r);
+  int* piv = reinterpret_cast<int*>(smem + P.wl.off_sc);
+  double* Gd = reinterpret_cast<double*>(smem + off_Gd);   // n*n
+  double* aug = reinterpret_cast<double*>(smem + off_aug); // n*2n
+  double* vec = reinterpret_cast<double*>(smem + off_vec); // max(A + n, 3*A3)
+  double* vn = vec + A;                                    // n
+  Tab* Tup = static_cast<Tab*>(P.ws.Tup) + (size_t)w * n * A;
+  Tab* Tdn = static_cast<Tab*>(P.ws.Tdn) + (size_t)w * n * A;
+  double* Mdn;  // n rows of A: row j = lambda phi_dn(r_j)
+  double* Mup;  // n rows of A: row i = phi_up(r_i)^T lambda
+  if constexpr (sizeof(Tab) == sizeof(double)) {
+    Mdn = reinterpret_cast<double*>(Tup);
+    Mup = reinterpret_cast<double*>(Tdn);
+  } else {
+    Mdn = P.ws.scratch + (size_t)w * 2 * n * A;
+    Mup = Mdn + (size_t)n * A;
+  }
+  for (int t = threadIdx.x; t < N * 3; t += blockDim.x) r[t] = P.ws.r[(size_t)w * N * 3 + t];
   __syncthreads();
-  // M_up rows -> Tdn rows
   for (int i = 0; i < n; ++i) {
-    ao_fill_block(s.det, s.atom_pos, k.r[3 * i], k.r[3 * i + 1], k.r[3 * i + 2], k.vA0);
+    ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * i], r[3 * i + 1], r[3 * i + 2], vec);
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
       double acc = 0.0;
-      for (int a = 0; a < A; ++a) acc += k.vA0[a] * s.lam[(size_t)a * A + b];
-      k.Tdn[(size_t)i * A + b] = acc;
+      for (int a = 0; a < A; ++a) acc += vec[a] * s.lam[(size_t)a * A + b];
+      Mup[(size_t)i * A + b] = acc;
     }
     __syncthreads();
   }
-  // G columns and M_dn rows -> Tup rows
   for (int j = 0; j < s.n_dn; ++j) {
     const int e = s.n_up + j;
-    ao_fill_block(s.det, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.vA0);
+    ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
     __syncthreads();
-    rows_dot(k.Tdn, n, A, k.vA0, k.vn0);
+    rows_dot<double>(Mup, n, A, vec, vn);
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
       double acc = 0.0;
-      for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * k.vA0[b];
-      k.Tup[(size_t)j * A + a] = acc;
+      for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * vec[b];
+      Mdn[(size_t)j * A + a] = acc;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) k.G[i * n + j] = k.vn0[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Gd[i * n + j] = vn[i];
     __syncthreads();
   }
   // Gauss-Jordan on [G | I]
-  double* aug = reinterpret_cast<double*>(smem + off_aug);
   const int n2 = 2 * n;
   for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
     const int rr = t / n2, cc = t % n2;
-    aug[t] = cc < n ? k.G[rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
+    aug[t] = cc < n ? Gd[rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
   }
   __syncthreads();
-  int* piv = reinterpret_cast<int*>(k.sc);
   for (int c = 0; c < n; ++c) {
     if (threadIdx.x == 0) {
       int p = c;
@@ -1021,52 +1319,68 @@ __global__ void k_walker_init(KParams P, int off_aug, int off_phi3) {
       if (rr != c) aug[rr * n2 + c] = 0.0;
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < n * n; t += blockDim.x) k.Gi[t] = aug[(t / n) * n2 + n + (t % n)];
+  Tab* Gw = static_cast<Tab*>(P.ws.G) + (size_t)w * n * n;
+  Tab* Giw = static_cast<Tab*>(P.ws.Ginv) + (size_t)w * n * n;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    Gw[t] = (Tab)Gd[t];
+    Giw[t] = (Tab)aug[(t / n) * n2 + n + (t % n)];
+  }
   __syncthreads();
-  // T_up[k][a] = sum_j M_dn[j][a] G^-1[j][k] ; T_dn[k][b] = sum_i G^-1[k][i] M_up[i][b]  (in place per column)
+  // T_up[k][a] = sum_j M_dn[j][a] G^-1[j][k] ; T_dn[k][b] = sum_i G^-1[k][i] M_up[i][b]  (per column)
   for (int a = threadIdx.x; a < A; a += blockDim.x) {
     double m[JQMC_MAX_NUP];
-    for (int j = 0; j < n; ++j) m[j] = k.Tup[(size_t)j * A + a];
+    for (int j = 0; j < n; ++j) m[j] = Mdn[(size_t)j * A + a];
     for (int kk = 0; kk < n; ++kk) {
       double acc = 0.0;
-      for (int j = 0; j < n; ++j) acc += m[j] * k.Gi[j * n + kk];
-      k.Tup[(size_t)kk * A + a] = acc;
+      for (int j = 0; j < n; ++j) acc += m[j] * aug[j * n2 + n + kk];
+      Tup[(size_t)kk * A + a] = (Tab)acc;
     }
-    for (int j = 0; j < n; ++j) m[j] = k.Tdn[(size_t)j * A + a];
+    for (int j = 0; j < n; ++j) m[j] = Mup[(size_t)j * A + a];
     for (int kk = 0; kk < n; ++kk) {
       double acc = 0.0;
-      for (int j = 0; j < n; ++j) acc += k.Gi[kk * n + j] * m[j];
-      k.Tdn[(size_t)kk * A + a] = acc;
+      for (int j = 0; j < n; ++j) acc += aug[kk * n2 + n + j] * m[j];
+      Tdn[(size_t)kk * A + a] = (Tab)acc;
     }
+  }
+  // AO derivative tables at every electron
+  {
+    Tab* dpw = static_cast<Tab*>(P.ws.dphi) + (size_t)w * N * 4 * A;
+    Tab* dp3w = s.has_j3 ? static_cast<Tab*>(P.ws.dphi3) + (size_t)w * N * 5 * A3 : nullptr;
+    for (int e = 0; e < N; ++e)
+      fill_dtables<Tab>(s, r[3 * e], r[3 * e + 1], r[3 * e + 2], dpw + (size_t)e * 4 * A, dp3w ? dp3w + (size_t)e * 5 * A3 : nullptr);
   }
   // J3 field
   if (s.has_j3) {
-    const int A3 = k.A3;
     double* phi3 = reinterpret_cast<double*>(smem + off_phi3);  // N*A3
+    double* tot_up = vec;
+    double* tot_dn = vec + A3;
+    double* pfx = vec + 2 * A3;
+    __syncthreads();
     for (int p = threadIdx.x; p < N * s.j3.nshell; p += blockDim.x) {
       const int e = p / s.j3.nshell, sh = p % s.j3.nshell;
       double* out = phi3 + (size_t)e * A3;
       auto f = [&](int a, double v) { out[a] = v; };
-      shell_val(s.j3, s.atom_pos, sh, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], f);
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
     }
     __syncthreads();
-    // v30 = total up, v31 = total dn, v32 = running prefix of the current spin
     for (int c = threadIdx.x; c < A3; c += blockDim.x) {
       double tu = 0.0, td = 0.0;
       for (int e = 0; e < s.n_up; ++e) tu += phi3[(size_t)e * A3 + c];
       for (int e = s.n_up; e < N; ++e) td += phi3[(size_t)e * A3 + c];
-      k.v30[c] = tu;
-      k.v31[c] = td;
-      k.v32[c] = 0.0;
+      tot_up[c] = tu;
+      tot_dn[c] = td;
+      pfx[c] = 0.0;
     }
     __syncthreads();
-    double* h = k.h3;
+    Tab* h = static_cast<Tab*>(P.ws.h3) + (size_t)w * N * A3;
     for (int e = 0; e < N; ++e) {
       const bool up = e < s.n_up;
       if (e == s.n_up)
-        for (int c = threadIdx.x; c < A3; c += blockDim.x) k.v32[c] = 0.0;
+        for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] = 0.0;
       __syncthreads();
-      const double* tot_same = up ? k.v30 : k.v31;
+      const double* tot_same = up ? tot_up : tot_dn;
       const double* pe = phi3 + (size_t)e * A3;
       for (int c = threadIdx.x; c < A3; c += blockDim.x) {
         // h = j1 + J^T pfx + J (tot_same - pfx - phi_e) + (up ? J tot_dn : J^T tot_up)
@@ -1074,26 +1388,25 @@ __global__ void k_walker_init(KParams P, int off_aug, int off_phi3) {
         for (int cp = 0; cp < A3; ++cp) {
           const double Jcpc = s.j3mat[(size_t)cp * A3 + c];    // J[cp][c]
           const double Jccp = s.j3matT[(size_t)cp * A3 + c];   // J[c][cp]
-          const double pf = k.v32[cp];
+          const double pf = pfx[cp];
           acc += Jcpc * pf + Jccp * (tot_same[cp] - pf - pe[cp]);
-          acc += up ? Jccp * k.v31[cp] : Jcpc * k.v30[cp];
+          acc += up ? Jccp * tot_dn[cp] : Jcpc * tot_up[cp];
         }
-        h[(size_t)e * A3 + c] = acc;
+        h[(size_t)e * A3 + c] = (Tab)acc;
       }
       __syncthreads();
-      for (int c = threadIdx.x; c < A3; c += blockDim.x) k.v32[c] += pe[c];
+      for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] += pe[c];
       __syncthreads();
     }
   }
-  store_walker(k, P.ws, w);
 }
 
-// ln|det G|, sign (LU with partial pivoting on a copy of G) and J
+// ln|det G|, sign (LU with partial pivoting on a copy of G) and J   (FP64 form)
 __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
   load_walker(k, P.ws, w);
   const int n = k.n, N = k.N;
   double* a = reinterpret_cast<double*>(smem + off_aug);
@@ -1125,13 +1438,13 @@ __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, 
   double j = 0.0;
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
     const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
-    if (s.has_j1) j += j1_at(s, x, y, z);
-    if (s.has_j2) j += 0.5 * j2_at(s, k.r, e, x, y, z);
+    if (s.has_j1) j += j1_at<double>(s, x, y, z);
+    if (s.has_j2) j += 0.5 * j2_at<double>(s, k.r, e, x, y, z);
     if (s.has_j3) {
       const double* h = k.h3 + (size_t)e * k.A3;
       double acc = 0.0;
       auto f = [&](int aa, double v) { acc += v * (h[aa] + s.j3vec[aa]); };
-      for (int sh = 0; sh < s.j3.nshell; ++sh) shell_val(s.j3, s.atom_pos, sh, x, y, z, f);
+      ao_visit<double>(s.j3, s.atom_pos, x, y, z, f);
       j += 0.5 * acc;
     }
   }
@@ -1139,7 +1452,7 @@ __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, 
   if (threadIdx.x == 0) jas[w] = j;
 }
 
-__device__ double as_factor_block(const Work& k) {
+__device__ double as_factor_block(const Work<double>& k) {
   const int n = k.n;
   double F = 0.0;
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) F += k.Gi[t] * k.Gi[t];
@@ -1156,13 +1469,13 @@ __device__ double as_factor_block(const Work& k) {
   return SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
 }
 
-// VMC: K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523)
+// VMC: K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523)   (FP64 form)
 __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt,
                             double eps_AS, int* accept, int off_cand) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
   load_walker(k, P.ws, w);
   const int n = k.n, A = k.A, A3 = k.A3;
   double* cand = reinterpret_cast<double*>(smem + off_cand);  // n*n candidate G^-1
@@ -1172,7 +1485,6 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
   for (int step = 0; step < K; ++step) {
     const int* id = idraw + ((size_t)w * K + step) * 4;
     const double* fd = fdraw + ((size_t)w * K + step) * 2;
-    // proposal (thread 0), broadcast via sc
     if (threadIdx.x == 0) {
       const int sel = id[0];
       const bool is_up = sel < s.n_up;
@@ -1197,7 +1509,7 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
       k.sc[1] = nx; k.sc[2] = ny; k.sc[3] = nz;
       k.sc[4] = Tr;
       double dJ = 0.0;
-      if (s.has_j1) dJ += j1_at(s, nx, ny, nz) - j1_at(s, ox, oy, oz);
+      if (s.has_j1) dJ += j1_at<double>(s, nx, ny, nz) - j1_at<double>(s, ox, oy, oz);
       k.sc[5] = dJ;
     }
     __syncthreads();
@@ -1205,30 +1517,28 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
     const double nx = k.sc[1], ny = k.sc[2], nz = k.sc[3];
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
-    // J2 and J3 ratio parts
     double dJ = 0.0;
     if (s.has_j2)
       for (int m = threadIdx.x; m < k.N; m += blockDim.x) {
         if (m == e) continue;
         const double ax = nx - k.r[3 * m], ay = ny - k.r[3 * m + 1], az = nz - k.r[3 * m + 2];
         const double bx = k.r[3 * e] - k.r[3 * m], by = k.r[3 * e + 1] - k.r[3 * m + 1], bz = k.r[3 * e + 2] - k.r[3 * m + 2];
-        dJ += j2_pair(s.j2_type, s.j2_param, sqrt(ax * ax + ay * ay + az * az)) -
-              j2_pair(s.j2_type, s.j2_param, sqrt(bx * bx + by * by + bz * bz));
+        dJ += j2_pair<double>(s.j2_type, s.j2_param, sqrt(ax * ax + ay * ay + az * az)) -
+              j2_pair<double>(s.j2_type, s.j2_param, sqrt(bx * bx + by * by + bz * bz));
       }
-    ao_fill_block(s.det, s.atom_pos, nx, ny, nz, k.vA0);
+    ao_fill_block<double, double>(s.det, s.atom_pos, nx, ny, nz, k.vA0);
     if (s.has_j3) {
-      ao_fill_block(s.j3, s.atom_pos, nx, ny, nz, k.v30);
-      ao_fill_block(s.j3, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.v31);
+      ao_fill_block<double, double>(s.j3, s.atom_pos, nx, ny, nz, k.v30);
+      ao_fill_block<double, double>(s.j3, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.v31);
     }
     __syncthreads();
     if (s.has_j3)
       for (int a = threadIdx.x; a < A3; a += blockDim.x) dJ += (k.v30[a] - k.v31[a]) * k.h3[(size_t)e * A3 + a];
     dJ = block_sum(dJ, k.red);
-    rows_dot(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
+    rows_dot<double>(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
     __syncthreads();
     const double ratio = k.vn0[i];
     const double inv = 1.0 / ratio;
-    // candidate G, G^-1 for the AS factor of the proposed state
     if (up) {
       for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
         const int rr = t / n, cc = t % n;
@@ -1277,7 +1587,7 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
     }
     __syncthreads();
     if (k.sc[6] != 0.0) {
-      sm_move(k, e, nx, ny, nz);
+      sm_move<double>(k, e, nx, ny, nz);
       R_old = R_new;
       ++nacc;
     }
@@ -1287,25 +1597,25 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
   store_walker(k, P.ws, w);
 }
 
-// VMC local energy and weight (hamiltonians.py:225-290, jqmc_mcmc.py:725-747)
+// VMC local energy and weight (hamiltonians.py:225-290, jqmc_mcmc.py:725-747)   (FP64 form)
 __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, double eps_AS, double* eL, double* wL) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
   Terms t = make_terms(P.ml, smem);
   load_walker(k, P.ws, w);
   if (threadIdx.x == 0) rotation(angles[3 * w], angles[3 * w + 1], angles[3 * w + 2], t.R);
   __syncthreads();
-  electron_terms(k, t, 0.0);
-  mesh_terms(k, t, 0.0, false);
+  electron_terms<double>(k, t, 0.0);
+  mesh_terms<double, double>(k, t, 0.0, false);
   double acc = 0.0;
   for (int e = threadIdx.x; e < k.N; e += blockDim.x) acc += t.ke[e] + t.ei[e];
   if (s.ecp_flag)
     for (int q = threadIdx.x; q < k.N * s.nv; q += blockDim.x) acc += t.V[q];
   acc = block_sum(acc, k.red);
-  const double ee = coulomb_ee(k);
-  const double loc = ecp_local_sum(k);
+  const double ee = coulomb_ee(k.r, k.N, k.red);
+  const double loc = ecp_local_sum(s, k.r, k.N, k.red);
   const double R = as_factor_block(k);
   if (threadIdx.x == 0) {
     eL[w] = acc + ee + s.ion_ion + loc;
@@ -1316,12 +1626,14 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
 
 // LRDMC GFMC_n projections; K steps fused.  K == 0 with energy outputs computes
 // e_L and V_diag at the current positions with the rotation of draw[w].
+// R: mesh arithmetic, Tab: table storage and updates.
+template <class R, class Tab>
 __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
                         double* eL, double* vdiag) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work k = make_work(s, P.wl, smem, P.ws, w);
+  Work<Tab> k = make_work<Tab>(s, P.wl, smem, P.ws, w);
   Terms t = make_terms(P.ml, smem);
   load_walker(k, P.ws, w);
   const int N = k.N;
@@ -1331,10 +1643,10 @@ __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, doubl
     const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * 4;
     if (threadIdx.x == 0) rotation(d[0], d[1], d[2], t.R);
     __syncthreads();
-    electron_terms(k, t, alat);
-    mesh_terms(k, t, alat, true);
+    electron_terms<Tab>(k, t, alat);
+    mesh_terms<R, Tab>(k, t, alat, true);
     double diag, nondiag;
-    lrdmc_sums(k, t, alat, &diag, &nondiag);
+    lrdmc_sums(s, k.r, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
       if (threadIdx.x == 0) {
         eL[w] = diag + nondiag;
@@ -1384,7 +1696,10 @@ __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, doubl
       k.sc[0] = e; k.sc[1] = px; k.sc[2] = py; k.sc[3] = pz;
     }
     __syncthreads();
-    const double ratio = sm_move(k, (int)k.sc[0], k.sc[1], k.sc[2], k.sc[3]);
+    const int me = (int)k.sc[0];
+    const double mx = k.sc[1], my = k.sc[2], mz = k.sc[3];
+    __syncthreads();
+    const double ratio = sm_move<Tab>(k, me, mx, my, mz);
     if (threadIdx.x == 0 && ratio == 0.0) atomicOr(P.ws.status + w, JQMC_ST_ZERO_RATIO);
   }
   if (K > 0) {
@@ -1397,8 +1712,7 @@ __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, doubl
 }
 
 __global__ void k_branch_comb(int W, const double* __restrict__ wv, double* cum) {
-  // cumulative normalised weights, sequential as np.cumsum (one thread), then a
-  // parallel left searchsorted for the comb points (k + zeta) / W
+  // cumulative normalised weights, sequential as np.cumsum (one thread)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     double tot = 0.0;
     for (int j = 0; j < W; ++j) tot += wv[j];
@@ -1419,17 +1733,13 @@ __global__ void k_branch_search(int W, const double* __restrict__ cum, double ze
   chosen[kq] = lo < W ? lo : W - 1;
 }
 
-__global__ void k_gather(const double* __restrict__ src, double* __restrict__ dst, long long per, const int* chosen, int W) {
+template <class T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, long long per, const int* chosen, int W) {
   const long long tot = per * W;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
     const long long w = t / per, o = t % per;
     dst[t] = src[(long long)chosen[w] * per + o];
   }
-}
-
-__global__ void k_gather_int(const int* __restrict__ src, int* __restrict__ dst, const int* chosen, int W) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < W) dst[t] = src[chosen[t]];
 }
 
 // FP64 FMA throughput probe: 8 independent FMA chains per thread.
@@ -1445,10 +1755,21 @@ __global__ void k_probe_fp64(long long iters, double* out) {
   if (s == 12345.0) out[0] = s;  // keeps the chains live
 }
 
+// FP32 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void k_probe_fp32(long long iters, float* out) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+  float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+  const float m = 0.9999999f, c = 1e-9f;
+  for (long long i = 0; i < iters; ++i) {
+    a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+    a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+  }
+  const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.0f) out[0] = s;  // keeps the chains live
+}
+
 // ------------------------------------------------------------------ host side
 inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
-
-KParams make_params(const jqmc_system* sys, const jqmc_walkers* w);
 
 }  // namespace
 
@@ -1461,24 +1782,30 @@ namespace {
 
 WS to_ws(const jqmc_walkers* w) {
   WS x;
-  x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3; x.status = w->status;
+  x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3;
+  x.dphi = w->dphi; x.dphi3 = w->dphi3;
+  x.scratch = w->scratch; x.status = w->status;
   return x;
 }
 
 bool walkers_ok(const jqmc_system* sys, const jqmc_walkers* w) {
   if (!sys || !w || w->nwalk <= 0) return false;
-  if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status) return false;
-  if (sys->s.has_j3 && !w->h3) return false;
+  if (w->precision != JQMC_PREC_FP64 && w->precision != JQMC_PREC_MIXED) return false;
+  if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status || !w->dphi) return false;
+  if (sys->s.has_j3 && (!w->h3 || !w->dphi3)) return false;
+  if (w->precision == JQMC_PREC_MIXED && !w->scratch) return false;
   return true;
 }
+
+int tab_bytes(const jqmc_walkers* w) { return w->precision == JQMC_PREC_MIXED ? 4 : 8; }
 
 KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   KParams P;
   P.s = sys->s;
   P.ws = to_ws(w);
   P.tl = table_layout(sys->s);
-  P.wl = work_layout(sys->s, P.tl.bytes);
-  P.ml = terms_layout(sys->s, P.wl.bytes);
+  P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
+  P.ml = terms_layout(sys->s, P.wl.bytes, w->precision == JQMC_PREC_MIXED);
   P.nwalk = w->nwalk;
   return P;
 }
@@ -1487,6 +1814,24 @@ int launch_check(const void* fn, int smem) {
   if (smem > 227 * 1024) return JQMC_E_SMEM;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return JQMC_E_CUDA;
   return JQMC_OK;
+}
+
+int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const double* d_draw, double alat, double E_scf,
+                 double* d_w, double* d_eL, double* d_vd, void* stream) {
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  if (w->precision == JQMC_PREC_MIXED) {
+    auto fn = k_lrdmc<float, float>;
+    int rc = launch_check((const void*)fn, smem);
+    if (rc) return rc;
+    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd);
+  } else {
+    auto fn = k_lrdmc<double, double>;
+    int rc = launch_check((const void*)fn, smem);
+    if (rc) return rc;
+    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd);
+  }
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
 }  // namespace
@@ -1500,26 +1845,25 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   if (M <= 0 || M > JQMC_MAX_ATOM || d->n_up <= 0 || d->n_up > JQMC_MAX_NUP) return JQMC_E_LIMIT;
   if (d->n_up != d->n_dn) return JQMC_E_ARG;  // the walker kernels treat closed shells
   if (d->n_up + d->n_dn > JQMC_MAX_ELEC || A <= 0 || A > JQMC_MAX_AO) return JQMC_E_LIMIT;
+  if (d->n_up > A) return JQMC_E_ARG;          // G would be singular
   if (!d->atom_pos || !d->atom_zeff || !d->lambda || !d->det.shells || !d->det.prims) return JQMC_E_ARG;
   const int A3 = d->has_j3 ? d->j3.nao : 0;
   if (d->has_j3 && (A3 <= 0 || A3 > JQMC_MAX_AO || !d->j3.shells || !d->j3.prims || !d->j3_matrix)) return JQMC_E_ARG;
   if (d->has_j1 && !d->j1_zeff) return JQMC_E_ARG;
   if (d->ecp_flag && (!d->ecp_maxl1 || !d->ecp_chan || !d->ecp_terms || !d->mesh_points || !d->mesh_weights)) return JQMC_E_ARG;
   if (d->ecp_flag && !(d->nv == 4 || d->nv == 6 || d->nv == 12 || d->nv == 18)) return JQMC_E_ARG;
-  auto check_basis = [](const jqmc_basis_desc& b) {
+  auto check_basis = [M](const jqmc_basis_desc& b) {
+    int prev_atom = -1;
     for (int s = 0; s < b.nshell; ++s) {
       const int* sh = b.shells + 8 * s;
+      if (sh[0] < 0 || sh[0] >= M || sh[0] < prev_atom) return false;  // shells grouped by nucleus
+      prev_atom = sh[0];
       if (sh[1] < 0 || sh[1] > JQMC_LMAX || sh[2] <= 0 || sh[3] < 0 || sh[3] + sh[2] > b.nprim) return false;
       if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) return false;
     }
     return true;
   };
   if (!check_basis(d->det) || (d->has_j3 && !check_basis(d->j3))) return JQMC_E_ARG;
-  for (int s = 0; s < d->det.nshell; ++s)
-    if (d->det.shells[8 * s] < 0 || d->det.shells[8 * s] >= M) return JQMC_E_ARG;
-  if (d->has_j3)
-    for (int s = 0; s < d->j3.nshell; ++s)
-      if (d->j3.shells[8 * s] < 0 || d->j3.shells[8 * s] >= M) return JQMC_E_ARG;
   if (d->ecp_flag)
     for (int a = 0; a < M; ++a) {
       if (d->ecp_maxl1[a] < 0 || d->ecp_maxl1[a] >= kSlots) return JQMC_E_ARG;
@@ -1533,42 +1877,69 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   std::vector<unsigned char> host;
   auto put = [&host](const void* src, size_t bytes) -> size_t {
     const size_t off = (host.size() + 255) & ~size_t(255);
-    host.resize(off + bytes);
+    host.resize(off + (bytes ? bytes : 8));
     if (bytes) memcpy(host.data() + off, src, bytes);
     return off;
   };
   std::vector<double> lamT((size_t)A * A);
+  std::vector<float> lamf((size_t)A * A), lamTf((size_t)A * A);
   for (int a = 0; a < A; ++a)
-    for (int b = 0; b < A; ++b) lamT[(size_t)b * A + a] = d->lambda[(size_t)a * A + b];
+    for (int b = 0; b < A; ++b) {
+      const double v = d->lambda[(size_t)a * A + b];
+      lamT[(size_t)b * A + a] = v;
+      lamf[(size_t)a * A + b] = (float)v;
+      lamTf[(size_t)b * A + a] = (float)v;
+    }
   std::vector<double> j3m, j3mT, j3v;
+  std::vector<float> j3mf, j3mTf;
   if (d->has_j3) {
     j3m.resize((size_t)A3 * A3);
     j3mT.resize((size_t)A3 * A3);
+    j3mf.resize((size_t)A3 * A3);
+    j3mTf.resize((size_t)A3 * A3);
     j3v.resize(A3);
     for (int a = 0; a < A3; ++a) {
       for (int b = 0; b < A3; ++b) {
-        j3m[(size_t)a * A3 + b] = d->j3_matrix[(size_t)a * (A3 + 1) + b];
-        j3mT[(size_t)b * A3 + a] = d->j3_matrix[(size_t)a * (A3 + 1) + b];
+        const double v = d->j3_matrix[(size_t)a * (A3 + 1) + b];
+        j3m[(size_t)a * A3 + b] = v;
+        j3mT[(size_t)b * A3 + a] = v;
+        j3mf[(size_t)a * A3 + b] = (float)v;
+        j3mTf[(size_t)b * A3 + a] = (float)v;
       }
       j3v[a] = d->j3_matrix[(size_t)a * (A3 + 1) + A3];
     }
   }
-  std::vector<double> zero(M, 0.0);
+  auto to_float = [](const double* p, size_t n) { std::vector<float> v(n); for (size_t i = 0; i < n; ++i) v[i] = (float)p[i]; return v; };
+  std::vector<float> dprf = to_float(d->det.prims, (size_t)d->det.nprim * 2);
+  std::vector<float> jprf = d->has_j3 ? to_float(d->j3.prims, (size_t)d->j3.nprim * 2) : std::vector<float>();
+  std::vector<double> zero(2 * M, 0.0);
   std::vector<int> zeroi(M * kSlots * 2 + M, 0);
+  std::vector<double> j1cA(2 * M, 0.0);
+  if (d->has_j1)
+    for (int a = 0; a < M; ++a) {
+      j1cA[2 * a] = pow(2.0 * d->j1_zeff[a], 0.25);
+      j1cA[2 * a + 1] = pow(2.0 * d->j1_zeff[a], 0.75);
+    }
   const size_t o_apos = put(d->atom_pos, (size_t)M * 24);
   const size_t o_az = put(d->atom_zeff, (size_t)M * 8);
   const size_t o_dsh = put(d->det.shells, (size_t)d->det.nshell * 32);
   const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
+  const size_t o_dprf = put(dprf.data(), dprf.size() * 4);
   const size_t o_lam = put(d->lambda, (size_t)A * A * 8);
   const size_t o_lamT = put(lamT.data(), (size_t)A * A * 8);
-  const size_t o_j1z = put(d->has_j1 ? d->j1_zeff : zero.data(), (size_t)M * 8);
-  size_t o_jsh = 0, o_jpr = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0;
+  const size_t o_lamf = put(lamf.data(), (size_t)A * A * 4);
+  const size_t o_lamTf = put(lamTf.data(), (size_t)A * A * 4);
+  const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
+  size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
     o_jsh = put(d->j3.shells, (size_t)d->j3.nshell * 32);
     o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
+    o_jprf = put(jprf.data(), jprf.size() * 4);
     o_j3m = put(j3m.data(), j3m.size() * 8);
     o_j3mT = put(j3mT.data(), j3mT.size() * 8);
     o_j3v = put(j3v.data(), j3v.size() * 8);
+    o_j3mf = put(j3mf.data(), j3mf.size() * 4);
+    o_j3mTf = put(j3mTf.data(), j3mTf.size() * 4);
   }
   const size_t o_maxl1 = put(d->ecp_flag ? d->ecp_maxl1 : zeroi.data(), (size_t)M * 4);
   const size_t o_chan = put(d->ecp_flag ? d->ecp_chan : zeroi.data(), (size_t)M * kSlots * 8);
@@ -1584,24 +1955,26 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     return JQMC_E_CUDA;
   }
   auto dp = [blob](size_t off) { return reinterpret_cast<const double*>(static_cast<unsigned char*>(blob) + off); };
+  auto fp = [blob](size_t off) { return reinterpret_cast<const float*>(static_cast<unsigned char*>(blob) + off); };
   auto ip = [blob](size_t off) { return reinterpret_cast<const int*>(static_cast<unsigned char*>(blob) + off); };
   jqmc_system* sys = new jqmc_system();
   Sys& s = sys->s;
   s.natom = M; s.n_up = d->n_up; s.n_dn = d->n_dn; s.N = d->n_up + d->n_dn;
   s.atom_pos = dp(o_apos); s.atom_zeff = dp(o_az);
   s.det.nshell = d->det.nshell; s.det.nao = A; s.det.nprim = d->det.nprim;
-  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr);
-  s.lam = dp(o_lam); s.lamT = dp(o_lamT);
-  s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_zeff = dp(o_j1z);
+  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf);
+  s.lam = dp(o_lam); s.lamT = dp(o_lamT); s.lamf = fp(o_lamf); s.lamTf = fp(o_lamTf);
+  s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_cA = dp(o_j1z);
   s.has_j2 = d->has_j2; s.j2_type = d->j2_type; s.j2_param = d->j2_param;
   s.has_j3 = d->has_j3;
   if (d->has_j3) {
     s.j3.nshell = d->j3.nshell; s.j3.nao = A3; s.j3.nprim = d->j3.nprim;
-    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr);
-    s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v);
+    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf);
+    s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v); s.j3matf = fp(o_j3mf); s.j3matTf = fp(o_j3mTf);
   } else {
-    s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr;
+    s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr; s.j3.primsf = nullptr;
     s.j3mat = s.j3matT = s.j3vec = nullptr;
+    s.j3matf = s.j3matTf = nullptr;
   }
   s.ecp_flag = d->ecp_flag;
   s.ecp_maxl1 = ip(o_maxl1); s.ecp_chan = ip(o_chan);
@@ -1621,11 +1994,13 @@ int jqmc_system_destroy(jqmc_system* sys) {
   return JQMC_OK;
 }
 
-int64_t jqmc_walker_bytes(const jqmc_system* sys) {
-  if (!sys) return JQMC_E_ARG;
+int64_t jqmc_walker_bytes(const jqmc_system* sys, int32_t precision) {
+  if (!sys || (precision != JQMC_PREC_FP64 && precision != JQMC_PREC_MIXED)) return JQMC_E_ARG;
   const Sys& s = sys->s;
   const int64_t n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
-  return 8 * (N * 3 + 2 * n * n + 2 * n * A + N * A3) + 4;
+  const int64_t tb = precision == JQMC_PREC_MIXED ? 4 : 8;
+  return 8 * N * 3 + tb * (2 * n * n + 2 * n * A + N * A3 + N * 4 * A + N * 5 * A3) + 4 +
+         (precision == JQMC_PREC_MIXED ? 8 * 2 * n * A : 0);
 }
 
 int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_t npts, double* d_out, void* stream) {
@@ -1641,18 +2016,29 @@ int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream
   if (!walkers_ok(sys, w)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
   const Sys& s = sys->s;
-  const int off_aug = P.wl.bytes;
-  const int off_phi3 = align16(off_aug + s.n_up * 2 * s.n_up * 8);
-  const int smem = align16(off_phi3 + (s.has_j3 ? s.N * s.j3.nao * 8 : 0));
-  int rc = launch_check((const void*)k_walker_init, smem);
-  if (rc) return rc;
-  k_walker_init<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, off_phi3);
+  const int n = s.n_up, A3 = s.has_j3 ? s.j3.nao : 1;
+  const int off_Gd = P.wl.bytes;
+  const int off_aug = align16(off_Gd + n * n * 8);
+  const int off_vec = align16(off_aug + n * 2 * n * 8);
+  const int vec_len = (s.det.nao + n > 3 * A3) ? s.det.nao + n : 3 * A3;
+  const int off_phi3 = align16(off_vec + vec_len * 8);
+  const int smem = align16(off_phi3 + (s.has_j3 ? s.N * A3 * 8 : 0));
+  if (w->precision == JQMC_PREC_MIXED) {
+    int rc = launch_check((const void*)k_walker_init<float>, smem);
+    if (rc) return rc;
+    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3);
+  } else {
+    int rc = launch_check((const void*)k_walker_init<double>, smem);
+    if (rc) return rc;
+    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3);
+  }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
 int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow,
                  void* stream) {
   if (!walkers_ok(sys, w) || !d_logdet || !d_sign || !d_jastrow) return JQMC_E_ARG;
+  if (w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
   const int off_aug = P.wl.bytes;
   const int smem = align16(off_aug + sys->s.n_up * sys->s.n_up * 8);
@@ -1665,6 +2051,7 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
 int jqmc_vmc_sweep(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const int32_t* d_idraw,
                    const double* d_fdraw, double Dt, double eps_AS, int32_t* d_accept, void* stream) {
   if (!walkers_ok(sys, w) || K < 0 || !d_idraw || !d_fdraw || !d_accept) return JQMC_E_ARG;
+  if (w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
   if (K == 0) return JQMC_OK;
   KParams P = make_params(sys, w);
   const int off_cand = P.wl.bytes;
@@ -1678,6 +2065,7 @@ int jqmc_vmc_sweep(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, con
 int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double eps_AS,
                      double* d_eL, double* d_wL, void* stream) {
   if (!walkers_ok(sys, w) || !d_angles || !d_eL || !d_wL) return JQMC_E_ARG;
+  if (w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
   const int smem = P.ml.bytes;
   int rc = launch_check((const void*)k_vmc_measure, smem);
@@ -1690,23 +2078,13 @@ int jqmc_lrdmc_project(const jqmc_system* sys, const jqmc_walkers* w, int32_t K,
                        double E_scf, double* d_w, void* stream) {
   if (!walkers_ok(sys, w) || K < 0 || !d_draw || !d_w || !(alat > 0.0)) return JQMC_E_ARG;
   if (K == 0) return JQMC_OK;
-  KParams P = make_params(sys, w);
-  const int smem = P.ml.bytes;
-  int rc = launch_check((const void*)k_lrdmc, smem);
-  if (rc) return rc;
-  k_lrdmc<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, nullptr, nullptr);
-  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+  return launch_lrdmc(sys, w, K, d_draw, alat, E_scf, d_w, nullptr, nullptr, stream);
 }
 
 int jqmc_lrdmc_energy(const jqmc_system* sys, const jqmc_walkers* w, const double* d_draw, double alat, double* d_eL,
                       double* d_vdiag, void* stream) {
   if (!walkers_ok(sys, w) || !d_draw || !d_eL || !d_vdiag || !(alat > 0.0)) return JQMC_E_ARG;
-  KParams P = make_params(sys, w);
-  const int smem = P.ml.bytes;
-  int rc = launch_check((const void*)k_lrdmc, smem);
-  if (rc) return rc;
-  k_lrdmc<<<w->nwalk, 128, smem, S(stream)>>>(P, 0, d_draw, alat, 0.0, nullptr, d_eL, d_vdiag);
-  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+  return launch_lrdmc(sys, w, 0, d_draw, alat, 0.0, nullptr, d_eL, d_vdiag, stream);
 }
 
 int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, double* d_cum, void* stream) {
@@ -1719,17 +2097,26 @@ int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_c
 int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jqmc_walkers* dst, const int32_t* d_chosen,
                        void* stream) {
   if (!walkers_ok(sys, src) || !walkers_ok(sys, dst) || !d_chosen || src->nwalk != dst->nwalk) return JQMC_E_ARG;
+  if (src->precision != dst->precision) return JQMC_E_ARG;
   const Sys& s = sys->s;
   const int W = src->nwalk;
   const long long n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
   const int grid = 4 * 152, bs = 256;
-  k_gather<<<grid, bs, 0, S(stream)>>>(src->r, dst->r, N * 3, d_chosen, W);
-  k_gather<<<grid, bs, 0, S(stream)>>>(src->G, dst->G, n * n, d_chosen, W);
-  k_gather<<<grid, bs, 0, S(stream)>>>(src->Ginv, dst->Ginv, n * n, d_chosen, W);
-  k_gather<<<grid, bs, 0, S(stream)>>>(src->Tup, dst->Tup, n * A, d_chosen, W);
-  k_gather<<<grid, bs, 0, S(stream)>>>(src->Tdn, dst->Tdn, n * A, d_chosen, W);
-  if (A3) k_gather<<<grid, bs, 0, S(stream)>>>(src->h3, dst->h3, N * A3, d_chosen, W);
-  k_gather_int<<<(W + 255) / 256, 256, 0, S(stream)>>>(src->status, dst->status, d_chosen, W);
+  k_gather<double><<<grid, bs, 0, S(stream)>>>(src->r, dst->r, N * 3, d_chosen, W);
+  auto tab = [&](const void* a, void* b, long long per) {
+    if (src->precision == JQMC_PREC_MIXED)
+      k_gather<float><<<grid, bs, 0, S(stream)>>>(static_cast<const float*>(a), static_cast<float*>(b), per, d_chosen, W);
+    else
+      k_gather<double><<<grid, bs, 0, S(stream)>>>(static_cast<const double*>(a), static_cast<double*>(b), per, d_chosen, W);
+  };
+  tab(src->G, dst->G, n * n);
+  tab(src->Ginv, dst->Ginv, n * n);
+  tab(src->Tup, dst->Tup, n * A);
+  tab(src->Tdn, dst->Tdn, n * A);
+  if (A3) tab(src->h3, dst->h3, N * A3);
+  tab(src->dphi, dst->dphi, N * 4 * A);
+  if (A3) tab(src->dphi3, dst->dphi3, N * 5 * A3);
+  k_gather<int><<<(W + 255) / 256, 256, 0, S(stream)>>>(src->status, dst->status, 1, d_chosen, W);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
@@ -1737,6 +2124,14 @@ int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops
   if (iters <= 0 || blocks <= 0 || !d_sink || !flops) return JQMC_E_ARG;
   const int bs = 256;
   k_probe_fp64<<<blocks, bs, 0, S(stream)>>>(iters, d_sink);
+  *flops = 2.0 * 8.0 * (double)iters * (double)blocks * bs;
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_probe_fp32(int64_t iters, int32_t blocks, float* d_sink, double* flops, void* stream) {
+  if (iters <= 0 || blocks <= 0 || !d_sink || !flops) return JQMC_E_ARG;
+  const int bs = 256;
+  k_probe_fp32<<<blocks, bs, 0, S(stream)>>>(iters, d_sink);
   *flops = 2.0 * 8.0 * (double)iters * (double)blocks * bs;
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }

@@ -10,16 +10,16 @@ raises.
 from __future__ import annotations
 
 import ctypes as C
-from math import comb
 
 import numpy as np
 import torch
 
 from . import _lib
-from .atomic_orbital import L_MAX, primitive_norm
+from .atomic_orbital import primitive_norm
 from .coulomb_potential import ECP_MESHES
 from .hamiltonians import Hamiltonian_data
-from .molecular_orbital import MOs_data
+
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
 
 
 def _ptr(a: np.ndarray, ctype):
@@ -160,8 +160,8 @@ class GpuSystem:
     def stream(self):
         return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
-    def walker_bytes(self) -> int:
-        return int(_lib.lib().jqmc_walker_bytes(self.handle))
+    def walker_bytes(self, precision: str = "fp64") -> int:
+        return int(_lib.lib().jqmc_walker_bytes(self.handle, PRECISIONS[precision]))
 
     def ao_vgl(self, points: torch.Tensor, basis: int = 0) -> torch.Tensor:
         """(5, nao, P) value/grad/lap of the geminal (0) or J3 (1) basis at points (P, 3)."""
@@ -174,23 +174,36 @@ class GpuSystem:
 
 
 class WalkerSet:
-    """Per-walker state tensors (layout of jqmc_walkers in include/jqmc_gpu.h)."""
+    """Per-walker state tensors (layout of jqmc_walkers in include/jqmc_gpu.h).
 
-    def __init__(self, system: GpuSystem, r_up, r_dn):
+    precision "fp64": every table double (the plain drop-in);
+    precision "mixed": G, G^-1, T tables and the J3 field in float, rebuilt in
+    double from the positions by ``init`` (an FP64 scratch of 2 n A doubles per
+    walker is held for that rebuild)."""
+
+    def __init__(self, system: GpuSystem, r_up, r_dn, precision: str = "fp64", scratch: torch.Tensor | None = None):
         self.sys = system
+        self.precision = precision
         dev = system.device
         r_up = torch.as_tensor(np.asarray(r_up), dtype=torch.float64)
         r_dn = torch.as_tensor(np.asarray(r_dn), dtype=torch.float64)
         W = r_up.shape[0]
         n, N, A, A3 = system.n_up, system.N, system.A, system.A3
+        tdt = torch.float64 if precision == "fp64" else torch.float32
         self.nwalk = W
         self.r = torch.cat([r_up, r_dn], dim=1).to(dev).contiguous()
-        self.G = torch.empty((W, n, n), dtype=torch.float64, device=dev)
+        self.G = torch.empty((W, n, n), dtype=tdt, device=dev)
         self.Ginv = torch.empty_like(self.G)
-        self.Tup = torch.empty((W, n, A), dtype=torch.float64, device=dev)
+        self.Tup = torch.empty((W, n, A), dtype=tdt, device=dev)
         self.Tdn = torch.empty_like(self.Tup)
-        self.h3 = torch.zeros((W, N, max(A3, 1)), dtype=torch.float64, device=dev)
+        self.h3 = torch.zeros((W, N, max(A3, 1)), dtype=tdt, device=dev)
+        self.dphi = torch.empty((W, N, 4, A), dtype=tdt, device=dev)
+        self.dphi3 = torch.empty((W, N, 5, max(A3, 1)), dtype=tdt, device=dev)
         self.status = torch.zeros(W, dtype=torch.int32, device=dev)
+        if precision == "mixed":
+            self.scratch = scratch if scratch is not None else torch.empty((W, 2, n, A), dtype=torch.float64, device=dev)
+        else:
+            self.scratch = None
         self.init()
 
     @classmethod
@@ -198,15 +211,19 @@ class WalkerSet:
         obj = cls.__new__(cls)
         obj.sys = other.sys
         obj.nwalk = other.nwalk
-        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "status"):
+        obj.precision = other.precision
+        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "status"):
             setattr(obj, name, torch.empty_like(getattr(other, name)))
+        obj.scratch = other.scratch   # the rebuild scratch is shared: it holds no state between calls
         return obj
 
     def desc(self) -> _lib.Walkers:
         d = _lib.Walkers()
         d.nwalk = self.nwalk
-        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "status"):
+        d.precision = PRECISIONS[self.precision]
+        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "status"):
             setattr(d, name, C.c_void_p(getattr(self, name).data_ptr()))
+        d.scratch = C.c_void_p(self.scratch.data_ptr()) if self.scratch is not None else None
         return d
 
     @property

@@ -32,7 +32,7 @@ class GFMC_n:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, num_walkers: int = 40, num_mcmc_per_measurement: int = 16,
                  mcmc_seed: int = 34467, E_scf: float = 0.0, alat: float = 0.1, random_discretized_mesh: bool = True,
                  non_local_move: str = "tmove", num_gfmc_collect_steps: int = 5, Nv: int = 6,
-                 init_r_up=None, init_r_dn=None, rebuild_after_branching: bool = True):
+                 init_r_up=None, init_r_dn=None, rebuild_after_branching: bool = True, precision: str = "fp64"):
         if non_local_move != "tmove":
             raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
         hamiltonian_data.sanity_check()
@@ -50,7 +50,8 @@ class GFMC_n:
             coul = hamiltonian_data.coulomb_potential_data
             init_r_up, init_r_dn = initial_electrons(st.positions, coul.effective_charges, self.sys.n_up, self.sys.n_dn,
                                                      num_walkers, mcmc_seed)
-        self.walkers = WalkerSet(self.sys, init_r_up, init_r_dn)
+        self.precision = precision
+        self.walkers = WalkerSet(self.sys, init_r_up, init_r_dn, precision=precision)
         self._spare = WalkerSet.empty_like(self.walkers)
         dev = self.sys.device
         self.gen = torch.Generator(device=dev)

@@ -37,6 +37,22 @@ def ao_vgl_flops(shells: np.ndarray) -> float:
     return f
 
 
+def lrdmc_step_split(gs, ecp_fraction: float):
+    """(mesh + move ops, electron-term ops) of one projection of one walker: the
+    first part runs in float in the mixed form, the second stays in double."""
+    keep = gs._keep
+    N, n, A, M = gs.N, gs.n_up, gs.A, len(keep["pos"])
+    A3 = gs.A3
+    det_p = ao_point_flops(keep["dsh"])
+    j3_p = ao_point_flops(keep["jsh"]) if A3 else 0.0
+    ratio = det_p + j3_p + M * (8 + EXP_FLOPS + 6) + N * 12 + EXP_FLOPS + 3
+    mesh = 6 * N * (ratio + 8) + gs.Nv * N * ecp_fraction * (ratio + 40 + 2 * EXP_FLOPS)
+    move = 2 * (det_p + j3_p) + 4 * A * n + 4 * n * n + 2 * A * A + 6 * A * n + 4 * n * n + 4 * A3 * A3 + N * A3
+    elec = N * (ao_vgl_flops(keep["dsh"]) + (ao_vgl_flops(keep["jsh"]) if A3 else 0.0) + M * (30 + EXP_FLOPS) + N * 27)
+    sums = 6 * N * 6 + N * N * 5 + N * M * (12 + EXP_FLOPS) + 12 * N * 3
+    return mesh + move, elec + sums
+
+
 def lrdmc_step_flops(gs, ecp_fraction: float) -> float:
     """FP64 operations of one GFMC_n projection of one walker (jqmc_gb300 kernels)."""
     keep = gs._keep
