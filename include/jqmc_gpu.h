@@ -31,6 +31,7 @@ extern "C" {
 #define JQMC_MAX_NUP 128
 #define JQMC_MAX_AO 4096
 #define JQMC_MAX_ATOM 512
+#define JQMC_ECACHE_STRIDE 24 /* doubles per electron in the energy cache    */
 
 /* Walker status bits (per walker, OR-ed by the kernels). */
 #define JQMC_ST_SINGULAR 1    /* zero pivot while inverting G                */
@@ -97,6 +98,9 @@ typedef struct {
                       /* AO at each electron (kept current by every move)       */
   void* dphi3;        /* nwalk*N*5*A3: value, grad x, y, z, Laplacian of the J3  */
                       /* AOs at each electron (unused if no J3)                  */
+  double* ecache;     /* nwalk*(N+1)*JQMC_ECACHE_STRIDE: per-electron e-ion and  */
+                      /* local-ECP energies, J1/J2 grad/lap, nearest nucleus and */
+                      /* non-local channel values; last row: e-e Coulomb total   */
   double* scratch;    /* JQMC_PREC_MIXED: nwalk*2*n*A doubles used by the FP64   */
                       /* rebuild in jqmc_walker_init; unused for JQMC_PREC_FP64  */
   int32_t* status;    /* nwalk JQMC_ST_* bits                                    */

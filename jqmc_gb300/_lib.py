@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libjqmc_gpu.so")
 JQMC_OK = 0
 ERRORS = {-1: "bad argument", -2: "size above a compiled maximum", -3: "CUDA runtime error", -4: "shared-memory footprint too large"}
 ECP_SLOTS = 8
+ECACHE_STRIDE = 24
 MAX_NUP = 128
 
 ST_SINGULAR, ST_ZERO_RATIO, ST_NAN = 1, 2, 4
@@ -43,7 +44,7 @@ class SystemDesc(C.Structure):
 
 class Walkers(C.Structure):
     _fields_ = [("nwalk", i32), ("precision", i32), ("r", vp), ("G", vp), ("Ginv", vp), ("Tup", vp), ("Tdn", vp), ("h3", vp),
-                ("dphi", vp), ("dphi3", vp), ("scratch", vp), ("status", vp)]
+                ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("status", vp)]
 
 
 PREC_FP64, PREC_MIXED = 0, 1

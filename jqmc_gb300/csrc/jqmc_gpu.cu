@@ -47,6 +47,25 @@ namespace {
 constexpr int kSlots = JQMC_ECP_SLOTS;
 constexpr int kRed = 64;  // doubles of reduction scratch
 
+// Per-electron energy cache (double): quantities that depend on one electron's
+// position, or on its pairs, kept current by every move instead of being
+// recomputed each step.  Row e (kEC doubles) per electron, then one row of
+// walker totals.
+constexpr int kEC = JQMC_ECACHE_STRIDE;
+enum {
+  EC_EI = 0,     // electron-ion Coulomb of electron e
+  EC_ELOC = 1,   // local ECP channel of electron e, summed over nuclei
+  EC_J1G = 2,    // grad J1 (3)
+  EC_J1L = 5,    // lap J1
+  EC_J2G = 6,    // grad J2 (3)
+  EC_J2L = 9,    // lap J2
+  EC_NEAR = 10,  // nearest nucleus (as double)
+  EC_DIST = 11,  // distance to it
+  EC_VL = 12,    // non-local channel values V_l at the nearest nucleus (kSlots)
+  EC_TOT_EE = 0  // totals row: e-e Coulomb
+};
+static_assert(EC_VL + kSlots <= kEC, "energy cache row too short");
+
 template <class R>
 struct Num;
 template <>
@@ -137,6 +156,7 @@ __device__ __forceinline__ const float* j3mT_of<float>(const Sys& s) { return s.
 struct WS {
   double* r;
   void *G, *Ginv, *Tup, *Tdn, *h3, *dphi, *dphi3;
+  double* ecache;
   double* scratch;
   int* status;
 };
@@ -640,6 +660,90 @@ __device__ float j12_delta_rel(const Sys& s, const float* dAe, const float* dEe,
   return acc;
 }
 
+// J2 pair function derivatives f'(d), f''(d)
+__device__ __forceinline__ void j2_pair_d(const Sys& s, double d, double& f1, double& f2) {
+  const double b = s.j2_param;
+  if (s.j2_type == 0) {
+    const double q = 1.0 + b * d;
+    f1 = 1.0 / (2.0 * q * q);
+    f2 = -b / (q * q * q);
+  } else {
+    const double ex = exp(-b * d);
+    f1 = 0.5 * ex;
+    f2 = -0.5 * b * ex;
+  }
+}
+
+// The one-electron fields of an energy-cache row at (x, y, z): e-ion Coulomb
+// (coulomb_potential.py:2285-2328), local ECP (coulomb_potential.py:1145-1246),
+// grad/lap J1 (jastrow_factor.py:961-1034), nearest nucleus and the non-local
+// channel values there (coulomb_potential.py:1478-1712 with NN = 1).
+__device__ void ecache_single(const Sys& s, double x, double y, double z, double* row) {
+  double ei = 0.0, eloc = 0.0, gx = 0.0, gy = 0.0, gz = 0.0, lap = 0.0, bd = 1e300;
+  int best = 0;
+  for (int a = 0; a < s.natom; ++a) {
+    const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (d < bd) { bd = d; best = a; }
+    ei += -s.atom_zeff[a] / d;
+    if (s.ecp_flag) eloc += ecp_channel(s, a, s.ecp_maxl1[a], d);
+    if (s.has_j1) {
+      const double aa = s.j1_param, c = s.j1_cA[2 * a], AA = s.j1_cA[2 * a + 1];
+      double f1, f2;
+      if (s.j1_type == 0) {
+        const double ex = exp(-aa * c * d);
+        f1 = -AA * c * ex / 2.0;
+        f2 = AA * aa * c * c * ex / 2.0;
+      } else {
+        const double q = 1.0 + aa * c * d;
+        f1 = -AA / (2.0 * q * q);
+        f2 = AA * aa * c / (q * q * q);
+      }
+      gx += f1 * dx / d; gy += f1 * dy / d; gz += f1 * dz / d;
+      lap += f2 + 2.0 * f1 / d;
+    }
+  }
+  row[EC_EI] = ei;
+  row[EC_ELOC] = eloc;
+  row[EC_J1G] = gx; row[EC_J1G + 1] = gy; row[EC_J1G + 2] = gz;
+  row[EC_J1L] = lap;
+  row[EC_NEAR] = (double)best;
+  row[EC_DIST] = bd;
+  const int lmax = s.ecp_flag ? s.ecp_maxl1[best] : 0;
+  for (int l = 0; l < kSlots; ++l) row[EC_VL + l] = l < lmax ? ecp_channel(s, best, l, bd) : 0.0;
+}
+
+// Fill the whole energy cache of one walker from its positions (block-cooperative).
+__device__ void ecache_init(const Sys& s, const double* r, double* ec, double* red) {
+  const int N = s.N;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) {
+    double* row = ec + (size_t)e * kEC;
+    ecache_single(s, r[3 * e], r[3 * e + 1], r[3 * e + 2], row);
+    double gx = 0.0, gy = 0.0, gz = 0.0, lap = 0.0;
+    if (s.has_j2)
+      for (int m = 0; m < N; ++m) {
+        if (m == e) continue;
+        const double dx = r[3 * e] - r[3 * m], dy = r[3 * e + 1] - r[3 * m + 1], dz = r[3 * e + 2] - r[3 * m + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        double f1, f2;
+        j2_pair_d(s, d, f1, f2);
+        gx += f1 * dx / d; gy += f1 * dy / d; gz += f1 * dz / d;
+        lap += f2 + 2.0 * f1 / d;
+      }
+    row[EC_J2G] = gx; row[EC_J2G + 1] = gy; row[EC_J2G + 2] = gz;
+    row[EC_J2L] = lap;
+  }
+  double ee = 0.0;
+  for (int p = threadIdx.x; p < N * N; p += blockDim.x) {
+    const int a = p / N, b = p % N;
+    if (b <= a) continue;
+    const double dx = r[3 * a] - r[3 * b], dy = r[3 * a + 1] - r[3 * b + 1], dz = r[3 * a + 2] - r[3 * b + 2];
+    ee += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+  }
+  ee = block_sum(ee, red);
+  if (threadIdx.x == 0) ec[(size_t)N * kEC + EC_TOT_EE] = ee;
+}
+
 // ------------------------------------------------------------------ per-walker workspace
 template <class Tab>
 struct Work {
@@ -653,6 +757,7 @@ struct Work {
   Tab* h3;
   Tab* dphi;     // global: N x 4 x A  (grad x, y, z, lap of the geminal AOs at each electron)
   Tab* dphi3;    // global: N x 5 x A3 (value, grad x, y, z, lap of the J3 AOs at each electron)
+  double* ec;    // global: (N + 1) x kEC energy cache
   Tab* vA0;      // A (shared)
   Tab* vA1;
   Tab* vA2;
@@ -715,6 +820,7 @@ __device__ Work<Tab> make_work(const Sys& s, const WorkLayout& L, unsigned char*
   k.h3 = s.has_j3 ? static_cast<Tab*>(ws.h3) + (size_t)w * k.N * k.A3 : nullptr;
   k.dphi = static_cast<Tab*>(ws.dphi) + (size_t)w * k.N * 4 * k.A;
   k.dphi3 = s.has_j3 ? static_cast<Tab*>(ws.dphi3) + (size_t)w * k.N * 5 * k.A3 : nullptr;
+  k.ec = ws.ecache + (size_t)w * (k.N + 1) * kEC;
   return k;
 }
 
@@ -884,6 +990,45 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     }
   }
   fill_dtables<Tab>(s, px, py, pz, k.dphi + (size_t)e * 4 * A, s.has_j3 ? k.dphi3 + (size_t)e * 5 * A3 : nullptr);
+  // energy cache: every pair with the moved electron (J2 terms of the partner,
+  // e-e Coulomb), then the moved electron's own row
+  {
+    const int N = k.N;
+    double dee = 0.0, jgx = 0.0, jgy = 0.0, jgz = 0.0, jl = 0.0;
+    for (int m = threadIdx.x; m < N; m += blockDim.x) {
+      if (m == e) continue;
+      const double mx = k.r[3 * m], my = k.r[3 * m + 1], mz = k.r[3 * m + 2];
+      const double oxm = mx - ox, oym = my - oy, ozm = mz - oz;      // r_m - r_e(old)
+      const double nxm = mx - px, nym = my - py, nzm = mz - pz;      // r_m - r_e(new)
+      const double dold = sqrt(oxm * oxm + oym * oym + ozm * ozm);
+      const double dnew = sqrt(nxm * nxm + nym * nym + nzm * nzm);
+      dee += 1.0 / dnew - 1.0 / dold;
+      if (s.has_j2) {
+        double f1o, f2o, f1n, f2n;
+        j2_pair_d(s, dold, f1o, f2o);
+        j2_pair_d(s, dnew, f1n, f2n);
+        double* row = k.ec + (size_t)m * kEC;
+        row[EC_J2G] += f1n * nxm / dnew - f1o * oxm / dold;
+        row[EC_J2G + 1] += f1n * nym / dnew - f1o * oym / dold;
+        row[EC_J2G + 2] += f1n * nzm / dnew - f1o * ozm / dold;
+        row[EC_J2L] += (f2n + 2.0 * f1n / dnew) - (f2o + 2.0 * f1o / dold);
+        jgx -= f1n * nxm / dnew; jgy -= f1n * nym / dnew; jgz -= f1n * nzm / dnew;
+        jl += f2n + 2.0 * f1n / dnew;
+      }
+    }
+    dee = block_sum(dee, k.red);
+    jgx = block_sum(jgx, k.red);
+    jgy = block_sum(jgy, k.red);
+    jgz = block_sum(jgz, k.red);
+    jl = block_sum(jl, k.red);
+    if (threadIdx.x == 0) {
+      double* row = k.ec + (size_t)e * kEC;
+      ecache_single(s, px, py, pz, row);
+      row[EC_J2G] = jgx; row[EC_J2G + 1] = jgy; row[EC_J2G + 2] = jgz;
+      row[EC_J2L] = jl;
+      k.ec[(size_t)N * kEC + EC_TOT_EE] += dee;
+    }
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     k.r[3 * e] = px;
@@ -954,9 +1099,11 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
 }
 
 // Phase A: per-electron continuum kinetic energy and the old-position values
-// the ratios need (wavefunction.py:1142-1207, jastrow_factor.py:961-1034,
+// the ratios need (wavefunction.py:1142-1207 with jastrow_factor.py:961-1034,
 // 3435-3558, 4077-4156).  One warp per electron: the cached AO derivative tables
-// are dotted with the electron's T row and J3 field in double; J1/J2 in double.
+// are dotted with the electron's T row and J3 field (lane sums in the table
+// type, warp sum in double); J1/J2 derivatives, Coulomb and ECP terms come from
+// the energy cache.
 template <class Tab>
 __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   const Sys& s = k.s;
@@ -976,93 +1123,53 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   for (int e = wid; e < k.N; e += nw) {
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
-    const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
     const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
     const Tab* dp = k.dphi + (size_t)e * 4 * A;
-    double gx = 0, gy = 0, gz = 0, lp = 0;
+    Tab tgx = Tab(0), tgy = Tab(0), tgz = Tab(0), tlp = Tab(0);
     for (int a = lane; a < A; a += 32) {
-      const double tv = (double)Trow[a];
-      gx += (double)dp[a] * tv;
-      gy += (double)dp[A + a] * tv;
-      gz += (double)dp[2 * A + a] * tv;
-      lp += (double)dp[3 * A + a] * tv;
+      const Tab tv = Trow[a];
+      tgx += dp[a] * tv;
+      tgy += dp[A + a] * tv;
+      tgz += dp[2 * A + a] * tv;
+      tlp += dp[3 * A + a] * tv;
     }
-    double c3 = 0, hx = 0, hy = 0, hz = 0, hl = 0;
+    Tab tc3 = Tab(0), thx = Tab(0), thy = Tab(0), thz = Tab(0), thl = Tab(0);
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
       for (int a = lane; a < A3; a += 32) {
-        const double hv = (double)h[a];
-        c3 += (double)q[a] * hv;
-        hx += (double)q[A3 + a] * hv;
-        hy += (double)q[2 * A3 + a] * hv;
-        hz += (double)q[3 * A3 + a] * hv;
-        hl += (double)q[4 * A3 + a] * hv;
+        const Tab hv = h[a];
+        tc3 += q[a] * hv;
+        thx += q[A3 + a] * hv;
+        thy += q[2 * A3 + a] * hv;
+        thz += q[3 * A3 + a] * hv;
+        thl += q[4 * A3 + a] * hv;
       }
     }
-    double jx = 0, jy = 0, jz = 0, jl = 0;
-    if (s.has_j1)
-      for (int a = lane; a < s.natom; a += 32) {
-        const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
-        const double d = sqrt(dx * dx + dy * dy + dz * dz);
-        const double aa = s.j1_param, c = s.j1_cA[2 * a], AA = s.j1_cA[2 * a + 1];
-        double f1, f2;
-        if (s.j1_type == 0) {
-          const double ex = exp(-aa * c * d);
-          f1 = -AA * c * ex / 2.0;
-          f2 = AA * aa * c * c * ex / 2.0;
-        } else {
-          const double q = 1.0 + aa * c * d;
-          f1 = -AA / (2.0 * q * q);
-          f2 = AA * aa * c / (q * q * q);
-        }
-        jx += f1 * dx / d; jy += f1 * dy / d; jz += f1 * dz / d;
-        jl += f2 + 2.0 * f1 / d;
-      }
-    if (s.has_j2) {
-      const double b = s.j2_param;
-      for (int m = lane; m < k.N; m += 32) {
-        if (m == e) continue;
-        const double dx = x - k.r[3 * m], dy = y - k.r[3 * m + 1], dz = z - k.r[3 * m + 2];
-        const double d = sqrt(dx * dx + dy * dy + dz * dz);
-        double f1, f2;
-        if (s.j2_type == 0) {
-          const double q = 1.0 + b * d;
-          f1 = 1.0 / (2.0 * q * q);
-          f2 = -b / (q * q * q);
-        } else {
-          const double ex = exp(-b * d);
-          f1 = 0.5 * ex;
-          f2 = -0.5 * b * ex;
-        }
-        jx += f1 * dx / d; jy += f1 * dy / d; jz += f1 * dz / d;
-        jl += f2 + 2.0 * f1 / d;
-      }
-    }
-    gx = warp_sum(gx); gy = warp_sum(gy); gz = warp_sum(gz); lp = warp_sum(lp);
-    c3 = warp_sum(c3); hx = warp_sum(hx); hy = warp_sum(hy); hz = warp_sum(hz); hl = warp_sum(hl);
-    jx = warp_sum(jx); jy = warp_sum(jy); jz = warp_sum(jz); jl = warp_sum(jl);
+    const double gx = warp_sum((double)tgx), gy = warp_sum((double)tgy), gz = warp_sum((double)tgz);
+    const double lp = warp_sum((double)tlp);
+    const double c3 = warp_sum((double)tc3), hx = warp_sum((double)thx), hy = warp_sum((double)thy);
+    const double hz = warp_sum((double)thz), hl = warp_sum((double)thl);
     if (lane == 0) {
-      const double Gx = gx + hx + jx, Gy = gy + hy + jy, Gz = gz + hz + jz;
-      const double L = lp - (gx * gx + gy * gy + gz * gz) + hl + jl;
-      double ei = 0.0, eid = 0.0, bd = 1e300;
-      int best = 0;
-      for (int a = 0; a < s.natom; ++a) {
-        const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
-        const double d = sqrt(dx * dx + dy * dy + dz * dz);
-        if (d < bd) { bd = d; best = a; }
-        ei += -s.atom_zeff[a] / d;
-        eid += -s.atom_zeff[a] / fmax(d, alat);
-      }
+      const double* row = k.ec + (size_t)e * kEC;
+      const double Gx = gx + hx + row[EC_J1G] + row[EC_J2G];
+      const double Gy = gy + hy + row[EC_J1G + 1] + row[EC_J2G + 1];
+      const double Gz = gz + hz + row[EC_J1G + 2] + row[EC_J2G + 2];
+      const double L = lp - (gx * gx + gy * gy + gz * gz) + hl + row[EC_J1L] + row[EC_J2L];
       t.ke[e] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
       t.c3[e] = c3;
-      t.ei[e] = ei;
-      t.eid[e] = eid;
-      t.eatom[e] = best;
-      t.edist[e] = bd;
-      if (s.ecp_flag) {
-        const int lmax = s.ecp_maxl1[best];
-        for (int l = 0; l < kSlots; ++l) t.vl[e * kSlots + l] = l < lmax ? ecp_channel(s, best, l, bd) : 0.0;
+      t.ei[e] = row[EC_EI];
+      t.eatom[e] = (int)row[EC_NEAR];
+      t.edist[e] = row[EC_DIST];
+      for (int l = 0; l < kSlots; ++l) t.vl[e * kSlots + l] = row[EC_VL + l];
+      if (!s.ecp_flag) {
+        const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
+        double eid = 0.0;
+        for (int a = 0; a < s.natom; ++a) {
+          const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+          eid += -s.atom_zeff[a] / fmax(sqrt(dx * dx + dy * dy + dz * dz), alat);
+        }
+        t.eid[e] = eid;
       }
     }
   }
@@ -1132,36 +1239,10 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
   __syncthreads();
 }
 
-// e-e Coulomb, block-reduced
-__device__ double coulomb_ee(const double* r, int N, double* red) {
-  double acc = 0.0;
-  for (int p = threadIdx.x; p < N * N; p += blockDim.x) {
-    const int a = p / N, b = p % N;
-    if (b <= a) continue;
-    const double dx = r[3 * a] - r[3 * b], dy = r[3 * a + 1] - r[3 * b + 1], dz = r[3 * a + 2] - r[3 * b + 2];
-    acc += 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
-  }
-  return block_sum(acc, red);
-}
-
-// local ECP channel summed over electrons and nuclei (coulomb_potential.py:1145-1246)
-__device__ double ecp_local_sum(const Sys& s, const double* r, int N, double* red) {
-  double acc = 0.0;
-  if (s.ecp_flag) {
-    for (int p = threadIdx.x; p < N * s.natom; p += blockDim.x) {
-      const int e = p / s.natom, a = p % s.natom;
-      const double dx = r[3 * e] - s.atom_pos[3 * a], dy = r[3 * e + 1] - s.atom_pos[3 * a + 1],
-                   dz = r[3 * e + 2] - s.atom_pos[3 * a + 2];
-      acc += ecp_channel(s, a, s.ecp_maxl1[a], sqrt(dx * dx + dy * dy + dz * dz));
-    }
-  }
-  return block_sum(acc, red);
-}
-
 // Phase C of the GFMC_n step: (diag, nondiag) sums (jqmc_gfmc.py:4806-5030).
-__device__ void lrdmc_sums(const Sys& s, const double* r, int N, double* red, Terms& t, double alat, double* diag_out,
+__device__ void lrdmc_sums(const Sys& s, const double* ec, int N, double* red, Terms& t, double alat, double* diag_out,
                            double* nondiag_out) {
-  double fn = 0.0, sp = 0.0, opt = 0.0;
+  double fn = 0.0, sp = 0.0, opt = 0.0, loc = 0.0;
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
     bool flip = false;
     double nd = 0.0;
@@ -1175,6 +1256,7 @@ __device__ void lrdmc_sums(const Sys& s, const double* r, int N, double* red, Te
     const double zv = t.ei[e] + t.ke[e] - nd;
     const double eu = s.ecp_flag ? t.ei[e] : t.eid[e];
     opt += flip ? fmax(zv, eu) : zv;
+    loc += ec[(size_t)e * kEC + EC_ELOC];
   }
   double vfn = 0.0, vsp = 0.0;
   if (s.ecp_flag)
@@ -1187,8 +1269,8 @@ __device__ void lrdmc_sums(const Sys& s, const double* r, int N, double* red, Te
   opt = block_sum(opt, red);
   vfn = block_sum(vfn, red);
   vsp = block_sum(vsp, red);
-  const double ee = coulomb_ee(r, N, red);
-  const double loc = ecp_local_sum(s, r, N, red);
+  loc = block_sum(loc, red);
+  const double ee = ec[(size_t)N * kEC + EC_TOT_EE];
   const double disc = ee + s.ion_ion + opt;
   const double dk = 3.0 / (2.0 * alat * alat) * N;
   if (s.ecp_flag) {
@@ -1342,6 +1424,8 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
       Tdn[(size_t)kk * A + a] = (Tab)acc;
     }
   }
+  // energy cache
+  ecache_init(s, r, P.ws.ecache + (size_t)w * (N + 1) * kEC, reinterpret_cast<double*>(smem + P.wl.off_red));
   // AO derivative tables at every electron
   {
     Tab* dpw = static_cast<Tab*>(P.ws.dphi) + (size_t)w * N * 4 * A;
@@ -1610,12 +1694,12 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
   electron_terms<double>(k, t, 0.0);
   mesh_terms<double, double>(k, t, 0.0, false);
   double acc = 0.0;
-  for (int e = threadIdx.x; e < k.N; e += blockDim.x) acc += t.ke[e] + t.ei[e];
+  for (int e = threadIdx.x; e < k.N; e += blockDim.x) acc += t.ke[e] + t.ei[e] + k.ec[(size_t)e * kEC + EC_ELOC];
   if (s.ecp_flag)
     for (int q = threadIdx.x; q < k.N * s.nv; q += blockDim.x) acc += t.V[q];
   acc = block_sum(acc, k.red);
-  const double ee = coulomb_ee(k.r, k.N, k.red);
-  const double loc = ecp_local_sum(s, k.r, k.N, k.red);
+  const double ee = k.ec[(size_t)k.N * kEC + EC_TOT_EE];
+  const double loc = 0.0;
   const double R = as_factor_block(k);
   if (threadIdx.x == 0) {
     eL[w] = acc + ee + s.ion_ion + loc;
@@ -1646,7 +1730,7 @@ __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, doubl
     electron_terms<Tab>(k, t, alat);
     mesh_terms<R, Tab>(k, t, alat, true);
     double diag, nondiag;
-    lrdmc_sums(s, k.r, N, k.red, t, alat, &diag, &nondiag);
+    lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
       if (threadIdx.x == 0) {
         eL[w] = diag + nondiag;
@@ -1655,20 +1739,54 @@ __global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, doubl
       break;
     }
     wl = wl * (1.0 / (diag - E_scf) * (-1.0 * nondiag));
-    // move choice: sequential cumsum over the normalised FN weights (thread 0)
-    if (threadIdx.x == 0) {
-      const int nk = 6 * N, ne = s.ecp_flag ? s.nv * N : 0;
-      double sum = 0.0;
-      for (int p = 0; p < nk; ++p) sum += fmin(t.el[p], 0.0);
-      for (int q = 0; q < ne; ++q) sum += fmin(t.V[q], 0.0);
-      const double u = d[3];
-      double cdf = 0.0;
-      int kk = nk + ne - 1;
-      for (int p = 0; p < nk + ne; ++p) {
-        const double x = p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0);
-        cdf += x / sum;
-        if (cdf >= u) { kk = p; break; }
+    const int nk = 6 * N, ne = s.ecp_flag ? s.nv * N : 0, np_ = nk + ne;
+    int* kchoice = reinterpret_cast<int*>(k.sc + 31);
+    if constexpr (sizeof(Tab) == sizeof(float)) {
+      // mixed form: warp-parallel inclusive scan of the normalised FN weights
+      if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int chunk = (np_ + 31) / 32, p0 = lane * chunk, p1 = min(p0 + chunk, np_);
+        double part = 0.0;
+        for (int p = p0; p < p1; ++p) part += p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0);
+        const double sum = warp_sum(part);
+        const double inv = 1.0 / sum;
+        double incl = part * inv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const double v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        double cdf = incl - part * inv;   // exclusive prefix of this lane's chunk
+        const double u = d[3];
+        int hit = -1;
+        for (int p = p0; p < p1; ++p) {
+          cdf += (p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0)) * inv;
+          if (cdf >= u) { hit = p; break; }
+        }
+        const unsigned any = __ballot_sync(0xffffffffu, hit >= 0);
+        const int first = __shfl_sync(0xffffffffu, hit, any ? __ffs(any) - 1 : 0);
+        if (lane == 0) *kchoice = any ? first : np_ - 1;
       }
+    } else {
+      // plain form: sequential cumsum in the reference's order (thread 0)
+      if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int p = 0; p < nk; ++p) sum += fmin(t.el[p], 0.0);
+        for (int q = 0; q < ne; ++q) sum += fmin(t.V[q], 0.0);
+        const double u = d[3];
+        double cdf = 0.0;
+        int kk = np_ - 1;
+        for (int p = 0; p < np_; ++p) {
+          const double x = p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0);
+          cdf += x / sum;
+          if (cdf >= u) { kk = p; break; }
+        }
+        *kchoice = kk;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int kk = *kchoice;
       double px, py, pz;
       int e;
       if (kk < nk) {
@@ -1783,7 +1901,7 @@ namespace {
 WS to_ws(const jqmc_walkers* w) {
   WS x;
   x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3;
-  x.dphi = w->dphi; x.dphi3 = w->dphi3;
+  x.dphi = w->dphi; x.dphi3 = w->dphi3; x.ecache = w->ecache;
   x.scratch = w->scratch; x.status = w->status;
   return x;
 }
@@ -1791,7 +1909,7 @@ WS to_ws(const jqmc_walkers* w) {
 bool walkers_ok(const jqmc_system* sys, const jqmc_walkers* w) {
   if (!sys || !w || w->nwalk <= 0) return false;
   if (w->precision != JQMC_PREC_FP64 && w->precision != JQMC_PREC_MIXED) return false;
-  if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status || !w->dphi) return false;
+  if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status || !w->dphi || !w->ecache) return false;
   if (sys->s.has_j3 && (!w->h3 || !w->dphi3)) return false;
   if (w->precision == JQMC_PREC_MIXED && !w->scratch) return false;
   return true;
@@ -1999,7 +2117,7 @@ int64_t jqmc_walker_bytes(const jqmc_system* sys, int32_t precision) {
   const Sys& s = sys->s;
   const int64_t n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
   const int64_t tb = precision == JQMC_PREC_MIXED ? 4 : 8;
-  return 8 * N * 3 + tb * (2 * n * n + 2 * n * A + N * A3 + N * 4 * A + N * 5 * A3) + 4 +
+  return 8 * N * 3 + 8 * (N + 1) * kEC + tb * (2 * n * n + 2 * n * A + N * A3 + N * 4 * A + N * 5 * A3) + 4 +
          (precision == JQMC_PREC_MIXED ? 8 * 2 * n * A : 0);
 }
 
@@ -2115,6 +2233,7 @@ int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jq
   tab(src->Tdn, dst->Tdn, n * A);
   if (A3) tab(src->h3, dst->h3, N * A3);
   tab(src->dphi, dst->dphi, N * 4 * A);
+  k_gather<double><<<grid, bs, 0, S(stream)>>>(src->ecache, dst->ecache, (N + 1) * kEC, d_chosen, W);
   if (A3) tab(src->dphi3, dst->dphi3, N * 5 * A3);
   k_gather<int><<<(W + 255) / 256, 256, 0, S(stream)>>>(src->status, dst->status, 1, d_chosen, W);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;

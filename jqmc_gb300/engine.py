@@ -118,7 +118,7 @@ class GpuSystem:
                 for slot in range(_lib.ECP_SLOTS):
                     chan[atom, slot, 0] = len(terms)
                     for (a, l, ex, co, pw) in zip(coul.nucleus_index, coul.ang_moms, coul.exponents, coul.coefficients, coul.powers):
-                        if a == atom and l == slot:
+                        if a == atom and l == slot and co != 0.0:
                             terms.append((co, pw, ex))
                     chan[atom, slot, 1] = len(terms) - chan[atom, slot, 0]
             keep["maxl1"] = np.ascontiguousarray(coul.max_ang_mom_plus_1, dtype=np.int32)
@@ -199,6 +199,7 @@ class WalkerSet:
         self.h3 = torch.zeros((W, N, max(A3, 1)), dtype=tdt, device=dev)
         self.dphi = torch.empty((W, N, 4, A), dtype=tdt, device=dev)
         self.dphi3 = torch.empty((W, N, 5, max(A3, 1)), dtype=tdt, device=dev)
+        self.ecache = torch.zeros((W, N + 1, _lib.ECACHE_STRIDE), dtype=torch.float64, device=dev)
         self.status = torch.zeros(W, dtype=torch.int32, device=dev)
         if precision == "mixed":
             self.scratch = scratch if scratch is not None else torch.empty((W, 2, n, A), dtype=torch.float64, device=dev)
@@ -212,7 +213,7 @@ class WalkerSet:
         obj.sys = other.sys
         obj.nwalk = other.nwalk
         obj.precision = other.precision
-        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "status"):
+        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "ecache", "status"):
             setattr(obj, name, torch.empty_like(getattr(other, name)))
         obj.scratch = other.scratch   # the rebuild scratch is shared: it holds no state between calls
         return obj
@@ -221,7 +222,7 @@ class WalkerSet:
         d = _lib.Walkers()
         d.nwalk = self.nwalk
         d.precision = PRECISIONS[self.precision]
-        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "status"):
+        for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "ecache", "status"):
             setattr(d, name, C.c_void_p(getattr(self, name).data_ptr()))
         d.scratch = C.c_void_p(self.scratch.data_ptr()) if self.scratch is not None else None
         return d
