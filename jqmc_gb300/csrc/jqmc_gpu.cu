@@ -42,6 +42,11 @@
 #include "jqmc_gpu.h"
 #include "solid_harmonics.cuh"
 
+// CTAs per SM the projection kernel is compiled for (register budget)
+#ifndef JQMC_LRDMC_MINB
+#define JQMC_LRDMC_MINB 3
+#endif
+
 namespace {
 
 constexpr int kSlots = JQMC_ECP_SLOTS;
@@ -1054,10 +1059,11 @@ struct Terms {
   double* R;      // 9 rotation
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
+  int* ecpe;      // N electrons whose nearest nucleus has non-local channels; ecpe[N] = count
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_vl, off_ea, off_el, off_V, off_R, off_dA, off_dE, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_vl, off_ea, off_el, off_V, off_R, off_dA, off_dE, off_ecpe, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form
@@ -1077,6 +1083,7 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_R = o; o = align16(o + 9 * 8);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
+  L.off_ecpe = o; o = align16(o + (N + 1) * 4);
   L.bytes = o;
   return L;
 }
@@ -1094,7 +1101,8 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
-  t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  t.dE = L.off_ecpe > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  t.ecpe = reinterpret_cast<int*>(smem + L.off_ecpe);
   return t;
 }
 
@@ -1162,6 +1170,8 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
       t.eatom[e] = (int)row[EC_NEAR];
       t.edist[e] = row[EC_DIST];
       for (int l = 0; l < kSlots; ++l) t.vl[e * kSlots + l] = row[EC_VL + l];
+      if (s.ecp_flag && s.ecp_maxl1[(int)row[EC_NEAR]] <= 0)
+        for (int v = 0; v < s.nv; ++v) t.V[e * s.nv + v] = 0.0;
       if (!s.ecp_flag) {
         const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
         double eid = 0.0;
@@ -1172,6 +1182,14 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
         t.eid[e] = eid;
       }
     }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int c = 0;
+    if (s.ecp_flag)
+      for (int e = 0; e < k.N; ++e)
+        if (s.ecp_maxl1[t.eatom[e]] > 0) t.ecpe[c++] = e;
+    t.ecpe[k.N] = c;
   }
   __syncthreads();
 }
@@ -1208,7 +1226,7 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
   const Sys& s = k.s;
   const int N = k.N, nv = s.nv;
   const int nkin = kinetic ? 6 * N : 0;
-  const int necp = s.ecp_flag ? nv * N : 0;
+  const int necp = s.ecp_flag ? nv * t.ecpe[N] : 0;
   for (int p = threadIdx.x; p < nkin + necp; p += blockDim.x) {
     if (p < nkin) {
       const int e = p / 6, kk = p % 6, ax = kk >> 1;
@@ -1216,10 +1234,9 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
       t.el[p] = -1.0 / (2.0 * alat * alat) *
                 (double)wf_ratio<R, Tab>(k, t, e, sg * t.R[0 * 3 + ax], sg * t.R[1 * 3 + ax], sg * t.R[2 * 3 + ax]);
     } else {
-      const int q = p - nkin, e = q / nv, v = q % nv;
+      const int qa = p - nkin, e = t.ecpe[qa / nv], v = qa % nv, q = e * nv + v;
       const int atom = t.eatom[e];
       const int lmax = s.ecp_maxl1[atom];
-      if (lmax <= 0) { t.V[q] = 0.0; continue; }
       const double* m = s.mesh_pts + 3 * v;
       const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
       const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
@@ -1712,7 +1729,7 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
 // e_L and V_diag at the current positions with the rotation of draw[w].
 // R: mesh arithmetic, Tab: table storage and updates.
 template <class R, class Tab>
-__global__ void k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
+__global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
                         double* eL, double* vdiag) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
