@@ -103,6 +103,9 @@ typedef struct {
                       /* non-local channel values; last row: e-e Coulomb total   */
   double* scratch;    /* JQMC_PREC_MIXED: nwalk*2*n*A doubles used by the FP64   */
                       /* rebuild in jqmc_walker_init; unused for JQMC_PREC_FP64  */
+  float* dcache;      /* JQMC_PREC_MIXED: nwalk*N*(natom+N)*3 floats of electron */
+                      /* displacements, required when that exceeds 64 KiB per    */
+                      /* walker (else kept in shared memory); may be NULL below  */
   int32_t* status;    /* nwalk JQMC_ST_* bits                                    */
 } jqmc_walkers;
 

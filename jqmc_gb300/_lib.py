@@ -44,7 +44,7 @@ class SystemDesc(C.Structure):
 
 class Walkers(C.Structure):
     _fields_ = [("nwalk", i32), ("precision", i32), ("r", vp), ("G", vp), ("Ginv", vp), ("Tup", vp), ("Tdn", vp), ("h3", vp),
-                ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("status", vp)]
+                ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("dcache", vp), ("status", vp)]
 
 
 PREC_FP64, PREC_MIXED = 0, 1

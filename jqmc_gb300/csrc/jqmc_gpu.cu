@@ -162,6 +162,7 @@ struct WS {
   double* r;
   void *G, *Ginv, *Tup, *Tdn, *h3, *dphi, *dphi3;
   double* ecache;
+  float* dcache;
   double* scratch;
   int* status;
 };
@@ -1066,7 +1067,7 @@ struct TermsLayout {
   int off_ke, off_c3, off_ei, off_eid, off_ed, off_vl, off_ea, off_el, off_V, off_R, off_dA, off_dE, off_ecpe, bytes;
 };
 
-// rel: reserve the float displacement caches of the mixed form
+// rel: reserve the float displacement caches of the mixed form in shared memory
 TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   TermsLayout L;
   const int N = s.N;
@@ -1088,7 +1089,12 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   return L;
 }
 
-__device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
+// Displacement caches bigger than this live in global memory (per walker).
+constexpr int kDcacheSmemMax = 64 * 1024;
+
+int dcache_bytes(const Sys& s) { return s.N * (s.natom + s.N) * 3 * 4; }
+
+__device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gdcache, const Sys& s) {
   Terms t;
   t.ke = reinterpret_cast<double*>(smem + L.off_ke);
   t.c3 = reinterpret_cast<double*>(smem + L.off_c3);
@@ -1102,6 +1108,10 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem) {
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
   t.dE = L.off_ecpe > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  if (gdcache) {
+    t.dA = gdcache;
+    t.dE = gdcache + (size_t)s.N * s.natom * 3;
+  }
   t.ecpe = reinterpret_cast<int*>(smem + L.off_ecpe);
   return t;
 }
@@ -1307,7 +1317,10 @@ struct KParams {
   WorkLayout wl;
   TermsLayout ml;
   int nwalk;
+  int dcache_global;   // mixed form: displacement caches in ws.dcache instead of shared memory
 };
+
+__device__ __forceinline__ size_t dcache_floats_dev(const Sys& s) { return (size_t)s.N * (s.natom + s.N) * 3; }
 
 __global__ void k_ao_vgl(Sys s, int basis, const double* __restrict__ r, long long npts, double* __restrict__ out) {
   const Basis& b = basis == 0 ? s.det : s.j3;
@@ -1704,7 +1717,7 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
   Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
-  Terms t = make_terms(P.ml, smem);
+  Terms t = make_terms(P.ml, smem, nullptr, s);
   load_walker(k, P.ws, w);
   if (threadIdx.x == 0) rotation(angles[3 * w], angles[3 * w + 1], angles[3 * w + 2], t.R);
   __syncthreads();
@@ -1735,7 +1748,8 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
   Work<Tab> k = make_work<Tab>(s, P.wl, smem, P.ws, w);
-  Terms t = make_terms(P.ml, smem);
+  float* gd = (P.dcache_global && sizeof(R) == sizeof(float)) ? P.ws.dcache + (size_t)w * (dcache_floats_dev(s)) : nullptr;
+  Terms t = make_terms(P.ml, smem, gd, s);
   load_walker(k, P.ws, w);
   const int N = k.N;
   const int nsteps = K > 0 ? K : 1;
@@ -1918,7 +1932,7 @@ namespace {
 WS to_ws(const jqmc_walkers* w) {
   WS x;
   x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3;
-  x.dphi = w->dphi; x.dphi3 = w->dphi3; x.ecache = w->ecache;
+  x.dphi = w->dphi; x.dphi3 = w->dphi3; x.ecache = w->ecache; x.dcache = w->dcache;
   x.scratch = w->scratch; x.status = w->status;
   return x;
 }
@@ -1929,6 +1943,7 @@ bool walkers_ok(const jqmc_system* sys, const jqmc_walkers* w) {
   if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status || !w->dphi || !w->ecache) return false;
   if (sys->s.has_j3 && (!w->h3 || !w->dphi3)) return false;
   if (w->precision == JQMC_PREC_MIXED && !w->scratch) return false;
+  if (w->precision == JQMC_PREC_MIXED && dcache_bytes(sys->s) > kDcacheSmemMax && !w->dcache) return false;
   return true;
 }
 
@@ -1940,7 +1955,9 @@ KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   P.ws = to_ws(w);
   P.tl = table_layout(sys->s);
   P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
-  P.ml = terms_layout(sys->s, P.wl.bytes, w->precision == JQMC_PREC_MIXED);
+  const bool mixed = w->precision == JQMC_PREC_MIXED;
+  P.dcache_global = mixed && dcache_bytes(sys->s) > kDcacheSmemMax;
+  P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global);
   P.nwalk = w->nwalk;
   return P;
 }

@@ -203,8 +203,12 @@ class WalkerSet:
         self.status = torch.zeros(W, dtype=torch.int32, device=dev)
         if precision == "mixed":
             self.scratch = scratch if scratch is not None else torch.empty((W, 2, n, A), dtype=torch.float64, device=dev)
+            M = len(system._keep["pos"])
+            big = N * (M + N) * 3 * 4 > 64 * 1024
+            self.dcache = torch.empty((W, N * (M + N) * 3), dtype=torch.float32, device=dev) if big else None
         else:
             self.scratch = None
+            self.dcache = None
         self.init()
 
     @classmethod
@@ -216,6 +220,7 @@ class WalkerSet:
         for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "ecache", "status"):
             setattr(obj, name, torch.empty_like(getattr(other, name)))
         obj.scratch = other.scratch   # the rebuild scratch is shared: it holds no state between calls
+        obj.dcache = other.dcache     # so are the displacement caches (rebuilt every projection step)
         return obj
 
     def desc(self) -> _lib.Walkers:
@@ -225,6 +230,7 @@ class WalkerSet:
         for name in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "ecache", "status"):
             setattr(d, name, C.c_void_p(getattr(self, name).data_ptr()))
         d.scratch = C.c_void_p(self.scratch.data_ptr()) if self.scratch is not None else None
+        d.dcache = C.c_void_p(self.dcache.data_ptr()) if self.dcache is not None else None
         return d
 
     @property
