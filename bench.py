@@ -1,13 +1,15 @@
 """Walker-path benchmark on GB300: LRDMC (GFMC_n) projections, mixed precision vs plain FP64.
 
-Workload (default): the 12-nucleus synthetic ring -- 6 C-like nuclei (Z_eff 4,
-semilocal ECP with l = 0, 1 non-local channels) at 2.64 bohr and 6 H at 4.69
-bohr, 30 electrons (15/15), 192 spherical GTOs, JAGP geminal, J1/J2/J3 (60 J3
-AOs); 8192 walkers; lattice spacing 0.2 bohr, 6 directions; T-move ECP
-(Nv = 6); 40 projections per branching.  One bench step = one branching
-cycle: 40 projections of every walker, the local energy, the weighted sums,
-the comb reconfiguration and the rebuild of G^-1 / T tables from positions.
-walker-steps per bench step = walkers x 40.
+Workload (default, --workload chain32): the 32-nucleus zig-zag chain -- 16
+C-like nuclei (Z_eff 4, semilocal ECP with l = 0, 1 non-local channels) and 16
+H, bond 2.6 bohr, 96 electrons (48/48), 736 spherical GTOs, JAGP geminal,
+J1/J2/J3 (64 J3 AOs); 16384 walkers; lattice spacing 0.2 bohr, 6 directions;
+T-move ECP (Nv = 6); 40 projections per branching.  (--workload ring12: the
+12-nucleus ring, 30 electrons, 192 AOs, 8192 walkers.)  One bench step = one
+branching cycle: 40 projections of every walker, the FP64 rebuild of G^-1 / T
+tables from the positions (LU + one refinement step), the local energy, the
+weighted sums and the comb reconfiguration.  walker-steps per bench step = walkers x 40.  The plain FP64 arm
+runs the same draws for fewer cycles (min(warmup, 1) + max(1, steps // 2)).
 
 value : walker-steps/s of the mixed-precision form with the draws resident in
         HBM; the plain FP64 form runs the same draws and is reported beside it
@@ -16,7 +18,7 @@ value : walker-steps/s of the mixed-precision form with the draws resident in
 e2e   : the mixed form through the public driver API (jqmc_gb300.jqmc_gfmc.GFMC_n.run_block)
         with the draws copied from pinned host memory each step and the step's
         sums read back to the host.
-Walker state is 8192 x 64 KB = 0.5 GB > L2 (129 MB), so no L2 flush is needed.
+Walker state is several GB (> L2, 129 MB), so no L2 flush is needed.
 
 --impl reference : the CPU oracle (NumPy restatement of the reference, which is
 Python/JAX and cannot run without JAX) on all host cores, one process per core,
@@ -49,12 +51,15 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="ring12", choices=["ring12", "water_like", "chain32"])
-    p.add_argument("--walkers", type=int, default=8192)
+    p.add_argument("--workload", default="chain32", choices=["ring12", "water_like", "chain32"])
+    p.add_argument("--walkers", type=int, default=None, help="default: 16384 for chain32, 8192 otherwise")
     p.add_argument("--nproj", type=int, default=40)
     p.add_argument("--alat", type=float, default=0.2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.walkers is None:
+        a.walkers = 16384 if a.workload == "chain32" else 8192
+    return a
 
 
 # ----------------------------------------------------------------------------- CPU oracle arm
@@ -176,14 +181,14 @@ def _probe(L, fn, dev, stream, dtype):
 
 def _time_form(drv, draws, zetas, warmup, steps, stream, world, dev):
     """Warm up, then time `steps` branching cycles with device-resident draws.
-    Returns (ms, per-step sums (steps, 4), list of project-launch ms)."""
+    Returns (ms, per-step sums (steps, 4), list of project-launch ms, list of rebuild-launch ms)."""
     import torch
     import torch.distributed as dist
 
     from jqmc_gb300.replicas import max_over_ranks
     cls = drv.walkers.__class__
-    orig = cls.lrdmc_project
-    events = []
+    orig, orig_rb = cls.lrdmc_project, cls.rebuild
+    events, events_rb = [], []
 
     def timed_project(self, d, alat, E_scf, w):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -193,10 +198,19 @@ def _time_form(drv, draws, zetas, warmup, steps, stream, world, dev):
         e1.record(stream)
         events.append((e0, e1))
 
+    def timed_rebuild(self):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        orig_rb(self)
+        e1.record(stream)
+        events_rb.append((e0, e1))
+
     for s in range(warmup):
         drv.run_block(draws[s], zetas[s])
     torch.cuda.synchronize()
     cls.lrdmc_project = timed_project
+    cls.rebuild = timed_rebuild
     try:
         if world > 1:
             dist.barrier()
@@ -210,9 +224,10 @@ def _time_form(drv, draws, zetas, warmup, steps, stream, world, dev):
         if world > 1:
             dist.barrier()
     finally:
-        cls.lrdmc_project = orig
+        cls.lrdmc_project, cls.rebuild = orig, orig_rb
     ms = max_over_ranks(t0.elapsed_time(t1), device=dev)
-    return ms, torch.stack(sums).cpu().numpy(), [a.elapsed_time(b) for a, b in events]
+    return (ms, torch.stack(sums).cpu().numpy(), [a.elapsed_time(b) for a, b in events],
+            [a.elapsed_time(b) for a, b in events_rb])
 
 
 def gpu_arm(a):
@@ -248,6 +263,8 @@ def gpu_arm(a):
     total = a.warmup + a.steps
     forms = {}
     draws_keep = None
+    # the plain FP64 comparison arm runs fewer branching cycles (it is ~8x slower)
+    plan = {"fp64": (min(a.warmup, 1), max(1, a.steps // 2)), "mixed": (a.warmup, a.steps)}
     for form in ("fp64", "mixed"):
         drv = GFMC_n(syn.hamiltonian, num_walkers=W, num_mcmc_per_measurement=K, mcmc_seed=7 + rank, alat=a.alat,
                      init_r_up=r_up, init_r_dn=r_dn, precision=form)
@@ -258,10 +275,11 @@ def gpu_arm(a):
         clk = ClockSampler(torch.cuda.current_device()) if (rank == 0 and form == "mixed") else None
         if clk:
             time.sleep(0.4)
-        ms, sums, proj = _time_form(drv, draws_keep, zetas, a.warmup, a.steps, stream, world, dev)
+        fw, fs = plan[form]
+        ms, sums, proj, rb = _time_form(drv, draws_keep, zetas, fw, fs, stream, world, dev)
         clocks = clk.stop() if clk else None
-        forms[form] = {"drv": drv, "ms": ms, "sums": sums, "proj": proj, "clocks": clocks,
-                       "value": W * K * a.steps * world / (ms / 1e3)}
+        forms[form] = {"drv": drv, "ms": ms, "sums": sums, "proj": proj, "rebuild": rb, "clocks": clocks, "steps": fs, "warmup": fw,
+                       "value": W * K * fs * world / (ms / 1e3)}
         if form == "fp64":
             # free the plain form's state before the mixed form allocates its own
             del drv
@@ -271,19 +289,31 @@ def gpu_arm(a):
     gs = mixed["drv"].sys
     dev = gs.device
 
-    # accuracy of the mixed form against the FP64 form
-    e_plain = plain["sums"][:, 2] / plain["sums"][:, 1]
-    e_mixed = mixed["sums"][:, 2] / mixed["sums"][:, 1]
+    # accuracy of the mixed form against the FP64 form, in the order of a branching
+    # cycle: both forms start from the same sampled configurations, project one full
+    # block (K steps) with the same draws (the mixed form's float rank-1 updates
+    # drift as in production), rebuild the carried tables in FP64, and evaluate e_L;
+    # e_L is compared on the walkers whose paths coincided
     ws_m = mixed["drv"].walkers
-    n_cmp = min(W, 2048)
+    n_cmp = min(W, 1024)
     r = ws_m.r[:n_cmp].cpu().numpy()
     ref = WalkerSet(gs, r[:, : gs.n_up], r[:, gs.n_up:], precision="fp64")
     mix = WalkerSet(gs, r[:, : gs.n_up], r[:, gs.n_up:], precision="mixed")
+    blk = draws_keep[0][:n_cmp].contiguous()
+    wr = torch.ones(n_cmp, dtype=torch.float64, device=dev)
+    wm = torch.ones_like(wr)
+    ref.lrdmc_project(blk, a.alat, 0.0, wr)
+    mix.lrdmc_project(blk, a.alat, 0.0, wm)
+    ref.rebuild()
+    mix.rebuild()
+    same = ((ref.r - mix.r).abs().amax(dim=(1, 2)) < 1e-6)
     last = draws_keep[-1][:n_cmp, -1].contiguous()
     e64, _ = ref.lrdmc_energy(last, a.alat)
     e32, _ = mix.lrdmc_energy(last, a.alat)
-    de = (e32 - e64).cpu().numpy()
+    de = (e32 - e64)[same].cpu().numpy()
+    relw = ((wm - wr).abs() / wr.abs())[same].cpu().numpy()
     eL_rms = float(np.sqrt(np.mean(de**2)))
+    same_frac = float(same.double().mean())
     del ref, mix
 
     # e2e through the public driver API (mixed form): draws from pinned host memory, sums to host
@@ -333,8 +363,8 @@ def gpu_arm(a):
     except (OSError, ValueError):
         peaks = {}
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
-    per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 7 if gs.A3 else 6,
-                "jqmc_walker_init": 1}
+    per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
+                "jqmc_lu_rebuild_refine": 1}
     if rank == 0:
         line = {
             "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -346,15 +376,20 @@ def gpu_arm(a):
                        "parallelism": "walkers (one CTA per walker)" + ("; replicas" if world > 1 else ""),
                        "l2": f"walker state {gs.walker_bytes('mixed') * W / 2**20:.0f} MiB (mixed) / "
                              f"{gs.walker_bytes('fp64') * W / 2**20:.0f} MiB (fp64) > L2, no flush"},
-            "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms"] / a.steps, "dtype": "f64"},
+            "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms"] / plain["steps"], "dtype": "f64",
+                           "steps": plain["steps"], "warmup": plain["warmup"],
+                           "phase_ms": {"projection": plain_ms, "rebuild": float(np.mean(plain["rebuild"]))}},
+            "phase_ms": {"projection": mix_ms, "rebuild": float(np.mean(mixed["rebuild"])),
+                         "rest": mixed["ms"] / a.steps - mix_ms - float(np.mean(mixed["rebuild"])),
+                         "note": "per branching cycle, CUDA events on the launching stream; rest = energy, sums, comb, gather"},
             "speedup_vs_plain_fp64": mixed["value"] / plain["value"],
-            "accuracy": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": n_cmp,
+            "accuracy": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": int(len(de)),
+                         "same_path_fraction": same_frac, "block_weight_rel_diff_max": float(np.max(relw)),
                          "dE_mean_Ha": float(np.mean(de)), "dE_mean_stderr_Ha": float(np.std(de) / np.sqrt(len(de))),
-                         "note": "mixed minus FP64 local energy on the same sampled configurations and rotation; "
-                                 "dE_mean is the bias the mixed form adds to <E>",
-                         "bar": "|dE_L| <= 1e-5 Ha rms per configuration; |d<E>| <= 1e-4 Ha",
-                         "timed_runs_E_Ha": {"mixed": float(np.mean(e_mixed)), "fp64": float(np.mean(e_plain)),
-                                             "note": "branching-cycle averages of the two timed runs (few cycles, not converged)"}},
+                         "note": "mixed minus FP64 local energy after one K-step projection block from the same sampled "
+                                 "configurations with the same draws and the FP64 rebuild of the carried tables (the "
+                                 "order of a branching cycle); dE_mean is the bias the mixed form adds to <E>",
+                         "bar": "|dE_L| <= 1e-5 Ha rms per configuration; |d<E>| <= 1e-4 Ha"},
             "e2e": e2e,
             "gpu_launches": sum(per_call.values()) * a.steps,
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,

@@ -102,7 +102,8 @@ typedef struct {
                       /* local-ECP energies, J1/J2 grad/lap, nearest nucleus and */
                       /* non-local channel values; last row: e-e Coulomb total   */
   double* scratch;    /* JQMC_PREC_MIXED: nwalk*2*n*A doubles used by the FP64   */
-                      /* rebuild in jqmc_walker_init; unused for JQMC_PREC_FP64  */
+                      /* rebuilds (jqmc_walker_init, jqmc_lu_rebuild_refine);    */
+                      /* unused for JQMC_PREC_FP64                               */
   float* dcache;      /* JQMC_PREC_MIXED: nwalk*N*(natom+N)*3 floats of electron */
                       /* displacements, required when that exceeds 64 KiB per    */
                       /* walker (else kept in shared memory); may be NULL below  */
@@ -131,6 +132,15 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
  * of the SVD pseudo-inverse of jqmc_mcmc.py:4249-4261 / jqmc_gfmc.py:691),
  * T tables and the J3 field. */
 int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream);
+
+/* Rebuild the tables that Sherman-Morrison updates carry -- G, G^-1 (LU with
+ * partial pivoting plus one FP64 refinement step X <- X + X(I - G X)), the T
+ * tables and the J3 field -- from the positions, in FP64, and store them in the
+ * walkers' table type.  The energy cache and the AO derivative tables are left
+ * as they are (every move recomputes them exactly).  Replaces the per-branching
+ * inverse recomputation of GFMC_n (jqmc/jqmc_gfmc.py:4706-4717, :6319) and is
+ * the periodic FP64 rebuild of the mixed-precision form. */
+int jqmc_lu_rebuild_refine(const jqmc_system* sys, const jqmc_walkers* w, void* stream);
 
 /* ln|det G| and its sign per walker from G (LU, jqmc/determinant.py:1026-1111),
  * plus the Jastrow value J (jastrow_factor.py:2127-2178).  JQMC_PREC_FP64 only. */

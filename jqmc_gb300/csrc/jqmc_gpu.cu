@@ -109,6 +109,8 @@ struct Sys {
   const double* lamT;  // transpose
   const float* lamf;
   const float* lamTf;
+  const float* laml;   // lam - (double)lamf: the low float of a float-float split
+  const float* lamTl;
   int has_j1, j1_type;
   double j1_param;
   const double* j1_cA;   // natom x 2: ((2Z)^(1/4), (2Z)^(3/4)) with Z the J1 effective charge
@@ -1120,9 +1122,9 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
 // the ratios need (wavefunction.py:1142-1207 with jastrow_factor.py:961-1034,
 // 3435-3558, 4077-4156).  One warp per electron: the cached AO derivative tables
 // are dotted with the electron's T row and J3 field (lane sums in the table
-// type, warp sum in double); J1/J2 derivatives, Coulomb and ECP terms come from
-// the energy cache.
-template <class Tab>
+// type Acc, warp sum in double); J1/J2 derivatives, Coulomb and ECP terms come
+// from the energy cache.
+template <class Tab, class Acc = Tab>
 __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1143,25 +1145,25 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     const int i = up ? e : e - s.n_up;
     const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
     const Tab* dp = k.dphi + (size_t)e * 4 * A;
-    Tab tgx = Tab(0), tgy = Tab(0), tgz = Tab(0), tlp = Tab(0);
+    Acc tgx = Acc(0), tgy = Acc(0), tgz = Acc(0), tlp = Acc(0);
     for (int a = lane; a < A; a += 32) {
-      const Tab tv = Trow[a];
-      tgx += dp[a] * tv;
-      tgy += dp[A + a] * tv;
-      tgz += dp[2 * A + a] * tv;
-      tlp += dp[3 * A + a] * tv;
+      const Acc tv = (Acc)Trow[a];
+      tgx += (Acc)dp[a] * tv;
+      tgy += (Acc)dp[A + a] * tv;
+      tgz += (Acc)dp[2 * A + a] * tv;
+      tlp += (Acc)dp[3 * A + a] * tv;
     }
-    Tab tc3 = Tab(0), thx = Tab(0), thy = Tab(0), thz = Tab(0), thl = Tab(0);
+    Acc tc3 = Acc(0), thx = Acc(0), thy = Acc(0), thz = Acc(0), thl = Acc(0);
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
       for (int a = lane; a < A3; a += 32) {
-        const Tab hv = h[a];
-        tc3 += q[a] * hv;
-        thx += q[A3 + a] * hv;
-        thy += q[2 * A3 + a] * hv;
-        thz += q[3 * A3 + a] * hv;
-        thl += q[4 * A3 + a] * hv;
+        const Acc hv = (Acc)h[a];
+        tc3 += (Acc)q[a] * hv;
+        thx += (Acc)q[A3 + a] * hv;
+        thy += (Acc)q[2 * A3 + a] * hv;
+        thz += (Acc)q[3 * A3 + a] * hv;
+        thl += (Acc)q[4 * A3 + a] * hv;
       }
     }
     const double gx = warp_sum((double)tgx), gy = warp_sum((double)tgy), gz = warp_sum((double)tgz);
@@ -1338,11 +1340,96 @@ __global__ void k_ao_vgl(Sys s, int basis, const double* __restrict__ r, long lo
   ao_visit_vgl<double>(b, s.atom_pos, x, y, z, f);
 }
 
+// One term of a compensated float-float dot product (algorithm Dot2 of Ogita,
+// Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005)
+// 1955-1988), with both factors given as float pairs x = xh + xl, y = yh + yl:
+// TwoProduct (by FMA) and TwoSum are exact, so s + c carries the dot product as
+// if accumulated with a 48-bit significand.  The _rn intrinsics keep the compiler
+// from contracting the error-free transformations into FMAs.
+__device__ __forceinline__ void dot2_step(float& s, float& c, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float pe = __fmaf_rn(xh, yh, -p);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  s = t;
+  c += (pe + se) + fmaf(xh, yl, xl * yh);
+}
+
+// Rows of M_up = Phi_up lam (up spin) or M_dn = Phi_dn lam^T (down spin) for
+// ROWS electrons per CTA, accumulated in float-float (Dot2) and stored as double
+// in the walkers' rebuild scratch: (nwalk, 2, n, A) with the M_dn block first,
+// as k_walker_init reads it.  Grid (nwalk, 2 * ceil(n / ROWS)).  The AO values
+// are evaluated in FP64 from the global basis tables and split into float pairs
+// in shared memory (ROWS x A float2); each thread owns columns b of the output
+// and reads the split lam column once per ROWS electrons.  This is the dense
+// lam-GEMM of the rebuild (the geminal assembly of jqmc/determinant.py:1380-1402).
+template <int ROWS>
+__global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
+  constexpr int kRebuildRows = ROWS;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Sys& s = P.s;
+  const int w = blockIdx.x;
+  const int n = s.n_up, A = s.det.nao;
+  const int nb = (n + kRebuildRows - 1) / kRebuildRows;
+  const int spin = blockIdx.y / nb, i0 = (blockIdx.y % nb) * kRebuildRows;
+  const int rows = min(kRebuildRows, n - i0);
+  float2* ph = reinterpret_cast<float2*>(smem);   // kRebuildRows x A
+  const double* r = P.ws.r + ((size_t)w * s.N + (size_t)spin * s.n_up + i0) * 3;
+  for (int ii = 0; ii < kRebuildRows; ++ii) {
+    float2* out = ph + (size_t)ii * A;
+    if (ii < rows) {
+      const double px = r[3 * ii], py = r[3 * ii + 1], pz = r[3 * ii + 2];
+      auto f = [&](int a, double v) {
+        const float hi = (float)v;
+        out[a] = make_float2(hi, (float)(v - (double)hi));
+      };
+      for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
+        double dx, dy, dz;
+        disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
+        shell_val_d<double>(s.det, sh, dx, dy, dz, f);
+      }
+    } else {
+      for (int a = threadIdx.x; a < A; a += blockDim.x) out[a] = make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  const float* __restrict__ Lh = spin == 0 ? s.lamf : s.lamTf;
+  const float* __restrict__ Ll = spin == 0 ? s.laml : s.lamTl;
+  double* M = P.ws.scratch + ((size_t)w * 2 + (spin == 0 ? 1 : 0)) * n * A + (size_t)i0 * A;
+  for (int b = threadIdx.x; b < A; b += blockDim.x) {
+    float sacc[kRebuildRows], cacc[kRebuildRows];
+#pragma unroll
+    for (int ii = 0; ii < kRebuildRows; ++ii) { sacc[ii] = 0.f; cacc[ii] = 0.f; }
+#pragma unroll 2
+    for (int a = 0; a < A; ++a) {
+      const float yh = __ldg(Lh + (size_t)a * A + b), yl = __ldg(Ll + (size_t)a * A + b);
+#pragma unroll
+      for (int ii = 0; ii < kRebuildRows; ++ii) {
+        const float2 x = ph[(size_t)ii * A + a];
+        dot2_step(sacc[ii], cacc[ii], x.x, x.y, yh, yl);
+      }
+    }
+#pragma unroll
+    for (int ii = 0; ii < kRebuildRows; ++ii)
+      if (ii < rows) M[(size_t)ii * A + b] = (double)sacc[ii] + (double)cacc[ii];
+  }
+}
+
 // Walker initialisation in FP64: G, G^-1 (Gauss-Jordan, partial pivoting), T
 // tables and J3 field, written in the table type Tab.  M_up / M_dn go to the
 // double scratch (for Tab == double the T buffers themselves).
+// mode bit 0 (kInitTablesOnly): leave the energy cache and the AO derivative
+// tables alone -- they are recomputed exactly at every move, so a rebuild of a
+// projected walker only needs the tables that accumulate rank-1 rounding.
+// mode bit 1 (kInitRefine): one step of iterative refinement of the inverse,
+// X <- X + X (I - G X), in FP64.
+// mode bit 2 (kInitMReady): M_up / M_dn are already in the scratch (k_rebuild_m).
+constexpr int kInitTablesOnly = 1;
+constexpr int kInitRefine = 2;
+constexpr int kInitMReady = 4;
 template <class Tab>
-__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int off_phi3) {
+__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int off_phi3, int mode) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
@@ -1366,7 +1453,8 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
   }
   for (int t = threadIdx.x; t < N * 3; t += blockDim.x) r[t] = P.ws.r[(size_t)w * N * 3 + t];
   __syncthreads();
-  for (int i = 0; i < n; ++i) {
+  const bool m_ready = (mode & kInitMReady) != 0;
+  for (int i = 0; i < n && !m_ready; ++i) {
     ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * i], r[3 * i + 1], r[3 * i + 2], vec);
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
@@ -1381,7 +1469,7 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
     ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
     __syncthreads();
     rows_dot<double>(Mup, n, A, vec, vn);
-    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+    for (int a = threadIdx.x; a < A && !m_ready; a += blockDim.x) {
       double acc = 0.0;
       for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * vec[b];
       Mdn[(size_t)j * A + a] = acc;
@@ -1433,9 +1521,34 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
   }
   Tab* Gw = static_cast<Tab*>(P.ws.G) + (size_t)w * n * n;
   Tab* Giw = static_cast<Tab*>(P.ws.Ginv) + (size_t)w * n * n;
-  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-    Gw[t] = (Tab)Gd[t];
-    Giw[t] = (Tab)aug[(t / n) * n2 + n + (t % n)];
+  if (mode & kInitRefine) {
+    // R = I - G X into the left half of aug (the identity left by the elimination)
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int rr = t / n, cc = t % n;
+      double acc = rr == cc ? 1.0 : 0.0;
+      for (int k = 0; k < n; ++k) acc -= Gd[rr * n + k] * aug[k * n2 + n + cc];
+      aug[rr * n2 + cc] = acc;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) Gw[t] = (Tab)Gd[t];
+    __syncthreads();
+    // X + X R into Gd (G is written out above), then back into the right half
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int rr = t / n, cc = t % n;
+      double acc = aug[rr * n2 + n + cc];
+      for (int k = 0; k < n; ++k) acc += aug[rr * n2 + n + k] * aug[k * n2 + cc];
+      Gd[t] = acc;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      aug[(t / n) * n2 + n + (t % n)] = Gd[t];
+      Giw[t] = (Tab)Gd[t];
+    }
+  } else {
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      Gw[t] = (Tab)Gd[t];
+      Giw[t] = (Tab)aug[(t / n) * n2 + n + (t % n)];
+    }
   }
   __syncthreads();
   // T_up[k][a] = sum_j M_dn[j][a] G^-1[j][k] ; T_dn[k][b] = sum_i G^-1[k][i] M_up[i][b]  (per column)
@@ -1454,10 +1567,10 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
       Tdn[(size_t)kk * A + a] = (Tab)acc;
     }
   }
-  // energy cache
-  ecache_init(s, r, P.ws.ecache + (size_t)w * (N + 1) * kEC, reinterpret_cast<double*>(smem + P.wl.off_red));
-  // AO derivative tables at every electron
-  {
+  if (!(mode & kInitTablesOnly)) {
+    // energy cache
+    ecache_init(s, r, P.ws.ecache + (size_t)w * (N + 1) * kEC, reinterpret_cast<double*>(smem + P.wl.off_red));
+    // AO derivative tables at every electron
     Tab* dpw = static_cast<Tab*>(P.ws.dphi) + (size_t)w * N * 4 * A;
     Tab* dp3w = s.has_j3 ? static_cast<Tab*>(P.ws.dphi3) + (size_t)w * N * 5 * A3 : nullptr;
     for (int e = 0; e < N; ++e)
@@ -1758,7 +1871,7 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
     const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * 4;
     if (threadIdx.x == 0) rotation(d[0], d[1], d[2], t.R);
     __syncthreads();
-    electron_terms<Tab>(k, t, alat);
+    electron_terms<Tab, R>(k, t, alat);
     mesh_terms<R, Tab>(k, t, alat, true);
     double diag, nondiag;
     lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
@@ -1973,7 +2086,9 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
   KParams P = make_params(sys, w);
   const int smem = P.ml.bytes;
   if (w->precision == JQMC_PREC_MIXED) {
-    auto fn = k_lrdmc<float, float>;
+    // projections: float arithmetic on the float tables; the local energy of a
+    // block (K == 0): FP64 arithmetic (AO values, ratios, sums) on the float tables
+    auto fn = K > 0 ? k_lrdmc<float, float> : k_lrdmc<double, float>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
     fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd);
@@ -2034,13 +2149,15 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     return off;
   };
   std::vector<double> lamT((size_t)A * A);
-  std::vector<float> lamf((size_t)A * A), lamTf((size_t)A * A);
+  std::vector<float> lamf((size_t)A * A), lamTf((size_t)A * A), laml((size_t)A * A), lamTl((size_t)A * A);
   for (int a = 0; a < A; ++a)
     for (int b = 0; b < A; ++b) {
       const double v = d->lambda[(size_t)a * A + b];
       lamT[(size_t)b * A + a] = v;
       lamf[(size_t)a * A + b] = (float)v;
       lamTf[(size_t)b * A + a] = (float)v;
+      laml[(size_t)a * A + b] = (float)(v - (double)(float)v);
+      lamTl[(size_t)b * A + a] = (float)(v - (double)(float)v);
     }
   std::vector<double> j3m, j3mT, j3v;
   std::vector<float> j3mf, j3mTf;
@@ -2081,6 +2198,8 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   const size_t o_lamT = put(lamT.data(), (size_t)A * A * 8);
   const size_t o_lamf = put(lamf.data(), (size_t)A * A * 4);
   const size_t o_lamTf = put(lamTf.data(), (size_t)A * A * 4);
+  const size_t o_laml = put(laml.data(), (size_t)A * A * 4);
+  const size_t o_lamTl = put(lamTl.data(), (size_t)A * A * 4);
   const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
   size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
@@ -2116,6 +2235,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.det.nshell = d->det.nshell; s.det.nao = A; s.det.nprim = d->det.nprim;
   s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf);
   s.lam = dp(o_lam); s.lamT = dp(o_lamT); s.lamf = fp(o_lamf); s.lamTf = fp(o_lamTf);
+  s.laml = fp(o_laml); s.lamTl = fp(o_lamTl);
   s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_cA = dp(o_j1z);
   s.has_j2 = d->has_j2; s.j2_type = d->j2_type; s.j2_param = d->j2_param;
   s.has_j3 = d->has_j3;
@@ -2164,7 +2284,7 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
-int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream) {
+static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream, int mode) {
   if (!walkers_ok(sys, w)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
   const Sys& s = sys->s;
@@ -2176,15 +2296,32 @@ int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream
   const int off_phi3 = align16(off_vec + vec_len * 8);
   const int smem = align16(off_phi3 + (s.has_j3 ? s.N * A3 * 8 : 0));
   if (w->precision == JQMC_PREC_MIXED) {
-    int rc = launch_check((const void*)k_walker_init<float>, smem);
+    // M_up, M_dn by the float-float lam-GEMM into the scratch, then the rest in FP64
+    const int rows = s.det.nao <= 2048 ? 8 : 4;
+    const int smem_m = rows * s.det.nao * 8;
+    const void* fm = rows == 8 ? (const void*)k_rebuild_m<8> : (const void*)k_rebuild_m<4>;
+    int rc = launch_check(fm, smem_m);
     if (rc) return rc;
-    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3);
+    const dim3 grid_m(w->nwalk, 2 * ((n + rows - 1) / rows));
+    if (rows == 8) k_rebuild_m<8><<<grid_m, 128, smem_m, S(stream)>>>(P);
+    else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
+    rc = launch_check((const void*)k_walker_init<float>, smem);
+    if (rc) return rc;
+    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3, mode | kInitMReady);
   } else {
     int rc = launch_check((const void*)k_walker_init<double>, smem);
     if (rc) return rc;
-    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3);
+    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3, mode);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream) {
+  return launch_walker_init(sys, w, stream, 0);
+}
+
+int jqmc_lu_rebuild_refine(const jqmc_system* sys, const jqmc_walkers* w, void* stream) {
+  return launch_walker_init(sys, w, stream, kInitTablesOnly | kInitRefine);
 }
 
 int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow,

@@ -245,6 +245,12 @@ class WalkerSet:
         d = self.desc()
         _lib.check(_lib.lib().jqmc_walker_init(self.sys.handle, C.byref(d), self.sys.stream), "jqmc_walker_init")
 
+    def rebuild(self):
+        """FP64 rebuild of G, G^-1 (+ one refinement step), T and the J3 field from
+        the positions; the exact per-electron caches are kept."""
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_lu_rebuild_refine(self.sys.handle, C.byref(d), self.sys.stream), "jqmc_lu_rebuild_refine")
+
     def log_psi(self):
         dev = self.sys.device
         ld = torch.empty(self.nwalk, dtype=torch.float64, device=dev)

@@ -3,11 +3,15 @@
 Mirrors ``GFMC_n`` of jqmc/jqmc_gfmc.py:4191-6990: the constructor arguments,
 ``run(num_mcmc_steps)``, the stored per-branching observables and ``get_E``.
 One "MCMC step" is one branching cycle: ``num_mcmc_per_measurement``
-projections of every walker (one fused ``jqmc_lrdmc_project`` launch), the
-local energy at the final positions (``jqmc_lrdmc_energy``), the weighted
-averages, and the comb reconfiguration (``jqmc_branch_comb`` +
-``jqmc_walker_gather``) with the walker state rebuilt from the positions
-(``jqmc_walker_init``), as the reference recomputes G^-1 after branching.
+projections of every walker (one fused ``jqmc_lrdmc_project`` launch), the FP64
+rebuild of G^-1 and the tables carried by rank-1 updates from the positions
+(``jqmc_lu_rebuild_refine``), the local energy at the final positions
+(``jqmc_lrdmc_energy``), the weighted averages, and the comb reconfiguration
+(``jqmc_branch_comb`` + ``jqmc_walker_gather``).  The reference recomputes G^-1
+from the positions after branching (jqmc_gfmc.py:6319); rebuilding just before
+the energy instead gives the same state after the gather (which copies the
+rebuilt tables) and lets the mixed-precision form measure E_L on fresh tables
+rather than on tables that carry a block of float rank-1 updates.
 
 Random numbers: per projection the three Euler angles U(-2pi, 2pi) and the move
 uniform; per branching one comb offset zeta.  They are drawn on the device from
@@ -79,6 +83,8 @@ class GFMC_n:
         ws = self.walkers
         w = torch.ones(self.num_walkers, dtype=torch.float64, device=self.sys.device)
         ws.lrdmc_project(draws, self.alat, self.E_scf, w)
+        if self.rebuild_after_branching:
+            ws.rebuild()
         last = draws[:, -1].contiguous()
         eL, vd = ws.lrdmc_energy(last, self.alat)
         f = w / (vd - self.E_scf)
@@ -86,8 +92,6 @@ class GFMC_n:
         branch_comb(w, zeta, self._chosen, self._cum)
         self._spare.gather_from(ws, self._chosen)
         self.walkers, self._spare = self._spare, self.walkers
-        if self.rebuild_after_branching:
-            self.walkers.init()
         return sums
 
     def run(self, num_mcmc_steps: int = 50, max_time: int = 86400) -> None:

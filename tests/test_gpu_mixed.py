@@ -87,3 +87,40 @@ def test_mixed_projection_follows_fp64(pair):
     print(f"{syn.name}: {frac:.3f} of walkers on the same path; weight rel diff max {float(relw.max()):.2e}")
     assert frac >= 0.95
     assert float(relw.max()) < 5e-6 * K
+
+
+def test_mixed_energy_after_block_and_rebuild(pair):
+    """Production order of a branching cycle: K = 40 projections with float rank-1
+    updates, the FP64 rebuild of the carried tables, then E_L.  On the walkers
+    whose paths coincide with the FP64 form's, E_L meets the same bars as on
+    freshly built tables."""
+    syn, gs, w64, w32 = pair
+    from jqmc_gb300.engine import WalkerSet
+    r = w64.r.cpu().numpy()
+    n = gs.n_up
+    W = r.shape[0]
+    a = WalkerSet(gs, r[:, :n], r[:, n:], precision="fp64")
+    b = WalkerSet(gs, r[:, :n], r[:, n:], precision="mixed")
+    K = 40
+    rng = np.random.default_rng(17)
+    dr = np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (W, K, 3)), rng.uniform(size=(W, K, 1))], axis=-1)
+    d = torch.as_tensor(dr, device=gs.device)
+    wa = torch.ones(W, dtype=torch.float64, device=gs.device)
+    wb = torch.ones_like(wa)
+    a.lrdmc_project(d, 0.2, 0.0, wa)
+    b.lrdmc_project(d, 0.2, 0.0, wb)
+    a.rebuild()
+    b.rebuild()
+    last = d[:, -1].contiguous()
+    e64, _ = a.lrdmc_energy(last, 0.2)
+    e32, _ = b.lrdmc_energy(last, 0.2)
+    same = (a.r - b.r).abs().amax(dim=(1, 2)) < 1e-6
+    de = (e32 - e64)[same].cpu().numpy()
+    rms = float(np.sqrt(np.mean(de**2)))
+    print(f"{syn.name}: after {K} projections + rebuild, e_L rms {rms:.3e} Ha on {len(de)} walkers, mean {np.mean(de):.2e}")
+    assert float(same.double().mean()) >= 0.9
+    assert rms <= 1e-5
+    assert abs(float(np.mean(de))) <= 1e-5
+    gi = (b.Ginv.double() - a.Ginv).abs().amax(dim=(1, 2)) / a.Ginv.abs().amax(dim=(1, 2))
+    assert float(gi[same].max()) < 1e-5
+    assert not b.status.any()
