@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--nproj", type=int, default=40)
     p.add_argument("--alat", type=float, default=0.2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the parameter-derivative leg")
     a = p.parse_args()
     if a.walkers is None:
         a.walkers = 16384 if a.workload == "chain32" else 8192
@@ -230,6 +231,46 @@ def _time_form(drv, draws, zetas, warmup, steps, stream, world, dev):
             [a.elapsed_time(b) for a, b in events_rb])
 
 
+def adjoint_leg(stream, dev, peak64, hbm_peak, walkers: int = 8192, reps: int = 5):
+    """Parameter derivatives of ln|psi| (J1, J2, J3 block, lambda block) on the
+    12-nucleus ring with 8192 walkers: one jqmc_dlnpsi_dparam launch per rep."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.adjoint import dlnpsi_dparams
+    from jqmc_gb300.engine import GpuSystem, WalkerSet
+    from jqmc_gb300.workload import dlnpsi_bytes, dlnpsi_flops
+    syn = synthetic.ring12()
+    gs = GpuSystem(syn.hamiltonian)
+    r_up, r_dn = syn.initial_electrons(walkers, seed=77)
+    ws = WalkerSet(gs, r_up, r_dn)
+    for _ in range(3):
+        blocks = dlnpsi_dparams(ws)
+    del blocks
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        blocks = dlnpsi_dparams(ws)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        del blocks
+    t = statistics.median(ms)
+    fl = dlnpsi_flops(gs) * walkers
+    by = dlnpsi_bytes(gs) * walkers
+    out = {"workload": "ring12 d ln psi / d (j1, j2, j3_matrix 60x61, lambda 192x192), FP64", "walkers": walkers,
+           "ms": t, "walker_derivatives_per_s": walkers / (t / 1e3),
+           "fp64_gflops": fl / (t / 1e3) / 1e9, "fp64_peak": peak64, "fp64_frac": fl / (t / 1e3) / 1e9 / peak64,
+           "hbm_gbs": by / (t / 1e3) / 1e9, "hbm_peak": hbm_peak,
+           "note": "CUDA events around dlnpsi_dparams (one kernel launch, blocks allocated by the caller); median of 5"}
+    del ws, gs
+    torch.cuda.empty_cache()
+    return out
+
+
 def gpu_arm(a):
     import ctypes
 
@@ -362,6 +403,7 @@ def gpu_arm(a):
             peaks = json.load(f)
     except (OSError, ValueError):
         peaks = {}
+    adjoint = adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")) if (rank == 0 and not a.no_adjoint) else None
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
                 "jqmc_lu_rebuild_refine": 1}
@@ -404,6 +446,7 @@ def gpu_arm(a):
                                  "peak_source": "MEASURED_PEAKS.json"},
                          "plain_fp64_kernel": {"bound": "fp64", "achieved": plain_ach, "peak": peak64, "frac": plain_ach / peak64,
                                                "avg_launch_ms": plain_ms}},
+            "adjoint": adjoint,
             "cpu_baseline": cpu_base,
             "clocks": mixed["clocks"],
         }

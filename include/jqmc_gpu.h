@@ -146,6 +146,22 @@ int jqmc_lu_rebuild_refine(const jqmc_system* sys, const jqmc_walkers* w, void* 
  * plus the Jastrow value J (jastrow_factor.py:2127-2178).  JQMC_PREC_FP64 only. */
 int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow, void* stream);
 
+/* Per-walker derivatives of ln|psi| with respect to the variational parameters,
+ * FP64 walkers only, from the positions and G^-1 (AO values are recomputed, not
+ * stored).  Replaces the per-walker grad(evaluate_ln_wavefunction) of
+ * jqmc_mcmc.py:856-876 with the blocks of collect_param_grads
+ * (jastrow_factor.py:2110-2124, determinant.py:389-399):
+ *   d_j1     nwalk           d ln psi / d jastrow_1b_param
+ *   d_j2     nwalk           d ln psi / d jastrow_2b_param
+ *   d_j3     nwalk*A3*(A3+1) d ln psi / d j_matrix (last column: one-body vector)
+ *   d_lambda nwalk*A*A       d ln psi / d lambda in the AO basis of the tables
+ *                            (a caller holding MO-basis lambda maps it with the
+ *                            MO coefficients: C_up D C_dn^T)
+ * d_work: nwalk*2*n*A doubles, required with d_lambda.  A NULL output skips its
+ * block; 0 is written for an absent J1 / J2 term. */
+int jqmc_dlnpsi_dparam(const jqmc_system* sys, const jqmc_walkers* w, double* d_j1, double* d_j2, double* d_j3,
+                       double* d_lambda, double* d_work, void* stream);
+
 /* K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523, fori_loop body),
  * explicit draws: d_idraw nwalk*K*4 int32 (sel in [0,N), up index, dn index,
  * axis), d_fdraw nwalk*K*2 double (standard normal, uniform).  Adds the number

@@ -1628,6 +1628,144 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
   }
 }
 
+// Per-walker derivatives of ln|psi| with respect to the variational parameters
+// (FP64 form), the blocks grad(evaluate_ln_wavefunction) yields in the reference
+// (jqmc_mcmc.py:856-876, collect_param_grads jastrow_factor.py:2110-2124 and
+// determinant.py:389-399):
+//   oj1[w]  d/da  of J1 = sum_{e,I} f1(a; |r_e - R_I|)       (jastrow_factor.py:649-726)
+//   oj2[w]  d/db  of J2 = sum_{p<q} f2(b; r_pq)              (jastrow_factor.py:1181-1251)
+//   oj3[w]  (A3, A3+1): d/dJ[a][b] = sum_{p<q same spin} phi_p[a] phi_q[b]
+//           + S_up[a] S_dn[b]; last column d/dj[a] = S_up[a] + S_dn[a]   (:1744-1801)
+//   olam[w] (A, A): d ln|det G| / d lambda[a][b] = sum_ij Ginv[j][i] phi_i[a] psi_j[b]
+//           with G[i][j] = phi_i^T lambda psi_j (determinant.py:1380-1402)
+// The AO values are recomputed from the positions (nothing is stored); the lambda
+// block uses work (nwalk * 2 * n * A doubles): Phi_up rows, then X = Ginv^T Psi_dn.
+// A NULL output skips its block.
+__global__ void k_dlnpsi_dparam(KParams P, int off_red, int off_su, int off_sd, int off_phi3, double* oj1, double* oj2,
+                                double* oj3, double* olam, double* work) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Sys& s = P.s;
+  const int w = blockIdx.x;
+  const int N = s.N, n = s.n_up, A = s.det.nao, M = s.natom;
+  double* r = reinterpret_cast<double*>(smem);
+  double* red = reinterpret_cast<double*>(smem + off_red);
+  for (int t = threadIdx.x; t < N * 3; t += blockDim.x) r[t] = P.ws.r[(size_t)w * N * 3 + t];
+  __syncthreads();
+  if (oj1) {
+    double acc = 0.0;
+    if (s.has_j1) {
+      const double a = s.j1_param;
+      for (int t = threadIdx.x; t < N * M; t += blockDim.x) {
+        const int e = t / M, at = t % M;
+        const double dx = r[3 * e] - s.atom_pos[3 * at], dy = r[3 * e + 1] - s.atom_pos[3 * at + 1];
+        const double dz = r[3 * e + 2] - s.atom_pos[3 * at + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        const double c = s.j1_cA[2 * at], Aa = s.j1_cA[2 * at + 1];
+        if (s.j1_type == 0) {
+          const double ex = exp(-a * c * d);
+          acc += -Aa * (c * d * ex / (2.0 * a) - (1.0 - ex) / (2.0 * a * a));
+        } else {
+          const double q = 1.0 + a * c * d;
+          acc += Aa * c * d * d / (2.0 * q * q);
+        }
+      }
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) oj1[w] = acc;
+  }
+  if (oj2) {
+    double acc = 0.0;
+    if (s.has_j2) {
+      const double b = s.j2_param;
+      for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+        const int p = t / N, q = t % N;
+        if (q <= p) continue;
+        const double dx = r[3 * p] - r[3 * q], dy = r[3 * p + 1] - r[3 * q + 1], dz = r[3 * p + 2] - r[3 * q + 2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        if (s.j2_type == 0) {
+          const double u = 1.0 + b * d;
+          acc += -d * d / (2.0 * u * u);
+        } else {
+          const double ex = exp(-b * d);
+          acc += d * ex / (2.0 * b) - (1.0 - ex) / (2.0 * b * b);
+        }
+      }
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) oj2[w] = acc;
+  }
+  if (oj3 && s.has_j3) {
+    const int A3 = s.j3.nao, nsh = s.j3.nshell;
+    double* su = reinterpret_cast<double*>(smem + off_su);
+    double* sd = reinterpret_cast<double*>(smem + off_sd);
+    double* phi3 = reinterpret_cast<double*>(smem + off_phi3);   // N x A3
+    for (int t = threadIdx.x; t < N * nsh; t += blockDim.x) {
+      const int e = t / nsh, sh = t % nsh;
+      double* out = phi3 + (size_t)e * A3;
+      auto f = [&](int a, double v) { out[a] = v; };
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < A3; a += blockDim.x) {
+      double tu = 0.0, td = 0.0;
+      for (int e = 0; e < n; ++e) tu += phi3[(size_t)e * A3 + a];
+      for (int e = n; e < N; ++e) td += phi3[(size_t)e * A3 + a];
+      su[a] = tu;
+      sd[a] = td;
+    }
+    __syncthreads();
+    double* o = oj3 + (size_t)w * A3 * (A3 + 1);
+    for (int t = threadIdx.x; t < A3 * A3; t += blockDim.x) {
+      const int a = t / A3, b = t % A3;
+      double acc = su[a] * sd[b];
+      for (int sp = 0; sp < 2; ++sp) {
+        double pa = 0.0;
+        for (int q = sp * n; q < (sp + 1) * n; ++q) {
+          acc += pa * phi3[(size_t)q * A3 + b];
+          pa += phi3[(size_t)q * A3 + a];
+        }
+      }
+      o[(size_t)a * (A3 + 1) + b] = acc;
+    }
+    for (int a = threadIdx.x; a < A3; a += blockDim.x) o[(size_t)a * (A3 + 1) + A3] = su[a] + sd[a];
+    __syncthreads();
+  }
+  if (olam) {
+    const int nsh = s.det.nshell;
+    double* Phi = work + (size_t)w * 2 * n * A;
+    double* X = Phi + (size_t)n * A;
+    for (int t = threadIdx.x; t < 2 * n * nsh; t += blockDim.x) {
+      const int e = t / nsh, sh = t % nsh;   // e < n: up electron e (Phi row); else down electron e - n (X row)
+      double* out = e < n ? Phi + (size_t)e * A : X + (size_t)(e - n) * A;
+      auto f = [&](int a, double v) { out[a] = v; };
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.det.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      shell_val_d<double>(s.det, sh, dx, dy, dz, f);
+    }
+    __syncthreads();
+    const double* Gi = static_cast<const double*>(P.ws.Ginv) + (size_t)w * n * n;
+    for (int b = threadIdx.x; b < A; b += blockDim.x) {
+      double col[JQMC_MAX_NUP];
+      for (int j = 0; j < n; ++j) col[j] = X[(size_t)j * A + b];
+      for (int i = 0; i < n; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc += Gi[j * n + i] * col[j];
+        X[(size_t)i * A + b] = acc;
+      }
+    }
+    __syncthreads();
+    double* o = olam + (size_t)w * A * A;
+    for (long long t = threadIdx.x; t < (long long)A * A; t += blockDim.x) {
+      const int a = (int)(t / A), b = (int)(t % A);
+      double acc = 0.0;
+      for (int i = 0; i < n; ++i) acc += Phi[(size_t)i * A + a] * X[(size_t)i * A + b];
+      o[t] = acc;
+    }
+  }
+}
+
 // ln|det G|, sign (LU with partial pivoting on a copy of G) and J   (FP64 form)
 __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2334,6 +2472,25 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
   int rc = launch_check((const void*)k_log_psi, smem);
   if (rc) return rc;
   k_log_psi<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, d_logdet, d_sign, d_jastrow);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_dlnpsi_dparam(const jqmc_system* sys, const jqmc_walkers* w, double* d_j1, double* d_j2, double* d_j3,
+                       double* d_lambda, double* d_work, void* stream) {
+  if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
+  if (d_lambda && !d_work) return JQMC_E_ARG;
+  const Sys& s = sys->s;
+  KParams P = make_params(sys, w);
+  const int A3 = s.has_j3 ? s.j3.nao : 1;
+  const int off_red = align16(s.N * 3 * 8);
+  const int off_su = align16(off_red + 33 * 8);
+  const int off_sd = align16(off_su + A3 * 8);
+  const int off_phi3 = align16(off_sd + A3 * 8);
+  const int smem = align16(off_phi3 + (s.has_j3 ? s.N * A3 * 8 : 8));
+  int rc = launch_check((const void*)k_dlnpsi_dparam, smem);
+  if (rc) return rc;
+  k_dlnpsi_dparam<<<w->nwalk, 128, smem, S(stream)>>>(P, off_red, off_su, off_sd, off_phi3, d_j1, d_j2,
+                                                      s.has_j3 ? d_j3 : nullptr, d_lambda, d_work);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 

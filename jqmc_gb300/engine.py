@@ -251,6 +251,22 @@ class WalkerSet:
         d = self.desc()
         _lib.check(_lib.lib().jqmc_lu_rebuild_refine(self.sys.handle, C.byref(d), self.sys.stream), "jqmc_lu_rebuild_refine")
 
+    def dlnpsi_dparam(self, lam: bool = True):
+        """Raw per-walker derivative blocks of ln|psi| (FP64 walkers): (d_j1 (W,),
+        d_j2 (W,), d_j3 (W, A3, A3+1) or None, d_lambda_AO (W, A, A) or None)."""
+        dev = self.sys.device
+        W, n, A, A3 = self.nwalk, self.sys.n_up, self.sys.A, self.sys.A3
+        j1 = torch.empty(W, dtype=torch.float64, device=dev)
+        j2 = torch.empty_like(j1)
+        j3 = torch.empty((W, A3, A3 + 1), dtype=torch.float64, device=dev) if A3 else None
+        dl = torch.empty((W, A, A), dtype=torch.float64, device=dev) if lam else None
+        work = torch.empty((W, 2, n, A), dtype=torch.float64, device=dev) if lam else None
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_dlnpsi_dparam(self.sys.handle, C.byref(d), ptr(j1), ptr(j2), ptr(j3), ptr(dl), ptr(work),
+                                                 self.sys.stream), "jqmc_dlnpsi_dparam")
+        return j1, j2, j3, dl
+
     def log_psi(self):
         dev = self.sys.device
         ld = torch.empty(self.nwalk, dtype=torch.float64, device=dev)

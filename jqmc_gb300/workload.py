@@ -37,37 +37,45 @@ def ao_vgl_flops(shells: np.ndarray) -> float:
     return f
 
 
-def lrdmc_step_split(gs, ecp_fraction: float):
-    """(mesh + move ops, electron-term ops) of one projection of one walker: the
-    first part runs in float in the mixed form, the second stays in double."""
+def _step_parts(gs, ecp_fraction: float):
+    """Operation counts of one GFMC_n projection of one walker, by phase, as the
+    walker kernels execute it (streaming caches: the AO derivative tables and the
+    per-electron energy cache are read every step and recomputed only for the
+    moved electron)."""
     keep = gs._keep
     N, n, A, M = gs.N, gs.n_up, gs.A, len(keep["pos"])
     A3 = gs.A3
     det_p = ao_point_flops(keep["dsh"])
     j3_p = ao_point_flops(keep["jsh"]) if A3 else 0.0
-    ratio = det_p + j3_p + M * (8 + EXP_FLOPS + 6) + N * 12 + EXP_FLOPS + 3
-    mesh = 6 * N * (ratio + 8) + gs.Nv * N * ecp_fraction * (ratio + 40 + 2 * EXP_FLOPS)
-    move = 2 * (det_p + j3_p) + 4 * A * n + 4 * n * n + 2 * A * A + 6 * A * n + 4 * n * n + 4 * A3 * A3 + N * A3
-    elec = N * (ao_vgl_flops(keep["dsh"]) + (ao_vgl_flops(keep["jsh"]) if A3 else 0.0) + M * (30 + EXP_FLOPS) + N * 27)
-    sums = 6 * N * 6 + N * N * 5 + N * M * (12 + EXP_FLOPS) + 12 * N * 3
-    return mesh + move, elec + sums
+    det_v = ao_vgl_flops(keep["dsh"])
+    j3_v = ao_vgl_flops(keep["jsh"]) if A3 else 0.0
+    # psi(r')/psi(r) at one mesh point: AO values dotted with the T row / J3 field,
+    # J1 over nuclei, J2 over electrons, the exponential of the Jastrow difference
+    ratio = det_p + j3_p + M * (12 + 2 * EXP_FLOPS) + N * 16 + EXP_FLOPS + 3
+    mesh = 6 * N * (ratio + 8) + gs.Nv * N * ecp_fraction * (ratio + 40)
+    # electron terms: cached derivative tables dotted with T rows and J3 fields
+    elec_dots = N * (2 * (4 * A + 5 * A3) + 40)
+    # rank-1 move: AO values at the old and new position, lam^T dphi, T/G/G^-1
+    # updates, J3 field update
+    move = 2 * (det_p + j3_p) + 2 * A * A + 10 * A * n + 8 * n * n + 2 * A3 * A3 + 2 * N * A3
+    # FP64 in both forms: derivative tables of the moved electron, its energy-cache
+    # row and the pair updates, the (diag, nondiag) sums and the move choice
+    fp64 = det_v + j3_v + M * (30 + EXP_FLOPS) + N * 27 + 6 * N * 6 + gs.Nv * N * 2 + 12 * N * 3
+    return mesh, elec_dots, move, fp64
+
+
+def lrdmc_step_split(gs, ecp_fraction: float):
+    """(float part, FP64 part) of one projection of one walker in the mixed form:
+    the mesh ratios, the electron-term dots and the rank-1 table updates run in
+    float; the moved electron's derivative tables, the energy cache, the sums and
+    the move choice stay in double."""
+    mesh, elec_dots, move, fp64 = _step_parts(gs, ecp_fraction)
+    return mesh + elec_dots + move, fp64
 
 
 def lrdmc_step_flops(gs, ecp_fraction: float) -> float:
-    """FP64 operations of one GFMC_n projection of one walker (jqmc_gb300 kernels)."""
-    keep = gs._keep
-    N, n, A, M = gs.N, gs.n_up, gs.A, len(keep["pos"])
-    A3 = gs.A3
-    det_p = ao_point_flops(keep["dsh"])
-    j3_p = ao_point_flops(keep["jsh"]) if A3 else 0.0
-    ratio = det_p + j3_p + M * (8 + EXP_FLOPS + 6) + N * 12 + EXP_FLOPS + 3
-    kin_mesh = 6 * N * (ratio + 8)
-    ecp_mesh = gs.Nv * N * ecp_fraction * (ratio + 40 + 2 * EXP_FLOPS)
-    elec = N * (ao_vgl_flops(keep["dsh"]) + (ao_vgl_flops(keep["jsh"]) if A3 else 0.0) + M * (30 + EXP_FLOPS) + N * 27)
-    sums = 6 * N * 6 + N * N * 5 + N * M * (12 + EXP_FLOPS)
-    move = 2 * (det_p + j3_p) + 4 * A * n + 4 * n * n + 2 * A * A + 6 * A * n + 4 * n * n + 4 * A3 * A3 + N * A3
-    cdf = 12 * N * 3
-    return kin_mesh + ecp_mesh + elec + sums + move + cdf
+    """Operations of one GFMC_n projection of one walker (all FP64 in the plain form)."""
+    return sum(_step_parts(gs, ecp_fraction))
 
 
 def lrdmc_step_bytes(gs) -> float:
@@ -75,3 +83,27 @@ def lrdmc_step_bytes(gs) -> float:
     T_up, T_dn (2 n A doubles each way), the J3 field (N A3), and G, G^-1 once per
     block (amortised, ignored)."""
     return 8.0 * (2 * 2 * gs.n_up * gs.A + 2 * gs.N * max(gs.A3, 0))
+
+
+def dlnpsi_flops(gs, lam: bool = True) -> float:
+    """FP64 operations of jqmc_dlnpsi_dparam for one walker: J1 / J2 parameter
+    sums, J3 AO values and the A3 x (A3+1) block, and (lam) the AO values of
+    every electron, X = G^-T Psi_dn (n^2 A) and the A x A block (n A^2)."""
+    keep = gs._keep
+    N, n, A, M, A3 = gs.N, gs.n_up, gs.A, len(keep["pos"]), gs.A3
+    f = N * M * (12 + EXP_FLOPS) + N * (N - 1) / 2 * 14
+    if A3:
+        f += N * ao_point_flops(keep["jsh"]) + 2 * N * A3 * A3 + 2 * N * A3
+    if lam:
+        f += N * ao_point_flops(keep["dsh"]) + 2 * n * n * A + 2 * n * A * A
+    return f
+
+
+def dlnpsi_bytes(gs, lam: bool = True) -> float:
+    """HBM bytes of jqmc_dlnpsi_dparam per walker: positions and G^-1 in, the
+    blocks out, the Phi / X work rows written and read back."""
+    n, A, N, A3 = gs.n_up, gs.A, gs.N, gs.A3
+    b = 8.0 * (3 * N + n * n + 2 + A3 * (A3 + 1))
+    if lam:
+        b += 8.0 * (A * A + 3 * 2 * n * A)
+    return b
