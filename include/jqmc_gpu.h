@@ -188,6 +188,18 @@ int jqmc_lrdmc_project(const jqmc_system* sys, const jqmc_walkers* w, int32_t K,
 int jqmc_lrdmc_energy(const jqmc_system* sys, const jqmc_walkers* w, const double* d_draw, double alat,
                       double* d_eL, double* d_vdiag, void* stream);
 
+/* Continuous-time LRDMC projections (GFMC_t, jqmc_gfmc.py:724-1107 and the
+ * while loop :1539-1620).  Each walker projects until its remaining time
+ * d_tau_left (in/out) is spent or its K draws are used: per step
+ * d_draw[w][k] = (alpha, beta, gamma, xi, u_move) (nwalk*K*5),
+ * tau_update = min(tau_left, ln(1 - xi) / V_nondiag), d_w *= exp(-tau_update e_L),
+ * and the move is made only while time is left.  d_nsteps (out): projections
+ * made by this call; d_eL (out): e_L of the step that spent the time (left
+ * unchanged for a walker whose draws ran out first -- call again with new
+ * draws).  Both precisions. */
+int jqmc_lrdmc_project_t(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const double* d_draw, double alat,
+                         double* d_w, double* d_tau_left, int32_t* d_nsteps, double* d_eL, void* stream);
+
 /* Stochastic reconfiguration with one comb draw zeta (jqmc_gfmc.py:2010-2090):
  * d_chosen[k] = first j with cumsum(w/sum w)[j] >= (k + zeta)/nwalk (clamped
  * to nwalk-1).  d_cum: caller-provided scratch of nwalk doubles that receives

@@ -73,6 +73,7 @@ def lib():
         L.jqmc_walker_init.argtypes = [vp, C.POINTER(Walkers), vp]
         L.jqmc_lu_rebuild_refine.argtypes = [vp, C.POINTER(Walkers), vp]
         L.jqmc_dlnpsi_dparam.argtypes = [vp, C.POINTER(Walkers), vp, vp, vp, vp, vp, vp]
+        L.jqmc_lrdmc_project_t.argtypes = [vp, C.POINTER(Walkers), i32, vp, f64, vp, vp, vp, vp, vp]
         L.jqmc_log_psi.argtypes = [vp, C.POINTER(Walkers), vp, vp, vp, vp]
         L.jqmc_vmc_sweep.argtypes = [vp, C.POINTER(Walkers), i32, vp, vp, f64, f64, vp, vp]
         L.jqmc_vmc_measure.argtypes = [vp, C.POINTER(Walkers), vp, f64, vp, vp, vp]
@@ -86,7 +87,7 @@ def lib():
         for name in ("jqmc_probe_fp64", "jqmc_system_create", "jqmc_system_destroy", "jqmc_ao_vgl", "jqmc_walker_init", "jqmc_log_psi",
                      "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
                      "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
-                     "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam"):
+                     "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -100,4 +101,4 @@ def check(rc: int, what: str) -> None:
 EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "jqmc_ao_vgl", "jqmc_walker_init",
             "jqmc_log_psi", "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
             "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
-            "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam")
+            "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t")

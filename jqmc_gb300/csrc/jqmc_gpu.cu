@@ -1312,6 +1312,13 @@ __device__ void lrdmc_sums(const Sys& s, const double* ec, int N, double* red, T
 }
 
 // ------------------------------------------------------------------ kernels
+// GFMC_t arguments of k_lrdmc (tau_left == nullptr: GFMC_n)
+struct TauArgs {
+  double* tau_left;   // in/out, per walker
+  int* nsteps;        // out: projections made in this launch
+  double* eL_last;    // out: e_L of the step that spent the remaining time
+};
+
 struct KParams {
   Sys s;
   WS ws;
@@ -1994,7 +2001,7 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
 // R: mesh arithmetic, Tab: table storage and updates.
 template <class R, class Tab>
 __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
-                        double* eL, double* vdiag) {
+                        double* eL, double* vdiag, TauArgs ta) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
   const Sys s = stage_tables(P.s, P.tl, smem);
@@ -2003,10 +2010,14 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
   Terms t = make_terms(P.ml, smem, gd, s);
   load_walker(k, P.ws, w);
   const int N = k.N;
-  const int nsteps = K > 0 ? K : 1;
+  const bool tmode = ta.tau_left != nullptr;    // GFMC_t: project until the walker's time is spent
+  const int dstride = tmode ? 5 : 4, uidx = tmode ? 4 : 3;
+  double tleft = tmode ? ta.tau_left[w] : 0.0;
+  int done = 0;
+  const int nsteps = (tmode && !(tleft > 0.0)) ? 0 : (K > 0 ? K : 1);
   double wl = K > 0 ? wgt[w] : 1.0;
   for (int step = 0; step < nsteps; ++step) {
-    const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * 4;
+    const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * dstride;
     if (threadIdx.x == 0) rotation(d[0], d[1], d[2], t.R);
     __syncthreads();
     electron_terms<Tab, R>(k, t, alat);
@@ -2020,7 +2031,20 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
       }
       break;
     }
-    wl = wl * (1.0 / (diag - E_scf) * (-1.0 * nondiag));
+    if (tmode) {
+      // jqmc_gfmc.py:995-1004: continuous-time weight and the time left
+      const double el = diag + nondiag;
+      const double tu = fmin(tleft, log(1.0 - d[3]) / nondiag);
+      wl = wl * exp(-tu * el);
+      tleft -= tu;
+      ++done;
+      if (!(tleft > 0.0)) {
+        if (threadIdx.x == 0) ta.eL_last[w] = el;
+        break;
+      }
+    } else {
+      wl = wl * (1.0 / (diag - E_scf) * (-1.0 * nondiag));
+    }
     const int nk = 6 * N, ne = s.ecp_flag ? s.nv * N : 0, np_ = nk + ne;
     int* kchoice = reinterpret_cast<int*>(k.sc + 31);
     if constexpr (sizeof(Tab) == sizeof(float)) {
@@ -2039,7 +2063,7 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
           if (lane >= o) incl += v;
         }
         double cdf = incl - part * inv;   // exclusive prefix of this lane's chunk
-        const double u = d[3];
+        const double u = d[uidx];
         int hit = -1;
         for (int p = p0; p < p1; ++p) {
           cdf += (p < nk ? fmin(t.el[p], 0.0) : fmin(t.V[p - nk], 0.0)) * inv;
@@ -2055,7 +2079,7 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
         double sum = 0.0;
         for (int p = 0; p < nk; ++p) sum += fmin(t.el[p], 0.0);
         for (int q = 0; q < ne; ++q) sum += fmin(t.V[q], 0.0);
-        const double u = d[3];
+        const double u = d[uidx];
         double cdf = 0.0;
         int kk = np_ - 1;
         for (int p = 0; p < np_; ++p) {
@@ -2106,6 +2130,10 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
     if (threadIdx.x == 0) {
       wgt[w] = wl;
       if (!isfinite(wl)) atomicOr(P.ws.status + w, JQMC_ST_NAN);
+      if (tmode) {
+        ta.tau_left[w] = tleft;
+        ta.nsteps[w] = done;
+      }
     }
     store_walker(k, P.ws, w);
   }
@@ -2220,7 +2248,7 @@ int launch_check(const void* fn, int smem) {
 }
 
 int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const double* d_draw, double alat, double E_scf,
-                 double* d_w, double* d_eL, double* d_vd, void* stream) {
+                 double* d_w, double* d_eL, double* d_vd, void* stream, TauArgs ta = TauArgs{nullptr, nullptr, nullptr}) {
   KParams P = make_params(sys, w);
   const int smem = P.ml.bytes;
   if (w->precision == JQMC_PREC_MIXED) {
@@ -2229,12 +2257,12 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
     auto fn = K > 0 ? k_lrdmc<float, float> : k_lrdmc<double, float>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
-    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd);
+    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);
   } else {
     auto fn = k_lrdmc<double, double>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
-    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd);
+    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
@@ -2531,6 +2559,13 @@ int jqmc_lrdmc_energy(const jqmc_system* sys, const jqmc_walkers* w, const doubl
                       double* d_vdiag, void* stream) {
   if (!walkers_ok(sys, w) || !d_draw || !d_eL || !d_vdiag || !(alat > 0.0)) return JQMC_E_ARG;
   return launch_lrdmc(sys, w, 0, d_draw, alat, 0.0, nullptr, d_eL, d_vdiag, stream);
+}
+
+int jqmc_lrdmc_project_t(const jqmc_system* sys, const jqmc_walkers* w, int32_t K, const double* d_draw, double alat,
+                         double* d_w, double* d_tau_left, int32_t* d_nsteps, double* d_eL, void* stream) {
+  if (!walkers_ok(sys, w) || K <= 0 || !d_draw || !d_w || !d_tau_left || !d_nsteps || !d_eL || !(alat > 0.0))
+    return JQMC_E_ARG;
+  return launch_lrdmc(sys, w, K, d_draw, alat, 0.0, d_w, nullptr, nullptr, stream, TauArgs{d_tau_left, d_nsteps, d_eL});
 }
 
 int jqmc_branch_comb(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, double* d_cum, void* stream) {

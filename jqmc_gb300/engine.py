@@ -299,6 +299,16 @@ class WalkerSet:
         _lib.check(_lib.lib().jqmc_lrdmc_project(self.sys.handle, C.byref(d), K, C.c_void_p(draws.data_ptr()), float(alat),
                                                  float(E_scf), C.c_void_p(w.data_ptr()), self.sys.stream), "jqmc_lrdmc_project")
 
+    def lrdmc_project_t(self, draws: torch.Tensor, alat: float, w: torch.Tensor, tau_left: torch.Tensor,
+                        nsteps: torch.Tensor, eL: torch.Tensor):
+        """GFMC_t projections until tau_left is spent or the K draws (W, K, 5) are used."""
+        K = draws.shape[1]
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_lrdmc_project_t(self.sys.handle, C.byref(d), K, C.c_void_p(draws.data_ptr()), float(alat),
+                                                   C.c_void_p(w.data_ptr()), C.c_void_p(tau_left.data_ptr()),
+                                                   C.c_void_p(nsteps.data_ptr()), C.c_void_p(eL.data_ptr()),
+                                                   self.sys.stream), "jqmc_lrdmc_project_t")
+
     def lrdmc_energy(self, last_draw: torch.Tensor, alat: float):
         eL = torch.empty(self.nwalk, dtype=torch.float64, device=self.sys.device)
         vd = torch.empty_like(eL)

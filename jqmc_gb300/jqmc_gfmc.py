@@ -121,3 +121,129 @@ class GFMC_n:
     def get_E(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
         e, e2, w = self.e_L[num_mcmc_warmup_steps:], self.e_L2[num_mcmc_warmup_steps:], self.w_L[num_mcmc_warmup_steps:]
         return jackknife_energy(e, e2, w, num_mcmc_bin_blocks)
+
+
+class GFMC_t:
+    """LRDMC driver with fixed projection time (GFMC_t), on one GPU.
+
+    Mirrors ``GFMC_t`` of jqmc/jqmc_gfmc.py:208-2390: the constructor arguments,
+    ``run(num_mcmc_steps)``, the stored per-branching observables and ``get_E``.
+    One "MCMC step" is one branching cycle: every walker projects for time ``tau``
+    (``jqmc_lrdmc_project_t`` in chunks of ``draws_per_call`` steps until no
+    walker has time left; per step ``tau_update = min(tau_left, ln(1-xi)/V_nondiag)``
+    and ``w *= exp(-tau_update e_L)``, jqmc_gfmc.py:724-1107), the FP64 rebuild of
+    the tables carried by rank-1 updates, e_L at the final configuration, the
+    weighted averages (jqmc_gfmc.py:1940-1996: sum w e_L / sum w) and the comb
+    reconfiguration.  The reference runs all walkers in one lock-step while loop
+    and keeps the e_L of its last iteration, which for a walker whose time was
+    already spent is e_L at its final configuration with a fresh rotation; here
+    each walker stops on its own and e_L is evaluated at the final configuration
+    with a fresh rotation.
+    """
+
+    def __init__(self, hamiltonian_data: Hamiltonian_data = None, num_walkers: int = 40, num_gfmc_collect_steps: int = 5,
+                 mcmc_seed: int = 34467, tau: float = 0.1, alat: float = 0.1, random_discretized_mesh: bool = True,
+                 non_local_move: str = "tmove", Nv: int = 6, init_r_up=None, init_r_dn=None, precision: str = "fp64",
+                 draws_per_call: int = 64, max_calls: int = 10000):
+        if non_local_move != "tmove":
+            raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+        if not tau > 0.0:
+            raise ValueError("tau must be positive")
+        hamiltonian_data.sanity_check()
+        self.hamiltonian_data = hamiltonian_data
+        self.num_walkers = num_walkers
+        self.num_gfmc_collect_steps = num_gfmc_collect_steps
+        self.tau = tau
+        self.alat = alat
+        self.random_discretized_mesh = random_discretized_mesh
+        self.draws_per_call = draws_per_call
+        self.max_calls = max_calls
+        self.sys = GpuSystem(hamiltonian_data, Nv=Nv)
+        if init_r_up is None:
+            st = hamiltonian_data.structure_data
+            coul = hamiltonian_data.coulomb_potential_data
+            init_r_up, init_r_dn = initial_electrons(st.positions, coul.effective_charges, self.sys.n_up, self.sys.n_dn,
+                                                     num_walkers, mcmc_seed)
+        self.precision = precision
+        self.walkers = WalkerSet(self.sys, init_r_up, init_r_dn, precision=precision)
+        self._spare = WalkerSet.empty_like(self.walkers)
+        dev = self.sys.device
+        self.gen = torch.Generator(device=dev)
+        self.gen.manual_seed(mcmc_seed)
+        self._np_rng = np.random.default_rng(mcmc_seed)
+        W = num_walkers
+        self._w = torch.empty(W, dtype=torch.float64, device=dev)
+        self._tau_left = torch.empty(W, dtype=torch.float64, device=dev)
+        self._nsteps = torch.zeros(W, dtype=torch.int32, device=dev)
+        self._eL_last = torch.zeros(W, dtype=torch.float64, device=dev)
+        self._chosen = torch.empty(W, dtype=torch.int32, device=dev)
+        self._cum = torch.empty(W, dtype=torch.float64, device=dev)
+        self._e_L, self._e_L2, self._w_L, self._proj = [], [], [], []
+        self.mcmc_counter = 0
+
+    def draws(self, K: int) -> torch.Tensor:
+        """(W, K, 5): three rotation angles U(-2pi, 2pi), xi, and the move uniform."""
+        d = torch.rand((self.num_walkers, K, 5), generator=self.gen, dtype=torch.float64, device=self.sys.device)
+        if self.random_discretized_mesh:
+            d[..., :3].mul_(4.0 * math.pi).sub_(2.0 * math.pi)
+        else:
+            d[..., :3].zero_()
+        return d
+
+    def project(self, draw_source=None):
+        """Project every walker for time tau; returns (w, total projections per walker)."""
+        ws = self.walkers
+        self._w.fill_(1.0)
+        self._tau_left.fill_(self.tau)
+        total = torch.zeros(self.num_walkers, dtype=torch.int64, device=self.sys.device)
+        for _ in range(self.max_calls):
+            d = draw_source(self.draws_per_call) if draw_source is not None else self.draws(self.draws_per_call)
+            ws.lrdmc_project_t(d, self.alat, self._w, self._tau_left, self._nsteps, self._eL_last)
+            total += self._nsteps
+            if not bool((self._tau_left > 0.0).any()):
+                return self._w, total
+        raise RuntimeError(f"GFMC_t: walkers still had time left after {self.max_calls} calls")
+
+    def run_block(self, zeta: float, draw_source=None):
+        """Projection for time tau + energy + reconfiguration.  Returns device scalars
+        (w_sum, sum w e_L, sum w e_L^2, mean projections per walker) before branching."""
+        w, total = self.project(draw_source)
+        ws = self.walkers
+        ws.rebuild()
+        ang = self.draws(1)[:, 0].contiguous()
+        eL, _ = ws.lrdmc_energy(ang, self.alat)
+        sums = torch.stack([w.sum(), (w * eL).sum(), (w * eL * eL).sum(), total.double().mean()])
+        branch_comb(w, zeta, self._chosen, self._cum)
+        self._spare.gather_from(ws, self._chosen)
+        self.walkers, self._spare = self._spare, self.walkers
+        return sums
+
+    def run(self, num_mcmc_steps: int = 50, max_time: int = 86400) -> None:
+        for _ in range(num_mcmc_steps):
+            zeta = float(self._np_rng.random())
+            sums = self.run_block(zeta).cpu().numpy()
+            self._w_L.append(sums[0] / self.num_walkers)
+            self._e_L.append(sums[1] / sums[0])
+            self._e_L2.append(sums[2] / sums[0])
+            self._proj.append(sums[3])
+            self.mcmc_counter += 1
+
+    @property
+    def w_L(self) -> np.ndarray:
+        return gfmc_G_L(np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1), self.num_gfmc_collect_steps)
+
+    @property
+    def e_L(self) -> np.ndarray:
+        return np.asarray(self._e_L, dtype=np.float64).reshape(-1, 1)[self.num_gfmc_collect_steps:]
+
+    @property
+    def e_L2(self) -> np.ndarray:
+        return np.asarray(self._e_L2, dtype=np.float64).reshape(-1, 1)[self.num_gfmc_collect_steps:]
+
+    @property
+    def average_projection_counter(self) -> np.ndarray:
+        return np.asarray(self._proj, dtype=np.float64)
+
+    def get_E(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
+        e, e2, w = self.e_L[num_mcmc_warmup_steps:], self.e_L2[num_mcmc_warmup_steps:], self.w_L[num_mcmc_warmup_steps:]
+        return jackknife_energy(e, e2, w, num_mcmc_bin_blocks)

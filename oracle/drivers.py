@@ -14,6 +14,10 @@ LRDMC step    (jqmc_gfmc.py:4779-5166, ``_body_step_core`` with the fresh
     fixed-node split, discretised diagonal, w *= -sum_nondiag / (sum_diag - E_scf),
     move chosen by a sequential cumsum over the normalised FN weights and a
     left searchsorted, Sherman-Morrison update of G^-1.
+GFMC_t step   (jqmc_gfmc.py:724-1107, ``_projection_t_core``):
+    draw = (alpha, beta, gamma, xi, u_move); the same elements; e_L = diag + nondiag,
+    tau_update = min(tau_left, ln(1 - xi) / nondiag), w *= exp(-tau_update e_L),
+    and the move is made only while tau_left > 0 after the update.
 Branching     (jqmc_gfmc.py:2010-2090 with one process): comb z_k = (k + zeta)/W
     over the cumulative normalised weights (sequential cumsum), left searchsorted.
 """
@@ -215,6 +219,24 @@ def lrdmc_step(o: OracleSystem, st: WalkerState, w: float, draw, alat: float, E_
     spin, i, rn = move_target(o, st, k, R, alat, Nv)
     sm_update(o, st, spin, i, rn)
     return w, diag, nondiag, k
+
+
+def lrdmc_step_t(o: OracleSystem, st: WalkerState, w: float, tau_left: float, draw, alat: float, Nv: int = 6):
+    """One GFMC_t projection (jqmc_gfmc.py:724-1107): draw = (alpha, beta, gamma, xi, u).
+    tau_update = min(tau_left, ln(1 - xi) / V_nondiag); w *= exp(-tau_update e_L);
+    the chosen move is made only while time is left.  Returns (w, tau_left, e_L, moved)."""
+    R = rotation_matrix(draw[0], draw[1], draw[2])
+    diag, nondiag, p, _, _ = lrdmc_terms(o, st, R, alat, Nv)
+    e_L = diag + nondiag
+    tau_update = min(tau_left, np.log(1.0 - float(draw[3])) / nondiag)
+    w = w * np.exp(-tau_update * e_L)
+    tau_left = tau_left - tau_update
+    if tau_left <= 0.0:
+        return w, tau_left, e_L, False
+    k = choose_move(p, float(draw[4]))
+    spin, i, rn = move_target(o, st, k, R, alat, Nv)
+    sm_update(o, st, spin, i, rn)
+    return w, tau_left, e_L, True
 
 
 def lrdmc_energy(o: OracleSystem, st: WalkerState, last_draw, alat: float, Nv: int = 6):

@@ -31,3 +31,18 @@ def test_gfmc_n_runs_and_reports_energy():
     E, Estd, _, _ = g.get_E(num_mcmc_warmup_steps=2, num_mcmc_bin_blocks=5)
     assert np.isfinite(E)
     assert not g.walkers.status.any()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gfmc_t_runs_and_reports_energy(precision):
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.jqmc_gfmc import GFMC_t
+    syn = synthetic.water_like()
+    g = GFMC_t(syn.hamiltonian, num_walkers=64, mcmc_seed=5, tau=0.05, alat=0.2, num_gfmc_collect_steps=2,
+               precision=precision, draws_per_call=16)
+    g.run(12)
+    assert np.all(np.isfinite(g.e_L)) and g.e_L.shape == (10, 1)
+    assert np.all(g.average_projection_counter > 1.0)
+    E, Estd, _, _ = g.get_E(num_mcmc_warmup_steps=2, num_mcmc_bin_blocks=4)
+    assert np.isfinite(E)
+    assert not g.walkers.status.any()

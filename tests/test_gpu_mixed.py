@@ -124,3 +124,33 @@ def test_mixed_energy_after_block_and_rebuild(pair):
     gi = (b.Ginv.double() - a.Ginv).abs().amax(dim=(1, 2)) / a.Ginv.abs().amax(dim=(1, 2))
     assert float(gi[same].max()) < 1e-5
     assert not b.status.any()
+
+
+def test_mixed_gfmc_t_follows_fp64(pair):
+    """GFMC_t projections with the same draws: the mixed form takes the same
+    moves as the FP64 form for most walkers, with weights and spent time agreeing."""
+    syn, gs, w64, w32 = pair
+    from jqmc_gb300.engine import WalkerSet
+    r = w64.r[:64].cpu().numpy()
+    n = gs.n_up
+    a = WalkerSet(gs, r[:, :n], r[:, n:], precision="fp64")
+    b = WalkerSet(gs, r[:, :n], r[:, n:], precision="mixed")
+    K = 40
+    rng = np.random.default_rng(23)
+    dr = np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (64, K, 3)), rng.uniform(size=(64, K, 2))], axis=-1)
+    d = torch.as_tensor(dr, device=gs.device)
+    out = []
+    for ws in (a, b):
+        w = torch.ones(64, dtype=torch.float64, device=gs.device)
+        tl = torch.full((64,), 0.01, dtype=torch.float64, device=gs.device)
+        ns = torch.zeros(64, dtype=torch.int32, device=gs.device)
+        el = torch.zeros(64, dtype=torch.float64, device=gs.device)
+        ws.lrdmc_project_t(d, 0.2, w, tl, ns, el)
+        out.append((w, tl, ns))
+    same = (a.r - b.r).abs().amax(dim=(1, 2)) < 1e-6
+    frac = float(same.double().mean())
+    relw = ((out[0][0] - out[1][0]).abs() / out[0][0].abs())[same]
+    print(f"{syn.name}: GFMC_t same path {frac:.3f}, weight rel diff max {float(relw.max()):.2e}")
+    assert frac >= 0.9
+    assert float(relw.max()) < 1e-4
+    assert not b.status.any()

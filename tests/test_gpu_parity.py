@@ -204,3 +204,44 @@ def test_lu_rebuild_refine(setup):
         st = D.init_state(o, r[w, :n], r[w, n:])
         assert rel(ws.Ginv[w].cpu().numpy(), st.Ginv) < 1e-10
     assert not ws.status.any()
+
+
+def test_lrdmc_projection_t_trajectory(setup):
+    """GFMC_t: projections until the time is spent, the draws split over two
+    calls (the second resumes with the time left); positions, weights, time
+    left, step counts and the final-step e_L against the oracle."""
+    from oracle import drivers as D
+    syn, gs, o = setup
+    W = 3
+    tau = 0.01 if syn.name == "water_like" else 0.0015
+    K1, K2 = 3, 9
+    ws, r_up, r_dn = _walkers(syn, gs, W, 14)
+    rng = np.random.default_rng(15)
+    dr = np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (W, K1 + K2, 3)), rng.uniform(size=(W, K1 + K2, 2))], axis=-1)
+    dev = gs.device
+    wt = torch.ones(W, dtype=torch.float64, device=dev)
+    tl = torch.full((W,), tau, dtype=torch.float64, device=dev)
+    ns = torch.zeros(W, dtype=torch.int32, device=dev)
+    el = torch.full((W,), np.nan, dtype=torch.float64, device=dev)
+    total = np.zeros(W, dtype=np.int64)
+    for a, b in ((0, K1), (K1, K1 + K2)):
+        ws.lrdmc_project_t(torch.as_tensor(dr[:, a:b].copy(), device=dev), 0.2, wt, tl, ns, el)
+        total += ns.cpu().numpy()
+    r = ws.r.cpu().numpy()
+    for w in range(W):
+        st = D.init_state(o, r_up[w], r_dn[w])
+        wl, left, steps, e_last = 1.0, tau, 0, np.nan
+        for k in range(K1 + K2):
+            if left <= 0.0:
+                break
+            wl, left, e, moved = D.lrdmc_step_t(o, st, wl, left, dr[w, k], 0.2)
+            steps += 1
+            if left <= 0.0:
+                e_last = e
+        assert total[w] == steps
+        assert rel(r[w], np.vstack([st.r_up, st.r_dn])) < 1e-12
+        assert abs(float(wt[w]) - wl) < RTOL * abs(wl)
+        assert abs(float(tl[w]) - left) < 1e-12
+        if left <= 0.0:
+            assert abs(float(el[w]) - e_last) < RTOL * max(1.0, abs(e_last))
+    assert not ws.status.any()
