@@ -37,6 +37,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <algorithm>
 #include <vector>
 
 #include "jqmc_gpu.h"
@@ -173,20 +174,22 @@ struct WS {
 struct TableLayout {
   int off_dsh, off_dpr, off_dprf, off_jsh, off_jpr, off_jprf, off_apos, off_azeff, off_j1z, off_maxl1, off_chan, off_terms,
       off_mpts, off_mw;
+  int f64prims;   // stage the double primitive tables (the float kernels read them from L1/L2)
   int bytes;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-TableLayout table_layout(const Sys& s) {
+TableLayout table_layout(const Sys& s, bool f64prims = true) {
   TableLayout L;
   int o = 0;
   const int jsh = s.has_j3 ? s.j3.nshell : 0, jpr = s.has_j3 ? s.j3.nprim : 0;
+  L.f64prims = f64prims ? 1 : 0;
   L.off_dsh = o; o = align16(o + s.det.nshell * 8 * 4);
-  L.off_dpr = o; o = align16(o + s.det.nprim * 2 * 8);
+  L.off_dpr = o; o = align16(o + (f64prims ? s.det.nprim * 2 * 8 : 0));
   L.off_dprf = o; o = align16(o + s.det.nprim * 2 * 4);
   L.off_jsh = o; o = align16(o + jsh * 8 * 4);
-  L.off_jpr = o; o = align16(o + jpr * 2 * 8);
+  L.off_jpr = o; o = align16(o + (f64prims ? jpr * 2 * 8 : 0));
   L.off_jprf = o; o = align16(o + jpr * 2 * 4);
   L.off_apos = o; o = align16(o + s.natom * 3 * 8);
   L.off_azeff = o; o = align16(o + s.natom * 8);
@@ -213,18 +216,22 @@ __device__ void copy_words(void* dst, const void* src, int bytes) {
 __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* smem) {
   Sys s = g;
   copy_words(smem + L.off_dsh, g.det.shells, g.det.nshell * 32);
-  copy_words(smem + L.off_dpr, g.det.prims, g.det.nprim * 16);
   copy_words(smem + L.off_dprf, g.det.primsf, g.det.nprim * 8);
   s.det.shells = reinterpret_cast<const int*>(smem + L.off_dsh);
-  s.det.prims = reinterpret_cast<const double*>(smem + L.off_dpr);
   s.det.primsf = reinterpret_cast<const float*>(smem + L.off_dprf);
+  if (L.f64prims) {
+    copy_words(smem + L.off_dpr, g.det.prims, g.det.nprim * 16);
+    s.det.prims = reinterpret_cast<const double*>(smem + L.off_dpr);
+  }
   if (g.has_j3) {
     copy_words(smem + L.off_jsh, g.j3.shells, g.j3.nshell * 32);
-    copy_words(smem + L.off_jpr, g.j3.prims, g.j3.nprim * 16);
     copy_words(smem + L.off_jprf, g.j3.primsf, g.j3.nprim * 8);
     s.j3.shells = reinterpret_cast<const int*>(smem + L.off_jsh);
-    s.j3.prims = reinterpret_cast<const double*>(smem + L.off_jpr);
     s.j3.primsf = reinterpret_cast<const float*>(smem + L.off_jprf);
+    if (L.f64prims) {
+      copy_words(smem + L.off_jpr, g.j3.prims, g.j3.nprim * 16);
+      s.j3.prims = reinterpret_cast<const double*>(smem + L.off_jpr);
+    }
   }
   copy_words(smem + L.off_apos, g.atom_pos, g.natom * 24);
   copy_words(smem + L.off_azeff, g.atom_zeff, g.natom * 8);
@@ -349,6 +356,56 @@ __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R
     case 4: emit_vgl<4, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
     case 5: emit_vgl<5, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
     default: emit_vgl<6, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
+  }
+}
+
+// P points at once: sum_{a in shell} phi_a(d_p) v[a] into acc[p].  The points
+// share the shell's primitive table and the v entries (loaded once); the P
+// evaluations are independent, which gives each lane P chains of work.
+template <int L, int P, class R, class V>
+__device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* dz, const R* rad, int ao0, int jlo, int nm,
+                                             const V* v, R* acc) {
+  R vv[2 * L + 1];
+#pragma unroll
+  for (int j = 0; j < 2 * L + 1; ++j) {
+    const int k = j - jlo;
+    vv[j] = (k >= 0 && k < nm) ? (R)v[ao0 + k] : R(0);
+  }
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    R S[2 * L + 1];
+    sh_val<L, R>(dx[p], dy[p], dz[p], S);
+    R part = R(0);
+#pragma unroll
+    for (int j = 0; j < 2 * L + 1; ++j) part += S[j] * vv[j];
+    acc[p] += rad[p] * part;
+  }
+}
+
+template <int P, class R, class V>
+__device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, R* acc) {
+  const int* sh = b.shells + 8 * s;
+  const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const R* pr = prims_of<R>(b) + 2 * p0;
+  R r2[P], rad[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    r2[p] = dx[p] * dx[p] + dy[p] * dy[p] + dz[p] * dz[p];
+    rad[p] = R(0);
+  }
+  for (int q = 0; q < np; ++q) {
+    const R Z = pr[2 * q], c = pr[2 * q + 1];
+#pragma unroll
+    for (int p = 0; p < P; ++p) rad[p] += c * Num<R>::ex(-Z * r2[p]);
+  }
+  switch (l) {
+    case 0: emit_dot_pts<0, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 1: emit_dot_pts<1, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 2: emit_dot_pts<2, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 3: emit_dot_pts<3, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 4: emit_dot_pts<4, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 5: emit_dot_pts<5, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    default: emit_dot_pts<6, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
   }
 }
 
@@ -1055,18 +1112,16 @@ struct Terms {
   double* ei;     // N  e-ion Coulomb per electron
   double* eid;    // N  discretised e-ion (distance floor alat)
   double* edist;  // N  distance to the nearest nucleus
-  double* vl;     // N*kSlots non-local channel values V_l(edist) at the nearest nucleus
   int* eatom;     // N  nearest nucleus
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
   double* R;      // 9 rotation
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
-  int* ecpe;      // N electrons whose nearest nucleus has non-local channels; ecpe[N] = count
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_vl, off_ea, off_el, off_V, off_R, off_dA, off_dE, off_ecpe, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_dA, off_dE, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form in shared memory
@@ -1079,14 +1134,12 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_ei = o; o = align16(o + N * 8);
   L.off_eid = o; o = align16(o + N * 8);
   L.off_ed = o; o = align16(o + N * 8);
-  L.off_vl = o; o = align16(o + N * kSlots * 8);
   L.off_ea = o; o = align16(o + N * 4);
   L.off_el = o; o = align16(o + 6 * N * 8);
   L.off_V = o; o = align16(o + (s.nv > 0 ? s.nv : 1) * N * 8);
   L.off_R = o; o = align16(o + 9 * 8);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
-  L.off_ecpe = o; o = align16(o + (N + 1) * 4);
   L.bytes = o;
   return L;
 }
@@ -1103,26 +1156,24 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.ei = reinterpret_cast<double*>(smem + L.off_ei);
   t.eid = reinterpret_cast<double*>(smem + L.off_eid);
   t.edist = reinterpret_cast<double*>(smem + L.off_ed);
-  t.vl = reinterpret_cast<double*>(smem + L.off_vl);
   t.eatom = reinterpret_cast<int*>(smem + L.off_ea);
   t.el = reinterpret_cast<double*>(smem + L.off_el);
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
-  t.dE = L.off_ecpe > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
   if (gdcache) {
     t.dA = gdcache;
     t.dE = gdcache + (size_t)s.N * s.natom * 3;
   }
-  t.ecpe = reinterpret_cast<int*>(smem + L.off_ecpe);
   return t;
 }
 
 // Phase A: per-electron continuum kinetic energy and the old-position values
 // the ratios need (wavefunction.py:1142-1207 with jastrow_factor.py:961-1034,
 // 3435-3558, 4077-4156).  One warp per electron: the cached AO derivative tables
-// are dotted with the electron's T row and J3 field (lane sums in the table
-// type Acc, warp sum in double); J1/J2 derivatives, Coulomb and ECP terms come
+// are dotted with the electron's T row and J3 field (lane and warp sums in the
+// accumulation type Acc); J1/J2 derivatives, Coulomb and ECP terms come
 // from the energy cache.
 template <class Tab, class Acc = Tab>
 __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
@@ -1166,10 +1217,10 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
         thl += (Acc)q[4 * A3 + a] * hv;
       }
     }
-    const double gx = warp_sum((double)tgx), gy = warp_sum((double)tgy), gz = warp_sum((double)tgz);
-    const double lp = warp_sum((double)tlp);
-    const double c3 = warp_sum((double)tc3), hx = warp_sum((double)thx), hy = warp_sum((double)thy);
-    const double hz = warp_sum((double)thz), hl = warp_sum((double)thl);
+    const double gx = (double)warp_sum(tgx), gy = (double)warp_sum(tgy), gz = (double)warp_sum(tgz);
+    const double lp = (double)warp_sum(tlp);
+    const double c3 = (double)warp_sum(tc3), hx = (double)warp_sum(thx), hy = (double)warp_sum(thy);
+    const double hz = (double)warp_sum(thz), hl = (double)warp_sum(thl);
     if (lane == 0) {
       const double* row = k.ec + (size_t)e * kEC;
       const double Gx = gx + hx + row[EC_J1G] + row[EC_J2G];
@@ -1181,7 +1232,6 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
       t.ei[e] = row[EC_EI];
       t.eatom[e] = (int)row[EC_NEAR];
       t.edist[e] = row[EC_DIST];
-      for (int l = 0; l < kSlots; ++l) t.vl[e * kSlots + l] = row[EC_VL + l];
       if (s.ecp_flag && s.ecp_maxl1[(int)row[EC_NEAR]] <= 0)
         for (int v = 0; v < s.nv; ++v) t.V[e * s.nv + v] = 0.0;
       if (!s.ecp_flag) {
@@ -1196,73 +1246,178 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int c = 0;
-    if (s.ecp_flag)
-      for (int e = 0; e < k.N; ++e)
-        if (s.ecp_maxl1[t.eatom[e]] > 0) t.ecpe[c++] = e;
-    t.ecpe[k.N] = c;
-  }
-  __syncthreads();
 }
 
-// psi(r')/psi(r) for electron e moved by (sx, sy, sz) (det x Jastrow), arithmetic in R
-template <class R, class Tab>
-__device__ R wf_ratio(const Work<Tab>& k, const Terms& t, int e, double sx, double sy, double sz) {
+// One J1 / J2 pair term of J(r_e + s) - J(r_e): d0 = r_e - X, move s; the
+// difference is formed from r'^2 - r^2 = (2 d0 + s).s so that small moves keep
+// their relative accuracy (jastrow_factor.py:649-726, 1181-1251).
+template <class R>
+__device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, int type, R a, R c, R A, bool j1) {
+  const R r2 = d0x * d0x + d0y * d0y + d0z * d0z;
+  const R dr2 = (R(2) * d0x + sx) * sx + (R(2) * d0y + sy) * sy + (R(2) * d0z + sz) * sz;
+  const R rr = Num<R>::sq(r2);
+  const R rp2 = r2 + dr2;
+  const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
+  const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
+  if (j1) {
+    if (type == 0) return A / (R(2) * a) * Num<R>::ex(-a * c * rr) * Num<R>::em1(-a * c * dr);
+    return -A * dr / (R(2) * (R(1) + a * c * rr) * (R(1) + a * c * rp));
+  }
+  if (type == 0) return dr / (R(2) * (R(1) + a * rr) * (R(1) + a * rp));
+  return -Num<R>::ex(-a * rr) * Num<R>::em1(-a * dr) / (R(2) * a);
+}
+
+// psi(r_e + s_p)/psi(r) for P moves s_p of electron e (det x Jastrow),
+// arithmetic in R, one warp: the lanes split the geminal and J3 shells, the
+// nuclei (J1) and the other electrons (J2); every lane returns all P ratios.
+// In the mixed form (R = float) the electron displacements come from the float
+// caches t.dA / t.dE; otherwise from the positions in double.
+template <int P, class R, class Tab>
+__device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const double* sx, const double* sy, const double* sz,
+                             R* ratio) {
   const Sys& s = k.s;
+  const int lane = threadIdx.x & 31;
   const bool up = e < s.n_up;
   const int i = up ? e : e - s.n_up;
   const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
-  if constexpr (sizeof(R) == sizeof(float)) {
-    if (t.dA) {
-      const float fx = (float)sx, fy = (float)sy, fz = (float)sz;
-      const float* dAe = t.dA + (size_t)e * s.natom * 3;
-      const float* dEe = t.dE + (size_t)e * k.N * 3;
-      const float det = ao_dot_rel<Tab>(s.det, dAe, fx, fy, fz, Trow);
-      float dJ = j12_delta_rel(s, dAe, dEe, e, fx, fy, fz);
-      if (s.has_j3) dJ += ao_dot_rel<Tab>(s.j3, dAe, fx, fy, fz, k.h3 + (size_t)e * k.A3) - (float)t.c3[e];
-      return det * __expf(dJ);
+  const bool rel = sizeof(R) == sizeof(float) && t.dA != nullptr;
+  const float* dAe = rel ? t.dA + (size_t)e * s.natom * 3 : nullptr;
+  const float* dEe = rel ? t.dE + (size_t)e * k.N * 3 : nullptr;
+  const double ex = k.r[3 * e], ey = k.r[3 * e + 1], ez = k.r[3 * e + 2];
+  auto dnuc = [&](int atom, R& x, R& y, R& z) {
+    if (rel) {
+      x = (R)dAe[3 * atom]; y = (R)dAe[3 * atom + 1]; z = (R)dAe[3 * atom + 2];
+    } else {
+      x = (R)(ex - s.atom_pos[3 * atom]); y = (R)(ey - s.atom_pos[3 * atom + 1]); z = (R)(ez - s.atom_pos[3 * atom + 2]);
+    }
+  };
+  R mx[P], my[P], mz[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) { mx[p] = (R)sx[p]; my[p] = (R)sy[p]; mz[p] = (R)sz[p]; }
+  R det[P], dj[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) { det[p] = R(0); dj[p] = R(0); }
+  R dx[P], dy[P], dz[P];
+  for (int idx = lane; idx < s.det.nshell; idx += 32) {
+    const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
+    R x, y, z;
+    dnuc(s.det.shells[8 * sh], x, y, z);
+#pragma unroll
+    for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
+    shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
+  }
+  if (s.has_j3) {
+    const Tab* h = k.h3 + (size_t)e * k.A3;
+    for (int idx = lane; idx < s.j3.nshell; idx += 32) {
+      const int sh = s.j3.shells[8 * idx + 7];
+      R x, y, z;
+      dnuc(s.j3.shells[8 * sh], x, y, z);
+#pragma unroll
+      for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
+      shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
     }
   }
-  const double px = k.r[3 * e] + sx, py = k.r[3 * e + 1] + sy, pz = k.r[3 * e + 2] + sz;
-  const R det = ao_dot<R, Tab>(s.det, s.atom_pos, px, py, pz, Trow);
-  R dJ = j12_delta<R>(s, k.r, e, px, py, pz);
-  if (s.has_j3) dJ += ao_dot<R, Tab>(s.j3, s.atom_pos, px, py, pz, k.h3 + (size_t)e * k.A3) - (R)t.c3[e];
-  return det * Num<R>::ex(dJ);
+  if (s.has_j1) {
+    const R a = (R)s.j1_param;
+    for (int at = lane; at < s.natom; at += 32) {
+      R x, y, z;
+      dnuc(at, x, y, z);
+      const R c = (R)s.j1_cA[2 * at], A = (R)s.j1_cA[2 * at + 1];
+#pragma unroll
+      for (int p = 0; p < P; ++p) dj[p] += pair_delta<R>(x, y, z, mx[p], my[p], mz[p], s.j1_type, a, c, A, true);
+    }
+  }
+  if (s.has_j2) {
+    const R b = (R)s.j2_param;
+    for (int m = lane; m < k.N; m += 32) {
+      if (m == e) continue;
+      R x, y, z;
+      if (rel) {
+        x = (R)dEe[3 * m]; y = (R)dEe[3 * m + 1]; z = (R)dEe[3 * m + 2];
+      } else {
+        x = (R)(ex - k.r[3 * m]); y = (R)(ey - k.r[3 * m + 1]); z = (R)(ez - k.r[3 * m + 2]);
+      }
+#pragma unroll
+      for (int p = 0; p < P; ++p) dj[p] += pair_delta<R>(x, y, z, mx[p], my[p], mz[p], s.j2_type, b, R(0), R(0), false);
+    }
+  }
+  const R c3 = s.has_j3 ? (R)t.c3[e] : R(0);
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    const R dsum = warp_sum(det[p]);
+    const R jsum = warp_sum(dj[p]);
+    ratio[p] = dsum * Num<R>::ex(jsum - c3);
+  }
 }
 
 // Phase B: kinetic lattice elements (wavefunction.py:1740-1860) and non-local ECP
-// elements (coulomb_potential.py:1478-1712, NN = 1).  Rotation R in t.R.
+// elements (coulomb_potential.py:1478-1712, NN = 1).  Rotation R in t.R.  One
+// warp per electron: its six lattice shifts, then its Nv quadrature points (if
+// its nearest nucleus carries a non-local channel), P points per chunk (6 in
+// float, 3 in double, for registers).
 template <class R, class Tab>
 __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
+  constexpr int P = sizeof(R) == sizeof(float) ? 6 : 3;
+  constexpr int nkc = 6 / P;   // chunks of lattice shifts
   const Sys& s = k.s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int N = k.N, nv = s.nv;
-  const int nkin = kinetic ? 6 * N : 0;
-  const int necp = s.ecp_flag ? nv * t.ecpe[N] : 0;
-  for (int p = threadIdx.x; p < nkin + necp; p += blockDim.x) {
-    if (p < nkin) {
-      const int e = p / 6, kk = p % 6, ax = kk >> 1;
-      const double sg = (kk & 1) ? -alat : alat;
-      t.el[p] = -1.0 / (2.0 * alat * alat) *
-                (double)wf_ratio<R, Tab>(k, t, e, sg * t.R[0 * 3 + ax], sg * t.R[1 * 3 + ax], sg * t.R[2 * 3 + ax]);
-    } else {
-      const int qa = p - nkin, e = t.ecpe[qa / nv], v = qa % nv, q = e * nv + v;
-      const int atom = t.eatom[e];
-      const int lmax = s.ecp_maxl1[atom];
-      const double* m = s.mesh_pts + 3 * v;
-      const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
-      const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
-      const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
-      const double Rx = s.atom_pos[3 * atom], Ry = s.atom_pos[3 * atom + 1], Rz = s.atom_pos[3 * atom + 2];
-      // rel = R - r; r' = r + rel + |rel| g ; cos = (-rel/|rel|) . (g/|g|)
-      const double relx = Rx - k.r[3 * e], rely = Ry - k.r[3 * e + 1], relz = Rz - k.r[3 * e + 2];
-      const double dist = sqrt(relx * relx + rely * rely + relz * relz);
-      const double gn = sqrt(gx * gx + gy * gy + gz * gz);
-      const double cth = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
-      const double ratio = (double)wf_ratio<R, Tab>(k, t, e, relx + dist * gx, rely + dist * gy, relz + dist * gz);
-      double vsum = 0.0;
-      for (int l = 0; l < lmax; ++l) vsum += t.vl[e * kSlots + l] * ((2 * l + 1) * legendre(l, cth) * s.mesh_w[v] * ratio);
-      t.V[q] = vsum;
+  const double kin = -1.0 / (2.0 * alat * alat);
+  for (int e = wid; e < N; e += nw) {
+    const int atom = t.eatom[e];
+    const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
+    const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
+    for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
+      // lane p < P sets up point p (in double), then every lane receives all P moves
+      double mx = 0.0, my = 0.0, mz = 0.0, ct = 0.0;
+      int v0 = 0, np = P;
+      if (c < nkc) {
+        if (lane < P) {
+          const int kk = c * P + lane, ax = kk >> 1;
+          const double sg = (kk & 1) ? -alat : alat;
+          mx = sg * t.R[ax]; my = sg * t.R[3 + ax]; mz = sg * t.R[6 + ax];
+        }
+      } else {
+        // rel = R - r; r' = r + rel + |rel| g ; cos = (-rel/|rel|) . (g/|g|)
+        v0 = (c - nkc) * P;
+        np = min(P, nv - v0);
+        if (lane < P) {
+          const double relx = s.atom_pos[3 * atom] - k.r[3 * e], rely = s.atom_pos[3 * atom + 1] - k.r[3 * e + 1];
+          const double relz = s.atom_pos[3 * atom + 2] - k.r[3 * e + 2];
+          const double dist = sqrt(relx * relx + rely * rely + relz * relz);
+          const double* m = s.mesh_pts + 3 * (lane < np ? v0 + lane : v0);
+          const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
+          const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
+          const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
+          const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+          ct = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
+          mx = relx + dist * gx; my = rely + dist * gy; mz = relz + dist * gz;
+        }
+      }
+      double sx[P], sy[P], sz[P];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        sx[p] = __shfl_sync(0xffffffffu, mx, p);
+        sy[p] = __shfl_sync(0xffffffffu, my, p);
+        sz[p] = __shfl_sync(0xffffffffu, mz, p);
+      }
+      R ratio[P];
+      wf_ratio_pts<P, R, Tab>(k, t, e, sx, sy, sz, ratio);
+      if (lane < np) {
+        R rr = R(0);
+#pragma unroll
+        for (int p = 0; p < P; ++p) rr = p == lane ? ratio[p] : rr;
+        const double rv = (double)rr;
+        if (c < nkc) {
+          t.el[6 * e + c * P + lane] = kin * rv;
+        } else {
+          const int v = v0 + lane, lmax = s.ecp_maxl1[atom];
+          double vsum = 0.0;
+          const double* vl = k.ec + (size_t)e * kEC + EC_VL;   // V_l at the nearest nucleus
+          for (int l = 0; l < lmax; ++l) vsum += vl[l] * ((2 * l + 1) * legendre(l, ct) * s.mesh_w[v] * rv);
+          t.V[e * nv + v] = vsum;
+        }
+      }
     }
   }
   __syncthreads();
@@ -2232,9 +2387,9 @@ KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   KParams P;
   P.s = sys->s;
   P.ws = to_ws(w);
-  P.tl = table_layout(sys->s);
-  P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
   const bool mixed = w->precision == JQMC_PREC_MIXED;
+  P.tl = table_layout(sys->s, !mixed);
+  P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
   P.dcache_global = mixed && dcache_bytes(sys->s) > kDcacheSmemMax;
   P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global);
   P.nwalk = w->nwalk;
@@ -2357,7 +2512,22 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     }
   const size_t o_apos = put(d->atom_pos, (size_t)M * 24);
   const size_t o_az = put(d->atom_zeff, (size_t)M * 8);
-  const size_t o_dsh = put(d->det.shells, (size_t)d->det.nshell * 32);
+  // Shell rows are copied with their 8th int set to a permutation of the shells
+  // sorted by (l, nprim): the warp-cooperative mesh evaluation walks the shells
+  // in that order, so the 32 lanes of an iteration take the same code path.
+  auto with_order = [](const jqmc_basis_desc& b) {
+    std::vector<int32_t> rows(b.shells, b.shells + (size_t)b.nshell * 8);
+    std::vector<int32_t> ord(b.nshell);
+    for (int k = 0; k < b.nshell; ++k) ord[k] = k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+      const int lx = rows[8 * x + 1], ly = rows[8 * y + 1];
+      return lx != ly ? lx < ly : rows[8 * x + 2] < rows[8 * y + 2];
+    });
+    for (int k = 0; k < b.nshell; ++k) rows[8 * k + 7] = ord[k];
+    return rows;
+  };
+  const std::vector<int32_t> dsh_rows = with_order(d->det);
+  const size_t o_dsh = put(dsh_rows.data(), (size_t)d->det.nshell * 32);
   const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
   const size_t o_dprf = put(dprf.data(), dprf.size() * 4);
   const size_t o_lam = put(d->lambda, (size_t)A * A * 8);
@@ -2369,7 +2539,8 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
   size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
-    o_jsh = put(d->j3.shells, (size_t)d->j3.nshell * 32);
+    const std::vector<int32_t> jsh_rows = with_order(d->j3);
+    o_jsh = put(jsh_rows.data(), (size_t)d->j3.nshell * 32);
     o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
     o_jprf = put(jprf.data(), jprf.size() * 4);
     o_j3m = put(j3m.data(), j3m.size() * 8);
