@@ -568,17 +568,19 @@ __device__ double ecp_channel(const Sys& s, int atom, int slot, double d) {
   return v / (d * d);
 }
 
-__device__ __forceinline__ double legendre(int l, double x) {
+template <class T>
+__device__ __forceinline__ T legendre_t(int l, T x) {
   switch (l) {
-    case 0: return 1.0;
+    case 0: return T(1);
     case 1: return x;
-    case 2: return 1.0 / 2.0 * (3.0 * x * x - 1);
-    case 3: return 1.0 / 2.0 * (5.0 * x * x * x - 3.0 * x);
-    case 4: return 1.0 / 8.0 * (35.0 * x * x * x * x - 30.0 * x * x + 3.0);
-    case 5: return 1.0 / 8.0 * (63.0 * x * x * x * x * x - 70 * x * x * x + 15 * x);
-    default: return 1.0 / 16.0 * (231.0 * x * x * x * x * x * x - 315.0 * x * x * x * x + 105.0 * x * x - 5);
+    case 2: return T(0.5) * (T(3) * x * x - T(1));
+    case 3: return T(0.5) * (T(5) * x * x * x - T(3) * x);
+    case 4: return T(0.125) * (T(35) * x * x * x * x - T(30) * x * x + T(3));
+    case 5: return T(0.125) * (T(63) * x * x * x * x * x - T(70) * x * x * x + T(15) * x);
+    default: return T(0.0625) * (T(231) * x * x * x * x * x * x - T(315) * x * x * x * x + T(105) * x * x - T(5));
   }
 }
+__device__ __forceinline__ double legendre(int l, double x) { return legendre_t<double>(l, x); }
 
 // nearest nucleus (lowest index on ties), as the stable argsort of jqmc/structure.py:393-405
 __device__ int nearest_atom(const Sys& s, double x, double y, double z) {
@@ -776,6 +778,55 @@ __device__ void ecache_single(const Sys& s, double x, double y, double z, double
   row[EC_DIST] = bd;
   const int lmax = s.ecp_flag ? s.ecp_maxl1[best] : 0;
   for (int l = 0; l < kSlots; ++l) row[EC_VL + l] = l < lmax ? ecp_channel(s, best, l, bd) : 0.0;
+}
+
+// The same row computed by one warp (every lane calls it): lanes over nuclei,
+// warp sums, the nearest nucleus as the (distance, index) minimum (lowest index
+// on ties, as the serial loop), and the channel values at it by lanes over l.
+__device__ void ecache_single_warp(const Sys& s, double x, double y, double z, double* row) {
+  const int lane = threadIdx.x & 31;
+  double ei = 0.0, eloc = 0.0, gx = 0.0, gy = 0.0, gz = 0.0, lap = 0.0, bd = 1e300;
+  int best = 0x7fffffff;
+  for (int a = lane; a < s.natom; a += 32) {
+    const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (d < bd) { bd = d; best = a; }
+    ei += -s.atom_zeff[a] / d;
+    if (s.ecp_flag) eloc += ecp_channel(s, a, s.ecp_maxl1[a], d);
+    if (s.has_j1) {
+      const double aa = s.j1_param, c = s.j1_cA[2 * a], AA = s.j1_cA[2 * a + 1];
+      double f1, f2;
+      if (s.j1_type == 0) {
+        const double ex = exp(-aa * c * d);
+        f1 = -AA * c * ex / 2.0;
+        f2 = AA * aa * c * c * ex / 2.0;
+      } else {
+        const double q = 1.0 + aa * c * d;
+        f1 = -AA / (2.0 * q * q);
+        f2 = AA * aa * c / (q * q * q);
+      }
+      gx += f1 * dx / d; gy += f1 * dy / d; gz += f1 * dz / d;
+      lap += f2 + 2.0 * f1 / d;
+    }
+  }
+  ei = warp_sum(ei); eloc = warp_sum(eloc);
+  gx = warp_sum(gx); gy = warp_sum(gy); gz = warp_sum(gz); lap = warp_sum(lap);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+    const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+    if (od < bd || (od == bd && ob < best)) { bd = od; best = ob; }
+  }
+  if (lane == 0) {
+    row[EC_EI] = ei;
+    row[EC_ELOC] = eloc;
+    row[EC_J1G] = gx; row[EC_J1G + 1] = gy; row[EC_J1G + 2] = gz;
+    row[EC_J1L] = lap;
+    row[EC_NEAR] = (double)best;
+    row[EC_DIST] = bd;
+  }
+  const int lmax = s.ecp_flag ? s.ecp_maxl1[best] : 0;
+  if (lane < kSlots) row[EC_VL + lane] = lane < lmax ? ecp_channel(s, best, lane, bd) : 0.0;
 }
 
 // Fill the whole energy cache of one walker from its positions (block-cooperative).
@@ -1086,12 +1137,14 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     jgy = block_sum(jgy, k.red);
     jgz = block_sum(jgz, k.red);
     jl = block_sum(jl, k.red);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
       double* row = k.ec + (size_t)e * kEC;
-      ecache_single(s, px, py, pz, row);
-      row[EC_J2G] = jgx; row[EC_J2G + 1] = jgy; row[EC_J2G + 2] = jgz;
-      row[EC_J2L] = jl;
-      k.ec[(size_t)N * kEC + EC_TOT_EE] += dee;
+      ecache_single_warp(s, px, py, pz, row);
+      if (threadIdx.x == 0) {
+        row[EC_J2G] = jgx; row[EC_J2G + 1] = jgy; row[EC_J2G + 2] = jgz;
+        row[EC_J2L] = jl;
+        k.ec[(size_t)N * kEC + EC_TOT_EE] += dee;
+      }
     }
   }
   __syncthreads();
@@ -1116,12 +1169,13 @@ struct Terms {
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
   double* R;      // 9 rotation
+  float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_dA, off_dE, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form in shared memory
@@ -1138,6 +1192,7 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_el = o; o = align16(o + 6 * N * 8);
   L.off_V = o; o = align16(o + (s.nv > 0 ? s.nv : 1) * N * 8);
   L.off_R = o; o = align16(o + 9 * 8);
+  L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
   L.bytes = o;
@@ -1160,6 +1215,7 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.el = reinterpret_cast<double*>(smem + L.off_el);
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
+  t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
   t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
   if (gdcache) {
@@ -1167,6 +1223,51 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
     t.dE = gdcache + (size_t)s.N * s.natom * 3;
   }
   return t;
+}
+
+// Float displacement caches of the mixed form: dA[e][a] = r_e - R_a,
+// dE[e][m] = r_e - r_m (differences in double, rounded once).  Filled at the
+// start of a launch, then only the moved electron's row and column change.
+template <class Tab>
+__device__ void dcache_fill(const Work<Tab>& k, Terms& t) {
+  if (!t.dA) return;
+  const Sys& s = k.s;
+  const int M = s.natom, N = k.N;
+  for (int p = threadIdx.x; p < N * (M + N); p += blockDim.x) {
+    const int e = p / (M + N), q = p % (M + N);
+    const double* X = q < M ? s.atom_pos + 3 * q : k.r + 3 * (q - M);
+    float* out = q < M ? t.dA + (size_t)(e * M + q) * 3 : t.dE + (size_t)(e * N + q - M) * 3;
+    out[0] = (float)(k.r[3 * e] - X[0]);
+    out[1] = (float)(k.r[3 * e + 1] - X[1]);
+    out[2] = (float)(k.r[3 * e + 2] - X[2]);
+  }
+  __syncthreads();
+}
+
+template <class Tab>
+__device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
+  if (!t.dA) return;
+  const Sys& s = k.s;
+  const int M = s.natom, N = k.N;
+  const double ex = k.r[3 * e], ey = k.r[3 * e + 1], ez = k.r[3 * e + 2];
+  for (int q = threadIdx.x; q < M + 2 * N; q += blockDim.x) {
+    float* out;
+    double dx, dy, dz;
+    if (q < M) {
+      out = t.dA + (size_t)(e * M + q) * 3;
+      dx = ex - s.atom_pos[3 * q]; dy = ey - s.atom_pos[3 * q + 1]; dz = ez - s.atom_pos[3 * q + 2];
+    } else if (q < M + N) {
+      const int m = q - M;
+      out = t.dE + (size_t)(e * N + m) * 3;
+      dx = ex - k.r[3 * m]; dy = ey - k.r[3 * m + 1]; dz = ez - k.r[3 * m + 2];
+    } else {
+      const int m = q - M - N;
+      out = t.dE + (size_t)(m * N + e) * 3;
+      dx = k.r[3 * m] - ex; dy = k.r[3 * m + 1] - ey; dz = k.r[3 * m + 2] - ez;
+    }
+    out[0] = (float)dx; out[1] = (float)dy; out[2] = (float)dz;
+  }
+  __syncthreads();
 }
 
 // Phase A: per-electron continuum kinetic energy and the old-position values
@@ -1180,18 +1281,13 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int A = k.A, A3 = k.A3;
-  if (t.dA) {
-    const int M = s.natom, N = k.N;
-    for (int p = threadIdx.x; p < N * (M + N); p += blockDim.x) {
-      const int e = p / (M + N), q = p % (M + N);
-      const double* X = q < M ? s.atom_pos + 3 * q : k.r + 3 * (q - M);
-      float* out = q < M ? t.dA + (size_t)(e * M + q) * 3 : t.dE + (size_t)(e * N + q - M) * 3;
-      out[0] = (float)(k.r[3 * e] - X[0]);
-      out[1] = (float)(k.r[3 * e + 1] - X[1]);
-      out[2] = (float)(k.r[3 * e + 2] - X[2]);
-    }
-  }
-  for (int e = wid; e < k.N; e += nw) {
+  // Each warp walks its electrons; lane (it mod 32) keeps the it-th electron's
+  // nine sums, and every 32 electrons (and at the end) all holding lanes finish
+  // their electron's terms in double at once, so the FP64 work issues once per
+  // 32 electrons instead of once per electron.
+  Acc kp[9];
+  int mine = -1, it = 0;
+  for (int e = wid; e < k.N; e += nw, ++it) {
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
     const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
@@ -1217,32 +1313,40 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
         thl += (Acc)q[4 * A3 + a] * hv;
       }
     }
-    const double gx = (double)warp_sum(tgx), gy = (double)warp_sum(tgy), gz = (double)warp_sum(tgz);
-    const double lp = (double)warp_sum(tlp);
-    const double c3 = (double)warp_sum(tc3), hx = (double)warp_sum(thx), hy = (double)warp_sum(thy);
-    const double hz = (double)warp_sum(thz), hl = (double)warp_sum(thl);
-    if (lane == 0) {
-      const double* row = k.ec + (size_t)e * kEC;
-      const double Gx = gx + hx + row[EC_J1G] + row[EC_J2G];
-      const double Gy = gy + hy + row[EC_J1G + 1] + row[EC_J2G + 1];
-      const double Gz = gz + hz + row[EC_J1G + 2] + row[EC_J2G + 2];
-      const double L = lp - (gx * gx + gy * gy + gz * gz) + hl + row[EC_J1L] + row[EC_J2L];
-      t.ke[e] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
-      t.c3[e] = c3;
-      t.ei[e] = row[EC_EI];
-      t.eatom[e] = (int)row[EC_NEAR];
-      t.edist[e] = row[EC_DIST];
-      if (s.ecp_flag && s.ecp_maxl1[(int)row[EC_NEAR]] <= 0)
-        for (int v = 0; v < s.nv; ++v) t.V[e * s.nv + v] = 0.0;
-      if (!s.ecp_flag) {
-        const double x = k.r[3 * e], y = k.r[3 * e + 1], z = k.r[3 * e + 2];
-        double eid = 0.0;
-        for (int a = 0; a < s.natom; ++a) {
-          const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
-          eid += -s.atom_zeff[a] / fmax(sqrt(dx * dx + dy * dy + dz * dz), alat);
+    const Acc v0 = warp_sum(tgx), v1 = warp_sum(tgy), v2 = warp_sum(tgz), v3 = warp_sum(tlp);
+    const Acc v4 = warp_sum(tc3), v5 = warp_sum(thx), v6 = warp_sum(thy), v7 = warp_sum(thz), v8 = warp_sum(thl);
+    if (lane == (it & 31)) {
+      kp[0] = v0; kp[1] = v1; kp[2] = v2; kp[3] = v3; kp[4] = v4; kp[5] = v5; kp[6] = v6; kp[7] = v7; kp[8] = v8;
+      mine = e;
+    }
+    if ((it & 31) == 31 || e + nw >= k.N) {
+      if (mine >= 0) {
+        const int me = mine;
+        const double gx = (double)kp[0], gy = (double)kp[1], gz = (double)kp[2], lp = (double)kp[3];
+        const double c3 = (double)kp[4], hx = (double)kp[5], hy = (double)kp[6], hz = (double)kp[7], hl = (double)kp[8];
+        const double* row = k.ec + (size_t)me * kEC;
+        const double Gx = gx + hx + row[EC_J1G] + row[EC_J2G];
+        const double Gy = gy + hy + row[EC_J1G + 1] + row[EC_J2G + 1];
+        const double Gz = gz + hz + row[EC_J1G + 2] + row[EC_J2G + 2];
+        const double L = lp - (gx * gx + gy * gy + gz * gz) + hl + row[EC_J1L] + row[EC_J2L];
+        t.ke[me] = -0.5 * (L + Gx * Gx + Gy * Gy + Gz * Gz);
+        t.c3[me] = c3;
+        t.ei[me] = row[EC_EI];
+        t.eatom[me] = (int)row[EC_NEAR];
+        t.edist[me] = row[EC_DIST];
+        if (s.ecp_flag && s.ecp_maxl1[(int)row[EC_NEAR]] <= 0)
+          for (int v = 0; v < s.nv; ++v) t.V[me * s.nv + v] = 0.0;
+        if (!s.ecp_flag) {
+          const double x = k.r[3 * me], y = k.r[3 * me + 1], z = k.r[3 * me + 2];
+          double eid = 0.0;
+          for (int a = 0; a < s.natom; ++a) {
+            const double dx = x - s.atom_pos[3 * a], dy = y - s.atom_pos[3 * a + 1], dz = z - s.atom_pos[3 * a + 2];
+            eid += -s.atom_zeff[a] / fmax(sqrt(dx * dx + dy * dy + dz * dz), alat);
+          }
+          t.eid[me] = eid;
         }
-        t.eid[e] = eid;
       }
+      mine = -1;
     }
   }
   __syncthreads();
@@ -1273,8 +1377,7 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 // In the mixed form (R = float) the electron displacements come from the float
 // caches t.dA / t.dE; otherwise from the positions in double.
 template <int P, class R, class Tab>
-__device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const double* sx, const double* sy, const double* sz,
-                             R* ratio) {
+__device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz, R* ratio) {
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
   const bool up = e < s.n_up;
@@ -1291,9 +1394,9 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const do
       x = (R)(ex - s.atom_pos[3 * atom]); y = (R)(ey - s.atom_pos[3 * atom + 1]); z = (R)(ez - s.atom_pos[3 * atom + 2]);
     }
   };
-  R mx[P], my[P], mz[P];
-#pragma unroll
-  for (int p = 0; p < P; ++p) { mx[p] = (R)sx[p]; my[p] = (R)sy[p]; mz[p] = (R)sz[p]; }
+  const R* mx = sx;
+  const R* my = sy;
+  const R* mz = sz;
   R det[P], dj[P];
 #pragma unroll
   for (int p = 0; p < P; ++p) { det[p] = R(0); dj[p] = R(0); }
@@ -1368,33 +1471,50 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
     const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
     const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
     for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
-      // lane p < P sets up point p (in double), then every lane receives all P moves
-      double mx = 0.0, my = 0.0, mz = 0.0, ct = 0.0;
+      // lane p < P sets up point p, then every lane receives all P moves.  The
+      // float form builds them from the float rotation, quadrature directions
+      // and displacement cache, so that the chunk issues no FP64 instruction.
+      R mx = R(0), my = R(0), mz = R(0), ct = R(0);
       int v0 = 0, np = P;
-      if (c < nkc) {
-        if (lane < P) {
-          const int kk = c * P + lane, ax = kk >> 1;
-          const double sg = (kk & 1) ? -alat : alat;
-          mx = sg * t.R[ax]; my = sg * t.R[3 + ax]; mz = sg * t.R[6 + ax];
-        }
-      } else {
-        // rel = R - r; r' = r + rel + |rel| g ; cos = (-rel/|rel|) . (g/|g|)
+      if (c >= nkc) {
         v0 = (c - nkc) * P;
         np = min(P, nv - v0);
-        if (lane < P) {
-          const double relx = s.atom_pos[3 * atom] - k.r[3 * e], rely = s.atom_pos[3 * atom + 1] - k.r[3 * e + 1];
-          const double relz = s.atom_pos[3 * atom + 2] - k.r[3 * e + 2];
-          const double dist = sqrt(relx * relx + rely * rely + relz * relz);
-          const double* m = s.mesh_pts + 3 * (lane < np ? v0 + lane : v0);
-          const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
-          const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
-          const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
-          const double gn = sqrt(gx * gx + gy * gy + gz * gz);
-          ct = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
-          mx = relx + dist * gx; my = rely + dist * gy; mz = relz + dist * gz;
+      }
+      if (lane < P) {
+        if constexpr (sizeof(R) == sizeof(float)) {
+          if (c < nkc) {
+            const int kk = c * P + lane, ax = kk >> 1;
+            const float sg = (kk & 1) ? -(float)alat : (float)alat;
+            mx = sg * t.Rf[ax]; my = sg * t.Rf[3 + ax]; mz = sg * t.Rf[6 + ax];
+          } else {
+            // rel = R - r; r' = r + rel + |rel| g ; cos = (-rel/|rel|) . (g/|g|)
+            const float* dAe = t.dA + ((size_t)e * s.natom + atom) * 3;
+            const float relx = -dAe[0], rely = -dAe[1], relz = -dAe[2];
+            const float dist = sqrtf(relx * relx + rely * rely + relz * relz);
+            const float* g = t.Rf + 9 + 4 * (lane < np ? v0 + lane : v0);
+            ct = -(relx * g[0] + rely * g[1] + relz * g[2]) / dist * g[3];
+            mx = relx + dist * g[0]; my = rely + dist * g[1]; mz = relz + dist * g[2];
+          }
+        } else {
+          if (c < nkc) {
+            const int kk = c * P + lane, ax = kk >> 1;
+            const double sg = (kk & 1) ? -alat : alat;
+            mx = sg * t.R[ax]; my = sg * t.R[3 + ax]; mz = sg * t.R[6 + ax];
+          } else {
+            const double relx = s.atom_pos[3 * atom] - k.r[3 * e], rely = s.atom_pos[3 * atom + 1] - k.r[3 * e + 1];
+            const double relz = s.atom_pos[3 * atom + 2] - k.r[3 * e + 2];
+            const double dist = sqrt(relx * relx + rely * rely + relz * relz);
+            const double* m = s.mesh_pts + 3 * (lane < np ? v0 + lane : v0);
+            const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
+            const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
+            const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
+            const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+            ct = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
+            mx = relx + dist * gx; my = rely + dist * gy; mz = relz + dist * gz;
+          }
         }
       }
-      double sx[P], sy[P], sz[P];
+      R sx[P], sy[P], sz[P];
 #pragma unroll
       for (int p = 0; p < P; ++p) {
         sx[p] = __shfl_sync(0xffffffffu, mx, p);
@@ -1407,15 +1527,15 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
         R rr = R(0);
 #pragma unroll
         for (int p = 0; p < P; ++p) rr = p == lane ? ratio[p] : rr;
-        const double rv = (double)rr;
         if (c < nkc) {
-          t.el[6 * e + c * P + lane] = kin * rv;
+          t.el[6 * e + c * P + lane] = (double)((R)kin * rr);
         } else {
           const int v = v0 + lane, lmax = s.ecp_maxl1[atom];
-          double vsum = 0.0;
           const double* vl = k.ec + (size_t)e * kEC + EC_VL;   // V_l at the nearest nucleus
-          for (int l = 0; l < lmax; ++l) vsum += vl[l] * ((2 * l + 1) * legendre(l, ct) * s.mesh_w[v] * rv);
-          t.V[e * nv + v] = vsum;
+          const R wv = (R)s.mesh_w[v] * rr;
+          R vsum = R(0);
+          for (int l = 0; l < lmax; ++l) vsum += (R)vl[l] * (R(2 * l + 1) * legendre_t<R>(l, ct) * wv);
+          t.V[e * nv + v] = (double)vsum;
         }
       }
     }
@@ -2171,10 +2291,27 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
   int done = 0;
   const int nsteps = (tmode && !(tleft > 0.0)) ? 0 : (K > 0 ? K : 1);
   double wl = K > 0 ? wgt[w] : 1.0;
+  dcache_fill(k, t);
   for (int step = 0; step < nsteps; ++step) {
     const double* d = draw + ((size_t)w * (K > 0 ? K : 1) + step) * dstride;
     if (threadIdx.x == 0) rotation(d[0], d[1], d[2], t.R);
     __syncthreads();
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // float rotation and rotated quadrature directions g_v = R m_v (with 1/|g_v|)
+      if (threadIdx.x < 9) {
+        t.Rf[threadIdx.x] = (float)t.R[threadIdx.x];
+      } else if (threadIdx.x >= 32 && threadIdx.x < 32 + s.nv) {
+        const int v = threadIdx.x - 32;
+        const double* m = s.mesh_pts + 3 * v;
+        const double gx = t.R[0] * m[0] + t.R[1] * m[1] + t.R[2] * m[2];
+        const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
+        const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
+        float* g = t.Rf + 9 + 4 * v;
+        g[0] = (float)gx; g[1] = (float)gy; g[2] = (float)gz;
+        g[3] = (float)(1.0 / sqrt(gx * gx + gy * gy + gz * gz));
+      }
+      __syncthreads();
+    }
     electron_terms<Tab, R>(k, t, alat);
     mesh_terms<R, Tab>(k, t, alat, true);
     double diag, nondiag;
@@ -2280,6 +2417,7 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
     __syncthreads();
     const double ratio = sm_move<Tab>(k, me, mx, my, mz);
     if (threadIdx.x == 0 && ratio == 0.0) atomicOr(P.ws.status + w, JQMC_ST_ZERO_RATIO);
+    dcache_update(k, t, me);
   }
   if (K > 0) {
     if (threadIdx.x == 0) {
