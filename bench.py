@@ -355,7 +355,13 @@ def gpu_arm(a):
     relw = ((wm - wr).abs() / wr.abs())[same].cpu().numpy()
     eL_rms = float(np.sqrt(np.mean(de**2)))
     same_frac = float(same.double().mean())
-    del ref, mix
+    # the same configurations with the block energy in FP64 arithmetic (precision
+    # "mixed_fp64_energy": identical float tables, built from the same positions)
+    rm = mix.r.cpu().numpy()
+    mixe = WalkerSet(gs, rm[:, : gs.n_up], rm[:, gs.n_up:], precision="mixed_fp64_energy")
+    ee, _ = mixe.lrdmc_energy(last, a.alat)
+    de_e = (ee - e64)[same].cpu().numpy()
+    del ref, mix, mixe
 
     # e2e through the public driver API (mixed form): draws from pinned host memory, sums to host
     drv = mixed["drv"]
@@ -428,9 +434,13 @@ def gpu_arm(a):
             "accuracy": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": int(len(de)),
                          "same_path_fraction": same_frac, "block_weight_rel_diff_max": float(np.max(relw)),
                          "dE_mean_Ha": float(np.mean(de)), "dE_mean_stderr_Ha": float(np.std(de) / np.sqrt(len(de))),
+                         "fp64_block_energy_variant": {"eL_rms_Ha": float(np.sqrt(np.mean(de_e**2))),
+                                                       "eL_max_Ha": float(np.max(np.abs(de_e))),
+                                                       "dE_mean_Ha": float(np.mean(de_e))},
                          "note": "mixed minus FP64 local energy after one K-step projection block from the same sampled "
                                  "configurations with the same draws and the FP64 rebuild of the carried tables (the "
-                                 "order of a branching cycle); dE_mean is the bias the mixed form adds to <E>",
+                                 "order of a branching cycle); block energy from float values with compensated "
+                                 "float-float sums; dE_mean is the bias the mixed form adds to <E>",
                          "bar": "|dE_L| <= 1e-5 Ha rms per configuration; |d<E>| <= 1e-4 Ha"},
             "e2e": e2e,
             "gpu_launches": sum(per_call.values()) * a.steps,

@@ -87,6 +87,68 @@ struct Num<float> {
   static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
 };
 
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Accumulators of the mesh and electron-term sums.  float / double: plain
+// sums.  F2: compensated float-float sum of float products (TwoProduct by FMA
+// and TwoSum, as in algorithm Dot2 of Ogita, Rump and Oishi, SIAM J. Sci.
+// Comput. 26 (2005) 1955-1988): FP32-pipe work with the cancellation error of
+// a double sum.  acc_out() reduces over the warp (every lane gets the result):
+// float for float, double for double and F2.
+struct F2 {
+  float s, c;
+};
+__device__ __forceinline__ void acc_zero(float& a) { a = 0.f; }
+__device__ __forceinline__ void acc_zero(double& a) { a = 0.0; }
+__device__ __forceinline__ void acc_zero(F2& a) { a.s = 0.f; a.c = 0.f; }
+__device__ __forceinline__ void acc_fma(float& a, float x, float y) { a += x * y; }
+__device__ __forceinline__ void acc_fma(double& a, double x, double y) { a += x * y; }
+__device__ __forceinline__ void two_sum_into(F2& a, float p) {
+  const float t = __fadd_rn(a.s, p);
+  const float z = __fsub_rn(t, a.s);
+  a.c += __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  a.s = t;
+}
+__device__ __forceinline__ void acc_fma(F2& a, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  a.c += __fmaf_rn(x, y, -p);
+  two_sum_into(a, p);
+}
+__device__ __forceinline__ void acc_add(float& a, float x) { a += x; }
+__device__ __forceinline__ void acc_add(double& a, double x) { a += x; }
+__device__ __forceinline__ void acc_add(F2& a, float x) { two_sum_into(a, x); }
+__device__ __forceinline__ float acc_out(float a) { return warp_sum(a); }
+__device__ __forceinline__ double acc_out(double a) { return warp_sum(a); }
+__device__ __forceinline__ double acc_out(F2 a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, a.s, o);
+    const float c2 = __shfl_xor_sync(0xffffffffu, a.c, o);
+    a.c += c2;
+    two_sum_into(a, s2);
+  }
+  return (double)a.s + (double)a.c;
+}
+template <class A> struct AccTraits { using out = A; using arith = A; static constexpr bool accurate = false; };
+template <> struct AccTraits<F2> { using out = double; using arith = float; static constexpr bool accurate = true; };
+// exponentials of the mesh: the fast intrinsic in the float projection, the
+// correctly rounded-to-1-ulp expf / expm1f where the sums are compensated
+template <class R, bool ACC>
+struct MeshExp {
+  static __device__ __forceinline__ R ex(R x) { return Num<R>::ex(x); }
+  static __device__ __forceinline__ R em1(R x) { return Num<R>::em1(x); }
+};
+template <>
+struct MeshExp<float, true> {
+  static __device__ __forceinline__ float ex(float x) { return expf(x); }
+  static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
+};
+
 struct Basis {
   int nshell, nao, nprim;
   const int* shells;
@@ -362,9 +424,9 @@ __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R
 // P points at once: sum_{a in shell} phi_a(d_p) v[a] into acc[p].  The points
 // share the shell's primitive table and the v entries (loaded once); the P
 // evaluations are independent, which gives each lane P chains of work.
-template <int L, int P, class R, class V>
+template <int L, int P, class R, class V, class Acc>
 __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* dz, const R* rad, int ao0, int jlo, int nm,
-                                             const V* v, R* acc) {
+                                             const V* v, Acc* acc) {
   R vv[2 * L + 1];
 #pragma unroll
   for (int j = 0; j < 2 * L + 1; ++j) {
@@ -378,12 +440,12 @@ __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* 
     R part = R(0);
 #pragma unroll
     for (int j = 0; j < 2 * L + 1; ++j) part += S[j] * vv[j];
-    acc[p] += rad[p] * part;
+    acc_fma(acc[p], rad[p], part);
   }
 }
 
-template <int P, class R, class V>
-__device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, R* acc) {
+template <int P, class R, class V, class Acc>
+__device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, Acc* acc) {
   const int* sh = b.shells + 8 * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const R* pr = prims_of<R>(b) + 2 * p0;
@@ -396,16 +458,16 @@ __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx
   for (int q = 0; q < np; ++q) {
     const R Z = pr[2 * q], c = pr[2 * q + 1];
 #pragma unroll
-    for (int p = 0; p < P; ++p) rad[p] += c * Num<R>::ex(-Z * r2[p]);
+    for (int p = 0; p < P; ++p) rad[p] += c * MeshExp<R, AccTraits<Acc>::accurate>::ex(-Z * r2[p]);
   }
   switch (l) {
-    case 0: emit_dot_pts<0, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 1: emit_dot_pts<1, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 2: emit_dot_pts<2, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 3: emit_dot_pts<3, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 4: emit_dot_pts<4, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 5: emit_dot_pts<5, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    default: emit_dot_pts<6, P, R>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 0: emit_dot_pts<0, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 1: emit_dot_pts<1, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 2: emit_dot_pts<2, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 3: emit_dot_pts<3, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 4: emit_dot_pts<4, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 5: emit_dot_pts<5, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    default: emit_dot_pts<6, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
   }
 }
 
@@ -439,15 +501,6 @@ __device__ __forceinline__ void ao_visit_vgl(const Basis& b, const double* apos,
   }
 }
 
-// sum_a phi_a(p) v[a]
-template <class R, class V>
-__device__ R ao_dot(const Basis& b, const double* apos, double px, double py, double pz, const V* v) {
-  R acc = R(0);
-  auto f = [&](int a, R val) { acc += val * (R)v[a]; };
-  ao_visit<R>(b, apos, px, py, pz, f);
-  return acc;
-}
-
 // all AO values at one point into out[] (block-cooperative, split by shell; no sync)
 template <class R, class V>
 __device__ void ao_fill_block(const Basis& b, const double* apos, double px, double py, double pz, V* out) {
@@ -460,12 +513,6 @@ __device__ void ao_fill_block(const Basis& b, const double* apos, double px, dou
 }
 
 // ------------------------------------------------------------------ reductions
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // Sum over the block; every thread receives the total.  red: >= 33 doubles.
 __device__ double block_sum(double v, double* red) {
@@ -580,7 +627,6 @@ __device__ __forceinline__ T legendre_t(int l, T x) {
     default: return T(0.0625) * (T(231) * x * x * x * x * x * x - T(315) * x * x * x * x + T(105) * x * x - T(5));
   }
 }
-__device__ __forceinline__ double legendre(int l, double x) { return legendre_t<double>(l, x); }
 
 // nearest nucleus (lowest index on ties), as the stable argsort of jqmc/structure.py:393-405
 __device__ int nearest_atom(const Sys& s, double x, double y, double z) {
@@ -627,104 +673,6 @@ __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp
       shell_vgl_d<double>(s.j3, sh, dx, dy, dz, f);
     }
   }
-}
-
-// J1 + J2 change when electron e moves to p, as sums of pair differences
-// f(r') - f(r) with r'^2 - r^2 = (2 d + s) . s (d = r_e - X, s = p - r_e), so
-// that the difference keeps the working precision of R even though J1 and J2
-// themselves are large (jastrow_factor.py:2288-2567 evaluate exp(J(r') - J(r))).
-template <class R>
-__device__ R j12_delta(const Sys& s, const double* r, int e, double px, double py, double pz) {
-  const double ex = r[3 * e], ey = r[3 * e + 1], ez = r[3 * e + 2];
-  const R sx = (R)(px - ex), sy = (R)(py - ey), sz = (R)(pz - ez);
-  R acc = R(0);
-  if (s.has_j1) {
-    const R a = (R)s.j1_param;
-    for (int at = 0; at < s.natom; ++at) {
-      R dx, dy, dz;
-      disp<R>(s.atom_pos, at, ex, ey, ez, dx, dy, dz);
-      const R r2 = dx * dx + dy * dy + dz * dz;
-      const R dr2 = (R(2) * dx + sx) * sx + (R(2) * dy + sy) * sy + (R(2) * dz + sz) * sz;
-      const R rr = Num<R>::sq(r2);
-      const R rp2 = r2 + dr2;
-      const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
-      const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
-      const R c = (R)s.j1_cA[2 * at], A = (R)s.j1_cA[2 * at + 1];
-      if (s.j1_type == 0) acc += A / (R(2) * a) * Num<R>::ex(-a * c * rr) * Num<R>::em1(-a * c * dr);
-      else acc += -A * dr / (R(2) * (R(1) + a * c * rr) * (R(1) + a * c * rp));
-    }
-  }
-  if (s.has_j2) {
-    const R b = (R)s.j2_param;
-    for (int m = 0; m < s.N; ++m) {
-      if (m == e) continue;
-      const R dx = (R)(ex - r[3 * m]), dy = (R)(ey - r[3 * m + 1]), dz = (R)(ez - r[3 * m + 2]);
-      const R r2 = dx * dx + dy * dy + dz * dz;
-      const R dr2 = (R(2) * dx + sx) * sx + (R(2) * dy + sy) * sy + (R(2) * dz + sz) * sz;
-      const R rr = Num<R>::sq(r2);
-      const R rp2 = r2 + dr2;
-      const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
-      const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
-      if (s.j2_type == 0) acc += dr / (R(2) * (R(1) + b * rr) * (R(1) + b * rp));
-      else acc += -Num<R>::ex(-b * rr) * Num<R>::em1(-b * dr) / (R(2) * b);
-    }
-  }
-  return acc;
-}
-
-// Mixed form: the same sums from cached float displacements d = r_e - X plus the
-// move vector s, so that a mesh point costs no double arithmetic.
-template <class V>
-__device__ float ao_dot_rel(const Basis& b, const float* dAe, float sx, float sy, float sz, const V* v) {
-  float acc = 0.0f;
-  auto f = [&](int a, float val) { acc += val * (float)v[a]; };
-  int last = -1;
-  float dx = 0.f, dy = 0.f, dz = 0.f;
-  for (int sh = 0; sh < b.nshell; ++sh) {
-    const int atom = b.shells[8 * sh];
-    if (atom != last) {
-      dx = dAe[3 * atom] + sx;
-      dy = dAe[3 * atom + 1] + sy;
-      dz = dAe[3 * atom + 2] + sz;
-      last = atom;
-    }
-    shell_val_d<float>(b, sh, dx, dy, dz, f);
-  }
-  return acc;
-}
-
-__device__ __forceinline__ float pair_dr(float dx, float dy, float dz, float sx, float sy, float sz, float& rr, float& rp) {
-  const float r2 = dx * dx + dy * dy + dz * dz;
-  const float dr2 = (2.f * dx + sx) * sx + (2.f * dy + sy) * sy + (2.f * dz + sz) * sz;
-  rr = sqrtf(r2);
-  const float rp2 = r2 + dr2;
-  rp = sqrtf(rp2 > 0.f ? rp2 : 0.f);
-  return (rp + rr > 0.f) ? dr2 / (rp + rr) : 0.f;
-}
-
-__device__ float j12_delta_rel(const Sys& s, const float* dAe, const float* dEe, int e, float sx, float sy, float sz) {
-  float acc = 0.0f;
-  if (s.has_j1) {
-    const float a = (float)s.j1_param;
-    for (int at = 0; at < s.natom; ++at) {
-      float rr, rp;
-      const float dr = pair_dr(dAe[3 * at], dAe[3 * at + 1], dAe[3 * at + 2], sx, sy, sz, rr, rp);
-      const float c = (float)s.j1_cA[2 * at], A = (float)s.j1_cA[2 * at + 1];
-      if (s.j1_type == 0) acc += A / (2.f * a) * __expf(-a * c * rr) * expm1f(-a * c * dr);
-      else acc += -A * dr / (2.f * (1.f + a * c * rr) * (1.f + a * c * rp));
-    }
-  }
-  if (s.has_j2) {
-    const float b = (float)s.j2_param;
-    for (int m = 0; m < s.N; ++m) {
-      if (m == e) continue;
-      float rr, rp;
-      const float dr = pair_dr(dEe[3 * m], dEe[3 * m + 1], dEe[3 * m + 2], sx, sy, sz, rr, rp);
-      if (s.j2_type == 0) acc += dr / (2.f * (1.f + b * rr) * (1.f + b * rp));
-      else acc += -__expf(-b * rr) * expm1f(-b * dr) / (2.f * b);
-    }
-  }
-  return acc;
 }
 
 // J2 pair function derivatives f'(d), f''(d)
@@ -1202,6 +1150,8 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
 // Displacement caches bigger than this live in global memory (per walker).
 constexpr int kDcacheSmemMax = 64 * 1024;
 
+bool is_mixed(int precision) { return precision == JQMC_PREC_MIXED || precision == JQMC_PREC_MIXED_E64; }
+
 int dcache_bytes(const Sys& s) { return s.N * (s.natom + s.N) * 3 * 4; }
 
 __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gdcache, const Sys& s) {
@@ -1278,6 +1228,8 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
 // from the energy cache.
 template <class Tab, class Acc = Tab>
 __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
+  using Out = typename AccTraits<Acc>::out;
+  using Ar = typename AccTraits<Acc>::arith;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int A = k.A, A3 = k.A3;
@@ -1285,36 +1237,37 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
   // nine sums, and every 32 electrons (and at the end) all holding lanes finish
   // their electron's terms in double at once, so the FP64 work issues once per
   // 32 electrons instead of once per electron.
-  Acc kp[9];
+  Out kp[9];
   int mine = -1, it = 0;
   for (int e = wid; e < k.N; e += nw, ++it) {
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
     const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
     const Tab* dp = k.dphi + (size_t)e * 4 * A;
-    Acc tgx = Acc(0), tgy = Acc(0), tgz = Acc(0), tlp = Acc(0);
+    Acc tgx, tgy, tgz, tlp, tc3, thx, thy, thz, thl;
+    acc_zero(tgx); acc_zero(tgy); acc_zero(tgz); acc_zero(tlp);
+    acc_zero(tc3); acc_zero(thx); acc_zero(thy); acc_zero(thz); acc_zero(thl);
     for (int a = lane; a < A; a += 32) {
-      const Acc tv = (Acc)Trow[a];
-      tgx += (Acc)dp[a] * tv;
-      tgy += (Acc)dp[A + a] * tv;
-      tgz += (Acc)dp[2 * A + a] * tv;
-      tlp += (Acc)dp[3 * A + a] * tv;
+      const Ar tv = (Ar)Trow[a];
+      acc_fma(tgx, (Ar)dp[a], tv);
+      acc_fma(tgy, (Ar)dp[A + a], tv);
+      acc_fma(tgz, (Ar)dp[2 * A + a], tv);
+      acc_fma(tlp, (Ar)dp[3 * A + a], tv);
     }
-    Acc tc3 = Acc(0), thx = Acc(0), thy = Acc(0), thz = Acc(0), thl = Acc(0);
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
       for (int a = lane; a < A3; a += 32) {
-        const Acc hv = (Acc)h[a];
-        tc3 += (Acc)q[a] * hv;
-        thx += (Acc)q[A3 + a] * hv;
-        thy += (Acc)q[2 * A3 + a] * hv;
-        thz += (Acc)q[3 * A3 + a] * hv;
-        thl += (Acc)q[4 * A3 + a] * hv;
+        const Ar hv = (Ar)h[a];
+        acc_fma(tc3, (Ar)q[a], hv);
+        acc_fma(thx, (Ar)q[A3 + a], hv);
+        acc_fma(thy, (Ar)q[2 * A3 + a], hv);
+        acc_fma(thz, (Ar)q[3 * A3 + a], hv);
+        acc_fma(thl, (Ar)q[4 * A3 + a], hv);
       }
     }
-    const Acc v0 = warp_sum(tgx), v1 = warp_sum(tgy), v2 = warp_sum(tgz), v3 = warp_sum(tlp);
-    const Acc v4 = warp_sum(tc3), v5 = warp_sum(thx), v6 = warp_sum(thy), v7 = warp_sum(thz), v8 = warp_sum(thl);
+    const Out v0 = acc_out(tgx), v1 = acc_out(tgy), v2 = acc_out(tgz), v3 = acc_out(tlp);
+    const Out v4 = acc_out(tc3), v5 = acc_out(thx), v6 = acc_out(thy), v7 = acc_out(thz), v8 = acc_out(thl);
     if (lane == (it & 31)) {
       kp[0] = v0; kp[1] = v1; kp[2] = v2; kp[3] = v3; kp[4] = v4; kp[5] = v5; kp[6] = v6; kp[7] = v7; kp[8] = v8;
       mine = e;
@@ -1355,8 +1308,9 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
 // One J1 / J2 pair term of J(r_e + s) - J(r_e): d0 = r_e - X, move s; the
 // difference is formed from r'^2 - r^2 = (2 d0 + s).s so that small moves keep
 // their relative accuracy (jastrow_factor.py:649-726, 1181-1251).
-template <class R>
+template <class R, bool ACC = false>
 __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, int type, R a, R c, R A, bool j1) {
+  using E = MeshExp<R, ACC>;
   const R r2 = d0x * d0x + d0y * d0y + d0z * d0z;
   const R dr2 = (R(2) * d0x + sx) * sx + (R(2) * d0y + sy) * sy + (R(2) * d0z + sz) * sz;
   const R rr = Num<R>::sq(r2);
@@ -1364,11 +1318,11 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
   const R rp = Num<R>::sq(rp2 > R(0) ? rp2 : R(0));
   const R dr = (rp + rr > R(0)) ? dr2 / (rp + rr) : R(0);
   if (j1) {
-    if (type == 0) return A / (R(2) * a) * Num<R>::ex(-a * c * rr) * Num<R>::em1(-a * c * dr);
+    if (type == 0) return A / (R(2) * a) * E::ex(-a * c * rr) * E::em1(-a * c * dr);
     return -A * dr / (R(2) * (R(1) + a * c * rr) * (R(1) + a * c * rp));
   }
   if (type == 0) return dr / (R(2) * (R(1) + a * rr) * (R(1) + a * rp));
-  return -Num<R>::ex(-a * rr) * Num<R>::em1(-a * dr) / (R(2) * a);
+  return -E::ex(-a * rr) * E::em1(-a * dr) / (R(2) * a);
 }
 
 // psi(r_e + s_p)/psi(r) for P moves s_p of electron e (det x Jastrow),
@@ -1376,8 +1330,10 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 // nuclei (J1) and the other electrons (J2); every lane returns all P ratios.
 // In the mixed form (R = float) the electron displacements come from the float
 // caches t.dA / t.dE; otherwise from the positions in double.
-template <int P, class R, class Tab>
-__device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz, R* ratio) {
+template <int P, class R, class Tab, class Acc>
+__device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz,
+                             typename AccTraits<Acc>::out* ratio) {
+  using Out = typename AccTraits<Acc>::out;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
   const bool up = e < s.n_up;
@@ -1397,9 +1353,9 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
   const R* mx = sx;
   const R* my = sy;
   const R* mz = sz;
-  R det[P], dj[P];
+  Acc det[P], dj[P];
 #pragma unroll
-  for (int p = 0; p < P; ++p) { det[p] = R(0); dj[p] = R(0); }
+  for (int p = 0; p < P; ++p) { acc_zero(det[p]); acc_zero(dj[p]); }
   R dx[P], dy[P], dz[P];
   for (int idx = lane; idx < s.det.nshell; idx += 32) {
     const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
@@ -1427,7 +1383,7 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
       dnuc(at, x, y, z);
       const R c = (R)s.j1_cA[2 * at], A = (R)s.j1_cA[2 * at + 1];
 #pragma unroll
-      for (int p = 0; p < P; ++p) dj[p] += pair_delta<R>(x, y, z, mx[p], my[p], mz[p], s.j1_type, a, c, A, true);
+      for (int p = 0; p < P; ++p) acc_add(dj[p], pair_delta<R, AccTraits<Acc>::accurate>(x, y, z, mx[p], my[p], mz[p], s.j1_type, a, c, A, true));
     }
   }
   if (s.has_j2) {
@@ -1441,15 +1397,15 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
         x = (R)(ex - k.r[3 * m]); y = (R)(ey - k.r[3 * m + 1]); z = (R)(ez - k.r[3 * m + 2]);
       }
 #pragma unroll
-      for (int p = 0; p < P; ++p) dj[p] += pair_delta<R>(x, y, z, mx[p], my[p], mz[p], s.j2_type, b, R(0), R(0), false);
+      for (int p = 0; p < P; ++p) acc_add(dj[p], pair_delta<R, AccTraits<Acc>::accurate>(x, y, z, mx[p], my[p], mz[p], s.j2_type, b, R(0), R(0), false));
     }
   }
-  const R c3 = s.has_j3 ? (R)t.c3[e] : R(0);
+  const Out c3 = s.has_j3 ? (Out)t.c3[e] : Out(0);
 #pragma unroll
   for (int p = 0; p < P; ++p) {
-    const R dsum = warp_sum(det[p]);
-    const R jsum = warp_sum(dj[p]);
-    ratio[p] = dsum * Num<R>::ex(jsum - c3);
+    const Out dsum = acc_out(det[p]);
+    const Out jsum = acc_out(dj[p]);
+    ratio[p] = dsum * Num<Out>::ex(jsum - c3);
   }
 }
 
@@ -1458,8 +1414,9 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
 // warp per electron: its six lattice shifts, then its Nv quadrature points (if
 // its nearest nucleus carries a non-local channel), P points per chunk (6 in
 // float, 3 in double, for registers).
-template <class R, class Tab>
+template <class R, class Tab, class Acc = R>
 __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
+  using Out = typename AccTraits<Acc>::out;
   constexpr int P = sizeof(R) == sizeof(float) ? 6 : 3;
   constexpr int nkc = 6 / P;   // chunks of lattice shifts
   const Sys& s = k.s;
@@ -1521,20 +1478,21 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
         sy[p] = __shfl_sync(0xffffffffu, my, p);
         sz[p] = __shfl_sync(0xffffffffu, mz, p);
       }
-      R ratio[P];
-      wf_ratio_pts<P, R, Tab>(k, t, e, sx, sy, sz, ratio);
+      Out ratio[P];
+      wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio);
       if (lane < np) {
-        R rr = R(0);
+        Out rr = Out(0);
 #pragma unroll
         for (int p = 0; p < P; ++p) rr = p == lane ? ratio[p] : rr;
         if (c < nkc) {
-          t.el[6 * e + c * P + lane] = (double)((R)kin * rr);
+          t.el[6 * e + c * P + lane] = (double)((Out)kin * rr);
         } else {
           const int v = v0 + lane, lmax = s.ecp_maxl1[atom];
           const double* vl = k.ec + (size_t)e * kEC + EC_VL;   // V_l at the nearest nucleus
-          const R wv = (R)s.mesh_w[v] * rr;
-          R vsum = R(0);
-          for (int l = 0; l < lmax; ++l) vsum += (R)vl[l] * (R(2 * l + 1) * legendre_t<R>(l, ct) * wv);
+          const Out wv = (Out)s.mesh_w[v] * rr;
+          const Out cto = (Out)ct;
+          Out vsum = Out(0);
+          for (int l = 0; l < lmax; ++l) vsum += (Out)vl[l] * (Out(2 * l + 1) * legendre_t<Out>(l, cto) * wv);
           t.V[e * nv + v] = (double)vsum;
         }
       }
@@ -2274,7 +2232,7 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
 // LRDMC GFMC_n projections; K steps fused.  K == 0 with energy outputs computes
 // e_L and V_diag at the current positions with the rotation of draw[w].
 // R: mesh arithmetic, Tab: table storage and updates.
-template <class R, class Tab>
+template <class R, class Tab, class Acc = R>
 __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
                         double* eL, double* vdiag, TauArgs ta) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2312,8 +2270,8 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
       }
       __syncthreads();
     }
-    electron_terms<Tab, R>(k, t, alat);
-    mesh_terms<R, Tab>(k, t, alat, true);
+    electron_terms<Tab, Acc>(k, t, alat);
+    mesh_terms<R, Tab, Acc>(k, t, alat, true);
     double diag, nondiag;
     lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
@@ -2511,21 +2469,21 @@ WS to_ws(const jqmc_walkers* w) {
 
 bool walkers_ok(const jqmc_system* sys, const jqmc_walkers* w) {
   if (!sys || !w || w->nwalk <= 0) return false;
-  if (w->precision != JQMC_PREC_FP64 && w->precision != JQMC_PREC_MIXED) return false;
+  if (w->precision != JQMC_PREC_FP64 && !is_mixed(w->precision)) return false;
   if (!w->r || !w->G || !w->Ginv || !w->Tup || !w->Tdn || !w->status || !w->dphi || !w->ecache) return false;
   if (sys->s.has_j3 && (!w->h3 || !w->dphi3)) return false;
-  if (w->precision == JQMC_PREC_MIXED && !w->scratch) return false;
-  if (w->precision == JQMC_PREC_MIXED && dcache_bytes(sys->s) > kDcacheSmemMax && !w->dcache) return false;
+  if (is_mixed(w->precision) && !w->scratch) return false;
+  if (is_mixed(w->precision) && dcache_bytes(sys->s) > kDcacheSmemMax && !w->dcache) return false;
   return true;
 }
 
-int tab_bytes(const jqmc_walkers* w) { return w->precision == JQMC_PREC_MIXED ? 4 : 8; }
+int tab_bytes(const jqmc_walkers* w) { return is_mixed(w->precision) ? 4 : 8; }
 
 KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   KParams P;
   P.s = sys->s;
   P.ws = to_ws(w);
-  const bool mixed = w->precision == JQMC_PREC_MIXED;
+  const bool mixed = is_mixed(w->precision);
   P.tl = table_layout(sys->s, !mixed);
   P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
   P.dcache_global = mixed && dcache_bytes(sys->s) > kDcacheSmemMax;
@@ -2544,10 +2502,12 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
                  double* d_w, double* d_eL, double* d_vd, void* stream, TauArgs ta = TauArgs{nullptr, nullptr, nullptr}) {
   KParams P = make_params(sys, w);
   const int smem = P.ml.bytes;
-  if (w->precision == JQMC_PREC_MIXED) {
+  if (is_mixed(w->precision)) {
     // projections: float arithmetic on the float tables; the local energy of a
-    // block (K == 0): FP64 arithmetic (AO values, ratios, sums) on the float tables
-    auto fn = K > 0 ? k_lrdmc<float, float> : k_lrdmc<double, float>;
+    // block (K == 0): float values with compensated float-float sums, or FP64
+    // arithmetic on the float tables (JQMC_PREC_MIXED_E64)
+    auto fn = K > 0 ? k_lrdmc<float, float, float>
+                    : (w->precision == JQMC_PREC_MIXED_E64 ? k_lrdmc<double, float, double> : k_lrdmc<float, float, F2>);
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
     fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);
@@ -2742,12 +2702,12 @@ int jqmc_system_destroy(jqmc_system* sys) {
 }
 
 int64_t jqmc_walker_bytes(const jqmc_system* sys, int32_t precision) {
-  if (!sys || (precision != JQMC_PREC_FP64 && precision != JQMC_PREC_MIXED)) return JQMC_E_ARG;
+  if (!sys || (precision != JQMC_PREC_FP64 && !is_mixed(precision))) return JQMC_E_ARG;
   const Sys& s = sys->s;
   const int64_t n = s.n_up, N = s.N, A = s.det.nao, A3 = s.has_j3 ? s.j3.nao : 0;
-  const int64_t tb = precision == JQMC_PREC_MIXED ? 4 : 8;
+  const int64_t tb = is_mixed(precision) ? 4 : 8;
   return 8 * N * 3 + 8 * (N + 1) * kEC + tb * (2 * n * n + 2 * n * A + N * A3 + N * 4 * A + N * 5 * A3) + 4 +
-         (precision == JQMC_PREC_MIXED ? 8 * 2 * n * A : 0);
+         (is_mixed(precision) ? 8 * 2 * n * A : 0);
 }
 
 int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_t npts, double* d_out, void* stream) {
@@ -2770,7 +2730,7 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
   const int vec_len = (s.det.nao + n > 3 * A3) ? s.det.nao + n : 3 * A3;
   const int off_phi3 = align16(off_vec + vec_len * 8);
   const int smem = align16(off_phi3 + (s.has_j3 ? s.N * A3 * 8 : 0));
-  if (w->precision == JQMC_PREC_MIXED) {
+  if (is_mixed(w->precision)) {
     // M_up, M_dn by the float-float lam-GEMM into the scratch, then the rest in FP64
     const int rows = s.det.nao <= 2048 ? 8 : 4;
     const int smem_m = rows * s.det.nao * 8;
@@ -2894,7 +2854,7 @@ int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jq
   const int grid = 4 * 152, bs = 256;
   k_gather<double><<<grid, bs, 0, S(stream)>>>(src->r, dst->r, N * 3, d_chosen, W);
   auto tab = [&](const void* a, void* b, long long per) {
-    if (src->precision == JQMC_PREC_MIXED)
+    if (is_mixed(src->precision))
       k_gather<float><<<grid, bs, 0, S(stream)>>>(static_cast<const float*>(a), static_cast<float*>(b), per, d_chosen, W);
     else
       k_gather<double><<<grid, bs, 0, S(stream)>>>(static_cast<const double*>(a), static_cast<double*>(b), per, d_chosen, W);

@@ -19,7 +19,7 @@ from .atomic_orbital import primitive_norm
 from .coulomb_potential import ECP_MESHES
 from .hamiltonians import Hamiltonian_data
 
-PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, "mixed_fp64_energy": _lib.PREC_MIXED_E64}
 
 
 def _ptr(a: np.ndarray, ctype):
@@ -178,8 +178,11 @@ class WalkerSet:
 
     precision "fp64": every table double (the plain drop-in);
     precision "mixed": G, G^-1, T tables and the J3 field in float, rebuilt in
-    double from the positions by ``init`` (an FP64 scratch of 2 n A doubles per
-    walker is held for that rebuild)."""
+    double from the positions by ``init`` / ``rebuild`` (an FP64 scratch of
+    2 n A doubles per walker is held for that rebuild); the block energy uses
+    float values with compensated float-float sums;
+    precision "mixed_fp64_energy": as "mixed", with the block energy in FP64
+    arithmetic on the float tables (more accuracy margin, slower energy)."""
 
     def __init__(self, system: GpuSystem, r_up, r_dn, precision: str = "fp64", scratch: torch.Tensor | None = None):
         self.sys = system
@@ -201,7 +204,7 @@ class WalkerSet:
         self.dphi3 = torch.empty((W, N, 5, max(A3, 1)), dtype=tdt, device=dev)
         self.ecache = torch.zeros((W, N + 1, _lib.ECACHE_STRIDE), dtype=torch.float64, device=dev)
         self.status = torch.zeros(W, dtype=torch.int32, device=dev)
-        if precision == "mixed":
+        if precision != "fp64":
             self.scratch = scratch if scratch is not None else torch.empty((W, 2, n, A), dtype=torch.float64, device=dev)
             M = len(system._keep["pos"])
             big = N * (M + N) * 3 * 4 > 64 * 1024
