@@ -412,7 +412,7 @@ def gpu_arm(a):
     adjoint = adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")) if (rank == 0 and not a.no_adjoint) else None
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
-                "jqmc_lu_rebuild_refine": 1}
+                "jqmc_lu_rebuild_refine": 2}   # k_rebuild_m + k_walker_init
     if rank == 0:
         line = {
             "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -445,7 +445,7 @@ def gpu_arm(a):
             "e2e": e2e,
             "gpu_launches": sum(per_call.values()) * a.steps,
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,
-                         "traffic": traffic, "kernel": "k_lrdmc<float,float,double> (jqmc_lrdmc_project, mixed)",
+                         "traffic": traffic, "kernel": "k_lrdmc<float,float,float> (jqmc_lrdmc_project, mixed)",
                          "flop_convention": f"FMA=2, add/mul/div/sqrt=1, exp={EXP_FLOPS:g}",
                          "peak_source": "measured in this run by jqmc_probe_fp32 (8 independent FMA chains per thread)",
                          "avg_launch_ms": mix_ms, "ecp_electron_fraction": ecp_frac,
