@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "walker-steps/s on 1 GB300: mixed-prec+batched vs plain FP64 at |Δ<E>|≤0.1 mHa"
+NCU_TRAFFIC_PER_WALKER_STEP = {"chain32": (4.629343e9 + 0.7037056e9) / (912 * 2)}
 UNIT = "walker-steps/s"
 
 
@@ -395,14 +396,12 @@ def gpu_arm(a):
     ach64 = f64 * W * K / (mix_ms / 1e3) / 1e9
     plain_flops = lrdmc_step_flops(gs, ecp_frac) * W * K
     plain_ach = plain_flops / (plain_ms / 1e3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "lrdmc_project_traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as f:
-                traffic = json.load(f).get(f"{a.workload}_mixed")
-        except (OSError, ValueError):
-            traffic = None
+    # DRAM bytes (read + write) per walker-step of the mixed projection kernel from
+    # one ncu capture of a small chain32 case (912 walkers x 2 projections: 4.63 GB
+    # read, 0.70 GB written), scaled to this launch by the walker-steps it
+    # processes (the kernel's traffic grows in proportion)
+    traffic_per_ws = NCU_TRAFFIC_PER_WALKER_STEP.get(a.workload)
+    traffic = traffic_per_ws * W * K if traffic_per_ws else None
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -445,7 +444,8 @@ def gpu_arm(a):
             "e2e": e2e,
             "gpu_launches": sum(per_call.values()) * a.steps,
             "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,
-                         "traffic": traffic, "kernel": "k_lrdmc<float,float,float> (jqmc_lrdmc_project, mixed)",
+                         "traffic": traffic, "traffic_unit": "bytes per launch (ncu, scaled from 912 walkers x 2 steps)",
+                         "kernel": "k_lrdmc<float,float,float> (jqmc_lrdmc_project, mixed)",
                          "flop_convention": f"FMA=2, add/mul/div/sqrt=1, exp={EXP_FLOPS:g}",
                          "peak_source": "measured in this run by jqmc_probe_fp32 (8 independent FMA chains per thread)",
                          "avg_launch_ms": mix_ms, "ecp_electron_fraction": ecp_frac,
