@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--alat", type=float, default=0.2)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the parameter-derivative leg")
+    p.add_argument("--no-batching", action="store_true", help="skip the many-molecule leg")
     a = p.parse_args()
     if a.walkers is None:
         a.walkers = 16384 if a.workload == "chain32" else 8192
@@ -272,6 +273,78 @@ def adjoint_leg(stream, dev, peak64, hbm_peak, walkers: int = 8192, reps: int = 
     return out
 
 
+def batching_leg(nmol: int = 64, steps: int = 500, K: int = 50, fp64_steps: int = 50):
+    """64 independent molecules (1-20 nuclei, Z_eff in {1, 4, 6}), walkers in
+    proportion to the electron count (256-4096), VMC in the mixed precision:
+    one CUDA graph of batched launches per electron-count bucket (CTA size
+    autotuned per bucket), table rebuild every K proposals; against sequential
+    per-molecule launches of the plain FP64 form with the same work per proposal
+    (neither keeps the energy caches current between measurements)."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.batching import MoleculeBatch
+    hams = [synthetic.random_molecule(sd).hamiltonian for sd in range(nmol)]
+    Ns = [h.wavefunction_data.geminal_data.num_electron_up + h.wavefunction_data.geminal_data.num_electron_dn for h in hams]
+    W = [int(np.clip(round(256 + 3840 * (n - 2) / 58), 256, 4096)) for n in Ns]
+    mb = MoleculeBatch(hams, W, precision="mixed", seed=11)
+    state_gb = sum(gs.walker_bytes("mixed") * w for gs, w in zip(mb.systems, W)) / 1e9
+    tuned = mb.autotune(K=4, candidates=(32, 64, 128), reps=1)
+    mb.capture(steps, K)
+    mb.replay()                                   # warm-up replay
+    torch.cuda.synchronize()
+    p0 = mb.proposals
+    acc0 = sum(int(b.accept.sum()) for b in mb.buckets)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    mb.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_mixed = e0.elapsed_time(e1)
+    total = mb.total_walkers
+    acc_mixed = (sum(int(b.accept.sum()) for b in mb.buckets) - acc0) / ((mb.proposals - p0) * total)
+    buckets = {str(b.bound): {"molecules": len(b.items), "walkers": b.total, "threads": b.threads} for b in mb.buckets}
+    launches = mb.graph_launches
+    mb.close()
+    del mb
+    torch.cuda.empty_cache()
+    # plain FP64: one launch per molecule, in sequence (each molecule's walkers are
+    # built, warmed up, timed and freed in turn; the launch times are summed)
+    ms_fp64, acc_fp64 = 0.0, 0
+    for k, (h, w) in enumerate(zip(hams, W)):
+        sb = MoleculeBatch([h], [w], precision="fp64", seed=11 + k)
+        bk = sb.buckets[0]
+        idr, fdr = sb.draws(bk, 4)
+        sb.sweep(bk, idr, fdr, threads=64)       # warm-up
+        idr, fdr = sb.draws(bk, fp64_steps)
+        torch.cuda.synchronize()
+        a0 = int(bk.accept.sum())
+        e0.record()
+        sb.sweep(bk, idr, fdr, threads=64)
+        e1.record()
+        torch.cuda.synchronize()
+        ms_fp64 += e0.elapsed_time(e1)
+        acc_fp64 += int(bk.accept.sum()) - a0
+        sb.close()
+        del sb, idr, fdr
+    acc_fp64 /= fp64_steps * total
+    torch.cuda.empty_cache()
+    v_mixed = total * steps / (ms_mixed / 1e3)
+    v_fp64 = total * fp64_steps / (ms_fp64 / 1e3)
+    return {"workload": f"{nmol} random molecules, {min(Ns)}-{max(Ns)} electrons, {total} walkers (256-4096 per molecule, "
+                        f"in proportion to the electron count), VMC",
+            "mixed_batched_graph": {"walker_steps_per_s": v_mixed, "proposals_per_walker": steps, "ms": ms_mixed,
+                                    "walker_state_GB": state_gb,
+                                    "rebuild_every": K, "graph_launches": launches, "accept_ratio": acc_mixed,
+                                    "buckets": buckets, "autotune": {str(k): v for k, v in tuned.items()}},
+            "fp64_per_molecule_sequential": {"walker_steps_per_s": v_fp64, "proposals_per_walker": fp64_steps, "ms": ms_fp64,
+                                             "launches": nmol, "accept_ratio": acc_fp64},
+            "speedup": v_mixed / v_fp64,
+            "note": "aggregate walker-steps/s; CUDA events around one graph replay (mixed) and around the 64 sequential "
+                    "launches (FP64); draws resident in HBM"}
+
+
 def gpu_arm(a):
     import ctypes
 
@@ -408,7 +481,12 @@ def gpu_arm(a):
             peaks = json.load(f)
     except (OSError, ValueError):
         peaks = {}
+    # the remaining legs run after the chain32 walker sets are released
+    del drv, ws_m, r_all, near
+    mixed.pop("drv")
+    torch.cuda.empty_cache()
     adjoint = adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")) if (rank == 0 and not a.no_adjoint) else None
+    batching = batching_leg() if (rank == 0 and not a.no_batching) else None
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 1, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
                 "jqmc_lu_rebuild_refine": 2}   # k_rebuild_m + k_walker_init
@@ -457,6 +535,7 @@ def gpu_arm(a):
                          "plain_fp64_kernel": {"bound": "fp64", "achieved": plain_ach, "peak": peak64, "frac": plain_ach / peak64,
                                                "avg_launch_ms": plain_ms}},
             "adjoint": adjoint,
+            "batching": batching,
             "cpu_baseline": cpu_base,
             "clocks": mixed["clocks"],
         }

@@ -238,6 +238,34 @@ int jqmc_probe_fp64(int64_t iters, int32_t blocks, double* d_sink, double* flops
 /* The same for FP32 FMA chains (measurement helper, no reference counterpart). */
 int jqmc_probe_fp32(int64_t iters, int32_t blocks, float* d_sink, double* flops, void* stream);
 
+/* ---- Batches of systems (many molecules in one launch) --------------------
+ * A batch binds N (system, walker set) pairs of one precision; the walkers of
+ * item i are walkers [off_i, off_i + nwalk_i) of the batch, off_i the running
+ * sum of the earlier items' walker counts.  One launch covers every walker of
+ * every item (each CTA finds its item), so molecules of uneven size share the
+ * GPU; the per-item kernel parameters live on the device, so the launches can
+ * be captured in a CUDA graph.  Replaces the per-molecule VMC driver loop of
+ * jqmc_mcmc.py (MCMC.run, :456-1000) for many independent molecules. */
+typedef struct jqmc_batch jqmc_batch;
+int jqmc_batch_create(int32_t nitem, const jqmc_system* const* systems, const jqmc_walkers* walkers, jqmc_batch** out);
+int jqmc_batch_destroy(jqmc_batch* b);
+int jqmc_batch_walkers(const jqmc_batch* b);   /* total walkers of the batch */
+
+/* K Metropolis proposals for every walker of the batch (the jqmc_vmc_sweep
+ * step, jqmc_mcmc.py:4316-4523): d_idraw total*K*4 and d_fdraw total*K*2 in
+ * batch walker order, d_accept total.  JQMC_PREC_MIXED batches run the
+ * proposals with float tables (AO values, ratio, candidate G^-1 for the AS
+ * factor, rank-1 updates) and double acceptance.  threads: CTA size (32..256,
+ * a multiple of 32).  caches == 0 skips keeping the AO derivative tables and
+ * the energy cache current (call jqmc_batch_rebuild with full = 1 before an
+ * energy is measured). */
+int jqmc_vmc_sweep_batch(const jqmc_batch* b, int32_t K, const int32_t* d_idraw, const double* d_fdraw, double Dt,
+                         double eps_AS, int32_t* d_accept, int32_t threads, int32_t caches, void* stream);
+
+/* full == 0: jqmc_lu_rebuild_refine for every walker of the batch; full != 0:
+ * jqmc_walker_init (all state, including the energy cache and derivative tables). */
+int jqmc_batch_rebuild(const jqmc_batch* b, int32_t full, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

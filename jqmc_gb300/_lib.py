@@ -74,6 +74,11 @@ def lib():
         L.jqmc_lu_rebuild_refine.argtypes = [vp, C.POINTER(Walkers), vp]
         L.jqmc_dlnpsi_dparam.argtypes = [vp, C.POINTER(Walkers), vp, vp, vp, vp, vp, vp]
         L.jqmc_lrdmc_project_t.argtypes = [vp, C.POINTER(Walkers), i32, vp, f64, vp, vp, vp, vp, vp]
+        L.jqmc_batch_create.argtypes = [i32, C.POINTER(vp), C.POINTER(Walkers), C.POINTER(vp)]
+        L.jqmc_batch_destroy.argtypes = [vp]
+        L.jqmc_batch_walkers.argtypes = [vp]
+        L.jqmc_vmc_sweep_batch.argtypes = [vp, i32, vp, vp, f64, f64, vp, i32, i32, vp]
+        L.jqmc_batch_rebuild.argtypes = [vp, i32, vp]
         L.jqmc_log_psi.argtypes = [vp, C.POINTER(Walkers), vp, vp, vp, vp]
         L.jqmc_vmc_sweep.argtypes = [vp, C.POINTER(Walkers), i32, vp, vp, f64, f64, vp, vp]
         L.jqmc_vmc_measure.argtypes = [vp, C.POINTER(Walkers), vp, f64, vp, vp, vp]
@@ -87,7 +92,8 @@ def lib():
         for name in ("jqmc_probe_fp64", "jqmc_system_create", "jqmc_system_destroy", "jqmc_ao_vgl", "jqmc_walker_init", "jqmc_log_psi",
                      "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
                      "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
-                     "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t"):
+                     "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
+                     "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -101,4 +107,5 @@ def check(rc: int, what: str) -> None:
 EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "jqmc_ao_vgl", "jqmc_walker_init",
             "jqmc_log_psi", "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
             "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
-            "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t")
+            "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
+            "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild")

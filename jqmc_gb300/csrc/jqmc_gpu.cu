@@ -548,14 +548,74 @@ __device__ double block_min(double v, double* red) {
 
 // out[k] = sum_a M[k*A + a] x[a] for k < n (one warp per row)
 template <class T>
-__device__ void rows_dot(const T* M, int n, int A, const T* x, T* out) {
+__device__ void rows_dot(const T* __restrict__ M, int n, int A, const T* __restrict__ x, T* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = wid; k < n; k += nw) {
-    T acc = T(0);
-    for (int a = lane; a < A; a += 32) acc += M[(size_t)k * A + a] * x[a];
-    acc = warp_sum(acc);
+    const T* row = M + (size_t)k * A;
+    T acc0 = T(0), acc1 = T(0);
+    int a = lane;
+    for (; a + 32 < A; a += 64) {   // two independent loads in flight per lane
+      acc0 += row[a] * x[a];
+      acc1 += row[a + 32] * x[a + 32];
+    }
+    if (a < A) acc0 += row[a] * x[a];
+    const T acc = warp_sum(acc0 + acc1);
     if (lane == 0) out[k] = acc;
   }
+}
+
+// Loads kept in flight per thread by the column helpers below.
+constexpr int kMLP = 4;
+
+// v[j*A + b] += c[j] * x for j < n (one column b of a table): the loads of a
+// group of kMLP rows are issued before their stores, so a thread keeps kMLP
+// memory requests in flight instead of one load-modify-store at a time.
+template <class Tab>
+__device__ __forceinline__ void column_axpy(Tab* __restrict__ v, size_t A, int b, int n, const Tab* __restrict__ c, Tab x) {
+  for (int j0 = 0; j0 < n; j0 += kMLP) {
+    Tab t[kMLP];
+#pragma unroll
+    for (int u = 0; u < kMLP; ++u)
+      if (j0 + u < n) t[u] = v[(size_t)(j0 + u) * A + b];
+#pragma unroll
+    for (int u = 0; u < kMLP; ++u)
+      if (j0 + u < n) v[(size_t)(j0 + u) * A + b] = t[u] + c[j0 + u] * x;
+  }
+}
+
+// sum_j v[j*A + b] c[j] with kMLP partial sums
+template <class Tab>
+__device__ __forceinline__ Tab column_dot(const Tab* __restrict__ v, size_t A, int b, int n, const Tab* __restrict__ c) {
+  Tab acc[kMLP];
+#pragma unroll
+  for (int u = 0; u < kMLP; ++u) acc[u] = Tab(0);
+  for (int j0 = 0; j0 < n; j0 += kMLP) {
+#pragma unroll
+    for (int u = 0; u < kMLP; ++u)
+      if (j0 + u < n) acc[u] += v[(size_t)(j0 + u) * A + b] * c[j0 + u];
+  }
+  Tab r = Tab(0);
+#pragma unroll
+  for (int u = 0; u < kMLP; ++u) r += acc[u];
+  return r;
+}
+
+// sum_a L[a*A + b] x[a] (column b of a row-major A x A matrix) with kMLP partial sums
+template <class Tab>
+__device__ __forceinline__ Tab matvec_col(const Tab* __restrict__ L, int A, int b, const Tab* __restrict__ x) {
+  Tab acc[kMLP];
+#pragma unroll
+  for (int u = 0; u < kMLP; ++u) acc[u] = Tab(0);
+  int a = 0;
+  for (; a + kMLP <= A; a += kMLP) {
+#pragma unroll
+    for (int u = 0; u < kMLP; ++u) acc[u] += L[(size_t)(a + u) * A + b] * x[a + u];
+  }
+  for (; a < A; ++a) acc[0] += L[(size_t)a * A + b] * x[a];
+  Tab r = Tab(0);
+#pragma unroll
+  for (int u = 0; u < kMLP; ++u) r += acc[u];
+  return r;
 }
 
 // ------------------------------------------------------------------ physics helpers
@@ -924,7 +984,7 @@ __device__ void store_walker(const Work<Tab>& k, const WS& ws, int w) {
 //          T_up += G^-1[j,:] (x) (lambda dphi - T_up^T G q) / ratio
 // (every right-hand side uses the tables before the move).  Arithmetic in Tab.
 template <class Tab>
-__device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) {
+__device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz, bool caches = true) {
   const Sys& s = k.s;
   const int n = k.n, A = k.A, A3 = k.A3;
   const bool up = e < s.n_up;
@@ -962,18 +1022,15 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     }
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
-      Tab dl = Tab(0);
-      for (int a = 0; a < A; ++a) dl += lam[(size_t)a * A + b] * k.vA1[a];
-      Tab mw = Tab(0);
-      for (int j = 0; j < n; ++j) mw += k.Tdn[(size_t)j * A + b] * k.vn2[j];
+      const Tab dl = matvec_col<Tab>(lam, A, b, k.vA1);
+      const Tab mw = column_dot<Tab>(k.Tdn, A, b, n, k.vn2);
       k.vA2[b] = (dl - mw) * inv;
     }
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
-      const Tab xb = k.vA2[b];
-      for (int j = 0; j < n; ++j) k.Tdn[(size_t)j * A + b] += k.vn3[j] * xb;
+      column_axpy<Tab>(k.Tdn, A, b, n, k.vn3, k.vA2[b]);
       const Tab ti = k.Tup[(size_t)i * A + b];
-      for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + b] -= ti * k.vn1[t] * inv;
+      column_axpy<Tab>(k.Tup, A, b, n, k.vn1, -ti * inv);
     }
     Tab* gn = (n <= scn_cap) ? scn : k.vA2;
     __syncthreads();
@@ -1001,18 +1058,15 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     }
     __syncthreads();
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
-      Tab dm = Tab(0);
-      for (int b = 0; b < A; ++b) dm += lamT[(size_t)b * A + a] * k.vA1[b];
-      Tab mq = Tab(0);
-      for (int t = 0; t < n; ++t) mq += k.Tup[(size_t)t * A + a] * k.vn2[t];
+      const Tab dm = matvec_col<Tab>(lamT, A, a, k.vA1);
+      const Tab mq = column_dot<Tab>(k.Tup, A, a, n, k.vn2);
       k.vA2[a] = (dm - mq) * inv;
     }
     __syncthreads();
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
-      const Tab xa = k.vA2[a];
-      for (int t = 0; t < n; ++t) k.Tup[(size_t)t * A + a] += xa * k.vn3[t];
+      column_axpy<Tab>(k.Tup, A, a, n, k.vn3, k.vA2[a]);
       const Tab tj = k.Tdn[(size_t)i * A + a];
-      for (int t = 0; t < n; ++t) k.Tdn[(size_t)t * A + a] -= k.vn1[t] * tj * inv;
+      column_axpy<Tab>(k.Tdn, A, a, n, k.vn1, -tj * inv);
     }
     Tab* cn = (n <= scn_cap) ? scn : k.vA2;
     __syncthreads();
@@ -1053,45 +1107,47 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
       k.h3[(size_t)m * A3 + c] += useJ ? k.v32[c] : k.v30[c];
     }
   }
-  fill_dtables<Tab>(s, px, py, pz, k.dphi + (size_t)e * 4 * A, s.has_j3 ? k.dphi3 + (size_t)e * 5 * A3 : nullptr);
-  // energy cache: every pair with the moved electron (J2 terms of the partner,
-  // e-e Coulomb), then the moved electron's own row
-  {
-    const int N = k.N;
-    double dee = 0.0, jgx = 0.0, jgy = 0.0, jgz = 0.0, jl = 0.0;
-    for (int m = threadIdx.x; m < N; m += blockDim.x) {
-      if (m == e) continue;
-      const double mx = k.r[3 * m], my = k.r[3 * m + 1], mz = k.r[3 * m + 2];
-      const double oxm = mx - ox, oym = my - oy, ozm = mz - oz;      // r_m - r_e(old)
-      const double nxm = mx - px, nym = my - py, nzm = mz - pz;      // r_m - r_e(new)
-      const double dold = sqrt(oxm * oxm + oym * oym + ozm * ozm);
-      const double dnew = sqrt(nxm * nxm + nym * nym + nzm * nzm);
-      dee += 1.0 / dnew - 1.0 / dold;
-      if (s.has_j2) {
-        double f1o, f2o, f1n, f2n;
-        j2_pair_d(s, dold, f1o, f2o);
-        j2_pair_d(s, dnew, f1n, f2n);
-        double* row = k.ec + (size_t)m * kEC;
-        row[EC_J2G] += f1n * nxm / dnew - f1o * oxm / dold;
-        row[EC_J2G + 1] += f1n * nym / dnew - f1o * oym / dold;
-        row[EC_J2G + 2] += f1n * nzm / dnew - f1o * ozm / dold;
-        row[EC_J2L] += (f2n + 2.0 * f1n / dnew) - (f2o + 2.0 * f1o / dold);
-        jgx -= f1n * nxm / dnew; jgy -= f1n * nym / dnew; jgz -= f1n * nzm / dnew;
-        jl += f2n + 2.0 * f1n / dnew;
+  if (caches) {
+    fill_dtables<Tab>(s, px, py, pz, k.dphi + (size_t)e * 4 * A, s.has_j3 ? k.dphi3 + (size_t)e * 5 * A3 : nullptr);
+    // energy cache: every pair with the moved electron (J2 terms of the partner,
+    // e-e Coulomb), then the moved electron's own row
+    {
+      const int N = k.N;
+      double dee = 0.0, jgx = 0.0, jgy = 0.0, jgz = 0.0, jl = 0.0;
+      for (int m = threadIdx.x; m < N; m += blockDim.x) {
+        if (m == e) continue;
+        const double mx = k.r[3 * m], my = k.r[3 * m + 1], mz = k.r[3 * m + 2];
+        const double oxm = mx - ox, oym = my - oy, ozm = mz - oz;      // r_m - r_e(old)
+        const double nxm = mx - px, nym = my - py, nzm = mz - pz;      // r_m - r_e(new)
+        const double dold = sqrt(oxm * oxm + oym * oym + ozm * ozm);
+        const double dnew = sqrt(nxm * nxm + nym * nym + nzm * nzm);
+        dee += 1.0 / dnew - 1.0 / dold;
+        if (s.has_j2) {
+          double f1o, f2o, f1n, f2n;
+          j2_pair_d(s, dold, f1o, f2o);
+          j2_pair_d(s, dnew, f1n, f2n);
+          double* row = k.ec + (size_t)m * kEC;
+          row[EC_J2G] += f1n * nxm / dnew - f1o * oxm / dold;
+          row[EC_J2G + 1] += f1n * nym / dnew - f1o * oym / dold;
+          row[EC_J2G + 2] += f1n * nzm / dnew - f1o * ozm / dold;
+          row[EC_J2L] += (f2n + 2.0 * f1n / dnew) - (f2o + 2.0 * f1o / dold);
+          jgx -= f1n * nxm / dnew; jgy -= f1n * nym / dnew; jgz -= f1n * nzm / dnew;
+          jl += f2n + 2.0 * f1n / dnew;
+        }
       }
-    }
-    dee = block_sum(dee, k.red);
-    jgx = block_sum(jgx, k.red);
-    jgy = block_sum(jgy, k.red);
-    jgz = block_sum(jgz, k.red);
-    jl = block_sum(jl, k.red);
-    if (threadIdx.x < 32) {
-      double* row = k.ec + (size_t)e * kEC;
-      ecache_single_warp(s, px, py, pz, row);
-      if (threadIdx.x == 0) {
-        row[EC_J2G] = jgx; row[EC_J2G + 1] = jgy; row[EC_J2G + 2] = jgz;
-        row[EC_J2L] = jl;
-        k.ec[(size_t)N * kEC + EC_TOT_EE] += dee;
+      dee = block_sum(dee, k.red);
+      jgx = block_sum(jgx, k.red);
+      jgy = block_sum(jgy, k.red);
+      jgz = block_sum(jgz, k.red);
+      jl = block_sum(jl, k.red);
+      if (threadIdx.x < 32) {
+        double* row = k.ec + (size_t)e * kEC;
+        ecache_single_warp(s, px, py, pz, row);
+        if (threadIdx.x == 0) {
+          row[EC_J2G] = jgx; row[EC_J2G + 1] = jgy; row[EC_J2G + 2] = jgz;
+          row[EC_J2L] = jl;
+          k.ec[(size_t)N * kEC + EC_TOT_EE] += dee;
+        }
       }
     }
   }
@@ -1605,14 +1661,13 @@ __device__ __forceinline__ void dot2_step(float& s, float& c, float xh, float xl
 // and reads the split lam column once per ROWS electrons.  This is the dense
 // lam-GEMM of the rebuild (the geminal assembly of jqmc/determinant.py:1380-1402).
 template <int ROWS>
-__global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
+__device__ void rebuild_m_body(const KParams& P, int w, int by, unsigned char* smem) {
   constexpr int kRebuildRows = ROWS;
-  extern __shared__ __align__(16) unsigned char smem[];
   const Sys& s = P.s;
-  const int w = blockIdx.x;
   const int n = s.n_up, A = s.det.nao;
   const int nb = (n + kRebuildRows - 1) / kRebuildRows;
-  const int spin = blockIdx.y / nb, i0 = (blockIdx.y % nb) * kRebuildRows;
+  if (by >= 2 * nb) return;   // batched launches size grid.y for the largest molecule
+  const int spin = by / nb, i0 = (by % nb) * kRebuildRows;
   const int rows = min(kRebuildRows, n - i0);
   float2* ph = reinterpret_cast<float2*>(smem);   // kRebuildRows x A
   const double* r = P.ws.r + ((size_t)w * s.N + (size_t)spin * s.n_up + i0) * 3;
@@ -1656,6 +1711,12 @@ __global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
   }
 }
 
+template <int ROWS>
+__global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  rebuild_m_body<ROWS>(P, blockIdx.x, blockIdx.y, smem);
+}
+
 // Walker initialisation in FP64: G, G^-1 (Gauss-Jordan, partial pivoting), T
 // tables and J3 field, written in the table type Tab.  M_up / M_dn go to the
 // double scratch (for Tab == double the T buffers themselves).
@@ -1669,9 +1730,8 @@ constexpr int kInitTablesOnly = 1;
 constexpr int kInitRefine = 2;
 constexpr int kInitMReady = 4;
 template <class Tab>
-__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int off_phi3, int mode) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int w = blockIdx.x;
+__device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_aug, int off_vec, int mode,
+                                 unsigned char* smem) {
   const Sys s = stage_tables(P.s, P.tl, smem);
   const int n = s.n_up, A = s.det.nao, N = s.N, A3 = s.has_j3 ? s.j3.nao : 1;
   double* r = reinterpret_cast<double*>(smem + P.wl.off_r);
@@ -1816,39 +1876,44 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
     for (int e = 0; e < N; ++e)
       fill_dtables<Tab>(s, r[3 * e], r[3 * e + 1], r[3 * e + 2], dpw + (size_t)e * 4 * A, dp3w ? dp3w + (size_t)e * 5 * A3 : nullptr);
   }
-  // J3 field
+  // J3 field, in two passes over the electrons so that only four A3-vectors are
+  // held: the spin totals of phi3, then each field with the running prefix (the
+  // electron's J3 AO values are evaluated again in the second pass)
   if (s.has_j3) {
-    double* phi3 = reinterpret_cast<double*>(smem + off_phi3);  // N*A3
     double* tot_up = vec;
     double* tot_dn = vec + A3;
     double* pfx = vec + 2 * A3;
-    __syncthreads();
-    for (int p = threadIdx.x; p < N * s.j3.nshell; p += blockDim.x) {
-      const int e = p / s.j3.nshell, sh = p % s.j3.nshell;
-      double* out = phi3 + (size_t)e * A3;
-      auto f = [&](int a, double v) { out[a] = v; };
-      double dx, dy, dz;
-      disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
-      shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
-    }
+    double* pe = vec + 3 * A3;
+    auto fill_phi3 = [&](int e) {
+      auto f = [&](int a, double v) { pe[a] = v; };
+      for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
+        double dx, dy, dz;
+        disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+        shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
+      }
+    };
     __syncthreads();
     for (int c = threadIdx.x; c < A3; c += blockDim.x) {
-      double tu = 0.0, td = 0.0;
-      for (int e = 0; e < s.n_up; ++e) tu += phi3[(size_t)e * A3 + c];
-      for (int e = s.n_up; e < N; ++e) td += phi3[(size_t)e * A3 + c];
-      tot_up[c] = tu;
-      tot_dn[c] = td;
+      tot_up[c] = 0.0;
+      tot_dn[c] = 0.0;
       pfx[c] = 0.0;
     }
-    __syncthreads();
+    for (int e = 0; e < N; ++e) {
+      __syncthreads();
+      fill_phi3(e);
+      __syncthreads();
+      double* tot = e < s.n_up ? tot_up : tot_dn;
+      for (int c = threadIdx.x; c < A3; c += blockDim.x) tot[c] += pe[c];
+    }
     Tab* h = static_cast<Tab*>(P.ws.h3) + (size_t)w * N * A3;
     for (int e = 0; e < N; ++e) {
       const bool up = e < s.n_up;
+      __syncthreads();
       if (e == s.n_up)
         for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] = 0.0;
+      fill_phi3(e);
       __syncthreads();
       const double* tot_same = up ? tot_up : tot_dn;
-      const double* pe = phi3 + (size_t)e * A3;
       for (int c = threadIdx.x; c < A3; c += blockDim.x) {
         // h = j1 + J^T pfx + J (tot_same - pfx - phi_e) + (up ? J tot_dn : J^T tot_up)
         double acc = s.j3vec[c];
@@ -1863,10 +1928,16 @@ __global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, i
       }
       __syncthreads();
       for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] += pe[c];
-      __syncthreads();
     }
   }
 }
+
+template <class Tab>
+__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int mode) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  walker_init_body<Tab>(P, blockIdx.x, off_Gd, off_aug, off_vec, mode, smem);
+}
+
 
 // Per-walker derivatives of ln|psi| with respect to the variational parameters
 // (FP64 form), the blocks grad(evaluate_ln_wavefunction) yields in the reference
@@ -2057,40 +2128,113 @@ __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, 
   if (threadIdx.x == 0) jas[w] = j;
 }
 
-__device__ double as_factor_block(const Work<double>& k) {
+template <class Tab>
+__device__ double as_factor_block(const Work<Tab>& k) {
   const int n = k.n;
-  double F = 0.0;
+  Tab F = Tab(0);
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) F += k.Gi[t] * k.Gi[t];
-  F = block_sum(F, k.red);
+  const double Fs = block_sum((double)F, k.red);
   double mn = 1e300;
   for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
-    double acc = 0.0;
+    Tab acc = Tab(0);
     if (t < n) for (int c = 0; c < n; ++c) acc += k.G[t * n + c] * k.G[t * n + c];
     else for (int rr = 0; rr < n; ++rr) acc += k.G[rr * n + (t - n)] * k.G[rr * n + (t - n)];
-    mn = fmin(mn, acc);
+    mn = fmin(mn, (double)acc);
   }
   mn = block_min(mn, k.red);
-  const double SF = mn * F;
+  const double SF = mn * Fs;
   return SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
 }
 
-// VMC: K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523)   (FP64 form)
-__global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt,
-                            double eps_AS, int* accept, int off_cand) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int w = blockIdx.x;
+// VMC: K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523)
+// Mixed form: the proposal of one step computed by warp 0 in float, lanes over
+// nuclei (jqmc_mcmc.py:4340-4400): nearest nucleus of the old and the new
+// position, the f_l step scale, the Gaussian move along one axis (positions in
+// double), the transition ratio and the J1 difference as a sum of pair
+// differences; writes k.sc[0..5] as the FP64 code does.  The same float f_l
+// values scale the move and enter the ratio, so the proposal densities stay
+// consistent.
+template <class Tab>
+__device__ void vmc_propose_warp(Work<Tab>& k, const Sys& s, const int* id, const double* fd, double Dt) {
+  const int lane = threadIdx.x & 31;
+  const int e = id[0] < s.n_up ? id[1] : s.n_up + id[2];
+  const double ox = k.r[3 * e], oy = k.r[3 * e + 1], oz = k.r[3 * e + 2];
+  auto nearest = [&](float sx, float sy, float sz, int& best, float& bd) {
+    bd = 3.0e38f;
+    best = 0x7fffffff;
+    for (int a = lane; a < s.natom; a += 32) {
+      const float dx = (float)(ox - s.atom_pos[3 * a]) + sx, dy = (float)(oy - s.atom_pos[3 * a + 1]) + sy;
+      const float dz = (float)(oz - s.atom_pos[3 * a + 2]) + sz;
+      const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+      if (d < bd) { bd = d; best = a; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+      if (od < bd || (od == bd && ob < best)) { bd = od; best = ob; }
+    }
+  };
+  auto fscale = [&](int a, float d) {
+    const float Z = (float)s.atom_zeff[a];
+    return 1.0f / (Z * Z) * (1.0f + Z * Z * d) / (1.0f + d);
+  };
+  int ao;
+  float dao;
+  nearest(0.f, 0.f, 0.f, ao, dao);
+  const float fl = fscale(ao, dao);
+  const float g = (float)fd[0] * (fl * (float)Dt);
+  const int ax = id[3];
+  const float mx = ax == 0 ? g : 0.f, my = ax == 1 ? g : 0.f, mz = ax == 2 ? g : 0.f;
+  int an;
+  float dan;
+  nearest(mx, my, mz, an, dan);
+  const float fp = fscale(an, dan);
+  const float dtf = (float)Dt;
+  const float d2 = g * g;
+  const float Tr = (fl / fp) * expf(-d2 * (1.0f / (2.0f * fp * fp * dtf * dtf) - 1.0f / (2.0f * fl * fl * dtf * dtf)));
+  float dj = 0.f;
+  if (s.has_j1) {
+    const float a = (float)s.j1_param;
+    for (int at = lane; at < s.natom; at += 32) {
+      const float dx = (float)(ox - s.atom_pos[3 * at]), dy = (float)(oy - s.atom_pos[3 * at + 1]);
+      const float dz = (float)(oz - s.atom_pos[3 * at + 2]);
+      dj += pair_delta<float, true>(dx, dy, dz, mx, my, mz, s.j1_type, a, (float)s.j1_cA[2 * at], (float)s.j1_cA[2 * at + 1],
+                                    true);
+    }
+    dj = warp_sum(dj);
+  }
+  if (lane == 0) {
+    k.sc[0] = e;
+    k.sc[1] = ox + (double)mx; k.sc[2] = oy + (double)my; k.sc[3] = oz + (double)mz;
+    k.sc[4] = (double)Tr;
+    k.sc[5] = (double)dj;
+  }
+}
+
+// proposal selection, f_l-scaled Gaussian move and T ratio in double on
+// thread 0; the determinant ratio from the T row, the candidate G^-1 / G for the
+// AS factor and the accepted rank-1 update in the table type Tab; J1/J2/J3
+// differences and the acceptance in double.  caches == 0: the AO derivative
+// tables and the energy cache are not kept current (they are rebuilt by
+// jqmc_walker_init before an energy is measured).
+template <class Tab>
+__device__ void vmc_sweep_body(const KParams& P, int w, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw,
+                               double Dt, double eps_AS, int* accept, int off_cand, bool caches, unsigned char* smem) {
   const Sys s = stage_tables(P.s, P.tl, smem);
-  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
+  Work<Tab> k = make_work<Tab>(s, P.wl, smem, P.ws, w);
   load_walker(k, P.ws, w);
   const int n = k.n, A = k.A, A3 = k.A3;
-  double* cand = reinterpret_cast<double*>(smem + off_cand);  // n*n candidate G^-1
-  double* Gc = cand + n * n;                                   // n*n candidate G
+  Tab* cand = reinterpret_cast<Tab*>(smem + off_cand);  // n*n candidate G^-1
+  Tab* Gc = cand + n * n;                                // n*n candidate G
   int nacc = 0;
   double R_old = as_factor_block(k);
   for (int step = 0; step < K; ++step) {
     const int* id = idraw + ((size_t)w * K + step) * 4;
     const double* fd = fdraw + ((size_t)w * K + step) * 2;
-    if (threadIdx.x == 0) {
+    if constexpr (sizeof(Tab) == sizeof(float)) {
+      if (threadIdx.x < 32) vmc_propose_warp<Tab>(k, s, id, fd, Dt);
+    } else if (threadIdx.x == 0) {
       const int sel = id[0];
       const bool is_up = sel < s.n_up;
       const int e = is_up ? id[1] : s.n_up + id[2];
@@ -2123,33 +2267,51 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
     const bool up = e < s.n_up;
     const int i = up ? e : e - s.n_up;
     double dJ = 0.0;
-    if (s.has_j2)
-      for (int m = threadIdx.x; m < k.N; m += blockDim.x) {
-        if (m == e) continue;
-        const double ax = nx - k.r[3 * m], ay = ny - k.r[3 * m + 1], az = nz - k.r[3 * m + 2];
-        const double bx = k.r[3 * e] - k.r[3 * m], by = k.r[3 * e + 1] - k.r[3 * m + 1], bz = k.r[3 * e + 2] - k.r[3 * m + 2];
-        dJ += j2_pair<double>(s.j2_type, s.j2_param, sqrt(ax * ax + ay * ay + az * az)) -
-              j2_pair<double>(s.j2_type, s.j2_param, sqrt(bx * bx + by * by + bz * bz));
+    if (s.has_j2) {
+      if constexpr (sizeof(Tab) == sizeof(float)) {
+        // pair differences from the float displacement r_e - r_m and the move
+        const float sx = (float)(nx - k.r[3 * e]), sy = (float)(ny - k.r[3 * e + 1]), sz = (float)(nz - k.r[3 * e + 2]);
+        const float b = (float)s.j2_param;
+        float dj2 = 0.f;
+        for (int m = threadIdx.x; m < k.N; m += blockDim.x) {
+          if (m == e) continue;
+          const float dx = (float)(k.r[3 * e] - k.r[3 * m]), dy = (float)(k.r[3 * e + 1] - k.r[3 * m + 1]);
+          const float dz = (float)(k.r[3 * e + 2] - k.r[3 * m + 2]);
+          dj2 += pair_delta<float, true>(dx, dy, dz, sx, sy, sz, s.j2_type, b, 0.f, 0.f, false);
+        }
+        dJ = (double)dj2;
+      } else {
+        for (int m = threadIdx.x; m < k.N; m += blockDim.x) {
+          if (m == e) continue;
+          const double ax = nx - k.r[3 * m], ay = ny - k.r[3 * m + 1], az = nz - k.r[3 * m + 2];
+          const double bx = k.r[3 * e] - k.r[3 * m], by = k.r[3 * e + 1] - k.r[3 * m + 1], bz = k.r[3 * e + 2] - k.r[3 * m + 2];
+          dJ += j2_pair<double>(s.j2_type, s.j2_param, sqrt(ax * ax + ay * ay + az * az)) -
+                j2_pair<double>(s.j2_type, s.j2_param, sqrt(bx * bx + by * by + bz * bz));
+        }
       }
-    ao_fill_block<double, double>(s.det, s.atom_pos, nx, ny, nz, k.vA0);
+    }
+    ao_fill_block<Tab, Tab>(s.det, s.atom_pos, nx, ny, nz, k.vA0);
     if (s.has_j3) {
-      ao_fill_block<double, double>(s.j3, s.atom_pos, nx, ny, nz, k.v30);
-      ao_fill_block<double, double>(s.j3, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.v31);
+      ao_fill_block<Tab, Tab>(s.j3, s.atom_pos, nx, ny, nz, k.v30);
+      ao_fill_block<Tab, Tab>(s.j3, s.atom_pos, k.r[3 * e], k.r[3 * e + 1], k.r[3 * e + 2], k.v31);
     }
     __syncthreads();
-    if (s.has_j3)
-      for (int a = threadIdx.x; a < A3; a += blockDim.x) dJ += (k.v30[a] - k.v31[a]) * k.h3[(size_t)e * A3 + a];
+    if (s.has_j3) {
+      Tab d3 = Tab(0);
+      for (int a = threadIdx.x; a < A3; a += blockDim.x) d3 += (k.v30[a] - k.v31[a]) * k.h3[(size_t)e * A3 + a];
+      dJ += (double)d3;
+    }
     dJ = block_sum(dJ, k.red);
-    rows_dot<double>(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
+    rows_dot<Tab>(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
     __syncthreads();
-    const double ratio = k.vn0[i];
-    const double inv = 1.0 / ratio;
+    const Tab ratio = k.vn0[i];
+    const Tab inv = Tab(1) / ratio;
     if (up) {
       for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
         const int rr = t / n, cc = t % n;
-        cand[t] = k.Gi[t] - k.Gi[rr * n + i] * (k.vn0[cc] - (cc == i ? 1.0 : 0.0)) * inv;
+        cand[t] = k.Gi[t] - k.Gi[rr * n + i] * (k.vn0[cc] - (cc == i ? Tab(1) : Tab(0))) * inv;
         if (rr == i) {
-          double g = 0.0;
+          Tab g = Tab(0);
           for (int q = 0; q < n; ++q) g += k.vn0[q] * k.G[q * n + cc];
           Gc[t] = g;
         } else {
@@ -2159,9 +2321,9 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
     } else {
       for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
         const int rr = t / n, cc = t % n;
-        cand[t] = k.Gi[t] - (k.vn0[rr] - (rr == i ? 1.0 : 0.0)) * k.Gi[i * n + cc] * inv;
+        cand[t] = k.Gi[t] - (k.vn0[rr] - (rr == i ? Tab(1) : Tab(0))) * k.Gi[i * n + cc] * inv;
         if (cc == i) {
-          double g = 0.0;
+          Tab g = Tab(0);
           for (int q = 0; q < n; ++q) g += k.G[rr * n + q] * k.vn0[q];
           Gc[t] = g;
         } else {
@@ -2170,29 +2332,41 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
       }
     }
     __syncthreads();
-    double F = 0.0;
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) F += cand[t] * cand[t];
-    F = block_sum(F, k.red);
+    Tab Fp = Tab(0);
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) Fp += cand[t] * cand[t];
+    const double F = block_sum((double)Fp, k.red);
     double mn = 1e300;
     for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
-      double acc = 0.0;
+      Tab acc = Tab(0);
       if (t < n) for (int c = 0; c < n; ++c) acc += Gc[t * n + c] * Gc[t * n + c];
       else for (int rr = 0; rr < n; ++rr) acc += Gc[rr * n + (t - n)] * Gc[rr * n + (t - n)];
-      mn = fmin(mn, acc);
+      mn = fmin(mn, (double)acc);
     }
     mn = block_min(mn, k.red);
     const double SF = mn * F;
-    const double R_new = SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
+    double R_new = 0.0;   // only thread 0 decides, so only it evaluates the power
     if (threadIdx.x == 0) {
-      const double Jr = exp(k.sc[5] + dJ);
-      const double Ras = (fmax(R_new, eps_AS) / R_new) / (fmax(R_old, eps_AS) / R_old);
-      const double Rr = pow(Ras * Jr * ratio, 2.0);
-      const double pacc = fmin(1.0, Rr * k.sc[4]);
-      k.sc[6] = (fd[1] < pacc) ? 1.0 : 0.0;
+      if constexpr (sizeof(Tab) == sizeof(float)) {
+        const float Rn = SF > 0.0 ? powf((float)SF, -0.375f) : 0.f;
+        const float Ro = (float)R_old, ea = (float)eps_AS;
+        const float Jr = expf((float)(k.sc[5] + dJ));
+        const float Ras = (fmaxf(Rn, ea) / Rn) / (fmaxf(Ro, ea) / Ro);
+        const float x = Ras * Jr * (float)ratio;
+        const float pacc = fminf(1.0f, x * x * (float)k.sc[4]);
+        k.sc[6] = (fd[1] < (double)pacc) ? 1.0 : 0.0;
+        R_new = (double)Rn;
+      } else {
+        R_new = SF > 0.0 ? pow(SF, -3.0 / 8.0) : 0.0;
+        const double Jr = exp(k.sc[5] + dJ);
+        const double Ras = (fmax(R_new, eps_AS) / R_new) / (fmax(R_old, eps_AS) / R_old);
+        const double Rr = pow(Ras * Jr * (double)ratio, 2.0);
+        const double pacc = fmin(1.0, Rr * k.sc[4]);
+        k.sc[6] = (fd[1] < pacc) ? 1.0 : 0.0;
+      }
     }
     __syncthreads();
     if (k.sc[6] != 0.0) {
-      sm_move<double>(k, e, nx, ny, nz);
+      sm_move<Tab>(k, e, nx, ny, nz, caches);
       R_old = R_new;
       ++nacc;
     }
@@ -2200,6 +2374,59 @@ __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, con
   }
   if (threadIdx.x == 0) accept[w] += nacc;
   store_walker(k, P.ws, w);
+}
+
+__global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt,
+                            double eps_AS, int* accept, int off_cand) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  vmc_sweep_body<double>(P, blockIdx.x, K, idraw, fdraw, Dt, eps_AS, accept, off_cand, true, smem);
+}
+
+// ------------------------------------------------------------------ batches of systems
+// One launch over the walkers of many systems (molecules): item i owns walkers
+// [woff[i], woff[i+1]) of the batch; each CTA finds its item by binary search
+// and runs the single-system body with that item's parameters.
+struct BatchItem {
+  KParams P;
+  int woff;        // first walker of the item in the batch
+  int off_cand;    // VMC sweep: candidate G^-1 / G offset in shared memory
+  int off_init[3]; // rebuild: off_Gd, off_aug, off_vec
+};
+
+__device__ __forceinline__ int batch_item(const int* __restrict__ woff, int nitem, int g) {
+  int lo = 0, hi = nitem - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (woff[mid] <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class Tab>
+__global__ void k_vmc_sweep_batch(const BatchItem* __restrict__ items, const int* __restrict__ woff, int nitem, int K,
+                                  const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt, double eps_AS,
+                                  int* accept, int caches) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const BatchItem& it = items[batch_item(woff, nitem, blockIdx.x)];
+  const size_t g0 = (size_t)it.woff;
+  vmc_sweep_body<Tab>(it.P, blockIdx.x - it.woff, K, idraw + g0 * K * 4, fdraw + g0 * K * 2, Dt, eps_AS, accept + g0,
+                      it.off_cand, caches != 0, smem);
+}
+
+template <int ROWS>
+__global__ void __launch_bounds__(128) k_rebuild_m_batch(const BatchItem* __restrict__ items, const int* __restrict__ woff,
+                                                         int nitem) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const BatchItem& it = items[batch_item(woff, nitem, blockIdx.x)];
+  rebuild_m_body<ROWS>(it.P, blockIdx.x - it.woff, blockIdx.y, smem);
+}
+
+template <class Tab>
+__global__ void k_walker_init_batch(const BatchItem* __restrict__ items, const int* __restrict__ woff, int nitem, int mode) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const BatchItem& it = items[batch_item(woff, nitem, blockIdx.x)];
+  walker_init_body<Tab>(it.P, blockIdx.x - it.woff, it.off_init[0], it.off_init[1], it.off_init[2], mode, smem);
 }
 
 // VMC local energy and weight (hamiltonians.py:225-290, jqmc_mcmc.py:725-747)   (FP64 form)
@@ -2492,9 +2719,25 @@ KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   return P;
 }
 
+// Raise a kernel's dynamic shared-memory limit when a launch needs more than
+// was set before on this device (so launches inside a stream capture make no
+// attribute calls once the kernels have run at their sizes).
 int launch_check(const void* fn, int smem) {
   if (smem > 227 * 1024) return JQMC_E_SMEM;
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<const void*, int>, int>> done;   // ((kernel, device), bytes)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return JQMC_E_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& d : done)
+    if (d.first.first == fn && d.first.second == dev) {
+      if (smem <= d.second) return JQMC_OK;
+      if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return JQMC_E_CUDA;
+      d.second = smem;
+      return JQMC_OK;
+    }
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return JQMC_E_CUDA;
+  done.push_back({{fn, dev}, smem});
   return JQMC_OK;
 }
 
@@ -2719,17 +2962,24 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
+// shared-memory layout of the init / rebuild kernel above the work layout; returns the bytes
+static int init_layout(const Sys& s, const KParams& P, int* off) {
+  const int n = s.n_up, A3 = s.has_j3 ? s.j3.nao : 1;
+  off[0] = P.wl.bytes;                                   // G (double)
+  off[1] = align16(off[0] + n * n * 8);                  // [G | I]
+  off[2] = align16(off[1] + n * 2 * n * 8);              // vectors
+  const int vec_len = (s.det.nao + n > 4 * A3) ? s.det.nao + n : 4 * A3;
+  return align16(off[2] + vec_len * 8);
+}
+
 static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream, int mode) {
   if (!walkers_ok(sys, w)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
   const Sys& s = sys->s;
-  const int n = s.n_up, A3 = s.has_j3 ? s.j3.nao : 1;
-  const int off_Gd = P.wl.bytes;
-  const int off_aug = align16(off_Gd + n * n * 8);
-  const int off_vec = align16(off_aug + n * 2 * n * 8);
-  const int vec_len = (s.det.nao + n > 3 * A3) ? s.det.nao + n : 3 * A3;
-  const int off_phi3 = align16(off_vec + vec_len * 8);
-  const int smem = align16(off_phi3 + (s.has_j3 ? s.N * A3 * 8 : 0));
+  const int n = s.n_up;
+  int off[3];
+  const int smem = init_layout(s, P, off);
+  const int off_Gd = off[0], off_aug = off[1], off_vec = off[2];
   if (is_mixed(w->precision)) {
     // M_up, M_dn by the float-float lam-GEMM into the scratch, then the rest in FP64
     const int rows = s.det.nao <= 2048 ? 8 : 4;
@@ -2742,11 +2992,11 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
     else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
     rc = launch_check((const void*)k_walker_init<float>, smem);
     if (rc) return rc;
-    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3, mode | kInitMReady);
+    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, mode | kInitMReady);
   } else {
     int rc = launch_check((const void*)k_walker_init<double>, smem);
     if (rc) return rc;
-    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, off_phi3, mode);
+    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, mode);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
@@ -2921,6 +3171,110 @@ int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int3
   // nothing needs clearing between calls
   k_branch_comb<<<1, 1, 0, S(stream)>>>(nwalk, d_w, scratch);
   k_branch_search<<<(nwalk + 127) / 128, 128, 0, S(stream)>>>(nwalk, scratch, zeta, d_chosen);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+
+// ------------------------------------------------------------------ batches of systems
+struct jqmc_batch {
+  int nitem = 0, total = 0, precision = 0, nmax_up = 0, rows = 8;
+  int smem_sweep = 0, smem_init = 0, smem_m = 0;
+  BatchItem* d_items = nullptr;
+  int* d_woff = nullptr;
+};
+
+int jqmc_batch_create(int32_t nitem, const jqmc_system* const* systems, const jqmc_walkers* walkers, jqmc_batch** out) {
+  if (!out || nitem <= 0 || !systems || !walkers) return JQMC_E_ARG;
+  *out = nullptr;
+  std::vector<BatchItem> items(nitem);
+  std::vector<int> woff(nitem);
+  jqmc_batch* b = new jqmc_batch();
+  b->precision = walkers[0].precision;
+  int total = 0;
+  bool small_ao = true;
+  for (int i = 0; i < nitem; ++i) {
+    const jqmc_system* sys = systems[i];
+    const jqmc_walkers* w = &walkers[i];
+    if (!walkers_ok(sys, w) || w->precision != b->precision) { delete b; return JQMC_E_ARG; }
+    const Sys& s = sys->s;
+    BatchItem& it = items[i];
+    it.P = make_params(sys, w);
+    it.woff = total;
+    woff[i] = total;
+    it.off_cand = it.P.wl.bytes;
+    const int tb = tab_bytes(w);
+    b->smem_sweep = std::max(b->smem_sweep, align16(it.off_cand + 2 * s.n_up * s.n_up * tb));
+    b->smem_init = std::max(b->smem_init, init_layout(s, it.P, it.off_init));
+    if (s.det.nao > 2048) small_ao = false;
+    b->nmax_up = std::max(b->nmax_up, s.n_up);
+    total += w->nwalk;
+  }
+  b->rows = small_ao ? 8 : 4;
+  for (int i = 0; i < nitem; ++i) b->smem_m = std::max(b->smem_m, b->rows * systems[i]->s.det.nao * 8);
+  b->nitem = nitem;
+  b->total = total;
+  if (cudaMalloc(&b->d_items, sizeof(BatchItem) * nitem) != cudaSuccess ||
+      cudaMalloc(&b->d_woff, sizeof(int) * nitem) != cudaSuccess ||
+      cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem) * nitem, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_woff, woff.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (b->d_items) cudaFree(b->d_items);
+    if (b->d_woff) cudaFree(b->d_woff);
+    delete b;
+    return JQMC_E_CUDA;
+  }
+  *out = b;
+  return JQMC_OK;
+}
+
+int jqmc_batch_destroy(jqmc_batch* b) {
+  if (!b) return JQMC_E_ARG;
+  cudaDeviceSynchronize();
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->d_woff) cudaFree(b->d_woff);
+  delete b;
+  return JQMC_OK;
+}
+
+int jqmc_batch_walkers(const jqmc_batch* b) { return b ? b->total : JQMC_E_ARG; }
+
+int jqmc_vmc_sweep_batch(const jqmc_batch* b, int32_t K, const int32_t* d_idraw, const double* d_fdraw, double Dt,
+                         double eps_AS, int32_t* d_accept, int32_t threads, int32_t caches, void* stream) {
+  if (!b || K < 0 || !d_idraw || !d_fdraw || !d_accept) return JQMC_E_ARG;
+  if (threads < 32 || threads > 256 || threads % 32) return JQMC_E_ARG;
+  if (K == 0) return JQMC_OK;
+  if (is_mixed(b->precision)) {
+    int rc = launch_check((const void*)k_vmc_sweep_batch<float>, b->smem_sweep);
+    if (rc) return rc;
+    k_vmc_sweep_batch<float><<<b->total, threads, b->smem_sweep, S(stream)>>>(b->d_items, b->d_woff, b->nitem, K, d_idraw,
+                                                                              d_fdraw, Dt, eps_AS, d_accept, caches);
+  } else {
+    int rc = launch_check((const void*)k_vmc_sweep_batch<double>, b->smem_sweep);
+    if (rc) return rc;
+    k_vmc_sweep_batch<double><<<b->total, threads, b->smem_sweep, S(stream)>>>(b->d_items, b->d_woff, b->nitem, K, d_idraw,
+                                                                               d_fdraw, Dt, eps_AS, d_accept, caches);
+  }
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_batch_rebuild(const jqmc_batch* b, int32_t full, void* stream) {
+  if (!b) return JQMC_E_ARG;
+  const int mode = full ? 0 : (kInitTablesOnly | kInitRefine);
+  if (is_mixed(b->precision)) {
+    const void* fm = b->rows == 8 ? (const void*)k_rebuild_m_batch<8> : (const void*)k_rebuild_m_batch<4>;
+    int rc = launch_check(fm, b->smem_m);
+    if (rc) return rc;
+    const dim3 grid_m(b->total, 2 * ((b->nmax_up + b->rows - 1) / b->rows));
+    if (b->rows == 8) k_rebuild_m_batch<8><<<grid_m, 128, b->smem_m, S(stream)>>>(b->d_items, b->d_woff, b->nitem);
+    else k_rebuild_m_batch<4><<<grid_m, 128, b->smem_m, S(stream)>>>(b->d_items, b->d_woff, b->nitem);
+    rc = launch_check((const void*)k_walker_init_batch<float>, b->smem_init);
+    if (rc) return rc;
+    k_walker_init_batch<float><<<b->total, 128, b->smem_init, S(stream)>>>(b->d_items, b->d_woff, b->nitem,
+                                                                           mode | kInitMReady);
+  } else {
+    int rc = launch_check((const void*)k_walker_init_batch<double>, b->smem_init);
+    if (rc) return rc;
+    k_walker_init_batch<double><<<b->total, 128, b->smem_init, S(stream)>>>(b->d_items, b->d_woff, b->nitem, mode);
+  }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
