@@ -262,8 +262,10 @@ int jqmc_batch_walkers(const jqmc_batch* b);   /* total walkers of the batch */
 int jqmc_vmc_sweep_batch(const jqmc_batch* b, int32_t K, const int32_t* d_idraw, const double* d_fdraw, double Dt,
                          double eps_AS, int32_t* d_accept, int32_t threads, int32_t caches, void* stream);
 
-/* full == 0: jqmc_lu_rebuild_refine for every walker of the batch; full != 0:
- * jqmc_walker_init (all state, including the energy cache and derivative tables). */
+/* full == 0: the drift-control rebuild of jqmc_lu_rebuild_refine for every
+ * walker of the batch (JQMC_PREC_MIXED: the J3 field computed in float, as it
+ * is stored); full != 0: jqmc_walker_init (all state in FP64, including the
+ * energy cache and derivative tables; call it before an energy is measured). */
 int jqmc_batch_rebuild(const jqmc_batch* b, int32_t full, void* stream);
 
 #ifdef __cplusplus

@@ -983,8 +983,8 @@ __device__ void store_walker(const Work<Tab>& k, const WS& ws, int w) {
 //          G^-1 -= q G^-1[j,:] / ratio, T_dn -= q (x) T_dn[j] / ratio,
 //          T_up += G^-1[j,:] (x) (lambda dphi - T_up^T G q) / ratio
 // (every right-hand side uses the tables before the move).  Arithmetic in Tab.
-template <class Tab>
-__device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz, bool caches = true) {
+template <class Tab, bool CACHES = true>
+__device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) {
   const Sys& s = k.s;
   const int n = k.n, A = k.A, A3 = k.A3;
   const bool up = e < s.n_up;
@@ -1107,7 +1107,7 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz, 
       k.h3[(size_t)m * A3 + c] += useJ ? k.v32[c] : k.v30[c];
     }
   }
-  if (caches) {
+  if constexpr (CACHES) {
     fill_dtables<Tab>(s, px, py, pz, k.dphi + (size_t)e * 4 * A, s.has_j3 ? k.dphi3 + (size_t)e * 5 * A3 : nullptr);
     // energy cache: every pair with the moved electron (J2 terms of the partner,
     // e-e Coulomb), then the moved electron's own row
@@ -1653,8 +1653,8 @@ __device__ __forceinline__ void dot2_step(float& s, float& c, float xh, float xl
 }
 
 // Rows of M_up = Phi_up lam (up spin) or M_dn = Phi_dn lam^T (down spin) for
-// ROWS electrons per CTA, accumulated in float-float (Dot2) and stored as double
-// in the walkers' rebuild scratch: (nwalk, 2, n, A) with the M_dn block first,
+// ROWS electrons per CTA, accumulated in float-float (Dot2) and stored as
+// float-float pairs in the walkers' rebuild scratch: (nwalk, 2, n, A) with the M_dn block first,
 // as k_walker_init reads it.  Grid (nwalk, 2 * ceil(n / ROWS)).  The AO values
 // are evaluated in FP64 from the global basis tables and split into float pairs
 // in shared memory (ROWS x A float2); each thread owns columns b of the output
@@ -1691,7 +1691,9 @@ __device__ void rebuild_m_body(const KParams& P, int w, int by, unsigned char* s
   __syncthreads();
   const float* __restrict__ Lh = spin == 0 ? s.lamf : s.lamTf;
   const float* __restrict__ Ll = spin == 0 ? s.laml : s.lamTl;
-  double* M = P.ws.scratch + ((size_t)w * 2 + (spin == 0 ? 1 : 0)) * n * A + (size_t)i0 * A;
+  // the (s, c) float-float pair is kept as it is (the value is s + c): the rest
+  // of the rebuild continues in float-float
+  float2* M = reinterpret_cast<float2*>(P.ws.scratch) + ((size_t)w * 2 + (spin == 0 ? 1 : 0)) * n * A + (size_t)i0 * A;
   for (int b = threadIdx.x; b < A; b += blockDim.x) {
     float sacc[kRebuildRows], cacc[kRebuildRows];
 #pragma unroll
@@ -1707,7 +1709,7 @@ __device__ void rebuild_m_body(const KParams& P, int w, int by, unsigned char* s
     }
 #pragma unroll
     for (int ii = 0; ii < kRebuildRows; ++ii)
-      if (ii < rows) M[(size_t)ii * A + b] = (double)sacc[ii] + (double)cacc[ii];
+      if (ii < rows) M[(size_t)ii * A + b] = make_float2(sacc[ii], cacc[ii]);
   }
 }
 
@@ -1715,6 +1717,65 @@ template <int ROWS>
 __global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   rebuild_m_body<ROWS>(P, blockIdx.x, blockIdx.y, smem);
+}
+
+// J3 field h_e = dJ3/dphi3(r_e) of every electron (the gradient of J3 with
+// respect to one electron's J3 AO vector, jastrow_factor.py:4077-4156), with
+// arithmetic type J and stored as Tab, in two passes over the electrons so that
+// only four A3-vectors are held: the spin totals of phi3, then each field with
+// the running prefix (the electron's J3 AO values are evaluated again).
+// buf: 4 A3 values of type J.  Block-cooperative.
+template <class J, class Tab>
+__device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J* jm, const J* jmT) {
+  const int N = s.N, A3 = s.j3.nao;
+  J* tot_up = buf;
+  J* tot_dn = buf + A3;
+  J* pfx = buf + 2 * A3;
+  J* pe = buf + 3 * A3;
+  auto fill_phi3 = [&](int e) {
+    auto f = [&](int a, J v) { pe[a] = v; };
+    for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
+      J dx, dy, dz;
+      disp<J>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      shell_val_d<J>(s.j3, sh, dx, dy, dz, f);
+    }
+  };
+  __syncthreads();
+  for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+    tot_up[c] = J(0);
+    tot_dn[c] = J(0);
+    pfx[c] = J(0);
+  }
+  for (int e = 0; e < N; ++e) {
+    __syncthreads();
+    fill_phi3(e);
+    __syncthreads();
+    J* tot = e < s.n_up ? tot_up : tot_dn;
+    for (int c = threadIdx.x; c < A3; c += blockDim.x) tot[c] += pe[c];
+  }
+  for (int e = 0; e < N; ++e) {
+    const bool up = e < s.n_up;
+    __syncthreads();
+    if (e == s.n_up)
+      for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] = J(0);
+    fill_phi3(e);
+    __syncthreads();
+    const J* tot_same = up ? tot_up : tot_dn;
+    for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+      // h = j1 + J^T pfx + J (tot_same - pfx - phi_e) + (up ? J tot_dn : J^T tot_up)
+      J acc = (J)s.j3vec[c];
+      for (int cp = 0; cp < A3; ++cp) {
+        const J Jcpc = jm[(size_t)cp * A3 + c];    // J[cp][c]
+        const J Jccp = jmT[(size_t)cp * A3 + c];   // J[c][cp]
+        const J pf = pfx[cp];
+        acc += Jcpc * pf + Jccp * (tot_same[cp] - pf - pe[cp]);
+        acc += up ? Jccp * tot_dn[cp] : Jcpc * tot_up[cp];
+      }
+      h[(size_t)e * A3 + c] = (Tab)acc;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] += pe[c];
+  }
 }
 
 // Walker initialisation in FP64: G, G^-1 (Gauss-Jordan, partial pivoting), T
@@ -1726,9 +1787,13 @@ __global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
 // mode bit 1 (kInitRefine): one step of iterative refinement of the inverse,
 // X <- X + X (I - G X), in FP64.
 // mode bit 2 (kInitMReady): M_up / M_dn are already in the scratch (k_rebuild_m).
+// mode bit 3 (kInitJ3Table): compute the J3 field in the table type (the float
+// form's drift-control rebuild between VMC measurements; an energy is measured
+// only after a full build, whose field is FP64).
 constexpr int kInitTablesOnly = 1;
 constexpr int kInitRefine = 2;
 constexpr int kInitMReady = 4;
+constexpr int kInitJ3Table = 8;
 template <class Tab>
 __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_aug, int off_vec, int mode,
                                  unsigned char* smem) {
@@ -1764,19 +1829,50 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
     }
     __syncthreads();
   }
-  for (int j = 0; j < s.n_dn; ++j) {
-    const int e = s.n_up + j;
-    ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
-    __syncthreads();
-    rows_dot<double>(Mup, n, A, vec, vn);
-    for (int a = threadIdx.x; a < A && !m_ready; a += blockDim.x) {
-      double acc = 0.0;
-      for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * vec[b];
-      Mdn[(size_t)j * A + a] = acc;
+  if constexpr (sizeof(Tab) == sizeof(float)) {
+    // mixed form: M_up / M_dn are float-float pairs from k_rebuild_m; G column j
+    // = M_up phi_dn(r_j) by compensated float-float dot products (one warp per row)
+    const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
+    float2* vec2 = reinterpret_cast<float2*>(vec);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = 0; j < s.n_dn; ++j) {
+      const int e = s.n_up + j;
+      ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
+      __syncthreads();
+      for (int a = threadIdx.x; a < A; a += blockDim.x) {   // split in place (same slot)
+        const double v = vec[a];
+        const float hi = (float)v;
+        vec2[a] = make_float2(hi, (float)(v - (double)hi));
+      }
+      __syncthreads();
+      for (int i = wid; i < n; i += nw) {
+        F2 acc;
+        acc_zero(acc);
+        const float2* row = Mup2 + (size_t)i * A;
+        for (int a = lane; a < A; a += 32) {
+          const float2 m = row[a], p = vec2[a];
+          dot2_step(acc.s, acc.c, m.x, m.y, p.x, p.y);
+        }
+        const double g = acc_out(acc);
+        if (lane == 0) Gd[i * n + j] = g;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) Gd[i * n + j] = vn[i];
-    __syncthreads();
+  } else {
+    for (int j = 0; j < s.n_dn; ++j) {
+      const int e = s.n_up + j;
+      ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
+      __syncthreads();
+      rows_dot<double>(Mup, n, A, vec, vn);
+      for (int a = threadIdx.x; a < A && !m_ready; a += blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < A; ++b) acc += s.lamT[(size_t)b * A + a] * vec[b];
+        Mdn[(size_t)j * A + a] = acc;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) Gd[i * n + j] = vn[i];
+      __syncthreads();
+    }
   }
   // Gauss-Jordan on [G | I]
   const int n2 = 2 * n;
@@ -1852,19 +1948,57 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
   }
   __syncthreads();
   // T_up[k][a] = sum_j M_dn[j][a] G^-1[j][k] ; T_dn[k][b] = sum_i G^-1[k][i] M_up[i][b]  (per column)
-  for (int a = threadIdx.x; a < A; a += blockDim.x) {
-    double m[JQMC_MAX_NUP];
-    for (int j = 0; j < n; ++j) m[j] = Mdn[(size_t)j * A + a];
-    for (int kk = 0; kk < n; ++kk) {
-      double acc = 0.0;
-      for (int j = 0; j < n; ++j) acc += m[j] * aug[j * n2 + n + kk];
-      Tup[(size_t)kk * A + a] = (Tab)acc;
+  if constexpr (sizeof(Tab) == sizeof(float)) {
+    // mixed form: G^-1 split into float pairs (over the G buffer, free now) and
+    // compensated float-float sums, eight rows of T per pass over a column of M
+    float2* Gi2 = reinterpret_cast<float2*>(Gd);
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const double v = aug[(t / n) * n2 + n + (t % n)];
+      const float hi = (float)v;
+      Gi2[t] = make_float2(hi, (float)(v - (double)hi));
     }
-    for (int j = 0; j < n; ++j) m[j] = Mup[(size_t)j * A + a];
-    for (int kk = 0; kk < n; ++kk) {
-      double acc = 0.0;
-      for (int j = 0; j < n; ++j) acc += aug[kk * n2 + n + j] * m[j];
-      Tdn[(size_t)kk * A + a] = (Tab)acc;
+    __syncthreads();
+    const float2* Mdn2 = reinterpret_cast<const float2*>(Mdn);
+    const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
+    constexpr int KB = 8;
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+      for (int k0 = 0; k0 < n; k0 += KB) {
+        float us[KB], uc[KB], ds[KB], dc[KB];
+#pragma unroll
+        for (int u = 0; u < KB; ++u) { us[u] = 0.f; uc[u] = 0.f; ds[u] = 0.f; dc[u] = 0.f; }
+        for (int j = 0; j < n; ++j) {
+          const float2 md = Mdn2[(size_t)j * A + a], mu = Mup2[(size_t)j * A + a];
+#pragma unroll
+          for (int u = 0; u < KB; ++u) {
+            const int kk = k0 + u < n ? k0 + u : n - 1;
+            const float2 gjk = Gi2[j * n + kk], gkj = Gi2[kk * n + j];
+            dot2_step(us[u], uc[u], md.x, md.y, gjk.x, gjk.y);
+            dot2_step(ds[u], dc[u], gkj.x, gkj.y, mu.x, mu.y);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < KB; ++u)
+          if (k0 + u < n) {
+            Tup[(size_t)(k0 + u) * A + a] = (Tab)(us[u] + uc[u]);
+            Tdn[(size_t)(k0 + u) * A + a] = (Tab)(ds[u] + dc[u]);
+          }
+      }
+    }
+  } else {
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+      double m[JQMC_MAX_NUP];
+      for (int j = 0; j < n; ++j) m[j] = Mdn[(size_t)j * A + a];
+      for (int kk = 0; kk < n; ++kk) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc += m[j] * aug[j * n2 + n + kk];
+        Tup[(size_t)kk * A + a] = (Tab)acc;
+      }
+      for (int j = 0; j < n; ++j) m[j] = Mup[(size_t)j * A + a];
+      for (int kk = 0; kk < n; ++kk) {
+        double acc = 0.0;
+        for (int j = 0; j < n; ++j) acc += aug[kk * n2 + n + j] * m[j];
+        Tdn[(size_t)kk * A + a] = (Tab)acc;
+      }
     }
   }
   if (!(mode & kInitTablesOnly)) {
@@ -1878,57 +2012,15 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
   }
   // J3 field, in two passes over the electrons so that only four A3-vectors are
   // held: the spin totals of phi3, then each field with the running prefix (the
-  // electron's J3 AO values are evaluated again in the second pass)
+  // electron's J3 AO values are evaluated again in the second pass).  In FP64
+  // (the field enters every J3 ratio and the J3 gradients of the kinetic
+  // energy), or in the table type with kInitJ3Table.
   if (s.has_j3) {
-    double* tot_up = vec;
-    double* tot_dn = vec + A3;
-    double* pfx = vec + 2 * A3;
-    double* pe = vec + 3 * A3;
-    auto fill_phi3 = [&](int e) {
-      auto f = [&](int a, double v) { pe[a] = v; };
-      for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
-        double dx, dy, dz;
-        disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
-        shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
-      }
-    };
-    __syncthreads();
-    for (int c = threadIdx.x; c < A3; c += blockDim.x) {
-      tot_up[c] = 0.0;
-      tot_dn[c] = 0.0;
-      pfx[c] = 0.0;
-    }
-    for (int e = 0; e < N; ++e) {
-      __syncthreads();
-      fill_phi3(e);
-      __syncthreads();
-      double* tot = e < s.n_up ? tot_up : tot_dn;
-      for (int c = threadIdx.x; c < A3; c += blockDim.x) tot[c] += pe[c];
-    }
     Tab* h = static_cast<Tab*>(P.ws.h3) + (size_t)w * N * A3;
-    for (int e = 0; e < N; ++e) {
-      const bool up = e < s.n_up;
-      __syncthreads();
-      if (e == s.n_up)
-        for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] = 0.0;
-      fill_phi3(e);
-      __syncthreads();
-      const double* tot_same = up ? tot_up : tot_dn;
-      for (int c = threadIdx.x; c < A3; c += blockDim.x) {
-        // h = j1 + J^T pfx + J (tot_same - pfx - phi_e) + (up ? J tot_dn : J^T tot_up)
-        double acc = s.j3vec[c];
-        for (int cp = 0; cp < A3; ++cp) {
-          const double Jcpc = s.j3mat[(size_t)cp * A3 + c];    // J[cp][c]
-          const double Jccp = s.j3matT[(size_t)cp * A3 + c];   // J[c][cp]
-          const double pf = pfx[cp];
-          acc += Jcpc * pf + Jccp * (tot_same[cp] - pf - pe[cp]);
-          acc += up ? Jccp * tot_dn[cp] : Jcpc * tot_up[cp];
-        }
-        h[(size_t)e * A3 + c] = (Tab)acc;
-      }
-      __syncthreads();
-      for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] += pe[c];
-    }
+    if (sizeof(Tab) == sizeof(float) && (mode & kInitJ3Table))
+      j3_field<Tab, Tab>(s, h, r, reinterpret_cast<Tab*>(vec), j3m_of<Tab>(s), j3mT_of<Tab>(s));
+    else
+      j3_field<double, Tab>(s, h, r, vec, s.j3mat, s.j3matT);
   }
 }
 
@@ -2218,9 +2310,9 @@ __device__ void vmc_propose_warp(Work<Tab>& k, const Sys& s, const int* id, cons
 // differences and the acceptance in double.  caches == 0: the AO derivative
 // tables and the energy cache are not kept current (they are rebuilt by
 // jqmc_walker_init before an energy is measured).
-template <class Tab>
+template <class Tab, bool CACHES>
 __device__ void vmc_sweep_body(const KParams& P, int w, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw,
-                               double Dt, double eps_AS, int* accept, int off_cand, bool caches, unsigned char* smem) {
+                               double Dt, double eps_AS, int* accept, int off_cand, unsigned char* smem) {
   const Sys s = stage_tables(P.s, P.tl, smem);
   Work<Tab> k = make_work<Tab>(s, P.wl, smem, P.ws, w);
   load_walker(k, P.ws, w);
@@ -2366,7 +2458,7 @@ __device__ void vmc_sweep_body(const KParams& P, int w, int K, const int* __rest
     }
     __syncthreads();
     if (k.sc[6] != 0.0) {
-      sm_move<Tab>(k, e, nx, ny, nz, caches);
+      sm_move<Tab, CACHES>(k, e, nx, ny, nz);
       R_old = R_new;
       ++nacc;
     }
@@ -2379,7 +2471,7 @@ __device__ void vmc_sweep_body(const KParams& P, int w, int K, const int* __rest
 __global__ void k_vmc_sweep(KParams P, int K, const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt,
                             double eps_AS, int* accept, int off_cand) {
   extern __shared__ __align__(16) unsigned char smem[];
-  vmc_sweep_body<double>(P, blockIdx.x, K, idraw, fdraw, Dt, eps_AS, accept, off_cand, true, smem);
+  vmc_sweep_body<double, true>(P, blockIdx.x, K, idraw, fdraw, Dt, eps_AS, accept, off_cand, smem);
 }
 
 // ------------------------------------------------------------------ batches of systems
@@ -2403,15 +2495,15 @@ __device__ __forceinline__ int batch_item(const int* __restrict__ woff, int nite
   return lo;
 }
 
-template <class Tab>
+template <class Tab, bool CACHES>
 __global__ void k_vmc_sweep_batch(const BatchItem* __restrict__ items, const int* __restrict__ woff, int nitem, int K,
                                   const int* __restrict__ idraw, const double* __restrict__ fdraw, double Dt, double eps_AS,
-                                  int* accept, int caches) {
+                                  int* accept) {
   extern __shared__ __align__(16) unsigned char smem[];
   const BatchItem& it = items[batch_item(woff, nitem, blockIdx.x)];
   const size_t g0 = (size_t)it.woff;
-  vmc_sweep_body<Tab>(it.P, blockIdx.x - it.woff, K, idraw + g0 * K * 4, fdraw + g0 * K * 2, Dt, eps_AS, accept + g0,
-                      it.off_cand, caches != 0, smem);
+  vmc_sweep_body<Tab, CACHES>(it.P, blockIdx.x - it.woff, K, idraw + g0 * K * 4, fdraw + g0 * K * 2, Dt, eps_AS, accept + g0,
+                              it.off_cand, smem);
 }
 
 template <int ROWS>
@@ -3242,23 +3334,20 @@ int jqmc_vmc_sweep_batch(const jqmc_batch* b, int32_t K, const int32_t* d_idraw,
   if (!b || K < 0 || !d_idraw || !d_fdraw || !d_accept) return JQMC_E_ARG;
   if (threads < 32 || threads > 256 || threads % 32) return JQMC_E_ARG;
   if (K == 0) return JQMC_OK;
-  if (is_mixed(b->precision)) {
-    int rc = launch_check((const void*)k_vmc_sweep_batch<float>, b->smem_sweep);
-    if (rc) return rc;
-    k_vmc_sweep_batch<float><<<b->total, threads, b->smem_sweep, S(stream)>>>(b->d_items, b->d_woff, b->nitem, K, d_idraw,
-                                                                              d_fdraw, Dt, eps_AS, d_accept, caches);
-  } else {
-    int rc = launch_check((const void*)k_vmc_sweep_batch<double>, b->smem_sweep);
-    if (rc) return rc;
-    k_vmc_sweep_batch<double><<<b->total, threads, b->smem_sweep, S(stream)>>>(b->d_items, b->d_woff, b->nitem, K, d_idraw,
-                                                                               d_fdraw, Dt, eps_AS, d_accept, caches);
-  }
+  const bool mixed = is_mixed(b->precision);
+  using KFn = void (*)(const BatchItem*, const int*, int, int, const int*, const double*, double, double, int*);
+  const KFn fn = mixed ? (caches ? (KFn)k_vmc_sweep_batch<float, true> : (KFn)k_vmc_sweep_batch<float, false>)
+                       : (caches ? (KFn)k_vmc_sweep_batch<double, true> : (KFn)k_vmc_sweep_batch<double, false>);
+  int rc = launch_check((const void*)fn, b->smem_sweep);
+  if (rc) return rc;
+  fn<<<b->total, threads, b->smem_sweep, S(stream)>>>(b->d_items, b->d_woff, b->nitem, K, d_idraw, d_fdraw, Dt, eps_AS,
+                                                      d_accept);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 
 int jqmc_batch_rebuild(const jqmc_batch* b, int32_t full, void* stream) {
   if (!b) return JQMC_E_ARG;
-  const int mode = full ? 0 : (kInitTablesOnly | kInitRefine);
+  const int mode = full ? 0 : (kInitTablesOnly | kInitRefine | kInitJ3Table);
   if (is_mixed(b->precision)) {
     const void* fm = b->rows == 8 ? (const void*)k_rebuild_m_batch<8> : (const void*)k_rebuild_m_batch<4>;
     int rc = launch_check(fm, b->smem_m);
