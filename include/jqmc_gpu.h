@@ -165,6 +165,13 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
 int jqmc_dlnpsi_dparam(const jqmc_system* sys, const jqmc_walkers* w, double* d_j1, double* d_j2, double* d_j3,
                        double* d_lambda, double* d_work, void* stream);
 
+/* d ln|psi| / dR for every nucleus (FP64 walkers, current positions and cached
+ * tables): the Pulay term force_PP of jqmc_mcmc.py:780-845 (dln_Psi/dR without
+ * space warp), which the reference obtains as grad(evaluate_ln_wavefunction)
+ * with respect to the nuclear positions (jqmc_mcmc.py:782-793).
+ * d_out: nwalk*natom*3. */
+int jqmc_dlnpsi_dR(const jqmc_system* sys, const jqmc_walkers* w, double* d_out, void* stream);
+
 /* K Metropolis proposals per walker (jqmc_mcmc.py:4316-4523, fori_loop body),
  * explicit draws: d_idraw nwalk*K*4 int32 (sel in [0,N), up index, dn index,
  * axis), d_fdraw nwalk*K*2 double (standard normal, uniform).  Adds the number

@@ -2169,6 +2169,83 @@ __global__ void k_dlnpsi_dparam(KParams P, int off_red, int off_su, int off_sd, 
   }
 }
 
+// d ln|psi| / dR_I for every nucleus I (FP64 walkers), the Pulay part of the
+// force (force_PP of jqmc_mcmc.py:780-845 without space warp).  Every AO sits
+// on a nucleus, d phi_a(r - R_I)/dR_I = -grad phi_a, so the derivative is minus
+// each electron's grad ln psi restricted to the AOs on I: geminal AOs through
+// the T rows (grad ln det_e = sum_a grad phi_a(r_e) T_e[a]), J3 AOs through the
+// J3 field, and the J1 pair terms.  Reads the walker's cached derivative tables;
+// out: nwalk x natom x 3.
+__global__ void k_dlnpsi_dR(KParams P, int off_acc, double* out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
+  load_walker(k, P.ws, w);
+  const int N = k.N, n = k.n, A = k.A, M = s.natom;
+  double* acc = reinterpret_cast<double*>(smem + off_acc);   // M x 3
+  for (int t = threadIdx.x; t < 3 * M; t += blockDim.x) acc[t] = 0.0;
+  __syncthreads();
+  const int nsh = s.det.nshell;
+  for (int p = threadIdx.x; p < N * nsh; p += blockDim.x) {
+    const int e = p / nsh, sh = p % nsh;
+    const int* row = s.det.shells + 8 * sh;
+    const int atom = row[0], ao0 = row[4], nm = row[5];
+    const double* T = (e < n ? k.Tup + (size_t)e * A : k.Tdn + (size_t)(e - n) * A);
+    const double* dp = k.dphi + (size_t)e * 4 * A;
+    double gx = 0.0, gy = 0.0, gz = 0.0;
+    for (int a = ao0; a < ao0 + nm; ++a) {
+      gx += dp[a] * T[a];
+      gy += dp[A + a] * T[a];
+      gz += dp[2 * A + a] * T[a];
+    }
+    atomicAdd(acc + 3 * atom, -gx);
+    atomicAdd(acc + 3 * atom + 1, -gy);
+    atomicAdd(acc + 3 * atom + 2, -gz);
+  }
+  if (s.has_j3) {
+    const int A3 = k.A3, nsh3 = s.j3.nshell;
+    for (int p = threadIdx.x; p < N * nsh3; p += blockDim.x) {
+      const int e = p / nsh3, sh = p % nsh3;
+      const int* row = s.j3.shells + 8 * sh;
+      const int atom = row[0], ao0 = row[4], nm = row[5];
+      const double* h = k.h3 + (size_t)e * A3;
+      const double* q = k.dphi3 + (size_t)e * 5 * A3;
+      double gx = 0.0, gy = 0.0, gz = 0.0;
+      for (int c = ao0; c < ao0 + nm; ++c) {
+        gx += q[A3 + c] * h[c];
+        gy += q[2 * A3 + c] * h[c];
+        gz += q[3 * A3 + c] * h[c];
+      }
+      atomicAdd(acc + 3 * atom, -gx);
+      atomicAdd(acc + 3 * atom + 1, -gy);
+      atomicAdd(acc + 3 * atom + 2, -gz);
+    }
+  }
+  if (s.has_j1) {
+    const double aa = s.j1_param;
+    for (int p = threadIdx.x; p < N * M; p += blockDim.x) {
+      const int e = p / M, at = p % M;
+      const double dx = k.r[3 * e] - s.atom_pos[3 * at], dy = k.r[3 * e + 1] - s.atom_pos[3 * at + 1];
+      const double dz = k.r[3 * e + 2] - s.atom_pos[3 * at + 2];
+      const double d = sqrt(dx * dx + dy * dy + dz * dz);
+      const double c = s.j1_cA[2 * at], AA = s.j1_cA[2 * at + 1];
+      double f1;   // d f1 / d |r - R|
+      if (s.j1_type == 0) {
+        f1 = -AA * c * exp(-aa * c * d) / 2.0;
+      } else {
+        const double q = 1.0 + aa * c * d;
+        f1 = -AA / (2.0 * q * q);
+      }
+      atomicAdd(acc + 3 * at, -f1 * dx / d);
+      atomicAdd(acc + 3 * at + 1, -f1 * dy / d);
+      atomicAdd(acc + 3 * at + 2, -f1 * dz / d);
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 3 * M; t += blockDim.x) out[(size_t)w * 3 * M + t] = acc[t];
+}
+
 // ln|det G|, sign (LU with partial pivoting on a copy of G) and J   (FP64 form)
 __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -3130,6 +3207,17 @@ int jqmc_dlnpsi_dparam(const jqmc_system* sys, const jqmc_walkers* w, double* d_
   if (rc) return rc;
   k_dlnpsi_dparam<<<w->nwalk, 128, smem, S(stream)>>>(P, off_red, off_su, off_sd, off_phi3, d_j1, d_j2,
                                                       s.has_j3 ? d_j3 : nullptr, d_lambda, d_work);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_dlnpsi_dR(const jqmc_system* sys, const jqmc_walkers* w, double* d_out, void* stream) {
+  if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_out) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int off_acc = P.wl.bytes;
+  const int smem = align16(off_acc + sys->s.natom * 3 * 8);
+  int rc = launch_check((const void*)k_dlnpsi_dR, smem);
+  if (rc) return rc;
+  k_dlnpsi_dR<<<w->nwalk, 128, smem, S(stream)>>>(P, off_acc, d_out);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 

@@ -21,16 +21,21 @@ import math
 import numpy as np
 import torch
 
+from .adjoint import dlnpsi_dparams
 from .engine import GpuSystem, WalkerSet
+from .forces import ELGradientFD, dlnpsi_dR
 from .hamiltonians import Hamiltonian_data
-from .statistics import jackknife_energy
+from .statistics import jackknife_energy, jackknife_force
 from ._init_config import initial_electrons
 
 
 class MCMC:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, mcmc_seed: int = 34467, num_walkers: int = 40,
                  num_mcmc_per_measurement: int = 16, Dt: float = 2.0, epsilon_AS: float = 1e-1, Nv: int = 6,
-                 init_r_up=None, init_r_dn=None):
+                 init_r_up=None, init_r_dn=None, comput_log_WF_param_deriv: bool = False,
+                 comput_position_deriv: bool = False, use_swct: bool = False, force_fd_step: float = 5e-4):
+        if comput_position_deriv and use_swct:
+            raise NotImplementedError("the space-warp coordinate transformation of the forces is not on the GPU path")
         hamiltonian_data.sanity_check()
         self.hamiltonian_data = hamiltonian_data
         self.num_walkers = num_walkers
@@ -51,6 +56,12 @@ class MCMC:
         self._e_L, self._w_L = [], []
         self.mcmc_counter = 0
         self._proposals = 0
+        # per-measurement derivative observables (jqmc_mcmc.py:756-876)
+        self.comput_log_WF_param_deriv = comput_log_WF_param_deriv
+        self.comput_position_deriv = comput_position_deriv
+        self._param_grads = {}
+        self._force_HF, self._force_PP, self._E_L_force_PP = [], [], []
+        self._el_grad = ELGradientFD(hamiltonian_data, h=force_fd_step, Nv=Nv) if comput_position_deriv else None
 
     def draws(self, K: int | None = None):
         K = self.num_mcmc_per_measurement if K is None else K
@@ -74,10 +85,35 @@ class MCMC:
 
     def run(self, num_mcmc_steps: int = 0, max_time: int = 86400) -> None:
         for _ in range(num_mcmc_steps):
-            eL, wL = self.run_block(*self.draws())
+            idraw, fdraw, angles = self.draws()
+            eL, wL = self.run_block(idraw, fdraw, angles)
             self._e_L.append(eL.cpu().numpy())
             self._w_L.append(wL.cpu().numpy())
+            if self.comput_log_WF_param_deriv:
+                for name, g in dlnpsi_dparams(self.walkers).items():
+                    self._param_grads.setdefault(name, []).append(g.cpu().numpy())
+            if self.comput_position_deriv:
+                fpp = dlnpsi_dR(self.walkers)
+                r = self.walkers.r.cpu().numpy()
+                n = self.sys.n_up
+                fhf = self._el_grad(r[:, :n], r[:, n:], angles, self.epsilon_AS)
+                self._force_HF.append(fhf.cpu().numpy())
+                self._force_PP.append(fpp.cpu().numpy())
+                self._E_L_force_PP.append((eL[:, None, None] * fpp).cpu().numpy())
             self.mcmc_counter += 1
+
+    @property
+    def dln_Psi_dc(self) -> dict:
+        """Per-measurement, per-walker d ln psi / d theta blocks (collect_param_grads names)."""
+        return {k: np.asarray(v) for k, v in self._param_grads.items()}
+
+    def get_aF(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
+        """(force_mean, force_std), (natom, 3) in Hartree/bohr (jqmc_mcmc.py:1191-1380)."""
+        if not self.comput_position_deriv:
+            raise ValueError("construct MCMC with comput_position_deriv=True to measure forces")
+        k = num_mcmc_warmup_steps
+        return jackknife_force(self.w_L[k:], self.e_L[k:], np.asarray(self._force_HF)[k:], np.asarray(self._force_PP)[k:],
+                               np.asarray(self._E_L_force_PP)[k:], num_mcmc_bin_blocks)
 
     @property
     def e_L(self) -> np.ndarray:

@@ -36,3 +36,32 @@ def gfmc_G_L(w_L: np.ndarray, num_gfmc_collect_steps: int) -> np.ndarray:
     A = w_L.shape[0]
     n = num_gfmc_collect_steps
     return np.stack([np.prod(w_L[k - n:k], axis=0) for k in range(n, A)]) if A > n else np.zeros((0,) + w_L.shape[1:])
+
+
+def jackknife_force(w_L: np.ndarray, e_L: np.ndarray, force_HF: np.ndarray, force_PP: np.ndarray,
+                    E_L_force_PP: np.ndarray, num_bin_blocks: int):
+    """(force_mean, force_std), each (natom, 3), from (M, nw) weights and energies
+    and (M, nw, natom, 3) per-walker force terms: F = -<force_HF> - 2 (<E_L force_PP>
+    - <E_L> <force_PP>), jackknife over (bin, walker) samples (jqmc_mcmc.py:1191-1380)."""
+    M = e_L.shape[0]
+    if M < num_bin_blocks:
+        raise ValueError(f"{M} samples cannot form {num_bin_blocks} bins")
+
+    def binned(x):
+        return np.concatenate([np.sum(a, axis=0) for a in np.array_split(x, num_bin_blocks, axis=0)], axis=0)
+
+    wb = binned(w_L)                                          # (bins * nw,)
+    web = binned(w_L * e_L)
+    fhb = binned(np.einsum("iw,iwjk->iwjk", w_L, force_HF))   # (bins * nw, natom, 3)
+    fpb = binned(np.einsum("iw,iwjk->iwjk", w_L, force_PP))
+    efb = binned(np.einsum("iw,iwjk->iwjk", w_L, E_L_force_PP))
+    ws, wes = wb.sum(), web.sum()
+    fhs, fps, efs = fhb.sum(axis=0), fpb.sum(axis=0), efb.sum(axis=0)
+    den = (ws - wb)[:, None, None]
+    f_hf = -(fhs[None] - fhb) / den
+    f_pulay = -2.0 * ((efs[None] - efb) / den - ((wes - web)[:, None, None] / den) * ((fps[None] - fpb) / den))
+    fj = f_hf + f_pulay
+    Mt = fj.shape[0]
+    mean = fj.mean(axis=0)
+    std = np.sqrt((Mt - 1) / Mt * np.sum((fj - mean) ** 2, axis=0))
+    return mean, std

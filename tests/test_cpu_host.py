@@ -153,3 +153,35 @@ def test_engine_refuses_without_gpu():
     from jqmc_gb300.engine import GpuSystem
     with pytest.raises(JqmcError):
         GpuSystem(synthetic.water_like().hamiltonian)
+
+
+def test_jackknife_force_matches_direct_evaluation():
+    """statistics.jackknife_force against a per-sample loop of the same estimator."""
+    from jqmc_gb300.statistics import jackknife_force
+    rng = np.random.default_rng(3)
+    M, nw, na, bins = 20, 4, 2, 5
+    w = rng.uniform(0.5, 1.5, (M, nw))
+    e = rng.normal(-10, 1, (M, nw))
+    fhf = rng.normal(0, 1, (M, nw, na, 3))
+    fpp = rng.normal(0, 1, (M, nw, na, 3))
+    efpp = e[..., None, None] * fpp
+    mean, std = jackknife_force(w, e, fhf, fpp, efpp, bins)
+    split = lambda x: [a.sum(axis=0) for a in np.array_split(x, bins, axis=0)]  # noqa: E731
+    wb = np.concatenate(split(w))
+    web = np.concatenate(split(w * e))
+    fh = np.concatenate(split(w[..., None, None] * fhf))
+    fp = np.concatenate(split(w[..., None, None] * fpp))
+    ef = np.concatenate(split(w[..., None, None] * efpp))
+    samples = []
+    for j in range(len(wb)):
+        W = wb.sum() - wb[j]
+        E = (web.sum() - web[j]) / W
+        FH = (fh.sum(0) - fh[j]) / W
+        FP = (fp.sum(0) - fp[j]) / W
+        EF = (ef.sum(0) - ef[j]) / W
+        samples.append(-FH - 2.0 * (EF - E * FP))
+    samples = np.array(samples)
+    ref_mean = samples.mean(axis=0)
+    ref_std = np.sqrt((len(samples) - 1) * np.mean((samples - ref_mean) ** 2, axis=0))
+    assert np.allclose(mean, ref_mean, rtol=1e-12, atol=1e-12)
+    assert np.allclose(std, ref_std, rtol=1e-12, atol=1e-12)
