@@ -81,9 +81,10 @@ typedef struct {
 #define JQMC_PREC_MIXED 1     /* G, G^-1, T_up, T_dn, h3 float; AO values, ratios  */
                               /* and rank-1 updates float; AO gradients/Laplacians,*/
                               /* energy cache, weights and the table rebuild double;*/
-                              /* block energy (jqmc_lrdmc_energy): float values    */
-                              /* with compensated float-float sums                 */
-#define JQMC_PREC_MIXED_E64 2 /* as JQMC_PREC_MIXED, block energy in FP64 arithmetic */
+                              /* block energy (jqmc_lrdmc_energy) in FP64 arithmetic */
+#define JQMC_PREC_MIXED_FASTE 2 /* as JQMC_PREC_MIXED, block energy from float values */
+                                /* with compensated float-float sums (faster; rare    */
+                                /* configurations with errors near 1e-3 Ha)           */
 
 /* Per-walker state, all device arrays (N = n_up + n_dn, n = n_up, A = det.nao,
  * A3 = j3.nao).  Electron-major layouts: electron e's vectors are contiguous.

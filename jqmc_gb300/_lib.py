@@ -47,7 +47,7 @@ class Walkers(C.Structure):
                 ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("dcache", vp), ("status", vp)]
 
 
-PREC_FP64, PREC_MIXED, PREC_MIXED_E64 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_MIXED_FASTE = 0, 1, 2
 
 
 class JqmcError(RuntimeError):

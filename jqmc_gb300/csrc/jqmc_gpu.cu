@@ -94,6 +94,14 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Ask L2 for the 128-byte lines of [p, p + bytes), one line per lane (bounded
+// to the given range; a hint only, no data is returned).
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes, int lane) {
+  const char* c = static_cast<const char*>(p);
+  for (size_t off = (size_t)lane * 128; off < bytes; off += 32 * 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
+}
+
 // Accumulators of the mesh and electron-term sums.  float / double: plain
 // sums.  F2: compensated float-float sum of float products (TwoProduct by FMA
 // and TwoSum, as in algorithm Dot2 of Ogita, Rump and Oishi, SIAM J. Sci.
@@ -1206,7 +1214,7 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
 // Displacement caches bigger than this live in global memory (per walker).
 constexpr int kDcacheSmemMax = 64 * 1024;
 
-bool is_mixed(int precision) { return precision == JQMC_PREC_MIXED || precision == JQMC_PREC_MIXED_E64; }
+bool is_mixed(int precision) { return precision == JQMC_PREC_MIXED || precision == JQMC_PREC_MIXED_FASTE; }
 
 int dcache_bytes(const Sys& s) { return s.N * (s.natom + s.N) * 3 * 4; }
 
@@ -1300,6 +1308,12 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     const int i = up ? e : e - s.n_up;
     const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
     const Tab* dp = k.dphi + (size_t)e * 4 * A;
+    if (e + nw < k.N) {   // this warp's next electron: its derivative tables and T row
+      const int en = e + nw;
+      prefetch_l2(k.dphi + (size_t)en * 4 * A, (size_t)4 * A * sizeof(Tab), lane);
+      prefetch_l2((en < s.n_up ? k.Tup + (size_t)en * A : k.Tdn + (size_t)(en - s.n_up) * A), (size_t)A * sizeof(Tab), lane);
+      if (s.has_j3) prefetch_l2(k.dphi3 + (size_t)en * 5 * A3, (size_t)5 * A3 * sizeof(Tab), lane);
+    }
     Acc tgx, tgy, tgz, tlp, tc3, thx, thy, thz, thl;
     acc_zero(tgx); acc_zero(tgy); acc_zero(tgz); acc_zero(tlp);
     acc_zero(tc3); acc_zero(thx); acc_zero(thy); acc_zero(thz); acc_zero(thl);
@@ -1483,6 +1497,16 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
     const int atom = t.eatom[e];
     const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
     const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
+    if (e + nw < N) {   // this warp's next electron: its T row, J3 field and displacements
+      const int en = e + nw;
+      const Tab* Tn = (en < s.n_up ? k.Tup + (size_t)en * k.A : k.Tdn + (size_t)(en - s.n_up) * k.A);
+      prefetch_l2(Tn, (size_t)k.A * sizeof(Tab), lane);
+      if (s.has_j3) prefetch_l2(k.h3 + (size_t)en * k.A3, (size_t)k.A3 * sizeof(Tab), lane);
+      if (sizeof(R) == sizeof(float) && t.dA && __isGlobal(t.dA)) {   // (a shared-memory cache needs none)
+        prefetch_l2(t.dA + (size_t)en * s.natom * 3, (size_t)s.natom * 12, lane);
+        prefetch_l2(t.dE + (size_t)en * N * 3, (size_t)N * 12, lane);
+      }
+    }
     for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
       // lane p < P sets up point p, then every lane receives all P moves.  The
       // float form builds them from the float rotation, quadrature directions
@@ -2916,10 +2940,10 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
   const int smem = P.ml.bytes;
   if (is_mixed(w->precision)) {
     // projections: float arithmetic on the float tables; the local energy of a
-    // block (K == 0): float values with compensated float-float sums, or FP64
-    // arithmetic on the float tables (JQMC_PREC_MIXED_E64)
+    // block (K == 0): FP64 arithmetic on the float tables, or float values with
+    // compensated float-float sums (JQMC_PREC_MIXED_FASTE)
     auto fn = K > 0 ? k_lrdmc<float, float, float>
-                    : (w->precision == JQMC_PREC_MIXED_E64 ? k_lrdmc<double, float, double> : k_lrdmc<float, float, F2>);
+                    : (w->precision == JQMC_PREC_MIXED_FASTE ? k_lrdmc<float, float, F2> : k_lrdmc<double, float, double>);
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
     fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);

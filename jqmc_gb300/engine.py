@@ -19,7 +19,7 @@ from .atomic_orbital import primitive_norm
 from .coulomb_potential import ECP_MESHES
 from .hamiltonians import Hamiltonian_data
 
-PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, "mixed_fp64_energy": _lib.PREC_MIXED_E64}
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, "mixed_fast_energy": _lib.PREC_MIXED_FASTE}
 
 
 def _ptr(a: np.ndarray, ctype):
@@ -179,10 +179,11 @@ class WalkerSet:
     precision "fp64": every table double (the plain drop-in);
     precision "mixed": G, G^-1, T tables and the J3 field in float, rebuilt in
     double from the positions by ``init`` / ``rebuild`` (an FP64 scratch of
-    2 n A doubles per walker is held for that rebuild); the block energy uses
-    float values with compensated float-float sums;
-    precision "mixed_fp64_energy": as "mixed", with the block energy in FP64
-    arithmetic on the float tables (more accuracy margin, slower energy)."""
+    2 n A doubles per walker is held for that rebuild); the block energy in FP64
+    arithmetic on the float tables;
+    precision "mixed_fast_energy": as "mixed", with the block energy from float
+    values and compensated float-float sums (about ten times faster; rare
+    configurations carry errors near 1e-3 Ha)."""
 
     def __init__(self, system: GpuSystem, r_up, r_dn, precision: str = "fp64", scratch: torch.Tensor | None = None):
         self.sys = system

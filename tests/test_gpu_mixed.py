@@ -156,15 +156,14 @@ def test_mixed_gfmc_t_follows_fp64(pair):
     assert not b.status.any()
 
 
-def test_mixed_fp64_energy_variant(pair):
-    """precision "mixed_fp64_energy": the same float tables and projections, the
-    block energy in FP64 arithmetic; on fresh tables it agrees with the FP64 form
-    at least as well as the compensated float energy."""
+def test_mixed_fast_energy_variant(pair):
+    """precision "mixed_fast_energy": the same float tables and projections, the
+    block energy from float values with compensated float-float sums."""
     syn, gs, w64, w32 = pair
     from jqmc_gb300.engine import WalkerSet
     r = w64.r.cpu().numpy()
     n = gs.n_up
-    we = WalkerSet(gs, r[:, :n], r[:, n:], precision="mixed_fp64_energy")
+    we = WalkerSet(gs, r[:, :n], r[:, n:], precision="mixed_fast_energy")
     rng = np.random.default_rng(3)
     W = w64.nwalk
     d = torch.as_tensor(np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (W, 3)), rng.uniform(size=(W, 1))], axis=-1),
@@ -172,6 +171,6 @@ def test_mixed_fp64_energy_variant(pair):
     e64, _ = w64.lrdmc_energy(d, 0.2)
     ee, _ = we.lrdmc_energy(d, 0.2)
     rms = float(torch.sqrt(torch.mean((ee - e64) ** 2)))
-    print(f"{syn.name}: mixed tables + FP64 block energy vs fp64 e_L rms {rms:.3e} Ha")
+    print(f"{syn.name}: mixed tables + compensated float block energy vs fp64 e_L rms {rms:.3e} Ha")
     assert rms <= 1e-5
     assert torch.equal(we.Ginv, w32.Ginv)
