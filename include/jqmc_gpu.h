@@ -81,10 +81,19 @@ typedef struct {
 #define JQMC_PREC_MIXED 1     /* G, G^-1, T_up, T_dn, h3 float; AO values, ratios  */
                               /* and rank-1 updates float; AO gradients/Laplacians,*/
                               /* energy cache, weights and the table rebuild double;*/
-                              /* block energy (jqmc_lrdmc_energy) in FP64 arithmetic */
-#define JQMC_PREC_MIXED_FASTE 2 /* as JQMC_PREC_MIXED, block energy from float values */
-                                /* with compensated float-float sums (faster; rare    */
-                                /* configurations with errors near 1e-3 Ha)           */
+                              /* block energy (jqmc_lrdmc_energy): float values     */
+                              /* with compensated float-float sums; the walkers     */
+                              /* whose mesh ratios cancel strongly (factor above    */
+                              /* JQMC_FAST_ENERGY_CANCEL) recomputed in FP64        */
+#define JQMC_PREC_MIXED_FASTE 2 /* as JQMC_PREC_MIXED, the compensated energy alone */
+                                /* (rare configurations with errors of 1e-4 Ha)     */
+/* Cancellation factor above which a walker's block energy is recomputed in FP64:
+ * C = sum_i |w_i| M_i / sum_i |w_i ratio_i| over the walker's mesh elements
+ * (weight w_i, ratio psi(r')/psi(r) = sum_a phi_a(r') T_a times the Jastrow
+ * factor, M_i the same sum over |phi_a T_a|).  Sampled configurations have a
+ * median near 4; about 2.5 % exceed 10.  After jqmc_lrdmc_energy in
+ * JQMC_PREC_MIXED, C is the first double of each walker's scratch block. */
+#define JQMC_FAST_ENERGY_CANCEL 10.0
 
 /* Per-walker state, all device arrays (N = n_up + n_dn, n = n_up, A = det.nao,
  * A3 = j3.nao).  Electron-major layouts: electron e's vectors are contiguous.

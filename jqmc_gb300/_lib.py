@@ -48,6 +48,7 @@ class Walkers(C.Structure):
 
 
 PREC_FP64, PREC_MIXED, PREC_MIXED_FASTE = 0, 1, 2
+FAST_ENERGY_CANCEL = 10.0   # JQMC_FAST_ENERGY_CANCEL: cancellation factor above which a block energy is recomputed in FP64
 
 
 class JqmcError(RuntimeError):

@@ -110,10 +110,17 @@ __device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes, int lan
 // float for float, double for double and F2.
 struct F2 {
   float s, c;
+  float m;   // sum of |terms| (the scale of the rounding of the float inputs)
 };
 __device__ __forceinline__ void acc_zero(float& a) { a = 0.f; }
 __device__ __forceinline__ void acc_zero(double& a) { a = 0.0; }
-__device__ __forceinline__ void acc_zero(F2& a) { a.s = 0.f; a.c = 0.f; }
+__device__ __forceinline__ void acc_zero(F2& a) { a.s = 0.f; a.c = 0.f; a.m = 0.f; }
+__device__ __forceinline__ void acc_mag(float&, float) {}
+__device__ __forceinline__ void acc_mag(double&, double) {}
+__device__ __forceinline__ void acc_mag(F2& a, float v) { a.m += v; }
+__device__ __forceinline__ float acc_mag_out(float) { return 0.f; }
+__device__ __forceinline__ float acc_mag_out(double) { return 0.f; }
+__device__ __forceinline__ float acc_mag_out(F2 a) { return warp_sum(a.m); }
 __device__ __forceinline__ void acc_fma(float& a, float x, float y) { a += x * y; }
 __device__ __forceinline__ void acc_fma(double& a, double x, double y) { a += x * y; }
 __device__ __forceinline__ void two_sum_into(F2& a, float p) {
@@ -449,6 +456,12 @@ __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* 
 #pragma unroll
     for (int j = 0; j < 2 * L + 1; ++j) part += S[j] * vv[j];
     acc_fma(acc[p], rad[p], part);
+    if constexpr (AccTraits<Acc>::accurate) {
+      R pabs = R(0);
+#pragma unroll
+      for (int j = 0; j < 2 * L + 1; ++j) pabs += fabs(S[j] * vv[j]);
+      acc_mag(acc[p], fabs(rad[p]) * pabs);
+    }
   }
 }
 
@@ -477,6 +490,58 @@ __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx
     case 5: emit_dot_pts<5, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
     default: emit_dot_pts<6, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
   }
+}
+
+// shell_dot_pts with the squared distances given as float-float pairs
+// (r2h + r2l): exp(-Z (r2h + r2l)) = expf(-Z r2h) (1 - Z r2l) to second order,
+// so that the float AO values carry only the rounding of their own evaluation.
+template <int P, class V, class Acc>
+__device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const float* dx, const float* dy, const float* dz,
+                                                 const float* r2h, const float* r2l, const V* v, Acc* acc) {
+  const int* sh = b.shells + 8 * s;
+  const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
+  const float* pr = b.primsf + 2 * p0;
+  float rad[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) rad[p] = 0.f;
+  for (int q = 0; q < np; ++q) {
+    const float Z = pr[2 * q], c = pr[2 * q + 1];
+#pragma unroll
+    for (int p = 0; p < P; ++p) rad[p] += c * expf(-Z * r2h[p]) * (1.f - Z * r2l[p]);
+  }
+  switch (l) {
+    case 0: emit_dot_pts<0, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 1: emit_dot_pts<1, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 2: emit_dot_pts<2, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 3: emit_dot_pts<3, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 4: emit_dot_pts<4, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 5: emit_dot_pts<5, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    default: emit_dot_pts<6, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+  }
+}
+
+// d = (x0h + x0l) + m as a float pair (dh, dl) by TwoSum
+__device__ __forceinline__ void ff_add(float x0h, float x0l, float m, float& dh, float& dl) {
+  const float t = __fadd_rn(x0h, m);
+  const float z = __fsub_rn(t, x0h);
+  const float e = __fadd_rn(__fsub_rn(x0h, __fsub_rn(t, z)), __fsub_rn(m, z));
+  dh = t;
+  dl = e + x0l;
+}
+
+// |d|^2 for d = dh + dl (per component) as a float pair: exact squares of the
+// high parts by FMA, the cross terms 2 dh dl, and the rounding of the sum
+__device__ __forceinline__ void ff_r2(float xh, float xl, float yh, float yl, float zh, float zl, float& r2h, float& r2l) {
+  const float px = __fmul_rn(xh, xh), py = __fmul_rn(yh, yh), pz = __fmul_rn(zh, zh);
+  const float ex = __fmaf_rn(xh, xh, -px), ey = __fmaf_rn(yh, yh, -py), ez = __fmaf_rn(zh, zh, -pz);
+  const float s1 = __fadd_rn(px, py);
+  const float z1 = __fsub_rn(s1, px);
+  const float e1 = __fadd_rn(__fsub_rn(px, __fsub_rn(s1, z1)), __fsub_rn(py, z1));
+  const float s2 = __fadd_rn(s1, pz);
+  const float z2 = __fsub_rn(s2, s1);
+  const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, z2)), __fsub_rn(pz, z2));
+  r2h = s2;
+  r2l = (ex + ey + ez) + (e1 + e2) + 2.f * (xh * xl + yh * yl + zh * zl);
 }
 
 // Visit every AO of a basis at point p (shells are grouped by nucleus, so the
@@ -1402,7 +1467,7 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 // caches t.dA / t.dE; otherwise from the positions in double.
 template <int P, class R, class Tab, class Acc>
 __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz,
-                             typename AccTraits<Acc>::out* ratio) {
+                             typename AccTraits<Acc>::out* ratio, float* mag = nullptr, const float* sl = nullptr) {
   using Out = typename AccTraits<Acc>::out;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
@@ -1427,23 +1492,50 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
 #pragma unroll
   for (int p = 0; p < P; ++p) { acc_zero(det[p]); acc_zero(dj[p]); }
   R dx[P], dy[P], dz[P];
-  for (int idx = lane; idx < s.det.nshell; idx += 32) {
-    const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
-    R x, y, z;
-    dnuc(s.det.shells[8 * sh], x, y, z);
+  if constexpr (sizeof(R) == sizeof(float) && AccTraits<Acc>::accurate) {
+    // compensated energy: displacements as float pairs (the low part from the
+    // double positions), squared distances as float pairs
+    float dxl[P], dyl[P], dzl[P], r2h[P], r2l[P];
+    auto shells = [&](const Basis& b, const Tab* v, Acc* acc) {
+      for (int idx = lane; idx < b.nshell; idx += 32) {
+        const int sh = b.shells[8 * idx + 7];
+        const int atom = b.shells[8 * sh];
+        R x, y, z;
+        dnuc(atom, x, y, z);
+        const float xl = (float)((ex - s.atom_pos[3 * atom]) - (double)x);
+        const float yl = (float)((ey - s.atom_pos[3 * atom + 1]) - (double)y);
+        const float zl = (float)((ez - s.atom_pos[3 * atom + 2]) - (double)z);
 #pragma unroll
-    for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
-    shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
-  }
-  if (s.has_j3) {
-    const Tab* h = k.h3 + (size_t)e * k.A3;
-    for (int idx = lane; idx < s.j3.nshell; idx += 32) {
-      const int sh = s.j3.shells[8 * idx + 7];
+        for (int p = 0; p < P; ++p) {
+          ff_add(x, xl + sl[p], mx[p], dx[p], dxl[p]);
+          ff_add(y, yl + sl[P + p], my[p], dy[p], dyl[p]);
+          ff_add(z, zl + sl[2 * P + p], mz[p], dz[p], dzl[p]);
+          ff_r2(dx[p], dxl[p], dy[p], dyl[p], dz[p], dzl[p], r2h[p], r2l[p]);
+        }
+        shell_dot_pts_ff<P>(b, sh, dx, dy, dz, r2h, r2l, v, acc);
+      }
+    };
+    shells(s.det, Trow, det);
+    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj);
+  } else {
+    for (int idx = lane; idx < s.det.nshell; idx += 32) {
+      const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
       R x, y, z;
-      dnuc(s.j3.shells[8 * sh], x, y, z);
+      dnuc(s.det.shells[8 * sh], x, y, z);
 #pragma unroll
       for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
-      shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
+      shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
+    }
+    if (s.has_j3) {
+      const Tab* h = k.h3 + (size_t)e * k.A3;
+      for (int idx = lane; idx < s.j3.nshell; idx += 32) {
+        const int sh = s.j3.shells[8 * idx + 7];
+        R x, y, z;
+        dnuc(s.j3.shells[8 * sh], x, y, z);
+#pragma unroll
+        for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
+        shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
+      }
     }
   }
   if (s.has_j1) {
@@ -1475,7 +1567,11 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
   for (int p = 0; p < P; ++p) {
     const Out dsum = acc_out(det[p]);
     const Out jsum = acc_out(dj[p]);
-    ratio[p] = dsum * Num<Out>::ex(jsum - c3);
+    const Out jf = Num<Out>::ex(jsum - c3);
+    ratio[p] = dsum * jf;
+    if constexpr (AccTraits<Acc>::accurate) {
+      if (mag) mag[p] = acc_mag_out(det[p]) * (float)jf;   // sum |phi_a T_a| on the ratio's scale
+    }
   }
 }
 
@@ -1484,9 +1580,28 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
 // warp per electron: its six lattice shifts, then its Nv quadrature points (if
 // its nearest nucleus carries a non-local channel), P points per chunk (6 in
 // float, 3 in double, for registers).
+// The compensated block energy's error is dominated by walkers whose mesh
+// ratios psi(r')/psi(r) = sum_a phi_a(r') T_a come out of large cancellations
+// (near a node): the float rounding of the AO values is then relative to
+// sum_a |phi_a T_a|, not to the ratio.  Per walker the element-weighted mean
+// cancellation factor  C = sum_i |w_i| M_i / sum_i |w_i ratio_i|  (w_i the
+// element's weight, M_i = sum_a |phi_a T_a| times its Jastrow factor) ranks the
+// walkers by that error; its median is near 4 on sampled configurations.
+struct Cancellation {
+  float num = 0.f, den = 0.f;
+  __device__ void add(float wabs, float mag, float el) {
+    num += wabs * mag;
+    den += fabsf(el);
+  }
+};
+
+// Returns this thread's shares of the walker's cancellation factor (compensated
+// mode; zero otherwise).
 template <class R, class Tab, class Acc = R>
-__device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
+__device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
   using Out = typename AccTraits<Acc>::out;
+  constexpr bool kErr = AccTraits<Acc>::accurate;
+  Cancellation cancel;
   constexpr int P = sizeof(R) == sizeof(float) ? 6 : 3;
   constexpr int nkc = 6 / P;   // chunks of lattice shifts
   const Sys& s = k.s;
@@ -1512,13 +1627,14 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
       // float form builds them from the float rotation, quadrature directions
       // and displacement cache, so that the chunk issues no FP64 instruction.
       R mx = R(0), my = R(0), mz = R(0), ct = R(0);
+      float mxl = 0.f, myl = 0.f, mzl = 0.f;   // compensated form: low parts of the move
       int v0 = 0, np = P;
       if (c >= nkc) {
         v0 = (c - nkc) * P;
         np = min(P, nv - v0);
       }
       if (lane < P) {
-        if constexpr (sizeof(R) == sizeof(float)) {
+        if constexpr (sizeof(R) == sizeof(float) && !kErr) {
           if (c < nkc) {
             const int kk = c * P + lane, ax = kk >> 1;
             const float sg = (kk & 1) ? -(float)alat : (float)alat;
@@ -1533,10 +1649,11 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
             mx = relx + dist * g[0]; my = rely + dist * g[1]; mz = relz + dist * g[2];
           }
         } else {
+          double dmx, dmy, dmz;
           if (c < nkc) {
             const int kk = c * P + lane, ax = kk >> 1;
             const double sg = (kk & 1) ? -alat : alat;
-            mx = sg * t.R[ax]; my = sg * t.R[3 + ax]; mz = sg * t.R[6 + ax];
+            dmx = sg * t.R[ax]; dmy = sg * t.R[3 + ax]; dmz = sg * t.R[6 + ax];
           } else {
             const double relx = s.atom_pos[3 * atom] - k.r[3 * e], rely = s.atom_pos[3 * atom + 1] - k.r[3 * e + 1];
             const double relz = s.atom_pos[3 * atom + 2] - k.r[3 * e + 2];
@@ -1546,8 +1663,17 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
             const double gy = t.R[3] * m[0] + t.R[4] * m[1] + t.R[5] * m[2];
             const double gz = t.R[6] * m[0] + t.R[7] * m[1] + t.R[8] * m[2];
             const double gn = sqrt(gx * gx + gy * gy + gz * gz);
-            ct = (-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn);
-            mx = relx + dist * gx; my = rely + dist * gy; mz = relz + dist * gz;
+            ct = (R)((-relx / dist) * (gx / gn) + (-rely / dist) * (gy / gn) + (-relz / dist) * (gz / gn));
+            dmx = relx + dist * gx; dmy = rely + dist * gy; dmz = relz + dist * gz;
+          }
+          mx = (R)dmx; my = (R)dmy; mz = (R)dmz;
+          if constexpr (kErr) {
+            // the compensated form keeps the moves to FP64 accuracy: a float
+            // rounding of an ECP point (about 1e-7 |r - R_I|) moves the ratio
+            // by its gradient times that, which V_l near a core magnifies
+            mxl = (float)(dmx - (double)mx);
+            myl = (float)(dmy - (double)my);
+            mzl = (float)(dmz - (double)mz);
           }
         }
       }
@@ -1559,26 +1685,45 @@ __device__ void mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinet
         sz[p] = __shfl_sync(0xffffffffu, mz, p);
       }
       Out ratio[P];
-      wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio);
+      float mag[P];
+      if constexpr (kErr) {
+        float sl[3 * P];
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          sl[p] = __shfl_sync(0xffffffffu, mxl, p);
+          sl[P + p] = __shfl_sync(0xffffffffu, myl, p);
+          sl[2 * P + p] = __shfl_sync(0xffffffffu, mzl, p);
+        }
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl);
+      } else {
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio);
+      }
       if (lane < np) {
         Out rr = Out(0);
+        float mg = 0.f;
 #pragma unroll
-        for (int p = 0; p < P; ++p) rr = p == lane ? ratio[p] : rr;
+        for (int p = 0; p < P; ++p) {
+          rr = p == lane ? ratio[p] : rr;
+          if (kErr) mg = p == lane ? mag[p] : mg;
+        }
         if (c < nkc) {
           t.el[6 * e + c * P + lane] = (double)((Out)kin * rr);
+          if (kErr) cancel.add(fabsf((float)kin), mg, (float)(kin * rr));
         } else {
           const int v = v0 + lane, lmax = s.ecp_maxl1[atom];
           const double* vl = k.ec + (size_t)e * kEC + EC_VL;   // V_l at the nearest nucleus
-          const Out wv = (Out)s.mesh_w[v] * rr;
+          const Out wv = (Out)s.mesh_w[v];
           const Out cto = (Out)ct;
-          Out vsum = Out(0);
-          for (int l = 0; l < lmax; ++l) vsum += (Out)vl[l] * (Out(2 * l + 1) * legendre_t<Out>(l, cto) * wv);
-          t.V[e * nv + v] = (double)vsum;
+          Out vw = Out(0);   // the element's weight: V = vw * ratio
+          for (int l = 0; l < lmax; ++l) vw += (Out)vl[l] * (Out(2 * l + 1) * legendre_t<Out>(l, cto) * wv);
+          t.V[e * nv + v] = (double)(vw * rr);
+          if (kErr) cancel.add(fabsf((float)vw), mg, (float)(vw * rr));
         }
       }
     }
   }
   __syncthreads();
+  return cancel;
 }
 
 // Phase C of the GFMC_n step: (diag, nondiag) sums (jqmc_gfmc.py:4806-5030).
@@ -2652,11 +2797,22 @@ __global__ void k_vmc_measure(KParams P, const double* __restrict__ angles, doub
 // LRDMC GFMC_n projections; K steps fused.  K == 0 with energy outputs computes
 // e_L and V_diag at the current positions with the rotation of draw[w].
 // R: mesh arithmetic, Tab: table storage and updates.
+// Block-energy modes of k_lrdmc (mixed form): kEnergyBound writes the walker's
+// cancellation factor C of the compensated-float energy to the first double of
+// its rebuild scratch (free after the rebuild); kEnergyGate runs only the
+// walkers whose C exceeds kFastEnergyCancel and overwrites their energy.
+constexpr int kEnergyPlain = 0, kEnergyBound = 1, kEnergyGate = 2;
+constexpr double kFastEnergyCancel = JQMC_FAST_ENERGY_CANCEL;
+__device__ __forceinline__ double* energy_bound(const KParams& P, int w) {
+  return P.ws.scratch + (size_t)w * 2 * P.s.n_up * P.s.det.nao;
+}
+
 template <class R, class Tab, class Acc = R>
 __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
-                        double* eL, double* vdiag, TauArgs ta) {
+                        double* eL, double* vdiag, TauArgs ta, int emode) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
+  if (emode == kEnergyGate && !(*energy_bound(P, w) > kFastEnergyCancel)) return;   // uniform over the CTA
   const Sys s = stage_tables(P.s, P.tl, smem);
   Work<Tab> k = make_work<Tab>(s, P.wl, smem, P.ws, w);
   float* gd = (P.dcache_global && sizeof(R) == sizeof(float)) ? P.ws.dcache + (size_t)w * (dcache_floats_dev(s)) : nullptr;
@@ -2691,10 +2847,15 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
       __syncthreads();
     }
     electron_terms<Tab, Acc>(k, t, alat);
-    mesh_terms<R, Tab, Acc>(k, t, alat, true);
+    const Cancellation mc = mesh_terms<R, Tab, Acc>(k, t, alat, true);
     double diag, nondiag;
     lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
+      if (AccTraits<Acc>::accurate && emode == kEnergyBound) {
+        const double num = block_sum((double)mc.num, k.red);
+        const double den = block_sum((double)mc.den, k.red);
+        if (threadIdx.x == 0) *energy_bound(P, w) = den > 0.0 ? num / den : 0.0;
+      }
       if (threadIdx.x == 0) {
         eL[w] = diag + nondiag;
         vdiag[w] = diag;
@@ -2939,19 +3100,35 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
   KParams P = make_params(sys, w);
   const int smem = P.ml.bytes;
   if (is_mixed(w->precision)) {
-    // projections: float arithmetic on the float tables; the local energy of a
-    // block (K == 0): FP64 arithmetic on the float tables, or float values with
-    // compensated float-float sums (JQMC_PREC_MIXED_FASTE)
-    auto fn = K > 0 ? k_lrdmc<float, float, float>
-                    : (w->precision == JQMC_PREC_MIXED_FASTE ? k_lrdmc<float, float, F2> : k_lrdmc<double, float, double>);
-    int rc = launch_check((const void*)fn, smem);
-    if (rc) return rc;
-    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);
+    // projections: float arithmetic on the float tables.  The local energy of a
+    // block (K == 0): float values with compensated float-float sums, then FP64
+    // arithmetic for the walkers whose cancellation factor exceeds
+    // JQMC_FAST_ENERGY_CANCEL (JQMC_PREC_MIXED), or the compensated energy alone
+    // (JQMC_PREC_MIXED_FASTE)
+    if (K > 0) {
+      auto fn = k_lrdmc<float, float, float>;
+      int rc = launch_check((const void*)fn, smem);
+      if (rc) return rc;
+      fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+    } else {
+      const bool gate = w->precision == JQMC_PREC_MIXED;
+      auto fn = k_lrdmc<float, float, F2>;
+      int rc = launch_check((const void*)fn, smem);
+      if (rc) return rc;
+      fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
+                                             gate ? kEnergyBound : kEnergyPlain);
+      if (gate) {
+        auto fd = k_lrdmc<double, float, double>;
+        rc = launch_check((const void*)fd, smem);
+        if (rc) return rc;
+        fd<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyGate);
+      }
+    }
   } else {
     auto fn = k_lrdmc<double, double>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
-    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta);
+    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }

@@ -179,11 +179,13 @@ class WalkerSet:
     precision "fp64": every table double (the plain drop-in);
     precision "mixed": G, G^-1, T tables and the J3 field in float, rebuilt in
     double from the positions by ``init`` / ``rebuild`` (an FP64 scratch of
-    2 n A doubles per walker is held for that rebuild); the block energy in FP64
-    arithmetic on the float tables;
-    precision "mixed_fast_energy": as "mixed", with the block energy from float
-    values and compensated float-float sums (about ten times faster; rare
-    configurations carry errors near 1e-3 Ha)."""
+    2 n A doubles per walker is held for that rebuild); the block energy from
+    float values with compensated float-float sums, the walkers whose mesh
+    ratios cancel strongly (factor above ``_lib.FAST_ENERGY_CANCEL``, about
+    2.5 % of sampled configurations) recomputed in FP64 arithmetic on the float
+    tables;
+    precision "mixed_fast_energy": as "mixed", the compensated energy alone
+    (rare configurations carry errors of 1e-4 Ha)."""
 
     def __init__(self, system: GpuSystem, r_up, r_dn, precision: str = "fp64", scratch: torch.Tensor | None = None):
         self.sys = system
@@ -321,6 +323,15 @@ class WalkerSet:
                                                 C.c_void_p(eL.data_ptr()), C.c_void_p(vd.data_ptr()), self.sys.stream),
                    "jqmc_lrdmc_energy")
         return eL, vd
+
+    def energy_cancellation(self) -> torch.Tensor:
+        """Per-walker cancellation factors of the compensated block energy's mesh
+        ratios, as left by the last ``lrdmc_energy`` in precision "mixed" (the
+        first double of each walker's rebuild scratch; overwritten by the next
+        rebuild).  Walkers above ``_lib.FAST_ENERGY_CANCEL`` were recomputed in FP64."""
+        if self.precision != "mixed":
+            raise ValueError("cancellation factors are kept in precision 'mixed' only")
+        return self.scratch.view(self.nwalk, -1)[:, 0].clone()
 
     def gather_from(self, src: "WalkerSet", chosen: torch.Tensor):
         ds, dd = src.desc(), self.desc()

@@ -174,3 +174,35 @@ def test_mixed_fast_energy_variant(pair):
     print(f"{syn.name}: mixed tables + compensated float block energy vs fp64 e_L rms {rms:.3e} Ha")
     assert rms <= 1e-5
     assert torch.equal(we.Ginv, w32.Ginv)
+
+
+def test_adaptive_block_energy(pair):
+    """precision "mixed": the compensated-float energy; walkers whose mesh ratios
+    cancel strongly (factor above the threshold) are recomputed in FP64
+    arithmetic, the others keep the compensated value unchanged."""
+    syn, gs, w64, w32 = pair
+    from jqmc_gb300 import _lib
+    from jqmc_gb300.engine import WalkerSet
+    r = w64.r.cpu().numpy()
+    n = gs.n_up
+    we = WalkerSet(gs, r[:, :n], r[:, n:], precision="mixed_fast_energy")
+    rng = np.random.default_rng(5)
+    W = w64.nwalk
+    d = torch.as_tensor(np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (W, 3)), rng.uniform(size=(W, 1))], axis=-1),
+                        device=gs.device)
+    e64, v64 = w64.lrdmc_energy(d, 0.2)
+    ee, ve = we.lrdmc_energy(d, 0.2)
+    ea, va = w32.lrdmc_energy(d, 0.2)
+    cf = w32.energy_cancellation()
+    flag = cf > _lib.FAST_ENERGY_CANCEL
+    # sum |phi_a T_a| >= |sum phi_a T_a| element by element: the factor is at least 1
+    assert bool(torch.isfinite(cf).all()) and float(cf.min()) >= 0.999
+    assert float(flag.double().mean()) < 0.2
+    # unflagged walkers: the compensated energy, bit for bit
+    assert torch.equal(ea[~flag], ee[~flag]) and torch.equal(va[~flag], ve[~flag])
+    rms = float(torch.sqrt(torch.mean((ea - e64) ** 2)))
+    worst_flagged = float((ea - e64)[flag].abs().max()) if bool(flag.any()) else 0.0
+    print(f"{syn.name}: adaptive block energy rms {rms:.3e} Ha, {int(flag.sum())}/{W} walkers recomputed in FP64 "
+          f"(worst {worst_flagged:.3e} Ha), cancellation factor median {float(cf.median()):.2f}")
+    assert rms <= 1e-5
+    assert worst_flagged <= 5e-5
