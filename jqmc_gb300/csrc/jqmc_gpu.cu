@@ -973,6 +973,11 @@ struct WorkLayout {
   int off_r, off_G, off_Gi, off_vA, off_v3, off_vn, off_red, off_sc, bytes;
 };
 
+// Shared-memory offsets of the walker (re)initialisation (after the staged tables)
+struct InitLayout {
+  int r, red, sc, Gd, aug, vec, bytes;
+};
+
 WorkLayout work_layout(const Sys& s, int base, int tab_bytes) {
   WorkLayout L;
   const int A3 = s.has_j3 ? s.j3.nao : 1;
@@ -1964,15 +1969,15 @@ constexpr int kInitRefine = 2;
 constexpr int kInitMReady = 4;
 constexpr int kInitJ3Table = 8;
 template <class Tab>
-__device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_aug, int off_vec, int mode,
+__device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, int mode,
                                  unsigned char* smem) {
   const Sys s = stage_tables(P.s, P.tl, smem);
   const int n = s.n_up, A = s.det.nao, N = s.N, A3 = s.has_j3 ? s.j3.nao : 1;
-  double* r = reinterpret_cast<double*>(smem + P.wl.off_r);
-  int* piv = reinterpret_cast<int*>(smem + P.wl.off_sc);
-  double* Gd = reinterpret_cast<double*>(smem + off_Gd);   // n*n
-  double* aug = reinterpret_cast<double*>(smem + off_aug); // n*2n
-  double* vec = reinterpret_cast<double*>(smem + off_vec); // max(A + n, 3*A3)
+  double* r = reinterpret_cast<double*>(smem + IL.r);
+  int* piv = reinterpret_cast<int*>(smem + IL.sc);
+  double* Gd = reinterpret_cast<double*>(smem + IL.Gd);   // n*n
+  double* aug = reinterpret_cast<double*>(smem + IL.aug); // n*2n
+  double* vec = reinterpret_cast<double*>(smem + IL.vec); // max(A + n, 4*A3)
   double* vn = vec + A;                                    // n
   Tab* Tup = static_cast<Tab*>(P.ws.Tup) + (size_t)w * n * A;
   Tab* Tdn = static_cast<Tab*>(P.ws.Tdn) + (size_t)w * n * A;
@@ -2050,39 +2055,51 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
     aug[t] = cc < n ? Gd[rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
   }
   __syncthreads();
-  for (int c = 0; c < n; ++c) {
-    if (threadIdx.x == 0) {
-      int p = c;
-      double best = fabs(aug[c * n2 + c]);
-      for (int rr = c + 1; rr < n; ++rr) {
-        const double v = fabs(aug[rr * n2 + c]);
-        if (v > best) { best = v; p = rr; }
+  {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = 0; c < n; ++c) {
+      if (wid == 0) {
+        // partial pivoting: the first row of largest |G[r][c]|, r >= c (warp argmax)
+        double best = -1.0;
+        int p = n;
+        for (int rr = c + lane; rr < n; rr += 32) {
+          const double v = fabs(aug[rr * n2 + c]);
+          if (v > best) { best = v; p = rr; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+          const int op = __shfl_xor_sync(0xffffffffu, p, o);
+          if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+        }
+        if (lane == 0) {
+          piv[0] = p < n ? p : c;
+          if (!(best > 0.0)) atomicOr(P.ws.status + w, JQMC_ST_SINGULAR);
+        }
       }
-      piv[0] = p;
-      if (best == 0.0) atomicOr(P.ws.status + w, JQMC_ST_SINGULAR);
-    }
-    __syncthreads();
-    const int p = piv[0];
-    if (p != c)
-      for (int cc = threadIdx.x; cc < n2; cc += blockDim.x) {
-        const double tmp = aug[c * n2 + cc];
-        aug[c * n2 + cc] = aug[p * n2 + cc];
-        aug[p * n2 + cc] = tmp;
+      __syncthreads();
+      const int p = piv[0];
+      if (p != c)
+        for (int cc = threadIdx.x; cc < n2; cc += blockDim.x) {
+          const double tmp = aug[c * n2 + cc];
+          aug[c * n2 + cc] = aug[p * n2 + cc];
+          aug[p * n2 + cc] = tmp;
+        }
+      __syncthreads();
+      // row c / pivot; columns < c of row c are zero and column c is set to the
+      // unit column below, so neither is touched here
+      const double inv = 1.0 / aug[c * n2 + c];
+      for (int cc = c + 1 + threadIdx.x; cc < n2; cc += blockDim.x) aug[c * n2 + cc] *= inv;
+      __syncthreads();
+      for (int rr = wid; rr < n; rr += nw) {
+        if (rr == c) continue;
+        const double f = aug[rr * n2 + c];
+        for (int cc = c + 1 + lane; cc < n2; cc += 32) aug[rr * n2 + cc] -= f * aug[c * n2 + cc];
       }
-    __syncthreads();
-    const double pv = aug[c * n2 + c];
-    __syncthreads();
-    for (int cc = threadIdx.x; cc < n2; cc += blockDim.x) aug[c * n2 + cc] /= pv;
-    __syncthreads();
-    for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
-      const int rr = t / n2, cc = t % n2;
-      if (rr == c || cc == c) continue;
-      aug[t] -= aug[rr * n2 + c] * aug[c * n2 + cc];
+      __syncthreads();
+      for (int rr = threadIdx.x; rr < n; rr += blockDim.x) aug[rr * n2 + c] = rr == c ? 1.0 : 0.0;
+      __syncthreads();
     }
-    __syncthreads();
-    for (int rr = threadIdx.x; rr < n; rr += blockDim.x)
-      if (rr != c) aug[rr * n2 + c] = 0.0;
-    __syncthreads();
   }
   Tab* Gw = static_cast<Tab*>(P.ws.G) + (size_t)w * n * n;
   Tab* Giw = static_cast<Tab*>(P.ws.Ginv) + (size_t)w * n * n;
@@ -2172,7 +2189,7 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
   }
   if (!(mode & kInitTablesOnly)) {
     // energy cache
-    ecache_init(s, r, P.ws.ecache + (size_t)w * (N + 1) * kEC, reinterpret_cast<double*>(smem + P.wl.off_red));
+    ecache_init(s, r, P.ws.ecache + (size_t)w * (N + 1) * kEC, reinterpret_cast<double*>(smem + IL.red));
     // AO derivative tables at every electron
     Tab* dpw = static_cast<Tab*>(P.ws.dphi) + (size_t)w * N * 4 * A;
     Tab* dp3w = s.has_j3 ? static_cast<Tab*>(P.ws.dphi3) + (size_t)w * N * 5 * A3 : nullptr;
@@ -2194,9 +2211,9 @@ __device__ void walker_init_body(const KParams& P, int w, int off_Gd, int off_au
 }
 
 template <class Tab>
-__global__ void k_walker_init(KParams P, int off_Gd, int off_aug, int off_vec, int mode) {
+__global__ void k_walker_init(KParams P, InitLayout IL, int mode) {
   extern __shared__ __align__(16) unsigned char smem[];
-  walker_init_body<Tab>(P, blockIdx.x, off_Gd, off_aug, off_vec, mode, smem);
+  walker_init_body<Tab>(P, blockIdx.x, IL, mode, smem);
 }
 
 
@@ -2728,7 +2745,7 @@ struct BatchItem {
   KParams P;
   int woff;        // first walker of the item in the batch
   int off_cand;    // VMC sweep: candidate G^-1 / G offset in shared memory
-  int off_init[3]; // rebuild: off_Gd, off_aug, off_vec
+  InitLayout init; // shared-memory layout of the rebuild
 };
 
 __device__ __forceinline__ int batch_item(const int* __restrict__ woff, int nitem, int g) {
@@ -2764,7 +2781,7 @@ template <class Tab>
 __global__ void k_walker_init_batch(const BatchItem* __restrict__ items, const int* __restrict__ woff, int nitem, int mode) {
   extern __shared__ __align__(16) unsigned char smem[];
   const BatchItem& it = items[batch_item(woff, nitem, blockIdx.x)];
-  walker_init_body<Tab>(it.P, blockIdx.x - it.woff, it.off_init[0], it.off_init[1], it.off_init[2], mode, smem);
+  walker_init_body<Tab>(it.P, blockIdx.x - it.woff, it.init, mode, smem);
 }
 
 // VMC local energy and weight (hamiltonians.py:225-290, jqmc_mcmc.py:725-747)   (FP64 form)
@@ -3333,13 +3350,22 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
 }
 
 // shared-memory layout of the init / rebuild kernel above the work layout; returns the bytes
-static int init_layout(const Sys& s, const KParams& P, int* off) {
+// The rebuild's shared memory: the staged tables, then the positions, the
+// reduction buffer and the pivot slot, then G, [G | I] and the vectors (none of
+// the energy kernels' work buffers, so that two CTAs fit on an SM).
+static InitLayout init_layout(const Sys& s, const KParams& P) {
   const int n = s.n_up, A3 = s.has_j3 ? s.j3.nao : 1;
-  off[0] = P.wl.bytes;                                   // G (double)
-  off[1] = align16(off[0] + n * n * 8);                  // [G | I]
-  off[2] = align16(off[1] + n * 2 * n * 8);              // vectors
+  InitLayout L;
+  int o = P.tl.bytes;
+  L.r = o; o = align16(o + s.N * 3 * 8);
+  L.red = o; o = align16(o + kRed * 8);
+  L.sc = o; o = align16(o + 32 * 8);
+  L.Gd = o; o = align16(o + n * n * 8);                  // G (double)
+  L.aug = o; o = align16(o + n * 2 * n * 8);             // [G | I]
   const int vec_len = (s.det.nao + n > 4 * A3) ? s.det.nao + n : 4 * A3;
-  return align16(off[2] + vec_len * 8);
+  L.vec = o; o = align16(o + vec_len * 8);
+  L.bytes = o;
+  return L;
 }
 
 static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream, int mode) {
@@ -3347,9 +3373,8 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
   KParams P = make_params(sys, w);
   const Sys& s = sys->s;
   const int n = s.n_up;
-  int off[3];
-  const int smem = init_layout(s, P, off);
-  const int off_Gd = off[0], off_aug = off[1], off_vec = off[2];
+  const InitLayout IL = init_layout(s, P);
+  const int smem = IL.bytes;
   if (is_mixed(w->precision)) {
     // M_up, M_dn by the float-float lam-GEMM into the scratch, then the rest in FP64
     const int rows = s.det.nao <= 2048 ? 8 : 4;
@@ -3362,11 +3387,11 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
     else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
     rc = launch_check((const void*)k_walker_init<float>, smem);
     if (rc) return rc;
-    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, mode | kInitMReady);
+    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, IL, mode | kInitMReady);
   } else {
     int rc = launch_check((const void*)k_walker_init<double>, smem);
     if (rc) return rc;
-    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, off_Gd, off_aug, off_vec, mode);
+    k_walker_init<double><<<w->nwalk, 128, smem, S(stream)>>>(P, IL, mode);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
@@ -3585,7 +3610,8 @@ int jqmc_batch_create(int32_t nitem, const jqmc_system* const* systems, const jq
     it.off_cand = it.P.wl.bytes;
     const int tb = tab_bytes(w);
     b->smem_sweep = std::max(b->smem_sweep, align16(it.off_cand + 2 * s.n_up * s.n_up * tb));
-    b->smem_init = std::max(b->smem_init, init_layout(s, it.P, it.off_init));
+    it.init = init_layout(s, it.P);
+    b->smem_init = std::max(b->smem_init, it.init.bytes);
     if (s.det.nao > 2048) small_ao = false;
     b->nmax_up = std::max(b->nmax_up, s.n_up);
     total += w->nwalk;
