@@ -1971,7 +1971,9 @@ constexpr int kInitJ3Table = 8;
 template <class Tab>
 __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, int mode,
                                  unsigned char* smem) {
-  const Sys s = stage_tables(P.s, P.tl, smem);
+  // the tables stay in global memory (read through L1): a few passes per
+  // walker, and the shared memory they would take keeps a third CTA off the SM
+  const Sys s = P.s;
   const int n = s.n_up, A = s.det.nao, N = s.N, A3 = s.has_j3 ? s.j3.nao : 1;
   double* r = reinterpret_cast<double*>(smem + IL.r);
   int* piv = reinterpret_cast<int*>(smem + IL.sc);
@@ -2088,8 +2090,8 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
       __syncthreads();
       // row c / pivot; columns < c of row c are zero and column c is set to the
       // unit column below, so neither is touched here
-      const double inv = 1.0 / aug[c * n2 + c];
-      for (int cc = c + 1 + threadIdx.x; cc < n2; cc += blockDim.x) aug[c * n2 + cc] *= inv;
+      const double pv = aug[c * n2 + c];
+      for (int cc = c + 1 + threadIdx.x; cc < n2; cc += blockDim.x) aug[c * n2 + cc] /= pv;
       __syncthreads();
       for (int rr = wid; rr < n; rr += nw) {
         if (rr == c) continue;
@@ -3350,13 +3352,13 @@ int jqmc_ao_vgl(const jqmc_system* sys, int32_t basis, const double* d_r, int64_
 }
 
 // shared-memory layout of the init / rebuild kernel above the work layout; returns the bytes
-// The rebuild's shared memory: the staged tables, then the positions, the
-// reduction buffer and the pivot slot, then G, [G | I] and the vectors (none of
-// the energy kernels' work buffers, so that two CTAs fit on an SM).
-static InitLayout init_layout(const Sys& s, const KParams& P) {
+// The rebuild's shared memory: the positions, the reduction buffer and the
+// pivot slot, then G, [G | I] and the vectors -- no staged tables and none of
+// the energy kernels' work buffers, so that three CTAs fit on an SM.
+static InitLayout init_layout(const Sys& s, const KParams&) {
   const int n = s.n_up, A3 = s.has_j3 ? s.j3.nao : 1;
   InitLayout L;
-  int o = P.tl.bytes;
+  int o = 0;
   L.r = o; o = align16(o + s.N * 3 * 8);
   L.red = o; o = align16(o + kRed * 8);
   L.sc = o; o = align16(o + 32 * 8);
