@@ -115,11 +115,8 @@ struct F2 {
 __device__ __forceinline__ void acc_zero(float& a) { a = 0.f; }
 __device__ __forceinline__ void acc_zero(double& a) { a = 0.0; }
 __device__ __forceinline__ void acc_zero(F2& a) { a.s = 0.f; a.c = 0.f; a.m = 0.f; }
-__device__ __forceinline__ void acc_mag(float&, float) {}
-__device__ __forceinline__ void acc_mag(double&, double) {}
+// sums of |terms| (compensated accumulators only)
 __device__ __forceinline__ void acc_mag(F2& a, float v) { a.m += v; }
-__device__ __forceinline__ float acc_mag_out(float) { return 0.f; }
-__device__ __forceinline__ float acc_mag_out(double) { return 0.f; }
 __device__ __forceinline__ float acc_mag_out(F2 a) { return warp_sum(a.m); }
 __device__ __forceinline__ void acc_fma(float& a, float x, float y) { a += x * y; }
 __device__ __forceinline__ void acc_fma(double& a, double x, double y) { a += x * y; }
