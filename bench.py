@@ -20,6 +20,14 @@ e2e   : the mixed form through the public driver API (jqmc_gb300.jqmc_gfmc.GFMC_
         sums read back to the host.
 Walker state is several GB (> L2, 129 MB), so no L2 flush is needed.
 
+Further legs in the same line (rank 0; skipped with --no-adjoint,
+--no-batching, --no-vmc):
+adjoint  : per-walker d ln psi / d theta on ring12 (8192 walkers).
+batching : 64 molecules of uneven size, mixed VMC in one CUDA graph per
+           electron-count bucket, against sequential per-molecule FP64 launches.
+vmc      : VMC on the chain (16384 walkers), mixed batched sweep with its
+           drift-control rebuild against the same sweep in FP64, same draws.
+
 --impl reference : the CPU oracle (NumPy restatement of the reference, which is
 Python/JAX and cannot run without JAX) on all host cores, one process per core,
 each projecting its own walker; a bounded sample per step.
@@ -60,6 +68,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the parameter-derivative leg")
     p.add_argument("--no-batching", action="store_true", help="skip the many-molecule leg")
+    p.add_argument("--no-vmc", action="store_true", help="skip the chain32 VMC leg (mixed vs plain FP64)")
     a = p.parse_args()
     if a.walkers is None:
         a.walkers = 16384 if a.workload == "chain32" else 8192
@@ -346,6 +355,77 @@ def batching_leg(nmol: int = 64, steps: int = 500, K: int = 50, fp64_steps: int 
                     "launches (FP64); draws resident in HBM"}
 
 
+def vmc_leg(walkers: int = 16384, K: int = 32, rounds: int = 3):
+    """VMC on the 32-nucleus chain (96 electrons, 736 AOs), the VMC half of the
+    precision workload: the mixed form (float tables, warp-parallel float
+    proposal, batched sweep of one molecule) with its drift-control rebuild
+    after every K proposals, against the same sweep in FP64 from the same
+    configurations with the same draws.  Reports walker-steps/s of
+    both, the acceptance ratios and the fraction of walkers whose paths agree."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.batching import MoleculeBatch
+    syn = synthetic.chain32()
+    mb = MoleculeBatch([syn.hamiltonian], [walkers], precision="mixed", seed=5)
+    gs = mb.systems[0]
+    bk = mb.buckets[0]
+    tuned = mb.autotune(K=4, candidates=(64, 128), reps=1)
+    mb.rebuild(True)
+    start = mb.walkers[0].r.clone()
+    draws = [mb.draws(bk, K) for _ in range(rounds + 1)]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    mb.sweep(bk, *draws[0])   # warm-up round
+    mb.rebuild(False)
+    torch.cuda.synchronize()
+    a0 = int(bk.accept.sum())
+    e0.record()
+    for i in range(1, rounds + 1):
+        mb.sweep(bk, *draws[i])
+        mb.rebuild(False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_mixed = e0.elapsed_time(e1)
+    acc_mixed = (int(bk.accept.sum()) - a0) / (rounds * K * walkers)
+    r_mixed = mb.walkers[0].r.clone()
+    state_gb = gs.walker_bytes("mixed") * walkers / 1e9
+    mb.close()
+    del mb
+    torch.cuda.empty_cache()
+    # plain FP64: the same sweep in FP64 (no energy-cache upkeep either), from the
+    # same configurations with the same draws
+    sb = MoleculeBatch([syn.hamiltonian], [walkers], precision="fp64", seed=5)
+    sk = sb.buckets[0]
+    sb.walkers[0].r.copy_(start)
+    sb.rebuild(True)
+    sb.sweep(sk, *draws[0], threads=64)   # warm-up round
+    torch.cuda.synchronize()
+    a0 = int(sk.accept.sum())
+    e0.record()
+    for i in range(1, rounds + 1):
+        sb.sweep(sk, *draws[i], threads=64)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_fp64 = e0.elapsed_time(e1)
+    acc_fp64 = (int(sk.accept.sum()) - a0) / (rounds * K * walkers)
+    same = float(((sb.walkers[0].r - r_mixed).abs().amax(dim=(1, 2)) < 1e-6).double().mean())
+    sb.close()
+    del sb, draws, start, r_mixed
+    torch.cuda.empty_cache()
+    v_mixed = walkers * K * rounds / (ms_mixed / 1e3)
+    v_fp64 = walkers * K * rounds / (ms_fp64 / 1e3)
+    return {"workload": f"VMC chain32, {walkers} walkers, {rounds} x {K} single-electron proposals, step 0.4 bohr",
+            "mixed": {"walker_steps_per_s": v_mixed, "ms": ms_mixed, "accept_ratio": acc_mixed, "walker_state_GB": state_gb,
+                      "threads": bk.threads, "autotune": {str(k): v for k, v in tuned.items()},
+                      "rebuild_every": K},
+            "plain_fp64": {"walker_steps_per_s": v_fp64, "ms": ms_fp64, "accept_ratio": acc_fp64},
+            "speedup": v_mixed / v_fp64,
+            "same_path_fraction": same,
+            "note": "CUDA events around the timed rounds; mixed rounds include the FP64-accurate drift-control "
+                    "rebuild of the float tables; draws resident in HBM"}
+
+
 def gpu_arm(a):
     import ctypes
 
@@ -510,6 +590,12 @@ def gpu_arm(a):
     torch.cuda.empty_cache()
     adjoint = adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")) if (rank == 0 and not a.no_adjoint) else None
     batching = batching_leg() if (rank == 0 and not a.no_batching) else None
+    vmc = None
+    if rank == 0 and not a.no_vmc:
+        try:
+            vmc = vmc_leg()
+        except Exception as ex:   # recorded in the line instead of ending the run
+            vmc = {"error": repr(ex)}
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 2, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
                 "jqmc_lu_rebuild_refine": 2}   # k_rebuild_m + k_walker_init
@@ -571,6 +657,7 @@ def gpu_arm(a):
                                                "avg_launch_ms": plain_ms}},
             "adjoint": adjoint,
             "batching": batching,
+            "vmc": vmc,
             "cpu_baseline": cpu_base,
             "clocks": mixed["clocks"],
         }
