@@ -185,3 +185,60 @@ def test_jackknife_force_matches_direct_evaluation():
     ref_std = np.sqrt((len(samples) - 1) * np.mean((samples - ref_mean) ** 2, axis=0))
     assert np.allclose(mean, ref_mean, rtol=1e-12, atol=1e-12)
     assert np.allclose(std, ref_std, rtol=1e-12, atol=1e-12)
+
+
+def test_entry_points_reject_invalid_arguments():
+    """Every C-ABI entry point checks its handles, pointers and sizes before any
+    CUDA call: null handles, null buffers and out-of-range sizes return
+    JQMC_E_ARG (JQMC_E_LIMIT above a compiled maximum) without a device."""
+    import ctypes as C
+
+    from jqmc_gb300 import _lib
+    from jqmc_gb300.build import build
+    build()
+    L = _lib.lib()
+    E_ARG, E_LIMIT = -1, -2
+    fake = C.c_void_p(0x100)          # never dereferenced: every call below fails its checks first
+    w = _lib.Walkers()
+    w.nwalk, w.precision = 4, _lib.PREC_FP64
+    for f in ("r", "G", "Ginv", "Tup", "Tdn", "h3", "dphi", "dphi3", "ecache", "status"):
+        setattr(w, f, fake)
+    wp = C.byref(w)
+    out = C.c_void_p()
+    flops = C.c_double()
+    calls = {
+        "jqmc_system_create(desc=NULL)": L.jqmc_system_create(None, C.byref(out)),
+        "jqmc_system_destroy(NULL)": L.jqmc_system_destroy(None),
+        "jqmc_walker_bytes(NULL)": L.jqmc_walker_bytes(None, 0),
+        "jqmc_ao_vgl(NULL)": L.jqmc_ao_vgl(None, 0, fake, 8, fake, None),
+        "jqmc_walker_init(sys=NULL)": L.jqmc_walker_init(None, wp, None),
+        "jqmc_lu_rebuild_refine(sys=NULL)": L.jqmc_lu_rebuild_refine(None, wp, None),
+        "jqmc_log_psi(sys=NULL)": L.jqmc_log_psi(None, wp, fake, fake, fake, None),
+        "jqmc_dlnpsi_dparam(sys=NULL)": L.jqmc_dlnpsi_dparam(None, wp, fake, fake, fake, None, None, None),
+        "jqmc_dlnpsi_dR(sys=NULL)": L.jqmc_dlnpsi_dR(None, wp, fake, None),
+        "jqmc_vmc_sweep(sys=NULL)": L.jqmc_vmc_sweep(None, wp, 4, fake, fake, 0.4, 0.0, fake, None),
+        "jqmc_vmc_measure(sys=NULL)": L.jqmc_vmc_measure(None, wp, fake, 0.0, fake, fake, None),
+        "jqmc_lrdmc_project(sys=NULL)": L.jqmc_lrdmc_project(None, wp, 4, fake, 0.2, 0.0, fake, None),
+        "jqmc_lrdmc_energy(sys=NULL)": L.jqmc_lrdmc_energy(None, wp, fake, 0.2, fake, fake, None),
+        "jqmc_lrdmc_project_t(sys=NULL)": L.jqmc_lrdmc_project_t(None, wp, 4, fake, 0.2, fake, fake, fake, fake, None),
+        "jqmc_walker_gather(sys=NULL)": L.jqmc_walker_gather(None, wp, wp, fake, None),
+        "jqmc_branch_comb(nwalk=0)": L.jqmc_branch_comb(0, fake, 0.5, fake, fake, None),
+        "jqmc_branch_comb(zeta=1)": L.jqmc_branch_comb(8, fake, 1.0, fake, fake, None),
+        "jqmc_branch_comb(w=NULL)": L.jqmc_branch_comb(8, None, 0.5, fake, fake, None),
+        "jqmc_branch_comb_noalloc(nwalk=0)": L.jqmc_branch_comb_noalloc(0, fake, 0.5, fake, None),
+        "jqmc_probe_fp64(iters=0)": L.jqmc_probe_fp64(0, 1, fake, C.byref(flops), None),
+        "jqmc_probe_fp32(blocks=0)": L.jqmc_probe_fp32(10, 0, fake, C.byref(flops), None),
+        "jqmc_batch_create(nitem=0)": L.jqmc_batch_create(0, None, None, C.byref(out)),
+        "jqmc_batch_destroy(NULL)": L.jqmc_batch_destroy(None),
+        "jqmc_batch_walkers(NULL)": L.jqmc_batch_walkers(None),
+        "jqmc_vmc_sweep_batch(NULL)": L.jqmc_vmc_sweep_batch(None, 4, fake, fake, 0.4, 0.0, fake, 64, 0, None),
+        "jqmc_vmc_sweep_batch(threads=33)": L.jqmc_vmc_sweep_batch(fake, 4, fake, fake, 0.4, 0.0, fake, 33, 0, None),
+        "jqmc_batch_rebuild(NULL)": L.jqmc_batch_rebuild(None, 0, None),
+    }
+    bad = {k: v for k, v in calls.items() if v != E_ARG}
+    assert not bad, bad
+    # above the no-allocation comb's compiled maximum
+    assert L.jqmc_branch_comb_noalloc(262145, fake, 0.5, fake, None) == E_LIMIT
+    # every declared entry point is exercised above
+    tested = {k.split("(")[0] for k in calls}
+    assert tested == set(_lib.EXPORTED)
