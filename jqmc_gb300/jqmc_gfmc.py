@@ -32,13 +32,25 @@ from .statistics import gfmc_G_L, jackknife_energy
 from ._init_config import initial_electrons
 
 
+def _check_lrdmc_options(non_local_move: str, comput_position_deriv: bool) -> None:
+    if non_local_move != "tmove":
+        raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+    if comput_position_deriv:
+        raise NotImplementedError("LRDMC forces (comput_position_deriv) are not on the GPU path; "
+                                  "MCMC(comput_position_deriv=True) gives VMC forces")
+
+
 class GFMC_n:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, num_walkers: int = 40, num_mcmc_per_measurement: int = 16,
-                 mcmc_seed: int = 34467, E_scf: float = 0.0, alat: float = 0.1, random_discretized_mesh: bool = True,
-                 non_local_move: str = "tmove", num_gfmc_collect_steps: int = 5, Nv: int = 6,
-                 init_r_up=None, init_r_dn=None, rebuild_after_branching: bool = True, precision: str = "fp64"):
-        if non_local_move != "tmove":
-            raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+                 num_gfmc_collect_steps: int = 5, mcmc_seed: int = 34467, E_scf: float = 0.0, alat: float = 0.1,
+                 random_discretized_mesh: bool = True, non_local_move: str = "tmove", comput_position_deriv: bool = False,
+                 epsilon_PW: float = 0.0, use_swct: bool = False, Nv: int = 6, init_r_up=None, init_r_dn=None,
+                 rebuild_after_branching: bool = True, precision: str = "fp64"):
+        """The reference's GFMC_n (jqmc_gfmc.py:4222-4236) on the GPU path, with the
+        same arguments in the same order, then Nv, initial electrons, the rebuild
+        switch and the precision form.  LRDMC forces (comput_position_deriv) are
+        refused; epsilon_PW and use_swct only act on them."""
+        _check_lrdmc_options(non_local_move, comput_position_deriv)
         hamiltonian_data.sanity_check()
         self.hamiltonian_data = hamiltonian_data
         self.num_walkers = num_walkers
@@ -143,10 +155,13 @@ class GFMC_t:
 
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, num_walkers: int = 40, num_gfmc_collect_steps: int = 5,
                  mcmc_seed: int = 34467, tau: float = 0.1, alat: float = 0.1, random_discretized_mesh: bool = True,
-                 non_local_move: str = "tmove", Nv: int = 6, init_r_up=None, init_r_dn=None, precision: str = "fp64",
+                 non_local_move: str = "tmove", comput_position_deriv: bool = False, epsilon_PW: float = 0.0,
+                 use_swct: bool = False, Nv: int = 6, init_r_up=None, init_r_dn=None, precision: str = "fp64",
                  draws_per_call: int = 64, max_calls: int = 10000):
-        if non_local_move != "tmove":
-            raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+        """The reference's GFMC_t (jqmc_gfmc.py:208-221) on the GPU path, with the
+        same arguments in the same order, then Nv, initial electrons, the
+        precision form and the draw batching.  LRDMC forces are refused."""
+        _check_lrdmc_options(non_local_move, comput_position_deriv)
         if not tau > 0.0:
             raise ValueError("tau must be positive")
         hamiltonian_data.sanity_check()

@@ -31,17 +31,26 @@ from ._init_config import initial_electrons
 
 class MCMC:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, mcmc_seed: int = 34467, num_walkers: int = 40,
-                 num_mcmc_per_measurement: int = 16, Dt: float = 2.0, epsilon_AS: float = 1e-1, Nv: int = 6,
-                 init_r_up=None, init_r_dn=None, comput_log_WF_param_deriv: bool = False,
-                 comput_position_deriv: bool = False, use_swct: bool = False, force_fd_step: float = 5e-4):
+                 num_mcmc_per_measurement: int = 16, Dt: float = 2.0, epsilon_AS: float = 1e-1,
+                 comput_log_WF_param_deriv: bool = False, comput_e_L_param_deriv: bool = False,
+                 comput_position_deriv: bool = False, random_discretized_mesh: bool = True, use_swct: bool = False,
+                 Nv: int = 6, init_r_up=None, init_r_dn=None, force_fd_step: float = 5e-4):
+        """The reference's MCMC driver (jqmc_mcmc.py:129-143) on the GPU path, with
+        the same arguments in the same order, then Nv (quadrature points), initial
+        electrons and the finite-difference step of dE_L/dR.  Differences: use_swct
+        defaults to False and True is refused with forces (the space-warp
+        transformation is not built); comput_e_L_param_deriv=True is refused."""
         if comput_position_deriv and use_swct:
             raise NotImplementedError("the space-warp coordinate transformation of the forces is not on the GPU path")
+        if comput_e_L_param_deriv:
+            raise NotImplementedError("d e_L / d c (comput_e_L_param_deriv) is not on the GPU path")
         hamiltonian_data.sanity_check()
         self.hamiltonian_data = hamiltonian_data
         self.num_walkers = num_walkers
         self.num_mcmc_per_measurement = num_mcmc_per_measurement
         self.Dt = Dt
         self.epsilon_AS = epsilon_AS
+        self.random_discretized_mesh = random_discretized_mesh
         self.sys = GpuSystem(hamiltonian_data, Nv=Nv)
         if init_r_up is None:
             st = hamiltonian_data.structure_data
@@ -75,6 +84,8 @@ class MCMC:
         fdraw = torch.stack([torch.randn((W, K), generator=g, dtype=torch.float64, device=dev),
                              torch.rand((W, K), generator=g, dtype=torch.float64, device=dev)], dim=-1).contiguous()
         angles = (torch.rand((W, 3), generator=g, dtype=torch.float64, device=dev) * (4.0 * math.pi) - 2.0 * math.pi)
+        if not self.random_discretized_mesh:   # identity rotations (jqmc_mcmc.py:724-727)
+            angles.zero_()
         return idraw, fdraw, angles
 
     def run_block(self, idraw, fdraw, angles):

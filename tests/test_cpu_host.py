@@ -242,3 +242,36 @@ def test_entry_points_reject_invalid_arguments():
     # every declared entry point is exercised above
     tested = {k.split("(")[0] for k in calls}
     assert tested == set(_lib.EXPORTED)
+
+
+def test_drivers_keep_the_reference_signatures_and_refuse_unsupported_options():
+    """MCMC / GFMC_n / GFMC_t take the reference's arguments in the reference's
+    order (jqmc/jqmc_mcmc.py:129-143, jqmc/jqmc_gfmc.py:4222-4236 and :208-221),
+    and refuse the options that are not on the GPU path before touching a GPU."""
+    import inspect
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.jqmc_gfmc import GFMC_n, GFMC_t
+    from jqmc_gb300.jqmc_mcmc import MCMC
+    ref = {
+        MCMC: ["hamiltonian_data", "mcmc_seed", "num_walkers", "num_mcmc_per_measurement", "Dt", "epsilon_AS",
+               "comput_log_WF_param_deriv", "comput_e_L_param_deriv", "comput_position_deriv",
+               "random_discretized_mesh", "use_swct"],
+        GFMC_n: ["hamiltonian_data", "num_walkers", "num_mcmc_per_measurement", "num_gfmc_collect_steps", "mcmc_seed",
+                 "E_scf", "alat", "random_discretized_mesh", "non_local_move", "comput_position_deriv", "epsilon_PW",
+                 "use_swct"],
+        GFMC_t: ["hamiltonian_data", "num_walkers", "num_gfmc_collect_steps", "mcmc_seed", "tau", "alat",
+                 "random_discretized_mesh", "non_local_move", "comput_position_deriv", "epsilon_PW", "use_swct"],
+    }
+    for cls, names in ref.items():
+        params = list(inspect.signature(cls.__init__).parameters)[1:]
+        assert params[:len(names)] == names, cls.__name__
+    h = synthetic.water_like().hamiltonian
+    with pytest.raises(NotImplementedError):
+        MCMC(h, comput_e_L_param_deriv=True)
+    with pytest.raises(NotImplementedError):
+        MCMC(h, comput_position_deriv=True, use_swct=True)
+    with pytest.raises(NotImplementedError):
+        GFMC_n(h, comput_position_deriv=True)
+    with pytest.raises(NotImplementedError):
+        GFMC_t(h, non_local_move="dltmove")
