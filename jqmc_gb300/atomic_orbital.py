@@ -103,3 +103,30 @@ class AOs_sphe_data:
                     continue
             shells.append({"atom": atom, "l": l, "exps": e, "coefs": c, "aos": [ao], "ms": [m]})
         return shells
+
+
+# ---------------------------------------------------------------- evaluation (GPU, jqmc_ao_vgl)
+def compute_AOs(aos_data: AOs_sphe_data, r_carts) -> np.ndarray:
+    """AO values (num_ao, N) at r_carts (N, 3) (jqmc/atomic_orbital.py:1886)."""
+    from . import surface
+    return surface.as_numpy(surface.ao_vgl(aos_data, r_carts)[0])
+
+
+def compute_AOs_grad(aos_data: AOs_sphe_data, r_carts):
+    """(d/dx, d/dy, d/dz) of the AOs, each (num_ao, N) (jqmc/atomic_orbital.py:3346)."""
+    from . import surface
+    t = surface.as_numpy(surface.ao_vgl(aos_data, r_carts))
+    return t[1], t[2], t[3]
+
+
+def compute_AOs_laplacian(aos_data: AOs_sphe_data, r_carts) -> np.ndarray:
+    """Laplacians of the AOs (num_ao, N) (jqmc/atomic_orbital.py:2989)."""
+    from . import surface
+    return surface.as_numpy(surface.ao_vgl(aos_data, r_carts)[4])
+
+
+def compute_AOs_value_grad_lap(aos_data: AOs_sphe_data, r_carts):
+    """(val, gx, gy, gz, lap), each (num_ao, N) (jqmc/atomic_orbital.py:3594)."""
+    from . import surface
+    t = surface.as_numpy(surface.ao_vgl(aos_data, r_carts))
+    return t[0], t[1], t[2], t[3], t[4]

@@ -65,3 +65,26 @@ class Geminal_data:
             cd = dn.mo_coefficients
             return up.aos_data, cu.T @ lp @ cd, cu.T @ lu
         return up, lp, lu
+
+
+# ---------------------------------------------------------------- evaluation (GPU: walker initialisation + jqmc_log_psi)
+def compute_geminal_all_elements(geminal_data: Geminal_data, r_up_carts, r_dn_carts) -> np.ndarray:
+    """The geminal matrix G (n_up, n_dn) (jqmc/determinant.py:1336); (W, n_up, n_dn) for (W, n, 3) inputs."""
+    from . import surface
+    _, _, G, single = surface.geminal_log_det(geminal_data, r_up_carts, r_dn_carts)
+    g = surface.as_numpy(G)
+    return g[0] if single else g
+
+
+def compute_ln_det_geminal_all_elements(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
+    """ln|det G| (jqmc/determinant.py:1028)."""
+    from . import surface
+    ld, _, _, single = surface.geminal_log_det(geminal_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(ld, single)
+
+
+def compute_det_geminal_all_elements(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
+    """det G (jqmc/determinant.py:1186)."""
+    from . import surface
+    ld, sg, _, single = surface.geminal_log_det(geminal_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(sg * ld.exp(), single)

@@ -62,80 +62,89 @@ def _ion_ion(pos, z):
     return e
 
 
+def system_desc(ham: Hamiltonian_data, Nv: int = 6):
+    """(jqmc_system_desc, arrays it points into, sizes) for one Hamiltonian_data
+    (jqmc/hamiltonians.py:83); the arrays must outlive the descriptor."""
+    ham.sanity_check()
+    st = ham.structure_data
+    g = ham.wavefunction_data.geminal_data
+    if g.num_electron_up != g.num_electron_dn:
+        raise NotImplementedError("open-shell geminals (N_up != N_dn) are not supported by the walker kernels")
+    n_up, n_dn = g.num_electron_up, g.num_electron_dn
+    aos, lam_p, _ = g.ao_basis_lambda()
+    keep = {}
+    keep["pos"] = np.ascontiguousarray(st.positions, dtype=np.float64)
+    coul = ham.coulomb_potential_data
+    keep["zeff"] = np.ascontiguousarray(coul.effective_charges, dtype=np.float64)
+    keep["dsh"], keep["dpr"] = pack_basis(aos)
+    keep["lam"] = np.ascontiguousarray(lam_p, dtype=np.float64)
+    A = aos.num_ao
+    jd = ham.wavefunction_data.jastrow_data
+    d = _lib.SystemDesc()
+    d.natom, d.n_up, d.n_dn = st.natom, n_up, n_dn
+    d.atom_pos = _ptr(keep["pos"], C.c_double)
+    d.atom_zeff = _ptr(keep["zeff"], C.c_double)
+    d.det = _lib.BasisDesc(len(keep["dsh"]), A, len(keep["dpr"]), _ptr(keep["dsh"], C.c_int32), _ptr(keep["dpr"], C.c_double))
+    d.lambda_ = _ptr(keep["lam"], C.c_double)
+    j1 = jd.jastrow_one_body_data
+    if j1 is not None:
+        keep["j1z"] = np.ascontiguousarray(j1.effective_charges, dtype=np.float64)
+        d.has_j1, d.j1_type, d.j1_param = 1, {"exp": 0, "pade": 1}[j1.jastrow_1b_type], float(j1.jastrow_1b_param)
+        d.j1_zeff = _ptr(keep["j1z"], C.c_double)
+    j2 = jd.jastrow_two_body_data
+    if j2 is not None:
+        d.has_j2, d.j2_type, d.j2_param = 1, {"pade": 0, "exp": 1}[j2.jastrow_2b_type], float(j2.jastrow_2b_param)
+    j3 = jd.jastrow_three_body_data
+    A3 = 0
+    if j3 is not None:
+        keep["jsh"], keep["jpr"] = pack_basis(j3.orb_data)
+        keep["j3m"] = np.ascontiguousarray(j3.j_matrix, dtype=np.float64)
+        A3 = j3.orb_num
+        d.has_j3 = 1
+        d.j3 = _lib.BasisDesc(len(keep["jsh"]), A3, len(keep["jpr"]), _ptr(keep["jsh"], C.c_int32), _ptr(keep["jpr"], C.c_double))
+        d.j3_matrix = _ptr(keep["j3m"], C.c_double)
+    if coul.ecp_flag:
+        M = st.natom
+        chan = np.zeros((M, _lib.ECP_SLOTS, 2), dtype=np.int32)
+        terms = []
+        for atom in range(M):
+            for slot in range(_lib.ECP_SLOTS):
+                chan[atom, slot, 0] = len(terms)
+                for (a, l, ex, co, pw) in zip(coul.nucleus_index, coul.ang_moms, coul.exponents, coul.coefficients, coul.powers):
+                    if a == atom and l == slot and co != 0.0:
+                        terms.append((co, pw, ex))
+                chan[atom, slot, 1] = len(terms) - chan[atom, slot, 0]
+        keep["maxl1"] = np.ascontiguousarray(coul.max_ang_mom_plus_1, dtype=np.int32)
+        keep["chan"] = np.ascontiguousarray(chan)
+        keep["terms"] = np.ascontiguousarray(np.array(terms, dtype=np.float64).reshape(-1, 3))
+        w, pts = ECP_MESHES[Nv]
+        keep["mw"] = np.ascontiguousarray(w, dtype=np.float64)
+        keep["mp"] = np.ascontiguousarray(pts, dtype=np.float64)
+        d.ecp_flag = 1
+        d.ecp_maxl1 = _ptr(keep["maxl1"], C.c_int32)
+        d.ecp_chan = _ptr(keep["chan"], C.c_int32)
+        d.ecp_nterm = len(keep["terms"])
+        d.ecp_terms = _ptr(keep["terms"], C.c_double)
+        d.nv = Nv
+        d.mesh_points = _ptr(keep["mp"], C.c_double)
+        d.mesh_weights = _ptr(keep["mw"], C.c_double)
+    d.ion_ion = _ion_ion(keep["pos"], keep["zeff"])
+    return d, keep, {"n_up": n_up, "n_dn": n_dn, "A": A, "A3": A3}
+
+
 class GpuSystem:
     """Device copy of one Hamiltonian_data (jqmc/hamiltonians.py:83) for the walker kernels."""
 
     def __init__(self, ham: Hamiltonian_data, Nv: int = 6, device: int | None = None):
         if not torch.cuda.is_available():
             raise _lib.JqmcError("no CUDA device: the walker path runs only on the GPU")
-        ham.sanity_check()
         self.ham = ham
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         L = _lib.lib()
-        st = ham.structure_data
-        g = ham.wavefunction_data.geminal_data
-        if g.num_electron_up != g.num_electron_dn:
-            raise NotImplementedError("open-shell geminals (N_up != N_dn) are not supported by the walker kernels")
-        self.n_up, self.n_dn = g.num_electron_up, g.num_electron_dn
+        d, keep, info = system_desc(ham, Nv)
+        self.n_up, self.n_dn = info["n_up"], info["n_dn"]
         self.N = self.n_up + self.n_dn
-        aos, lam_p, _ = g.ao_basis_lambda()
-        keep = {}
-        keep["pos"] = np.ascontiguousarray(st.positions, dtype=np.float64)
-        coul = ham.coulomb_potential_data
-        keep["zeff"] = np.ascontiguousarray(coul.effective_charges, dtype=np.float64)
-        keep["dsh"], keep["dpr"] = pack_basis(aos)
-        keep["lam"] = np.ascontiguousarray(lam_p, dtype=np.float64)
-        self.A = aos.num_ao
-        jd = ham.wavefunction_data.jastrow_data
-        d = _lib.SystemDesc()
-        d.natom, d.n_up, d.n_dn = st.natom, self.n_up, self.n_dn
-        d.atom_pos = _ptr(keep["pos"], C.c_double)
-        d.atom_zeff = _ptr(keep["zeff"], C.c_double)
-        d.det = _lib.BasisDesc(len(keep["dsh"]), self.A, len(keep["dpr"]), _ptr(keep["dsh"], C.c_int32), _ptr(keep["dpr"], C.c_double))
-        d.lambda_ = _ptr(keep["lam"], C.c_double)
-        j1 = jd.jastrow_one_body_data
-        if j1 is not None:
-            keep["j1z"] = np.ascontiguousarray(j1.effective_charges, dtype=np.float64)
-            d.has_j1, d.j1_type, d.j1_param = 1, {"exp": 0, "pade": 1}[j1.jastrow_1b_type], float(j1.jastrow_1b_param)
-            d.j1_zeff = _ptr(keep["j1z"], C.c_double)
-        j2 = jd.jastrow_two_body_data
-        if j2 is not None:
-            d.has_j2, d.j2_type, d.j2_param = 1, {"pade": 0, "exp": 1}[j2.jastrow_2b_type], float(j2.jastrow_2b_param)
-        j3 = jd.jastrow_three_body_data
-        self.A3 = 0
-        if j3 is not None:
-            keep["jsh"], keep["jpr"] = pack_basis(j3.orb_data)
-            keep["j3m"] = np.ascontiguousarray(j3.j_matrix, dtype=np.float64)
-            self.A3 = j3.orb_num
-            d.has_j3 = 1
-            d.j3 = _lib.BasisDesc(len(keep["jsh"]), self.A3, len(keep["jpr"]), _ptr(keep["jsh"], C.c_int32), _ptr(keep["jpr"], C.c_double))
-            d.j3_matrix = _ptr(keep["j3m"], C.c_double)
-        if coul.ecp_flag:
-            M = st.natom
-            chan = np.zeros((M, _lib.ECP_SLOTS, 2), dtype=np.int32)
-            terms = []
-            for atom in range(M):
-                for slot in range(_lib.ECP_SLOTS):
-                    chan[atom, slot, 0] = len(terms)
-                    for (a, l, ex, co, pw) in zip(coul.nucleus_index, coul.ang_moms, coul.exponents, coul.coefficients, coul.powers):
-                        if a == atom and l == slot and co != 0.0:
-                            terms.append((co, pw, ex))
-                    chan[atom, slot, 1] = len(terms) - chan[atom, slot, 0]
-            keep["maxl1"] = np.ascontiguousarray(coul.max_ang_mom_plus_1, dtype=np.int32)
-            keep["chan"] = np.ascontiguousarray(chan)
-            keep["terms"] = np.ascontiguousarray(np.array(terms, dtype=np.float64).reshape(-1, 3))
-            w, pts = ECP_MESHES[Nv]
-            keep["mw"] = np.ascontiguousarray(w, dtype=np.float64)
-            keep["mp"] = np.ascontiguousarray(pts, dtype=np.float64)
-            d.ecp_flag = 1
-            d.ecp_maxl1 = _ptr(keep["maxl1"], C.c_int32)
-            d.ecp_chan = _ptr(keep["chan"], C.c_int32)
-            d.ecp_nterm = len(keep["terms"])
-            d.ecp_terms = _ptr(keep["terms"], C.c_double)
-            d.nv = Nv
-            d.mesh_points = _ptr(keep["mp"], C.c_double)
-            d.mesh_weights = _ptr(keep["mw"], C.c_double)
-        d.ion_ion = _ion_ion(keep["pos"], keep["zeff"])
+        self.A, self.A3 = info["A"], info["A3"]
         self.ion_ion = d.ion_ion
         self.Nv = Nv
         handle = C.c_void_p()

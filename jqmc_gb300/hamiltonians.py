@@ -19,3 +19,12 @@ class Hamiltonian_data:
         self.structure_data.sanity_check()
         self.coulomb_potential_data.sanity_check()
         self.wavefunction_data.sanity_check()
+
+
+# ---------------------------------------------------------------- evaluation (GPU: walker initialisation + jqmc_vmc_measure)
+def compute_local_energy(hamiltonian_data: Hamiltonian_data, r_up_carts, r_dn_carts, RT):
+    """E_L with the non-local ECP quadrature rotated by RT (jqmc/hamiltonians.py:179);
+    RT (3, 3) or one per configuration (W, 3, 3)."""
+    from . import surface
+    eL, single = surface.local_energy(hamiltonian_data, r_up_carts, r_dn_carts, RT)
+    return surface.scalar_or_array(eL, single)

@@ -85,3 +85,35 @@ class Jastrow_data:
         for part in (self.jastrow_one_body_data, self.jastrow_two_body_data, self.jastrow_three_body_data):
             if part is not None:
                 part.sanity_check()
+
+
+# ---------------------------------------------------------------- evaluation (GPU: jqmc_log_psi's Jastrow output)
+def compute_Jastrow_part(jastrow_data: Jastrow_data, r_up_carts, r_dn_carts):
+    """J = J1 + J2 + J3, without exp (jqmc/jastrow_factor.py:2127)."""
+    from . import surface
+    jj, single = surface.jastrow_value(jastrow_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(jj, single)
+
+
+def compute_Jastrow_one_body(jastrow_one_body_data: Jastrow_one_body_data, r_up_carts, r_dn_carts):
+    """J1 without exp (jqmc/jastrow_factor.py:649)."""
+    from . import surface
+    jj, single = surface.jastrow_value(Jastrow_data(jastrow_one_body_data=jastrow_one_body_data), r_up_carts, r_dn_carts,
+                                       key_obj=jastrow_one_body_data)
+    return surface.scalar_or_array(jj, single)
+
+
+def compute_Jastrow_two_body(jastrow_two_body_data: Jastrow_two_body_data, r_up_carts, r_dn_carts):
+    """J2 without exp (jqmc/jastrow_factor.py:1181)."""
+    from . import surface
+    jj, single = surface.jastrow_value(Jastrow_data(jastrow_two_body_data=jastrow_two_body_data), r_up_carts, r_dn_carts,
+                                       key_obj=jastrow_two_body_data)
+    return surface.scalar_or_array(jj, single)
+
+
+def compute_Jastrow_three_body(jastrow_three_body_data: Jastrow_three_body_data, r_up_carts, r_dn_carts):
+    """J3 without exp (jqmc/jastrow_factor.py:1744)."""
+    from . import surface
+    jj, single = surface.jastrow_value(Jastrow_data(jastrow_three_body_data=jastrow_three_body_data), r_up_carts,
+                                       r_dn_carts, key_obj=jastrow_three_body_data)
+    return surface.scalar_or_array(jj, single)

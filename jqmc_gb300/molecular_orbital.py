@@ -35,3 +35,30 @@ class MOs_data:
         if self.mo_coefficients.shape != (self.num_mo, self.aos_data.num_ao):
             raise ValueError(f"mo_coefficients.shape={self.mo_coefficients.shape} != ({self.num_mo}, {self.aos_data.num_ao})")
         self.aos_data.sanity_check()
+
+
+# ---------------------------------------------------------------- evaluation (GPU: AO tables, then C x AO)
+def compute_MOs(mos_data: MOs_data, r_carts) -> np.ndarray:
+    """MO values (num_mo, N) at r_carts (N, 3) (jqmc/molecular_orbital.py:240)."""
+    from . import surface
+    return surface.as_numpy(surface.mo_vgl(mos_data, r_carts)[0])
+
+
+def compute_MOs_grad(mos_data: MOs_data, r_carts):
+    """(d/dx, d/dy, d/dz) of the MOs, each (num_mo, N) (jqmc/molecular_orbital.py)."""
+    from . import surface
+    t = surface.as_numpy(surface.mo_vgl(mos_data, r_carts))
+    return t[1], t[2], t[3]
+
+
+def compute_MOs_laplacian(mos_data: MOs_data, r_carts) -> np.ndarray:
+    """Laplacians of the MOs (num_mo, N) (jqmc/molecular_orbital.py)."""
+    from . import surface
+    return surface.as_numpy(surface.mo_vgl(mos_data, r_carts)[4])
+
+
+def compute_MOs_value_grad_lap(mos_data: MOs_data, r_carts):
+    """(val, gx, gy, gz, lap) of the MOs, each (num_mo, N) (jqmc/molecular_orbital.py)."""
+    from . import surface
+    t = surface.as_numpy(surface.mo_vgl(mos_data, r_carts))
+    return t[0], t[1], t[2], t[3], t[4]

@@ -1,0 +1,237 @@
+"""The reference's module-level evaluation functions on the GPU path.
+
+jqmc exposes per-configuration functions beside its drivers:
+- jqmc.atomic_orbital.compute_AOs*, jqmc.molecular_orbital.compute_MOs*;
+- jqmc.determinant.compute_*geminal_all_elements;
+- jqmc.jastrow_factor.compute_Jastrow_*;
+- jqmc.wavefunction.evaluate_* and compute_kinetic_energy;
+- jqmc.hamiltonians.compute_local_energy.
+
+The modules of this package keep those names, and this file holds their
+bodies.  Each call runs the walker kernels on a device copy of the data object
+it receives (cached per object), with the configurations as walkers:
+- r_up_carts (n_up, 3) gives a Python float, as the reference returns;
+- (W, n_up, 3) gives an array over the W configurations.
+
+AO and MO tables take points (..., 3) and return (num_orb, ...).
+
+The kernels need a whole Hamiltonian, so partial objects are completed:
+- nuclear charges of zero and no ECP where only the wavefunction matters;
+- a stand-in geminal of s functions where only the Jastrow factor matters (its
+  determinant outputs are not read);
+- an identity pairing matrix over the AO set whose tables are asked for.
+
+There is no CPU evaluation: without the built library or a CUDA device these
+raise, like the drivers.
+"""
+
+from __future__ import annotations
+
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from .atomic_orbital import AOs_sphe_data
+from .coulomb_potential import Coulomb_potential_data
+from .determinant import Geminal_data
+from .engine import GpuSystem, WalkerSet
+from .hamiltonians import Hamiltonian_data
+from .jastrow_factor import Jastrow_data
+from .molecular_orbital import MOs_data
+from .structure import Structure_data
+from .wavefunction import Wavefunction_data
+
+_CACHE_SIZE = 8
+_cache: OrderedDict = OrderedDict()   # id(data object) -> (data object, GpuSystem)
+
+
+def _system(obj, build) -> GpuSystem:
+    """The device copy for ``obj`` (built by ``build()`` into a Hamiltonian on first use)."""
+    hit = _cache.get(id(obj))
+    if hit is not None and hit[0] is obj:
+        _cache.move_to_end(id(obj))
+        return hit[1]
+    gs = GpuSystem(build())
+    _cache[id(obj)] = (obj, gs)
+    while len(_cache) > _CACHE_SIZE:
+        _cache.popitem(last=False)
+    return gs
+
+
+def _no_charges(st: Structure_data) -> Coulomb_potential_data:
+    bare = Structure_data(positions=st.positions, atomic_numbers=(0,) * st.natom,
+                          element_symbols=st.element_symbols, atomic_labels=st.atomic_labels)
+    return Coulomb_potential_data(structure_data=bare, ecp_flag=False)
+
+
+def _structure_of(orb) -> Structure_data:
+    return orb.aos_data.structure_data if isinstance(orb, MOs_data) else orb.structure_data
+
+
+def _ham_for_aos(aos: AOs_sphe_data) -> Hamiltonian_data:
+    st = aos.structure_data
+    gem = Geminal_data(num_electron_up=1, num_electron_dn=1, orb_data_up_spin=aos, orb_data_dn_spin=aos,
+                       lambda_matrix=np.eye(aos.num_ao))
+    return Hamiltonian_data(structure_data=st, coulomb_potential_data=_no_charges(st),
+                            wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=gem))
+
+
+def _ham_for_wavefunction(wf: Wavefunction_data) -> Hamiltonian_data:
+    st = _structure_of(wf.geminal_data.orb_data_up_spin)
+    return Hamiltonian_data(structure_data=st, coulomb_potential_data=_no_charges(st), wavefunction_data=wf)
+
+
+def _ham_for_jastrow(jd: Jastrow_data, n_up: int, n_dn: int) -> Hamiltonian_data:
+    if jd.jastrow_one_body_data is not None:
+        st = jd.jastrow_one_body_data.structure_data
+    elif jd.jastrow_three_body_data is not None:
+        st = jd.jastrow_three_body_data.orb_data.structure_data
+    else:
+        st = Structure_data(positions=np.zeros((1, 3)), atomic_numbers=(0,))
+    # n_up s functions on nucleus 0 (the geminal needs at least n_up AOs); its
+    # determinant outputs are not read, and the J outputs do not depend on it
+    s_set = AOs_sphe_data(structure_data=st, nucleus_index=(0,) * n_up, num_ao=n_up, num_ao_prim=n_up,
+                          orbital_indices=tuple(range(n_up)), exponents=np.ones(n_up), coefficients=np.ones(n_up),
+                          angular_momentums=(0,) * n_up, magnetic_quantum_numbers=(0,) * n_up)
+    gem = Geminal_data(num_electron_up=n_up, num_electron_dn=n_dn, orb_data_up_spin=s_set, orb_data_dn_spin=s_set,
+                       lambda_matrix=np.eye(n_up, 2 * n_up - n_dn))
+    return Hamiltonian_data(structure_data=st, coulomb_potential_data=_no_charges(st),
+                            wavefunction_data=Wavefunction_data(jastrow_data=jd, geminal_data=gem))
+
+
+def _configs(r_up_carts, r_dn_carts):
+    """(r_up (W, n_up, 3), r_dn (W, n_dn, 3), single configuration?)"""
+    r_up = np.asarray(r_up_carts, dtype=np.float64)
+    r_dn = np.asarray(r_dn_carts, dtype=np.float64)
+    single = r_up.ndim == 2
+    if single:
+        r_up, r_dn = r_up[None], r_dn[None]
+    if r_up.ndim != 3 or r_dn.ndim != 3 or r_up.shape[-1] != 3 or r_dn.shape[-1] != 3 or r_up.shape[0] != r_dn.shape[0]:
+        raise ValueError(f"electron coordinates must be (n, 3) or (W, n, 3); got {r_up.shape} and {r_dn.shape}")
+    return r_up, r_dn, single
+
+
+def _walkers(gs: GpuSystem, r_up: np.ndarray, r_dn: np.ndarray) -> WalkerSet:
+    if r_up.shape[1] != gs.n_up or r_dn.shape[1] != gs.n_dn:
+        raise ValueError(f"expected {gs.n_up} up and {gs.n_dn} down electrons; got {r_up.shape[1]} and {r_dn.shape[1]}")
+    return WalkerSet(gs, r_up, r_dn, precision="fp64")
+
+
+def _out(t: torch.Tensor, single: bool):
+    a = t.detach().cpu().numpy()
+    return float(a[0]) if single else a
+
+
+# ---------------------------------------------------------------- AO / MO tables
+def ao_vgl(aos: AOs_sphe_data, r_carts) -> torch.Tensor:
+    """(5, num_ao, ...) value, d/dx, d/dy, d/dz, Laplacian at points (..., 3), on the device."""
+    gs = _system(aos, lambda: _ham_for_aos(aos))
+    r = np.asarray(r_carts, dtype=np.float64)
+    if r.shape[-1] != 3:
+        raise ValueError(f"points must be (..., 3); got {r.shape}")
+    lead = r.shape[:-1]
+    out = gs.ao_vgl(torch.as_tensor(r.reshape(-1, 3)), basis=0)
+    return out.reshape(5, aos.num_ao, *lead)
+
+
+def mo_vgl(mos: MOs_data, r_carts) -> torch.Tensor:
+    """(5, num_mo, ...) MO value, gradient and Laplacian: C times the AO tables."""
+    t = ao_vgl(mos.aos_data, r_carts)
+    c = torch.as_tensor(np.asarray(mos.mo_coefficients, dtype=np.float64), device=t.device)
+    return torch.einsum("ma,ka...->km...", c, t)
+
+
+def as_numpy(t: torch.Tensor) -> np.ndarray:
+    return t.detach().cpu().numpy()
+
+
+# ---------------------------------------------------------------- determinant and wavefunction
+def geminal_log_det(geminal: Geminal_data, r_up_carts, r_dn_carts):
+    """(ln|det G|, sign det G, G) for each configuration (walker initialisation + jqmc_log_psi)."""
+    wf = Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=geminal)
+    gs = _system(geminal, lambda: _ham_for_wavefunction(wf))
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    ws = _walkers(gs, r_up, r_dn)
+    ld, sg, _ = ws.log_psi()
+    return ld, sg, ws.G, single
+
+
+def wavefunction_parts(wf: Wavefunction_data, r_up_carts, r_dn_carts):
+    """(ln|det G|, sign, J) for each configuration."""
+    gs = _system(wf, lambda: _ham_for_wavefunction(wf))
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    ld, sg, jj = _walkers(gs, r_up, r_dn).log_psi()
+    return ld, sg, jj, single
+
+
+def jastrow_value(jd: Jastrow_data, r_up_carts, r_dn_carts, key_obj=None):
+    """J (without exp) for each configuration; the device copy is cached on
+    ``key_obj`` (the caller's data object; default ``jd``)."""
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    n_up, n_dn = r_up.shape[1], r_dn.shape[1]
+    owner = jd if key_obj is None else key_obj
+    key = (id(owner), n_up, n_dn)
+    hit = _cache.get(key)
+    if hit is not None and hit[0] is owner:
+        _cache.move_to_end(key)
+        gs = hit[1]
+    else:
+        gs = GpuSystem(_ham_for_jastrow(jd, n_up, n_dn))
+        _cache[key] = (owner, gs)
+        while len(_cache) > _CACHE_SIZE:
+            _cache.popitem(last=False)
+    _, _, jj = _walkers(gs, r_up, r_dn).log_psi()
+    return jj, single
+
+
+def kinetic_energy(wf: Wavefunction_data, r_up_carts, r_dn_carts):
+    """-1/2 sum_i lap_i psi / psi: the local energy of the wavefunction with no
+    nuclear charges and no ECP, less the electron-electron repulsion."""
+    gs = _system(wf, lambda: _ham_for_wavefunction(wf))
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    ws = _walkers(gs, r_up, r_dn)
+    angles = torch.zeros((ws.nwalk, 3), dtype=torch.float64, device=gs.device)
+    eL, _ = ws.vmc_measure(angles, 0.0)
+    r = ws.r
+    d = torch.cdist(r, r)
+    iu = torch.triu_indices(r.shape[1], r.shape[1], offset=1, device=r.device)
+    vee = (1.0 / d[:, iu[0], iu[1]]).sum(dim=1)
+    return eL - vee, single
+
+
+# ---------------------------------------------------------------- local energy
+def angles_from_RT(RT) -> np.ndarray:
+    """Euler angles (alpha, beta, gamma) with RT = R(alpha, beta, gamma)^T, the
+    rotation convention of the reference's drivers (jqmc_mcmc.py:724-727,
+    jqmc_gfmc.py:4721-4736); RT (3, 3) or (W, 3, 3)."""
+    rt = np.asarray(RT, dtype=np.float64)
+    if rt.shape[-2:] != (3, 3):
+        raise ValueError(f"RT must be (3, 3) or (W, 3, 3); got {rt.shape}")
+    R = np.swapaxes(rt, -1, -2)
+    eye = np.eye(3)
+    if not np.allclose(R @ np.swapaxes(R, -1, -2), eye, atol=1e-10) or not np.allclose(np.linalg.det(R), 1.0, atol=1e-10):
+        raise ValueError("RT must be a proper rotation matrix")
+    beta = np.arcsin(np.clip(-R[..., 2, 0], -1.0, 1.0))
+    alpha = np.arctan2(R[..., 2, 1], R[..., 2, 2])
+    gamma = np.arctan2(R[..., 1, 0], R[..., 0, 0])
+    return np.stack([alpha, beta, gamma], axis=-1)
+
+
+def local_energy(ham: Hamiltonian_data, r_up_carts, r_dn_carts, RT):
+    """E_L for each configuration, non-local ECP quadrature rotated by RT."""
+    gs = _system(ham, lambda: ham)
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    ang = angles_from_RT(RT).reshape(-1, 3)
+    W = r_up.shape[0]
+    if ang.shape[0] == 1 and W > 1:
+        ang = np.repeat(ang, W, axis=0)
+    if ang.shape[0] != W:
+        raise ValueError(f"{ang.shape[0]} rotations for {W} configurations")
+    ws = _walkers(gs, r_up, r_dn)
+    eL, _ = ws.vmc_measure(torch.as_tensor(ang, device=gs.device).contiguous(), 0.0)
+    return eL, single
+
+
+def scalar_or_array(t: torch.Tensor, single: bool):
+    return _out(t, single)

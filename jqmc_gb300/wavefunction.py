@@ -16,3 +16,39 @@ class Wavefunction_data:
     def sanity_check(self) -> None:
         self.jastrow_data.sanity_check()
         self.geminal_data.sanity_check()
+
+
+# ---------------------------------------------------------------- evaluation (GPU: walker initialisation + jqmc_log_psi / jqmc_vmc_measure)
+def evaluate_ln_wavefunction(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """ln|psi| = ln|det G| + J (jqmc/wavefunction.py:678)."""
+    from . import surface
+    ld, _, jj, single = surface.wavefunction_parts(wavefunction_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(ld + jj, single)
+
+
+def evaluate_wavefunction(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """psi = sign(det G) exp(ln|det G| + J) (jqmc/wavefunction.py:779)."""
+    from . import surface
+    ld, sg, jj, single = surface.wavefunction_parts(wavefunction_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(sg * (ld + jj).exp(), single)
+
+
+def evaluate_jastrow(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """exp(J) (jqmc/wavefunction.py:817)."""
+    from . import surface
+    _, _, jj, single = surface.wavefunction_parts(wavefunction_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(jj.exp(), single)
+
+
+def evaluate_determinant(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """det G (jqmc/wavefunction.py:846)."""
+    from . import surface
+    ld, sg, _, single = surface.wavefunction_parts(wavefunction_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(sg * ld.exp(), single)
+
+
+def compute_kinetic_energy(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """-1/2 sum_i lap_i psi / psi (jqmc/wavefunction.py:872)."""
+    from . import surface
+    t, single = surface.kinetic_energy(wavefunction_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(t, single)

@@ -275,3 +275,81 @@ def test_drivers_keep_the_reference_signatures_and_refuse_unsupported_options():
         GFMC_n(h, comput_position_deriv=True)
     with pytest.raises(NotImplementedError):
         GFMC_t(h, non_local_move="dltmove")
+
+
+def test_module_functions_keep_the_reference_names_and_need_a_gpu():
+    """The module-level evaluation functions exist under the reference's names
+    with its argument order; the RT -> Euler-angle inversion used by
+    compute_local_energy reproduces the rotation; without a GPU they raise."""
+    import inspect
+
+    from jqmc_gb300 import atomic_orbital, determinant, hamiltonians, jastrow_factor, molecular_orbital, wavefunction
+    from jqmc_gb300._lib import JqmcError
+    from jqmc_gb300.surface import angles_from_RT
+    from oracle.wf import rotation_matrix
+    expect = {
+        atomic_orbital: {n: ["aos_data", "r_carts"] for n in
+                         ("compute_AOs", "compute_AOs_grad", "compute_AOs_laplacian", "compute_AOs_value_grad_lap")},
+        molecular_orbital: {n: ["mos_data", "r_carts"] for n in
+                            ("compute_MOs", "compute_MOs_grad", "compute_MOs_laplacian", "compute_MOs_value_grad_lap")},
+        determinant: {n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
+                      ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
+                       "compute_det_geminal_all_elements")},
+        jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
+                         "compute_Jastrow_one_body": ["jastrow_one_body_data", "r_up_carts", "r_dn_carts"],
+                         "compute_Jastrow_two_body": ["jastrow_two_body_data", "r_up_carts", "r_dn_carts"],
+                         "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"]},
+        wavefunction: {n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
+                       ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow", "evaluate_determinant",
+                        "compute_kinetic_energy")},
+        hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"]},
+    }
+    for mod, fns in expect.items():
+        for name, args in fns.items():
+            assert list(inspect.signature(getattr(mod, name)).parameters) == args, (mod.__name__, name)
+    rng = np.random.default_rng(3)
+    for a in rng.uniform(-2 * np.pi, 2 * np.pi, size=(20, 3)):
+        RT = rotation_matrix(*a).T
+        back = rotation_matrix(*angles_from_RT(RT)).T
+        assert np.max(np.abs(back - RT)) < 1e-14
+    with pytest.raises(ValueError):
+        angles_from_RT(2.0 * np.eye(3))
+    import torch
+    if not torch.cuda.is_available():
+        from jqmc_gb300 import synthetic
+        syn = synthetic.water_like()
+        aos = syn.hamiltonian.wavefunction_data.geminal_data.ao_basis_lambda()[0]
+        with pytest.raises(JqmcError):
+            atomic_orbital.compute_AOs(aos, np.zeros((2, 3)))
+
+
+def test_system_descriptors_pass_the_library_validation():
+    """The descriptors built for the workloads and for the stand-in Hamiltonians
+    of the module-level functions pass jqmc_system_create's checks (on a machine
+    without a GPU the call then stops at the device allocation: JQMC_E_CUDA)."""
+    import ctypes as C
+
+    from jqmc_gb300 import _lib, synthetic
+    from jqmc_gb300.build import build
+    from jqmc_gb300.engine import system_desc
+    from jqmc_gb300.jastrow_factor import Jastrow_data
+    from jqmc_gb300.surface import _ham_for_aos, _ham_for_jastrow, _ham_for_wavefunction
+    build()
+    L = _lib.lib()
+    hams = []
+    for name in ("water_like", "ring12", "chain32"):
+        syn = synthetic.SYSTEMS[name]()
+        wf = syn.hamiltonian.wavefunction_data
+        jd = wf.jastrow_data
+        hams += [(name, syn.hamiltonian), (name + "/aos", _ham_for_aos(wf.geminal_data.ao_basis_lambda()[0])),
+                 (name + "/wavefunction", _ham_for_wavefunction(wf)),
+                 (name + "/jastrow", _ham_for_jastrow(jd, syn.n_up, syn.n_dn)),
+                 (name + "/j2", _ham_for_jastrow(Jastrow_data(jastrow_two_body_data=jd.jastrow_two_body_data),
+                                                 syn.n_up, syn.n_dn))]
+    for label, ham in hams:
+        d, keep, _ = system_desc(ham)
+        h = C.c_void_p()
+        rc = L.jqmc_system_create(C.byref(d), C.byref(h))
+        assert rc in (0, -3), (label, rc)    # JQMC_OK on a GPU machine, JQMC_E_CUDA without one
+        if rc == 0:
+            L.jqmc_system_destroy(h)

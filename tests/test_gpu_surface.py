@@ -1,0 +1,111 @@
+"""The reference's module-level evaluation functions (compute_AOs, compute_MOs,
+compute_*geminal_all_elements, compute_Jastrow_*, evaluate_*, compute_kinetic_energy,
+compute_local_energy) on the GPU path against the oracle, for single
+configurations (Python floats, as the reference returns) and walker batches."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module", params=["water_like", "ring12"])
+def setup(request):
+    from jqmc_gb300 import synthetic
+    from oracle.wf import OracleSystem
+    syn = synthetic.SYSTEMS[request.param]()
+    o = OracleSystem(syn.hamiltonian)
+    r_up, r_dn = syn.initial_electrons(3, seed=9)
+    return syn, o, np.asarray(r_up), np.asarray(r_dn)
+
+
+def test_ao_and_mo_tables(setup):
+    from jqmc_gb300 import atomic_orbital as AO
+    from jqmc_gb300 import molecular_orbital as MO
+    from jqmc_gb300.molecular_orbital import MOs_data
+    from oracle.ao import ao_vgl
+    syn, o, _, _ = setup
+    g = syn.hamiltonian.wavefunction_data.geminal_data
+    aos = g.ao_basis_lambda()[0]
+    pts = np.random.default_rng(4).normal(scale=2.0, size=(65, 3))
+    ref = ao_vgl(o.tab_up, pts)
+    assert rel(AO.compute_AOs(aos, pts), ref[0]) < 1e-12
+    gx, gy, gz = AO.compute_AOs_grad(aos, pts)
+    for got, k in ((gx, 1), (gy, 2), (gz, 3)):
+        assert rel(got, ref[k]) < 1e-12
+    assert rel(AO.compute_AOs_laplacian(aos, pts), ref[4]) < 1e-12
+    for got, want in zip(AO.compute_AOs_value_grad_lap(aos, pts), ref):
+        assert rel(got, want) < 1e-12
+    orb = g.orb_data_up_spin
+    if isinstance(orb, MOs_data):
+        mref = o.orb_vgl(o.tab_up, o.mo_up, pts)
+        assert rel(MO.compute_MOs(orb, pts), mref[0]) < 1e-12
+        for got, want in zip(MO.compute_MOs_value_grad_lap(orb, pts), mref):
+            assert rel(got, want) < 1e-12
+
+
+def test_geminal_and_wavefunction(setup):
+    from jqmc_gb300 import determinant as D
+    from jqmc_gb300 import wavefunction as WF
+    syn, o, r_up, r_dn = setup
+    wf = syn.hamiltonian.wavefunction_data
+    g = wf.geminal_data
+    for w in range(2):
+        G = o.geminal(r_up[w], r_dn[w])
+        assert rel(D.compute_geminal_all_elements(g, r_up[w], r_dn[w]), G) < 1e-12
+        sign, ld = o.ln_det(r_up[w], r_dn[w])
+        got = D.compute_ln_det_geminal_all_elements(g, r_up[w], r_dn[w])
+        assert isinstance(got, float) and abs(got - ld) < RTOL * max(1.0, abs(ld))
+        assert rel(D.compute_det_geminal_all_elements(g, r_up[w], r_dn[w]), sign * np.exp(ld)) < 1e-10
+        J = o.jastrow_total(r_up[w], r_dn[w])
+        lnpsi = WF.evaluate_ln_wavefunction(wf, r_up[w], r_dn[w])
+        assert abs(lnpsi - (ld + J)) < RTOL * max(1.0, abs(ld + J))
+        assert rel(WF.evaluate_jastrow(wf, r_up[w], r_dn[w]), np.exp(J)) < 1e-10
+        assert rel(WF.evaluate_wavefunction(wf, r_up[w], r_dn[w]), sign * np.exp(ld + J)) < 1e-10
+        tu, td = o.kinetic_elements(r_up[w], r_dn[w], np.linalg.inv(G))
+        T = float(np.sum(tu) + np.sum(td))
+        assert abs(WF.compute_kinetic_energy(wf, r_up[w], r_dn[w]) - T) < RTOL * max(1.0, abs(T))
+    # a batch of configurations gives one value per configuration
+    lds = D.compute_ln_det_geminal_all_elements(g, r_up, r_dn)
+    assert lds.shape == (3,)
+    assert rel(lds, [o.ln_det(r_up[w], r_dn[w])[1] for w in range(3)]) < RTOL
+
+
+def test_jastrow_parts(setup):
+    from jqmc_gb300 import jastrow_factor as JF
+    syn, o, r_up, r_dn = setup
+    jd = syn.hamiltonian.wavefunction_data.jastrow_data
+    for w in range(2):
+        J1, J2, J3 = o.jastrow(r_up[w], r_dn[w])
+        assert abs(JF.compute_Jastrow_part(jd, r_up[w], r_dn[w]) - (J1 + J2 + J3)) < RTOL * max(1.0, abs(J1 + J2 + J3))
+        if jd.jastrow_one_body_data is not None:
+            assert abs(JF.compute_Jastrow_one_body(jd.jastrow_one_body_data, r_up[w], r_dn[w]) - J1) < RTOL * max(1.0, abs(J1))
+        if jd.jastrow_two_body_data is not None:
+            assert abs(JF.compute_Jastrow_two_body(jd.jastrow_two_body_data, r_up[w], r_dn[w]) - J2) < RTOL * max(1.0, abs(J2))
+        if jd.jastrow_three_body_data is not None:
+            assert abs(JF.compute_Jastrow_three_body(jd.jastrow_three_body_data, r_up[w], r_dn[w]) - J3) < RTOL * max(1.0, abs(J3))
+
+
+def test_local_energy(setup):
+    from jqmc_gb300 import hamiltonians as H
+    from oracle.wf import rotation_matrix
+    syn, o, r_up, r_dn = setup
+    ham = syn.hamiltonian
+    ang = np.random.default_rng(8).uniform(-2 * np.pi, 2 * np.pi, size=(3, 3))
+    RT = np.stack([rotation_matrix(*a).T for a in ang])
+    ref = [o.local_energy(r_up[w], r_dn[w], RT[w], np.linalg.inv(o.geminal(r_up[w], r_dn[w]))) for w in range(3)]
+    got = H.compute_local_energy(ham, r_up[0], r_dn[0], RT[0])
+    assert isinstance(got, float) and abs(got - ref[0]) < RTOL * max(1.0, abs(ref[0]))
+    batch = H.compute_local_energy(ham, r_up, r_dn, RT)
+    assert batch.shape == (3,)
+    assert rel(batch, ref) < RTOL
