@@ -588,14 +588,19 @@ def gpu_arm(a):
     del drv, ws_m, r_all, near
     mixed.pop("drv")
     torch.cuda.empty_cache()
-    adjoint = adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")) if (rank == 0 and not a.no_adjoint) else None
-    batching = batching_leg() if (rank == 0 and not a.no_batching) else None
-    vmc = None
-    if rank == 0 and not a.no_vmc:
+    def leg(run, skip):
+        """A further leg on rank 0; an exception is recorded in the line instead of ending the run."""
+        if rank != 0 or skip:
+            return None
         try:
-            vmc = vmc_leg()
-        except Exception as ex:   # recorded in the line instead of ending the run
-            vmc = {"error": repr(ex)}
+            return run()
+        except Exception as ex:
+            torch.cuda.empty_cache()
+            return {"error": repr(ex)}
+
+    adjoint = leg(lambda: adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")), a.no_adjoint)
+    batching = leg(batching_leg, a.no_batching)
+    vmc = leg(vmc_leg, a.no_vmc)
     bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 2, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
                 "jqmc_lu_rebuild_refine": 2}   # k_rebuild_m + k_walker_init
