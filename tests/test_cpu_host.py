@@ -353,3 +353,16 @@ def test_system_descriptors_pass_the_library_validation():
         assert rc in (0, -3), (label, rc)    # JQMC_OK on a GPU machine, JQMC_E_CUDA without one
         if rc == 0:
             L.jqmc_system_destroy(h)
+
+
+def test_bucket_assignment():
+    """Electron-count buckets of the many-molecule batches: each molecule goes to
+    the smallest bucket that holds it; above the largest bucket is an error."""
+    from jqmc_gb300.batching import BUCKET_BOUNDS, bucket_of
+    assert BUCKET_BOUNDS == tuple(sorted(BUCKET_BOUNDS))
+    prev = 0
+    for b in BUCKET_BOUNDS:
+        assert bucket_of(prev + 1) == b and bucket_of(b) == b
+        prev = b
+    with pytest.raises(ValueError):
+        bucket_of(BUCKET_BOUNDS[-1] + 1)
