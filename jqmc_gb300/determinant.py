@@ -88,3 +88,26 @@ def compute_det_geminal_all_elements(geminal_data: Geminal_data, r_up_carts, r_d
     from . import surface
     ld, sg, _, single = surface.geminal_log_det(geminal_data, r_up_carts, r_dn_carts)
     return surface.scalar_or_array(sg * ld.exp(), single)
+
+
+def compute_AS_regularization_factor(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
+    """Attaccalite-Sorella regularization factor (jqmc/determinant.py:1291)."""
+    from . import surface
+    R, single = surface.geminal_as_factor(geminal_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(R, single)
+
+
+def compute_AS_regularization_factor_fast_update(geminal, geminal_inv):
+    """The same factor from a given G and G^-1, (n, n) or (W, n, n) (jqmc/determinant.py:1223),
+    evaluated on the GPU."""
+    import torch
+
+    from . import surface
+    if not torch.cuda.is_available():
+        raise surface.JqmcError("no CUDA device: the walker path runs only on the GPU")
+    G = torch.as_tensor(np.asarray(geminal, dtype=np.float64), device="cuda")
+    Gi = torch.as_tensor(np.asarray(geminal_inv, dtype=np.float64), device="cuda")
+    single = G.ndim == 2
+    if single:
+        G, Gi = G[None], Gi[None]
+    return surface.scalar_or_array(surface.as_factor(G, Gi), single)

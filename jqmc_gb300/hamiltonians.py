@@ -28,3 +28,10 @@ def compute_local_energy(hamiltonian_data: Hamiltonian_data, r_up_carts, r_dn_ca
     from . import surface
     eL, single = surface.local_energy(hamiltonian_data, r_up_carts, r_dn_carts, RT)
     return surface.scalar_or_array(eL, single)
+
+
+def compute_local_energy_fast(hamiltonian_data: Hamiltonian_data, r_up_carts, r_dn_carts, RT, geminal_inverse):
+    """E_L with a precomputed geminal inverse (jqmc/hamiltonians.py:225): the same value as
+    ``compute_local_energy``; the walker kernels form the inverse themselves, so
+    ``geminal_inverse`` is accepted and not read."""
+    return compute_local_energy(hamiltonian_data, r_up_carts, r_dn_carts, RT)

@@ -35,6 +35,7 @@ import torch
 from .atomic_orbital import AOs_sphe_data
 from .coulomb_potential import Coulomb_potential_data
 from .determinant import Geminal_data
+from ._lib import JqmcError
 from .engine import GpuSystem, WalkerSet
 from .hamiltonians import Hamiltonian_data
 from .jastrow_factor import Jastrow_data
@@ -155,6 +156,24 @@ def geminal_log_det(geminal: Geminal_data, r_up_carts, r_dn_carts):
     ws = _walkers(gs, r_up, r_dn)
     ld, sg, _ = ws.log_psi()
     return ld, sg, ws.G, single
+
+
+def as_factor(G: torch.Tensor, Ginv: torch.Tensor) -> torch.Tensor:
+    """Attaccalite-Sorella factor (min(min row |G|^2, min column |G|^2) |G^-1|_F^2)^(-3/8),
+    zero where that product is not positive (jqmc/determinant.py:1223-1260); G, Ginv (W, n, n)."""
+    F = (Ginv * Ginv).sum(dim=(1, 2))
+    S = torch.minimum((G * G).sum(dim=2).amin(dim=1), (G * G).sum(dim=1).amin(dim=1))
+    SF = S * F
+    return torch.where(SF > 0.0, SF.clamp_min(torch.finfo(SF.dtype).tiny) ** (-3.0 / 8.0), torch.zeros_like(SF))
+
+
+def geminal_as_factor(geminal: Geminal_data, r_up_carts, r_dn_carts):
+    """The AS factor of each configuration, from the walker initialisation's G and G^-1."""
+    wf = Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=geminal)
+    gs = _system(geminal, lambda: _ham_for_wavefunction(wf))
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    ws = _walkers(gs, r_up, r_dn)
+    return as_factor(ws.G, ws.Ginv), single
 
 
 def wavefunction_parts(wf: Wavefunction_data, r_up_carts, r_dn_carts):

@@ -52,3 +52,9 @@ def compute_kinetic_energy(wavefunction_data: Wavefunction_data, r_up_carts, r_d
     from . import surface
     t, single = surface.kinetic_energy(wavefunction_data, r_up_carts, r_dn_carts)
     return surface.scalar_or_array(t, single)
+
+
+def evaluate_ln_wavefunction_fast(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts, geminal_inv):
+    """ln|psi| with a precomputed geminal inverse (jqmc/wavefunction.py:723): the same value as
+    ``evaluate_ln_wavefunction``; ``geminal_inv`` is accepted and not read."""
+    return evaluate_ln_wavefunction(wavefunction_data, r_up_carts, r_dn_carts)

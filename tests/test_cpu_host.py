@@ -292,17 +292,21 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                          ("compute_AOs", "compute_AOs_grad", "compute_AOs_laplacian", "compute_AOs_value_grad_lap")},
         molecular_orbital: {n: ["mos_data", "r_carts"] for n in
                             ("compute_MOs", "compute_MOs_grad", "compute_MOs_laplacian", "compute_MOs_value_grad_lap")},
-        determinant: {n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
-                      ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
-                       "compute_det_geminal_all_elements")},
+        determinant: {**{n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
+                         ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
+                          "compute_det_geminal_all_elements", "compute_AS_regularization_factor")},
+                      "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_one_body": ["jastrow_one_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_two_body": ["jastrow_two_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"]},
-        wavefunction: {n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
-                       ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow", "evaluate_determinant",
-                        "compute_kinetic_energy")},
-        hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"]},
+        wavefunction: {**{n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
+                          ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow",
+                           "evaluate_determinant", "compute_kinetic_energy")},
+                       "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"]},
+        hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"],
+                       "compute_local_energy_fast": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT",
+                                                     "geminal_inverse"]},
     }
     for mod, fns in expect.items():
         for name, args in fns.items():
@@ -366,3 +370,20 @@ def test_bucket_assignment():
         prev = b
     with pytest.raises(ValueError):
         bucket_of(BUCKET_BOUNDS[-1] + 1)
+
+
+def test_as_factor_matches_the_oracle():
+    """The Attaccalite-Sorella factor of the module-level functions (torch, any
+    device) against the oracle's restatement, on random and singular matrices."""
+    import torch
+
+    from jqmc_gb300.surface import as_factor
+    from oracle.wf import OracleSystem
+    rng = np.random.default_rng(7)
+    G = rng.normal(size=(6, 5, 5))
+    G[3, 2] = 0.0                      # a zero row: the factor is 0, as the reference's where()
+    Gi = np.stack([np.linalg.pinv(g) for g in G])
+    got = as_factor(torch.as_tensor(G), torch.as_tensor(Gi)).numpy()
+    want = np.array([OracleSystem.as_factor(g, gi) for g, gi in zip(G, Gi)])
+    assert np.allclose(got, want, rtol=1e-14, atol=0.0), (got, want)
+    assert got[3] == 0.0

@@ -1,7 +1,8 @@
 """The reference's module-level evaluation functions (compute_AOs, compute_MOs,
-compute_*geminal_all_elements, compute_Jastrow_*, evaluate_*, compute_kinetic_energy,
-compute_local_energy) on the GPU path against the oracle, for single
-configurations (Python floats, as the reference returns) and walker batches."""
+compute_*geminal_all_elements, compute_AS_regularization_factor, compute_Jastrow_*,
+evaluate_*, compute_kinetic_energy, compute_local_energy(_fast)) on the GPU path
+against the oracle, for single configurations (Python floats, as the reference
+returns) and walker batches."""
 
 import numpy as np
 import pytest
@@ -67,9 +68,14 @@ def test_geminal_and_wavefunction(setup):
         got = D.compute_ln_det_geminal_all_elements(g, r_up[w], r_dn[w])
         assert isinstance(got, float) and abs(got - ld) < RTOL * max(1.0, abs(ld))
         assert rel(D.compute_det_geminal_all_elements(g, r_up[w], r_dn[w]), sign * np.exp(ld)) < 1e-10
+        Ginv = np.linalg.inv(G)
+        R_ref = o.as_factor(G, Ginv)
+        assert abs(D.compute_AS_regularization_factor(g, r_up[w], r_dn[w]) - R_ref) < RTOL * max(1e-300, abs(R_ref))
+        assert abs(D.compute_AS_regularization_factor_fast_update(G, Ginv) - R_ref) < 1e-13 * abs(R_ref)
         J = o.jastrow_total(r_up[w], r_dn[w])
         lnpsi = WF.evaluate_ln_wavefunction(wf, r_up[w], r_dn[w])
         assert abs(lnpsi - (ld + J)) < RTOL * max(1.0, abs(ld + J))
+        assert abs(WF.evaluate_ln_wavefunction_fast(wf, r_up[w], r_dn[w], Ginv) - lnpsi) <= 1e-12 * max(1.0, abs(lnpsi))
         assert rel(WF.evaluate_jastrow(wf, r_up[w], r_dn[w]), np.exp(J)) < 1e-10
         assert rel(WF.evaluate_wavefunction(wf, r_up[w], r_dn[w]), sign * np.exp(ld + J)) < 1e-10
         tu, td = o.kinetic_elements(r_up[w], r_dn[w], np.linalg.inv(G))
@@ -106,6 +112,8 @@ def test_local_energy(setup):
     ref = [o.local_energy(r_up[w], r_dn[w], RT[w], np.linalg.inv(o.geminal(r_up[w], r_dn[w]))) for w in range(3)]
     got = H.compute_local_energy(ham, r_up[0], r_dn[0], RT[0])
     assert isinstance(got, float) and abs(got - ref[0]) < RTOL * max(1.0, abs(ref[0]))
+    G0 = o.geminal(r_up[0], r_dn[0])
+    assert abs(H.compute_local_energy_fast(ham, r_up[0], r_dn[0], RT[0], np.linalg.inv(G0)) - got) <= 1e-12 * max(1.0, abs(got))
     batch = H.compute_local_energy(ham, r_up, r_dn, RT)
     assert batch.shape == (3,)
     assert rel(batch, ref) < RTOL
