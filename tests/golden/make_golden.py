@@ -132,6 +132,7 @@ def make(sysname: str, nwalk: int, seed: int):
     call("ao_vgl", lambda w: tuple(r_ao.compute_AOs_value_grad_lap(aos_det, rall(w))))
     call("geminal", lambda w: r_det.compute_geminal_all_elements(gem, r_up[w], r_dn[w]))
     call("det_debug", lambda w: r_det._compute_det_geminal_all_elements_debug(gem, r_up[w], r_dn[w]))
+    call("AS", lambda w: r_det.compute_AS_regularization_factor(gem, r_up[w], r_dn[w]))
     call("J1", lambda w: r_jas.compute_Jastrow_one_body(jas.jastrow_one_body_data, r_up[w], r_dn[w]))
     call("J2", lambda w: r_jas.compute_Jastrow_two_body(jas.jastrow_two_body_data, r_up[w], r_dn[w]))
     call("J3", lambda w: r_jas.compute_Jastrow_three_body(jas.jastrow_three_body_data, r_up[w], r_dn[w]))
@@ -155,6 +156,8 @@ def make(sysname: str, nwalk: int, seed: int):
     ginv = lambda w: np.linalg.inv(np.asarray(r_det.compute_geminal_all_elements(gem, r_up[w], r_dn[w])))  # noqa: E731
     call("det_ratio", lambda w: r_det._compute_ratio_determinant_part_rank1_update(gem, ginv(w), r_up[w], r_dn[w], *moved(w)))
     call("det_grad_lap", lambda w: tuple(r_det.compute_grads_and_laplacian_ln_Det_fast(gem, r_up[w], r_dn[w], ginv(w))))
+    call("AS_fast", lambda w: r_det.compute_AS_regularization_factor_fast_update(
+        np.asarray(r_det.compute_geminal_all_elements(gem, r_up[w], r_dn[w])), ginv(w)))
     call("kinetic", lambda w: tuple(r_wf.compute_kinetic_energy_all_elements_fast_update(wfd, r_up[w], r_dn[w], ginv(w))))
     call("bare_coulomb", lambda w: r_cp._compute_bare_coulomb_potential_debug(coul, r_up[w], r_dn[w]))
     call("ecp_local", lambda w: r_cp._compute_ecp_local_parts_all_pairs_debug(coul, r_up[w], r_dn[w]))

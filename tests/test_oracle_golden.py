@@ -1,8 +1,9 @@
 """Pin the CPU oracle against outputs of the reference's own functions.
 
 The fixtures in tests/golden/*.npz were produced by tests/golden/make_golden.py,
-which executes jqmc's per-walker functions (AO, geminal, Jastrow, Coulomb/ECP,
-kinetic, local energy, discretised kinetic mesh) on seeded synthetic systems.
+which executes jqmc's per-walker functions (AO, geminal, AS regularization,
+Jastrow, Coulomb/ECP, kinetic, local energy, discretised kinetic mesh) on seeded
+synthetic systems.
 Every oracle quantity must agree to 1e-10 relative (the FP64 parity bar).
 """
 
@@ -43,6 +44,7 @@ def test_oracle_matches_reference_functions(name, golden_dir):
         assert rel(J3, g["J3"][w]) < RTOL and rel(J3, g["J3_debug"][w]) < RTOL
         assert rel(J1 + J2 + J3, g["J"][w]) < RTOL
         Gi = np.linalg.inv(G)
+        assert rel(o.as_factor(G, Gi), g["AS"][w]) < RTOL and rel(o.as_factor(G, Gi), g["AS_fast"][w]) < RTOL
         gu, gd, lu, ld = o.det_grad_lap(ru, rd, Gi)
         for k, x in enumerate((gu, gd, lu, ld)):
             assert rel(x, g[f"det_grad_lap.{k}"][w]) < RTOL
@@ -83,3 +85,18 @@ def test_solid_harmonics_known_forms():
         h = 1e-6
         fd = np.stack([(solid_harmonics(l, d + h * e)[0] - solid_harmonics(l, d - h * e)[0]) / (2 * h) for e in np.eye(3)], -1)
         assert np.max(np.abs(fd - G)) < 1e-6 * max(1.0, np.max(np.abs(G)))
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_as_factor_matches_reference(name, golden_dir):
+    """The AS factor of the module-level functions (torch, evaluated here on CPU
+    tensors) against the reference's compute_AS_regularization_factor."""
+    import torch
+
+    from jqmc_gb300.surface import as_factor
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    o = OracleSystem(synthetic.SYSTEMS[name]().hamiltonian)
+    G = np.stack([o.geminal(g["r_up"][w], g["r_dn"][w]) for w in range(g["r_up"].shape[0])])
+    Gi = np.linalg.inv(G)
+    got = as_factor(torch.as_tensor(G), torch.as_tensor(Gi)).numpy()
+    assert rel(got, g["AS"]) < RTOL
