@@ -1,0 +1,87 @@
+"""TREXIO input and the TurboRVB known answers of the reference's tests.
+
+tests/golden/water_ccecp.npz holds the water ccECP/cc-pVQZ file of the
+reference's tests converted by jqmc_gb300.trexio_wrapper (the script beside
+it), the fixed configurations and the TurboRVB values of
+test_comparison_with_turborvb_ECP.py:105-130: (psi'/psi)^2, the kinetic energy
+and the potential, to the decimals the reference asserts (6, 6, 5).  The oracle
+reproduces them; the reader itself is checked on the reference's files when
+they are present.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TREXIO_DIR = "/root/reference/tests/trexio_example_files"
+
+
+def water_ccecp():
+    """(Hamiltonian_data without Jastrow, fixture arrays) from tests/golden/water_ccecp.npz."""
+    from jqmc_gb300.atomic_orbital import AOs_sphe_data
+    from jqmc_gb300.coulomb_potential import Coulomb_potential_data
+    from jqmc_gb300.determinant import Geminal_data
+    from jqmc_gb300.hamiltonians import Hamiltonian_data
+    from jqmc_gb300.jastrow_factor import Jastrow_data
+    from jqmc_gb300.molecular_orbital import MOs_data
+    from jqmc_gb300.structure import Structure_data
+    from jqmc_gb300.wavefunction import Wavefunction_data
+    g = np.load(os.path.join(HERE, "golden", "water_ccecp.npz"))
+    labels = tuple(str(x) for x in g["labels"])
+    st = Structure_data(positions=g["positions"], atomic_numbers=tuple(int(x) for x in g["atomic_numbers"]),
+                        element_symbols=labels, atomic_labels=labels)
+    aos = AOs_sphe_data(structure_data=st, nucleus_index=tuple(int(x) for x in g["ao_nucleus_index"]),
+                        num_ao=len(g["ao_l"]), num_ao_prim=len(g["ao_exponents"]),
+                        orbital_indices=tuple(int(x) for x in g["ao_orbital_indices"]), exponents=g["ao_exponents"],
+                        coefficients=g["ao_coefficients"], angular_momentums=tuple(int(x) for x in g["ao_l"]),
+                        magnetic_quantum_numbers=tuple(int(x) for x in g["ao_m"]))
+    mu = MOs_data(num_mo=g["mo_up"].shape[0], aos_data=aos, mo_coefficients=g["mo_up"])
+    md = MOs_data(num_mo=g["mo_dn"].shape[0], aos_data=aos, mo_coefficients=g["mo_dn"])
+    gem = Geminal_data(num_electron_up=int(g["n_up"]), num_electron_dn=int(g["n_dn"]), orb_data_up_spin=mu,
+                       orb_data_dn_spin=md, lambda_matrix=g["lambda_matrix"])
+    coul = Coulomb_potential_data(structure_data=st, ecp_flag=True, z_cores=tuple(int(x) for x in g["ecp_z_cores"]),
+                                  max_ang_mom_plus_1=tuple(int(x) for x in g["ecp_maxl1"]), num_ecps=len(g["ecp_l"]),
+                                  ang_moms=tuple(int(x) for x in g["ecp_l"]),
+                                  nucleus_index=tuple(int(x) for x in g["ecp_nucleus_index"]),
+                                  exponents=tuple(float(x) for x in g["ecp_exponents"]),
+                                  coefficients=tuple(float(x) for x in g["ecp_coefficients"]),
+                                  powers=tuple(int(x) for x in g["ecp_powers"]))
+    ham = Hamiltonian_data(structure_data=st, coulomb_potential_data=coul,
+                           wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=gem))
+    ham.sanity_check()
+    return ham, g
+
+
+def test_oracle_reproduces_turborvb():
+    from oracle.wf import OracleSystem
+    ham, g = water_ccecp()
+    o = OracleSystem(ham)
+    s0, l0 = o.ln_det(g["old_r_up"], g["old_r_dn"])
+    s1, l1 = o.ln_det(g["new_r_up"], g["new_r_dn"])
+    ratio_sq = (s0 * s1 * np.exp(l1 - l0)) ** 2
+    Ginv = np.linalg.inv(o.geminal(g["new_r_up"], g["new_r_dn"]))
+    tu, td = o.kinetic_elements(g["new_r_up"], g["new_r_dn"], Ginv)
+    v = (o.bare_coulomb(g["new_r_up"], g["new_r_dn"]) + o.ecp_local(g["new_r_up"], g["new_r_dn"])
+         + o.ecp_nonlocal(g["new_r_up"], g["new_r_dn"], np.eye(3), Ginv)[1])
+    np.testing.assert_almost_equal(ratio_sq, float(g["wf_ratio_sq"]), decimal=6)
+    np.testing.assert_almost_equal(np.sum(tu) + np.sum(td), float(g["kinetic"]), decimal=6)
+    np.testing.assert_almost_equal(v, float(g["potential"]), decimal=5)
+
+
+@pytest.mark.skipif(not os.path.isdir(TREXIO_DIR), reason="the reference's TREXIO files are not present")
+def test_reader_on_reference_files():
+    """Every spherical file converts (and matches the fixture for water);
+    Cartesian bases are refused."""
+    from jqmc_gb300.trexio_wrapper import read_trexio_file
+    ham, g = water_ccecp()
+    st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, "water_ccecp_ccpvqz.h5"))
+    assert np.array_equal(aos.coefficients, g["ao_coefficients"]) and np.array_equal(mu.mo_coefficients, g["mo_up"])
+    assert tuple(st.atomic_labels) == ("O", "H", "H") and tuple(st.atomic_numbers) == (8, 1, 1)
+    for name, nup, ndn in (("H2_ae_ccpvqz.h5", 1, 1), ("H2_ecp_ccpvtz.h5", 1, 1), ("H_ecp_ccpvqz.h5", 1, 0)):
+        st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, name))
+        gem.sanity_check()
+        assert (gem.num_electron_up, gem.num_electron_dn) == (nup, ndn)
+    with pytest.raises(NotImplementedError):
+        read_trexio_file(os.path.join(TREXIO_DIR, "N2_ecp_ccpvtz_cart.h5"))
