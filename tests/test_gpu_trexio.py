@@ -1,7 +1,7 @@
-"""The TurboRVB known answers of the reference's tests on the GPU path: the
-water ccECP/cc-pVQZ wavefunction read from TREXIO (tests/golden/water_ccecp.npz),
-(psi'/psi)^2, the kinetic energy and the potential through the module-level
-functions, to the decimals the reference asserts (6, 6, 5)."""
+"""The TurboRVB known answers of the reference's tests on the GPU path: TREXIO
+wavefunctions (tests/golden/{water_ccecp,h2_ae}.npz), (psi'/psi)^2, the kinetic
+energy and the potential through the module-level functions, to the decimals
+the reference asserts."""
 
 import numpy as np
 import pytest
@@ -11,16 +11,18 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def test_gpu_reproduces_turborvb():
+@pytest.mark.parametrize("fixture,case", [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("h2_ae.npz", "nojas")])
+def test_gpu_reproduces_turborvb(fixture, case):
     from jqmc_gb300 import hamiltonians as H
     from jqmc_gb300 import wavefunction as WF
-    from test_trexio import water_ccecp
-    ham, g = water_ccecp()
+    from test_trexio import trexio_case
+    ham, c = trexio_case(fixture, case)
     wf = ham.wavefunction_data
-    ratio_sq = (WF.evaluate_wavefunction(wf, g["new_r_up"], g["new_r_dn"])
-                / WF.evaluate_wavefunction(wf, g["old_r_up"], g["old_r_dn"])) ** 2
-    kin = WF.compute_kinetic_energy(wf, g["new_r_up"], g["new_r_dn"])
-    pot = H.compute_local_energy(ham, g["new_r_up"], g["new_r_dn"], np.eye(3)) - kin
-    np.testing.assert_almost_equal(ratio_sq, float(g["wf_ratio_sq"]), decimal=6)
-    np.testing.assert_almost_equal(kin, float(g["kinetic"]), decimal=6)
-    np.testing.assert_almost_equal(pot, float(g["potential"]), decimal=5)
+    ratio_sq = (WF.evaluate_wavefunction(wf, c["new_r_up"], c["new_r_dn"])
+                / WF.evaluate_wavefunction(wf, c["old_r_up"], c["old_r_dn"])) ** 2
+    kin = WF.compute_kinetic_energy(wf, c["new_r_up"], c["new_r_dn"])
+    pot = H.compute_local_energy(ham, c["new_r_up"], c["new_r_dn"], np.eye(3)) - kin
+    d = [int(x) for x in c["decimals"]]
+    np.testing.assert_almost_equal(ratio_sq, float(c["wf_ratio_sq"]), decimal=d[0])
+    np.testing.assert_almost_equal(kin, float(c["kinetic"]), decimal=d[1])
+    np.testing.assert_almost_equal(pot, float(c["potential"]), decimal=d[2])

@@ -1,12 +1,13 @@
 """TREXIO input and the TurboRVB known answers of the reference's tests.
 
-tests/golden/water_ccecp.npz holds the water ccECP/cc-pVQZ file of the
-reference's tests converted by jqmc_gb300.trexio_wrapper (the script beside
-it), the fixed configurations and the TurboRVB values of
-test_comparison_with_turborvb_ECP.py:105-130: (psi'/psi)^2, the kinetic energy
-and the potential, to the decimals the reference asserts (6, 6, 5).  The oracle
-reproduces them; the reader itself is checked on the reference's files when
-they are present.
+tests/golden/{water_ccecp,h2_ae}.npz hold TREXIO files of the reference's tests
+converted by jqmc_gb300.trexio_wrapper (the script beside them), with the fixed
+configurations, Jastrow parameters and TurboRVB values of
+test_comparison_with_turborvb_ECP.py (water ccECP, without Jastrow and with a
+two-body Jastrow) and test_comparison_with_turborvb_AE.py (H2, all electrons):
+(psi'/psi)^2, the kinetic energy and the potential, to the decimals the
+reference asserts.  The oracle reproduces them; the reader itself is checked
+on the reference's files when they are present.
 """
 
 import os
@@ -18,17 +19,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TREXIO_DIR = "/root/reference/tests/trexio_example_files"
 
 
-def water_ccecp():
-    """(Hamiltonian_data without Jastrow, fixture arrays) from tests/golden/water_ccecp.npz."""
+def trexio_case(fixture: str, case: str):
+    """(Hamiltonian_data, configurations and TurboRVB values) of one case of a
+    tests/golden fixture made by make_trexio_golden.py."""
     from jqmc_gb300.atomic_orbital import AOs_sphe_data
     from jqmc_gb300.coulomb_potential import Coulomb_potential_data
     from jqmc_gb300.determinant import Geminal_data
     from jqmc_gb300.hamiltonians import Hamiltonian_data
-    from jqmc_gb300.jastrow_factor import Jastrow_data
+    from jqmc_gb300.jastrow_factor import Jastrow_data, Jastrow_two_body_data
     from jqmc_gb300.molecular_orbital import MOs_data
     from jqmc_gb300.structure import Structure_data
     from jqmc_gb300.wavefunction import Wavefunction_data
-    g = np.load(os.path.join(HERE, "golden", "water_ccecp.npz"))
+    g = np.load(os.path.join(HERE, "golden", fixture))
     labels = tuple(str(x) for x in g["labels"])
     st = Structure_data(positions=g["positions"], atomic_numbers=tuple(int(x) for x in g["atomic_numbers"]),
                         element_symbols=labels, atomic_labels=labels)
@@ -41,33 +43,46 @@ def water_ccecp():
     md = MOs_data(num_mo=g["mo_dn"].shape[0], aos_data=aos, mo_coefficients=g["mo_dn"])
     gem = Geminal_data(num_electron_up=int(g["n_up"]), num_electron_dn=int(g["n_dn"]), orb_data_up_spin=mu,
                        orb_data_dn_spin=md, lambda_matrix=g["lambda_matrix"])
-    coul = Coulomb_potential_data(structure_data=st, ecp_flag=True, z_cores=tuple(int(x) for x in g["ecp_z_cores"]),
-                                  max_ang_mom_plus_1=tuple(int(x) for x in g["ecp_maxl1"]), num_ecps=len(g["ecp_l"]),
-                                  ang_moms=tuple(int(x) for x in g["ecp_l"]),
-                                  nucleus_index=tuple(int(x) for x in g["ecp_nucleus_index"]),
-                                  exponents=tuple(float(x) for x in g["ecp_exponents"]),
-                                  coefficients=tuple(float(x) for x in g["ecp_coefficients"]),
-                                  powers=tuple(int(x) for x in g["ecp_powers"]))
+    if bool(g["ecp_flag"]):
+        coul = Coulomb_potential_data(structure_data=st, ecp_flag=True, z_cores=tuple(int(x) for x in g["ecp_z_cores"]),
+                                      max_ang_mom_plus_1=tuple(int(x) for x in g["ecp_maxl1"]), num_ecps=len(g["ecp_l"]),
+                                      ang_moms=tuple(int(x) for x in g["ecp_l"]),
+                                      nucleus_index=tuple(int(x) for x in g["ecp_nucleus_index"]),
+                                      exponents=tuple(float(x) for x in g["ecp_exponents"]),
+                                      coefficients=tuple(float(x) for x in g["ecp_coefficients"]),
+                                      powers=tuple(int(x) for x in g["ecp_powers"]))
+    else:
+        coul = Coulomb_potential_data(structure_data=st, ecp_flag=False)
+    b = float(g[f"{case}_j2_param"])
+    jas = Jastrow_data(jastrow_two_body_data=None if np.isnan(b) else Jastrow_two_body_data(jastrow_2b_param=b))
     ham = Hamiltonian_data(structure_data=st, coulomb_potential_data=coul,
-                           wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=gem))
+                           wavefunction_data=Wavefunction_data(jastrow_data=jas, geminal_data=gem))
     ham.sanity_check()
-    return ham, g
+    c = {k[len(case) + 1:]: g[k] for k in g.files if k.startswith(case + "_")}
+    return ham, c
 
 
-def test_oracle_reproduces_turborvb():
+CASES = [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("h2_ae.npz", "nojas")]
+
+
+@pytest.mark.parametrize("fixture,case", CASES)
+def test_oracle_reproduces_turborvb(fixture, case):
     from oracle.wf import OracleSystem
-    ham, g = water_ccecp()
+    ham, c = trexio_case(fixture, case)
     o = OracleSystem(ham)
-    s0, l0 = o.ln_det(g["old_r_up"], g["old_r_dn"])
-    s1, l1 = o.ln_det(g["new_r_up"], g["new_r_dn"])
-    ratio_sq = (s0 * s1 * np.exp(l1 - l0)) ** 2
-    Ginv = np.linalg.inv(o.geminal(g["new_r_up"], g["new_r_dn"]))
-    tu, td = o.kinetic_elements(g["new_r_up"], g["new_r_dn"], Ginv)
-    v = (o.bare_coulomb(g["new_r_up"], g["new_r_dn"]) + o.ecp_local(g["new_r_up"], g["new_r_dn"])
-         + o.ecp_nonlocal(g["new_r_up"], g["new_r_dn"], np.eye(3), Ginv)[1])
-    np.testing.assert_almost_equal(ratio_sq, float(g["wf_ratio_sq"]), decimal=6)
-    np.testing.assert_almost_equal(np.sum(tu) + np.sum(td), float(g["kinetic"]), decimal=6)
-    np.testing.assert_almost_equal(v, float(g["potential"]), decimal=5)
+    s0, l0 = o.ln_det(c["old_r_up"], c["old_r_dn"])
+    s1, l1 = o.ln_det(c["new_r_up"], c["new_r_dn"])
+    dJ = o.jastrow_total(c["new_r_up"], c["new_r_dn"]) - o.jastrow_total(c["old_r_up"], c["old_r_dn"])
+    ratio_sq = (s0 * s1 * np.exp(l1 - l0 + dJ)) ** 2
+    Ginv = np.linalg.inv(o.geminal(c["new_r_up"], c["new_r_dn"]))
+    tu, td = o.kinetic_elements(c["new_r_up"], c["new_r_dn"], Ginv)
+    v = o.bare_coulomb(c["new_r_up"], c["new_r_dn"])
+    if o.ecp:
+        v += o.ecp_local(c["new_r_up"], c["new_r_dn"]) + o.ecp_nonlocal(c["new_r_up"], c["new_r_dn"], np.eye(3), Ginv)[1]
+    d = [int(x) for x in c["decimals"]]
+    np.testing.assert_almost_equal(ratio_sq, float(c["wf_ratio_sq"]), decimal=d[0])
+    np.testing.assert_almost_equal(np.sum(tu) + np.sum(td), float(c["kinetic"]), decimal=d[1])
+    np.testing.assert_almost_equal(v, float(c["potential"]), decimal=d[2])
 
 
 @pytest.mark.skipif(not os.path.isdir(TREXIO_DIR), reason="the reference's TREXIO files are not present")
@@ -75,7 +90,7 @@ def test_reader_on_reference_files():
     """Every spherical file converts (and matches the fixture for water);
     Cartesian bases are refused."""
     from jqmc_gb300.trexio_wrapper import read_trexio_file
-    ham, g = water_ccecp()
+    g = np.load(os.path.join(HERE, "golden", "water_ccecp.npz"))
     st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, "water_ccecp_ccpvqz.h5"))
     assert np.array_equal(aos.coefficients, g["ao_coefficients"]) and np.array_equal(mu.mo_coefficients, g["mo_up"])
     assert tuple(st.atomic_labels) == ("O", "H", "H") and tuple(st.atomic_numbers) == (8, 1, 1)
