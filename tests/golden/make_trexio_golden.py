@@ -7,14 +7,30 @@ parameters and TurboRVB values of the reference's tests, as
 tests/golden/water_ccecp.npz and tests/golden/h2_ae.npz:
 - water, no Jastrow: test_comparison_with_turborvb_ECP.py:75-130;
 - water, two-body Jastrow: test_comparison_with_turborvb_ECP.py:217-270;
-- H2 all-electron, no Jastrow: test_comparison_with_turborvb_AE.py:64-102.
-Per case c: c_old_r_up, c_old_r_dn, c_new_r_up, c_new_r_dn, c_j2_param (NaN
-for none), c_wf_ratio_sq, c_kinetic, c_potential (potential with RT =
+- water, two- and three-body Jastrow (jastrow_data_w_2b_3b_w_ecp.pkl):
+  test_comparison_with_turborvb_ECP.py:362-503;
+- water, two-, one- and three-body Jastrow (jastrow_data_w_2b_1b3b_w_ecp.pkl):
+  test_comparison_with_turborvb_ECP.py:504-645;
+- H2 all-electron, no Jastrow: test_comparison_with_turborvb_AE.py:64-102;
+- H2 all-electron, one-, two- and three-body Jastrow
+  (jastrow_data_w_1b_2b_1b3b_ae.pkl): test_comparison_with_turborvb_AE.py:163-261.
+Per case c: c_old_r_up, c_old_r_dn, c_new_r_up, c_new_r_dn, the Jastrow
+(c_j1_param and c_j2_param, NaN for none; c_j1_core, the core electrons per
+nucleus; c_j3_matrix, empty for none, with the three-body AO basis in
+c_j3_nucleus_index, c_j3_orbital_indices, c_j3_exponents, c_j3_coefficients,
+c_j3_l, c_j3_m), c_wf_ratio_sq, c_kinetic, c_potential (potential with RT =
 identity, Nv = 6, one nearest nucleus) and c_decimals (the decimals the
-reference asserts for the three).  Run: python tests/golden/make_trexio_golden.py
+reference asserts for the three).
+
+The reference stores the Jastrows of the last three cases as pickles of its
+own classes.  They are read here by a restricted unpickler that builds plain
+records for the reference's classes and admits only numpy arrays and dtypes
+besides, so no code of the reference runs.
+Run: python tests/golden/make_trexio_golden.py
 """
 
 import os
+import pickle
 import sys
 
 import numpy as np
@@ -27,8 +43,70 @@ REFERENCE = "/root/reference"
 from jqmc_gb300.trexio_wrapper import read_trexio_file  # noqa: E402
 
 
+EXAMPLES = os.path.join(REFERENCE, "tests", "trexio_example_files")
+
+
+class _Record:
+    """The attributes of one pickled object of the reference, as a dict."""
+
+    def __setstate__(self, state):
+        if isinstance(state, tuple):  # (__dict__, __slots__ state) of slotted dataclasses
+            merged = dict(state[0] or {})
+            merged.update(state[1] or {})
+            state = merged
+        self.state = dict(state)
+
+
+class _RestrictedUnpickler(pickle.Unpickler):
+    def find_class(self, module, name):
+        if module == "jqmc" or module.startswith("jqmc."):
+            return type(name, (_Record,), {})
+        if module in ("numpy.core.multiarray", "numpy._core.multiarray") and name == "_reconstruct":
+            return np._core.multiarray._reconstruct
+        if module == "numpy" and name in ("ndarray", "dtype"):
+            return getattr(np, name)
+        raise pickle.UnpicklingError(f"{module}.{name} is not admitted")
+
+
+def jastrow_arrays(pkl: str | None, positions: np.ndarray, natom: int) -> dict:
+    """Fixture arrays of the Jastrow pickled in ``pkl`` (none for None); the
+    nuclei of its one- and three-body parts must be those of the TREXIO file."""
+    out = dict(j1_param=np.nan, j1_core=np.zeros(natom), j2_param=np.nan, j3_matrix=np.zeros((0, 0)),
+               j3_nucleus_index=np.zeros(0, int), j3_orbital_indices=np.zeros(0, int), j3_exponents=np.zeros(0),
+               j3_coefficients=np.zeros(0), j3_l=np.zeros(0, int), j3_m=np.zeros(0, int))
+    if pkl is None:
+        return out
+    with open(os.path.join(EXAMPLES, pkl), "rb") as f:
+        jd = _RestrictedUnpickler(f).load().state
+    j1, j2, j3 = (jd.get(k) for k in ("jastrow_one_body_data", "jastrow_two_body_data", "jastrow_three_body_data"))
+    if j1 is not None:
+        a = j1.state
+        assert a.get("jastrow_1b_type", "exp") == "exp"
+        assert np.allclose(a["structure_data"].state["positions"], positions)
+        out.update(j1_param=float(a["jastrow_1b_param"]), j1_core=np.asarray(a["core_electrons"], dtype=np.float64))
+    if j2 is not None:
+        a = j2.state
+        assert a.get("jastrow_2b_type", "pade") == "pade"
+        out.update(j2_param=float(a["jastrow_2b_param"]))
+    if j3 is not None:
+        a = j3.state
+        o = a["orb_data"]
+        assert type(o).__name__ == "AOs_sphe_data"
+        o = o.state
+        assert np.allclose(o["structure_data"].state["positions"], positions)
+        out.update(j3_matrix=np.asarray(a["j_matrix"], dtype=np.float64),
+                   j3_nucleus_index=np.asarray(o["nucleus_index"], dtype=int),
+                   j3_orbital_indices=np.asarray(o["orbital_indices"], dtype=int),
+                   j3_exponents=np.asarray(o["exponents"], dtype=np.float64),
+                   j3_coefficients=np.asarray(o["coefficients"], dtype=np.float64),
+                   j3_l=np.asarray(o["angular_momentums"], dtype=int),
+                   j3_m=np.asarray(o["magnetic_quantum_numbers"], dtype=int))
+        assert len(out["j3_l"]) == int(o["num_ao"]) and len(out["j3_exponents"]) == int(o["num_ao_prim"])
+    return out
+
+
 def dump(h5name: str, outname: str, cases: dict) -> None:
-    st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(REFERENCE, "tests", "trexio_example_files", h5name))
+    st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(EXAMPLES, h5name))
     out = dict(
         positions=st.positions, atomic_numbers=np.array(st.atomic_numbers), labels=np.array(st.atomic_labels),
         ao_nucleus_index=np.array(aos.nucleus_index), ao_orbital_indices=np.array(aos.orbital_indices),
@@ -42,7 +120,12 @@ def dump(h5name: str, outname: str, cases: dict) -> None:
                    ecp_exponents=np.array(coul.exponents), ecp_coefficients=np.array(coul.coefficients),
                    ecp_powers=np.array(coul.powers))
     for name, c in cases.items():
-        for k, v in c.items():
+        c = dict(c)
+        j2 = c.pop("j2_param", np.nan)
+        arrays = jastrow_arrays(c.pop("jastrow_pkl", None), st.positions, len(st.atomic_numbers))
+        if not np.isnan(j2):
+            arrays["j2_param"] = j2
+        for k, v in {**c, **arrays}.items():
             out[f"{name}_{k}"] = np.asarray(v)
     np.savez_compressed(os.path.join(HERE, outname), **out)
     print("wrote", os.path.join(HERE, outname))
@@ -69,6 +152,26 @@ def main():
                          [-1.12726250654165, -0.678049640381367, -0.656537799033216]])
     j_new_up = j_old_up.copy()
     j_new_up[2] = [0.276215481293413, -0.270740090536313, 0.27986648725301]
+    j23_old_up = np.array([[-1.1345038587576, -0.698914730480577, -0.006290951981744008],
+                           [-2.30366220171161, 2.32528986358581, -0.20008513679678],
+                           [0.390190526911041, 0.422863618938476, 1.0981171776173],
+                           [-2.4014357356045, 0.623761374394509, 0.70010581636993]])
+    j23_old_dn = np.array([[-1.58454340030273, -1.01943210665261, 0.37014437052153],
+                           [1.90701925586575, 0.398999201990364, -0.745191606127732],
+                           [-2.00590358216444, 2.3178763219103, -0.195294104680795],
+                           [-0.103689059569662, -2.18500664943652, -1.56814885512335]])
+    j23_new_up = j23_old_up.copy()
+    j23_new_up[2] = [0.390190526911041, -0.270740090536313, 1.0981171776173]
+    j213_old_up = np.array([[-2.02906771233089, -0.726280132104733, -0.006290951981744008],
+                            [-0.332901524462574, 0.626165379953289, -0.60355949374895],
+                            [-0.197062006804461, -0.396462287261025, 0.207245244485559],
+                            [-2.13232697453793, 2.02938760506611, 0.626121128343523]])
+    j213_old_dn = np.array([[-2.27723556201111, -0.226423326809174, 0.525171318204107],
+                            [0.635659512640246, -0.128318768826431, -0.479396452798511],
+                            [-2.00590358216444, 1.90796788491204, -0.195294104680795],
+                            [-1.12726250654165, -0.739542218156325, -0.25704043697001]])
+    j213_new_dn = j213_old_dn.copy()
+    j213_new_dn[0] = [-2.27723556201111, 0.7469747620327, 0.525171318204107]
     dump("water_ccecp_ccpvqz.h5", "water_ccecp.npz", {
         "nojas": dict(old_r_up=w_old_up, old_r_dn=w_old_dn, new_r_up=w_new_up, new_r_dn=w_old_dn, j2_param=np.nan,
                       wf_ratio_sq=0.919592366177397, kinetic=14.6961809426982,
@@ -76,15 +179,28 @@ def main():
         "j2": dict(old_r_up=j_old_up, old_r_dn=j_old_dn, new_r_up=j_new_up, new_r_dn=j_old_dn, j2_param=0.676718854150191,
                    wf_ratio_sq=0.881124604511419, kinetic=11.1237599317225,
                    potential=-27.03387193107 + 0.243517439611676, decimals=(6, 6, 5)),
+        "j23": dict(old_r_up=j23_old_up, old_r_dn=j23_old_dn, new_r_up=j23_new_up, new_r_dn=j23_old_dn,
+                    jastrow_pkl="jastrow_data_w_2b_3b_w_ecp.pkl", wf_ratio_sq=0.858468162763939,
+                    kinetic=5.82890200054949, potential=-19.1676316230828 + 0.284240877900265, decimals=(6, 6, 5)),
+        "j213": dict(old_r_up=j213_old_up, old_r_dn=j213_old_dn, new_r_up=j213_old_up, new_r_dn=j213_new_dn,
+                     jastrow_pkl="jastrow_data_w_2b_1b3b_w_ecp.pkl", wf_ratio_sq=0.268078593287622,
+                     kinetic=9.84051921791642, potential=-27.1676371839677 + 0.02774284473669801, decimals=(6, 6, 5)),
     })
     h_old_up = np.array([[1.24966813461677, 1.61428085239132, -0.164635126284132]])
     h_old_dn = np.array([[0.429108885274501, -0.007401675646959482, -0.528818841020972]])
     h_new_dn = h_old_dn.copy()
     h_new_dn[0] = [0.429108885274501, -0.007401675646959482, -1.65889610184907]
+    j123_old_up = np.array([[-0.140725692347622, 1.794610704318, 0.541399181483924]])
+    j123_old_dn = np.array([[1.18814636744078, 0.02606967395580784, -1.62047650291381]])
+    j123_new_up = j123_old_up.copy()
+    j123_new_up[0] = [0.985621336113153, 1.794610704318, 0.541399181483924]
     dump("H2_ae_ccpvqz.h5", "h2_ae.npz", {
         "nojas": dict(old_r_up=h_old_up, old_r_dn=h_old_dn, new_r_up=h_old_up, new_r_dn=h_new_dn, j2_param=np.nan,
                       wf_ratio_sq=1.27268619372079, kinetic=1.00473369916001, potential=-2.32849688911382,
                       decimals=(6, 6, 3)),
+        "j123": dict(old_r_up=j123_old_up, old_r_dn=j123_old_dn, new_r_up=j123_new_up, new_r_dn=j123_old_dn,
+                     jastrow_pkl="jastrow_data_w_1b_2b_1b3b_ae.pkl", wf_ratio_sq=0.539734425254117,
+                     kinetic=0.06762960720224656, potential=-1.22497631738529, decimals=(6, 6, 2)),
     })
 
 

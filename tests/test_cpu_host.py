@@ -328,9 +328,10 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
 
 
 def test_system_descriptors_pass_the_library_validation():
-    """The descriptors built for the workloads and for the stand-in Hamiltonians
-    of the module-level functions pass jqmc_system_create's checks (on a machine
-    without a GPU the call then stops at the device allocation: JQMC_E_CUDA)."""
+    """The descriptors built for the workloads, for the TREXIO wavefunctions of
+    the TurboRVB cases and for the stand-in Hamiltonians of the module-level
+    functions pass jqmc_system_create's checks (on a machine without a GPU the
+    call then stops at the device allocation: JQMC_E_CUDA)."""
     import ctypes as C
 
     from jqmc_gb300 import _lib, synthetic
@@ -350,6 +351,10 @@ def test_system_descriptors_pass_the_library_validation():
                  (name + "/jastrow", _ham_for_jastrow(jd, syn.n_up, syn.n_dn)),
                  (name + "/j2", _ham_for_jastrow(Jastrow_data(jastrow_two_body_data=jd.jastrow_two_body_data),
                                                  syn.n_up, syn.n_dn))]
+    from test_trexio import CASES, trexio_case
+    for fixture, case in CASES:
+        ham, _ = trexio_case(fixture, case)
+        hams += [(f"{fixture}/{case}", ham), (f"{fixture}/{case}/wavefunction", _ham_for_wavefunction(ham.wavefunction_data))]
     for label, ham in hams:
         d, keep, _ = system_desc(ham)
         h = C.c_void_p()

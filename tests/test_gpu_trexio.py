@@ -1,5 +1,6 @@
 """The TurboRVB known answers of the reference's tests on the GPU path: TREXIO
-wavefunctions (tests/golden/{water_ccecp,h2_ae}.npz), (psi'/psi)^2, the kinetic
+wavefunctions with the reference's Jastrows (tests/golden/{water_ccecp,h2_ae}.npz,
+every case of test_trexio.CASES), (psi'/psi)^2, the kinetic
 energy and the potential through the module-level functions, to the decimals
 the reference asserts."""
 
@@ -11,7 +12,10 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("fixture,case", [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("h2_ae.npz", "nojas")])
+from test_trexio import CASES  # noqa: E402
+
+
+@pytest.mark.parametrize("fixture,case", CASES)
 def test_gpu_reproduces_turborvb(fixture, case):
     from jqmc_gb300 import hamiltonians as H
     from jqmc_gb300 import wavefunction as WF

@@ -2,10 +2,11 @@
 
 tests/golden/{water_ccecp,h2_ae}.npz hold TREXIO files of the reference's tests
 converted by jqmc_gb300.trexio_wrapper (the script beside them), with the fixed
-configurations, Jastrow parameters and TurboRVB values of
-test_comparison_with_turborvb_ECP.py (water ccECP, without Jastrow and with a
-two-body Jastrow) and test_comparison_with_turborvb_AE.py (H2, all electrons):
-(psi'/psi)^2, the kinetic energy and the potential, to the decimals the
+configurations, Jastrows and TurboRVB values of
+test_comparison_with_turborvb_ECP.py (water ccECP: no Jastrow; two-body;
+two- and three-body; one-, two- and three-body) and
+test_comparison_with_turborvb_AE.py (H2, all electrons: no Jastrow; one-, two-
+and three-body): (psi'/psi)^2, the kinetic energy and the potential, to the decimals the
 reference asserts.  The oracle reproduces them; the reader itself is checked
 on the reference's files when they are present.
 """
@@ -26,7 +27,8 @@ def trexio_case(fixture: str, case: str):
     from jqmc_gb300.coulomb_potential import Coulomb_potential_data
     from jqmc_gb300.determinant import Geminal_data
     from jqmc_gb300.hamiltonians import Hamiltonian_data
-    from jqmc_gb300.jastrow_factor import Jastrow_data, Jastrow_two_body_data
+    from jqmc_gb300.jastrow_factor import (Jastrow_data, Jastrow_one_body_data, Jastrow_three_body_data,
+                                           Jastrow_two_body_data)
     from jqmc_gb300.molecular_orbital import MOs_data
     from jqmc_gb300.structure import Structure_data
     from jqmc_gb300.wavefunction import Wavefunction_data
@@ -53,16 +55,29 @@ def trexio_case(fixture: str, case: str):
                                       powers=tuple(int(x) for x in g["ecp_powers"]))
     else:
         coul = Coulomb_potential_data(structure_data=st, ecp_flag=False)
-    b = float(g[f"{case}_j2_param"])
-    jas = Jastrow_data(jastrow_two_body_data=None if np.isnan(b) else Jastrow_two_body_data(jastrow_2b_param=b))
+    c = {k[len(case) + 1:]: g[k] for k in g.files if k.startswith(case + "_")}
+    a, b = float(c["j1_param"]), float(c["j2_param"])
+    j1 = None if np.isnan(a) else Jastrow_one_body_data(jastrow_1b_param=a, structure_data=st,
+                                                         core_electrons=tuple(float(x) for x in c["j1_core"]))
+    j2 = None if np.isnan(b) else Jastrow_two_body_data(jastrow_2b_param=b)
+    j3 = None
+    if c["j3_matrix"].size:
+        j3_aos = AOs_sphe_data(structure_data=st, nucleus_index=tuple(int(x) for x in c["j3_nucleus_index"]),
+                               num_ao=len(c["j3_l"]), num_ao_prim=len(c["j3_exponents"]),
+                               orbital_indices=tuple(int(x) for x in c["j3_orbital_indices"]),
+                               exponents=c["j3_exponents"], coefficients=c["j3_coefficients"],
+                               angular_momentums=tuple(int(x) for x in c["j3_l"]),
+                               magnetic_quantum_numbers=tuple(int(x) for x in c["j3_m"]))
+        j3 = Jastrow_three_body_data(orb_data=j3_aos, j_matrix=c["j3_matrix"])
+    jas = Jastrow_data(jastrow_one_body_data=j1, jastrow_two_body_data=j2, jastrow_three_body_data=j3)
     ham = Hamiltonian_data(structure_data=st, coulomb_potential_data=coul,
                            wavefunction_data=Wavefunction_data(jastrow_data=jas, geminal_data=gem))
     ham.sanity_check()
-    c = {k[len(case) + 1:]: g[k] for k in g.files if k.startswith(case + "_")}
     return ham, c
 
 
-CASES = [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("h2_ae.npz", "nojas")]
+CASES = [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("water_ccecp.npz", "j23"),
+         ("water_ccecp.npz", "j213"), ("h2_ae.npz", "nojas"), ("h2_ae.npz", "j123")]
 
 
 @pytest.mark.parametrize("fixture,case", CASES)
