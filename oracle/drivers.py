@@ -45,11 +45,21 @@ def init_state(o: OracleSystem, r_up, r_dn) -> WalkerState:
     return WalkerState(r_up, r_dn, G, np.linalg.inv(G))
 
 
-def _f_l(o: OracleSystem, r):
+def step_scale(o: OracleSystem, r):
+    """f(r) = (1 + Z^2 d) / (Z^2 (1 + d)), d the distance to the nearest nucleus
+    and Z its effective charge: the proposal's Gaussian width is f(r) Dt
+    (jqmc_mcmc.py:4355-4361)."""
     a = o.nearest(r)
     Z = o.Zeff[a]
     d = np.linalg.norm(r - o.R[a])
     return 1.0 / Z**2 * (1.0 + Z**2 * d) / (1.0 + d)
+
+
+def transition_ratio(o: OracleSystem, old, new, Dt: float) -> float:
+    """T(new -> old) / T(old -> new) of the position-dependent Gaussian proposal
+    (jqmc_mcmc.py:4395-4401)."""
+    f_l, f_p = step_scale(o, old), step_scale(o, new)
+    return (f_l / f_p) * np.exp(-(np.linalg.norm(new - old) ** 2) * (1.0 / (2.0 * f_p**2 * Dt**2) - 1.0 / (2.0 * f_l**2 * Dt**2)))
 
 
 def vmc_proposal(o: OracleSystem, st: WalkerState, idraw, fdraw, Dt: float, eps_AS: float) -> bool:
@@ -59,12 +69,10 @@ def vmc_proposal(o: OracleSystem, st: WalkerState, idraw, fdraw, Dt: float, eps_
     is_up = sel < o.n_up
     idx = up_i if is_up else dn_i
     old = (st.r_up if is_up else st.r_dn)[idx].copy()
-    f_l = _f_l(o, old)
-    g = gauss * (f_l * Dt)
+    g = gauss * (step_scale(o, old) * Dt)
     new = old.copy()
     new[axis] += g
-    f_p = _f_l(o, new)
-    T_ratio = (f_l / f_p) * np.exp(-(np.linalg.norm(new - old) ** 2) * (1.0 / (2.0 * f_p**2 * Dt**2) - 1.0 / (2.0 * f_l**2 * Dt**2)))
+    T_ratio = transition_ratio(o, old, new, Dt)
     ru, rd = st.r_up.copy(), st.r_dn.copy()
     (ru if is_up else rd)[idx] = new
     J_ratio = np.exp(o.jastrow_total(ru, rd) - o.jastrow_total(st.r_up, st.r_dn))

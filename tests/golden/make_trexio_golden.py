@@ -11,6 +11,8 @@ tests/golden/water_ccecp.npz and tests/golden/h2_ae.npz:
   test_comparison_with_turborvb_ECP.py:362-503;
 - water, two-, one- and three-body Jastrow (jastrow_data_w_2b_1b3b_w_ecp.pkl):
   test_comparison_with_turborvb_ECP.py:504-645;
+- the same wavefunction through one whole Metropolis step (case j213step):
+  test_comparison_with_turborvb_ECP.py:646-950;
 - H2 all-electron, no Jastrow: test_comparison_with_turborvb_AE.py:64-102;
 - H2 all-electron, one-, two- and three-body Jastrow
   (jastrow_data_w_1b_2b_1b3b_ae.pkl): test_comparison_with_turborvb_AE.py:163-261.
@@ -20,7 +22,11 @@ nucleus; c_j3_matrix, empty for none, with the three-body AO basis in
 c_j3_nucleus_index, c_j3_orbital_indices, c_j3_exponents, c_j3_coefficients,
 c_j3_l, c_j3_m), c_wf_ratio_sq, c_kinetic, c_potential (potential with RT =
 identity, Nv = 6, one nearest nucleus) and c_decimals (the decimals the
-reference asserts for the three).
+reference asserts for the three).  Case j213step adds the proposal's time step
+dt and AS cutoff eps_as, TurboRVB's step scales fa and fb, T_ratio, the
+geminals geminal_old and geminal_new (up electrons along rows), s_old, s_new,
+f_old, f_new, r_as_old, r_as_new, reweight and final_ratio; its wf_ratio_sq
+includes the AS ratio, as TurboRVB reports it.
 
 The reference stores the Jastrows of the last three cases as pickles of its
 own classes.  They are read here by a restricted unpickler that builds plain
@@ -172,6 +178,27 @@ def main():
                             [-1.12726250654165, -0.739542218156325, -0.25704043697001]])
     j213_new_dn = j213_old_dn.copy()
     j213_new_dn[0] = [-2.27723556201111, 0.7469747620327, 0.525171318204107]
+    s_old_up = np.array([[-1.13450385875760, -0.698914730480577, -6.290951981744008e-003],
+                         [-2.25378719009775, 0.693895756460611, -4.612006323250584e-002],
+                         [-0.753191857352684, 0.314330338959413, 0.456739833308641],
+                         [-1.60902246286275, 0.499927465264998, 0.700105816369930]])
+    s_old_dn = np.array([[-1.52590493546481, -1.13601932859996, 0.586518269898014],
+                         [0.635659512640246, 0.398999201990364, -0.745191606127732],
+                         [-2.00590358216444, -0.465069404417879, 0.360171216755478],
+                         [-0.302866379660751, -0.890252305196045, 0.345597836490454]])
+    s_new_up = s_old_up.copy()
+    s_new_up[2] = [-0.753191857352684, -1.183650619518406e-002, 0.456739833308641]
+    # TurboRVB prints the geminals with down electrons along rows
+    s_geminal_old = np.array([
+        [0.186887184114679, 7.221020612173907e-003, 2.919097229181558e-002, 5.283664938570871e-002],
+        [2.711743127945612e-002, -1.872067172512451e-002, 5.968147400894821e-002, -1.363982711796792e-002],
+        [0.196787090743597, 9.308561211374290e-002, 5.042625023653007e-003, 0.135256480405370],
+        [0.152575006966341, -3.569426461507245e-002, 9.441528784169728e-002, 1.156481954187638e-002]]).T
+    s_geminal_new = np.array([
+        [0.186887184114679, 7.221020612173907e-03, 7.892154586169434e-02, 5.283664938570871e-02],
+        [2.711743127945612e-02, -1.872067172512451e-02, 6.631227501216763e-02, -1.363982711796792e-02],
+        [0.196787090743597, 9.308561211374290e-02, 4.145830624511430e-02, 0.135256480405370],
+        [0.152575006966341, -3.569426461507245e-02, 0.140717058457383, 1.156481954187638e-02]]).T
     dump("water_ccecp_ccpvqz.h5", "water_ccecp.npz", {
         "nojas": dict(old_r_up=w_old_up, old_r_dn=w_old_dn, new_r_up=w_new_up, new_r_dn=w_old_dn, j2_param=np.nan,
                       wf_ratio_sq=0.919592366177397, kinetic=14.6961809426982,
@@ -185,6 +212,14 @@ def main():
         "j213": dict(old_r_up=j213_old_up, old_r_dn=j213_old_dn, new_r_up=j213_old_up, new_r_dn=j213_new_dn,
                      jastrow_pkl="jastrow_data_w_2b_1b3b_w_ecp.pkl", wf_ratio_sq=0.268078593287622,
                      kinetic=9.84051921791642, potential=-27.1676371839677 + 0.02774284473669801, decimals=(6, 6, 5)),
+        "j213step": dict(old_r_up=s_old_up, old_r_dn=s_old_dn, new_r_up=s_new_up, new_r_dn=s_old_dn,
+                         jastrow_pkl="jastrow_data_w_2b_1b3b_w_ecp.pkl", wf_ratio_sq=0.846407844801284,
+                         kinetic=13.8637480286375, potential=-30.808883190726 + 0.168465630163985, decimals=(6, 6, 5),
+                         dt=2.0, eps_as=0.30, moved=(0, 2), fa=0.470249568592385, fb=0.437344721251066,
+                         t_ratio=1.06518922117014, final_ratio=0.901584512996174, geminal_old=s_geminal_old,
+                         geminal_new=s_geminal_new, f_old=53823.3438428566, f_new=54231.8526090902,
+                         s_old=4.833741852724715e-003, s_new=5.669181330133306e-003, r_as_old=0.124245223553222,
+                         r_as_new=0.116703654039403, reweight=0.151330476290540),
     })
     h_old_up = np.array([[1.24966813461677, 1.61428085239132, -0.164635126284132]])
     h_old_dn = np.array([[0.429108885274501, -0.007401675646959482, -0.528818841020972]])

@@ -7,7 +7,9 @@ test_comparison_with_turborvb_ECP.py (water ccECP: no Jastrow; two-body;
 two- and three-body; one-, two- and three-body) and
 test_comparison_with_turborvb_AE.py (H2, all electrons: no Jastrow; one-, two-
 and three-body): (psi'/psi)^2, the kinetic energy and the potential, to the decimals the
-reference asserts.  The oracle reproduces them; the reader itself is checked
+reference asserts.  One case (j213step) follows a whole Metropolis step of
+TurboRVB: the proposal's step scales and transition ratio, the geminals, the
+AS regularisation and the final acceptance ratio.  The oracle reproduces them; the reader itself is checked
 on the reference's files when they are present.
 """
 
@@ -77,7 +79,12 @@ def trexio_case(fixture: str, case: str):
 
 
 CASES = [("water_ccecp.npz", "nojas"), ("water_ccecp.npz", "j2"), ("water_ccecp.npz", "j23"),
-         ("water_ccecp.npz", "j213"), ("h2_ae.npz", "nojas"), ("h2_ae.npz", "j123")]
+         ("water_ccecp.npz", "j213"), ("water_ccecp.npz", "j213step"), ("h2_ae.npz", "nojas"), ("h2_ae.npz", "j123")]
+
+
+def as_ratio_sq(R_old: float, R_new: float, eps: float) -> float:
+    """The AS factor's share of (psi'/psi)^2 with cutoff eps (jqmc_mcmc.py:4485-4491)."""
+    return ((max(R_new, eps) / R_new) / (max(R_old, eps) / R_old)) ** 2
 
 
 @pytest.mark.parametrize("fixture,case", CASES)
@@ -89,6 +96,9 @@ def test_oracle_reproduces_turborvb(fixture, case):
     s1, l1 = o.ln_det(c["new_r_up"], c["new_r_dn"])
     dJ = o.jastrow_total(c["new_r_up"], c["new_r_dn"]) - o.jastrow_total(c["old_r_up"], c["old_r_dn"])
     ratio_sq = (s0 * s1 * np.exp(l1 - l0 + dJ)) ** 2
+    if "eps_as" in c:
+        G0, G1 = o.geminal(c["old_r_up"], c["old_r_dn"]), o.geminal(c["new_r_up"], c["new_r_dn"])
+        ratio_sq *= as_ratio_sq(o.as_factor(G0, np.linalg.inv(G0)), o.as_factor(G1, np.linalg.inv(G1)), float(c["eps_as"]))
     Ginv = np.linalg.inv(o.geminal(c["new_r_up"], c["new_r_dn"]))
     tu, td = o.kinetic_elements(c["new_r_up"], c["new_r_dn"], Ginv)
     v = o.bare_coulomb(c["new_r_up"], c["new_r_dn"])
@@ -98,6 +108,46 @@ def test_oracle_reproduces_turborvb(fixture, case):
     np.testing.assert_almost_equal(ratio_sq, float(c["wf_ratio_sq"]), decimal=d[0])
     np.testing.assert_almost_equal(np.sum(tu) + np.sum(td), float(c["kinetic"]), decimal=d[1])
     np.testing.assert_almost_equal(v, float(c["potential"]), decimal=d[2])
+
+
+def test_oracle_reproduces_turborvb_metropolis_step():
+    """The rest of TurboRVB's Metropolis step on water with the two-, one- and
+    three-body Jastrow (test_comparison_with_turborvb_ECP.py:646-950): step
+    scales, T_ratio, the geminals, S = min over columns of sum_i G_ij^2,
+    F = |G^-1|_F^2, R_AS = (S F)^(-3/8), reweight (R_AS / max(R_AS, eps))^2 and
+    the final ratio, to the reference's 6 decimals (F to 1e-10 relative).
+    The oracle's R_AS takes the smaller of the row and column minima, as the
+    library does; it equals TurboRVB's here."""
+    from oracle.drivers import step_scale, transition_ratio
+    from oracle.wf import OracleSystem
+    ham, c = trexio_case("water_ccecp.npz", "j213step")
+    o = OracleSystem(ham)
+    spin, idx = (int(x) for x in c["moved"])
+    key = "r_up" if spin == 0 else "r_dn"
+    old, new = c["old_" + key][idx], c["new_" + key][idx]
+    dt, eps = float(c["dt"]), float(c["eps_as"])
+    np.testing.assert_almost_equal(step_scale(o, old), float(c["fa"]), decimal=6)
+    np.testing.assert_almost_equal(step_scale(o, new), float(c["fb"]), decimal=6)
+    T = transition_ratio(o, old, new, dt)
+    np.testing.assert_almost_equal(T, float(c["t_ratio"]), decimal=6)
+    R = {}
+    for when in ("old", "new"):
+        G = o.geminal(c[f"{when}_r_up"], c[f"{when}_r_dn"])
+        Gi = np.linalg.inv(G)
+        np.testing.assert_almost_equal(G, c[f"geminal_{when}"], decimal=6)
+        S = np.min(np.sum(G**2, axis=0))
+        F = np.sum(Gi**2)
+        np.testing.assert_almost_equal(S, float(c[f"s_{when}"]), decimal=6)
+        np.testing.assert_allclose(F, float(c[f"f_{when}"]), rtol=1e-10)
+        R[when] = o.as_factor(G, Gi)
+        np.testing.assert_almost_equal((S * F) ** -0.375, float(c[f"r_as_{when}"]), decimal=6)
+        np.testing.assert_almost_equal(R[when], float(c[f"r_as_{when}"]), decimal=6)
+    np.testing.assert_almost_equal((R["new"] / max(R["new"], eps)) ** 2, float(c["reweight"]), decimal=6)
+    s0, l0 = o.ln_det(c["old_r_up"], c["old_r_dn"])
+    s1, l1 = o.ln_det(c["new_r_up"], c["new_r_dn"])
+    dJ = o.jastrow_total(c["new_r_up"], c["new_r_dn"]) - o.jastrow_total(c["old_r_up"], c["old_r_dn"])
+    ratio_sq = (s0 * s1 * np.exp(l1 - l0 + dJ)) ** 2 * as_ratio_sq(R["old"], R["new"], eps)
+    np.testing.assert_almost_equal(ratio_sq * T, float(c["final_ratio"]), decimal=6)
 
 
 @pytest.mark.skipif(not os.path.isdir(TREXIO_DIR), reason="the reference's TREXIO files are not present")
