@@ -4,6 +4,9 @@
   (MCMC.get_E) and jqmc_gfmc.py:6500-6600 (GFMC_n.get_E, one process).
 * ``gfmc_G_L`` -- products of the last ``num_gfmc_collect_steps`` averaged
   weights, jqmc_gfmc.py:136-152.
+* ``jackknife_force`` -- forces, jqmc_mcmc.py:1191-1380.
+* ``jackknife_generalized_force`` -- dE/dc of the variational parameters,
+  jqmc_mcmc.py:1515-1700 (MCMC.get_gF, one process).
 """
 
 from __future__ import annotations
@@ -65,3 +68,31 @@ def jackknife_force(w_L: np.ndarray, e_L: np.ndarray, force_HF: np.ndarray, forc
     mean = fj.mean(axis=0)
     std = np.sqrt((Mt - 1) / Mt * np.sum((fj - mean) ** 2, axis=0))
     return mean, std
+
+
+def jackknife_generalized_force(w_L: np.ndarray, e_L: np.ndarray, O: np.ndarray, num_bin_blocks: int):
+    """(f_mean, f_std), each (K,), from (M, nw) weights and energies and (M, nw, K)
+    derivatives d ln psi / dc: f = -2 (<e_L O> - <e_L> <O>), jackknife over the
+    (bin, walker) samples with a centred second pass for the spread."""
+    M = e_L.shape[0]
+    if M < num_bin_blocks:
+        raise ValueError(f"{M} samples cannot form {num_bin_blocks} bins")
+    if O.shape[:2] != e_L.shape or w_L.shape != e_L.shape:
+        raise ValueError(f"shapes w_L {w_L.shape}, e_L {e_L.shape} and O {O.shape} disagree")
+
+    def binned(x):
+        return np.concatenate([np.sum(a, axis=0) for a in np.array_split(x, num_bin_blocks, axis=0)], axis=0)
+
+    wb = binned(w_L)                                 # (bins * nw,)
+    web = binned(w_L * e_L)
+    wOb = binned(w_L[:, :, None] * O)                # (bins * nw, K)
+    weOb = binned((w_L * e_L)[:, :, None] * O)
+    den = wb.sum() - wb
+    eO_j = (weOb.sum(axis=0)[None] - weOb) / den[:, None]
+    e_j = (web.sum() - web) / den
+    O_j = (wOb.sum(axis=0)[None] - wOb) / den[:, None]
+    fj = -2.0 * (eO_j - e_j[:, None] * O_j)
+    Mt = fj.shape[0]
+    mean = fj.sum(axis=0) / Mt
+    var = np.sum((fj - mean) ** 2, axis=0) / Mt
+    return mean, np.sqrt((Mt - 1) * var)

@@ -17,6 +17,18 @@ class Wavefunction_data:
         self.jastrow_data.sanity_check()
         self.geminal_data.sanity_check()
 
+    def get_variational_blocks(self, **flags) -> list:
+        """Variational parameter blocks (jqmc/wavefunction.py:515); flags opt_J1_param,
+        opt_J2_param, opt_J3_param, opt_JNN_param, opt_lambda_param and the AO-basis flags."""
+        from .variational import get_variational_blocks
+        return get_variational_blocks(self, **flags)
+
+    def apply_block_updates(self, blocks: list, thetas, learning_rate: float) -> "Wavefunction_data":
+        """The wavefunction with every block moved by learning_rate * its slice of thetas
+        (jqmc/wavefunction.py:292)."""
+        from .variational import apply_block_updates
+        return apply_block_updates(self, blocks, thetas, learning_rate)
+
 
 # ---------------------------------------------------------------- evaluation (GPU: walker initialisation + jqmc_log_psi / jqmc_vmc_measure)
 def evaluate_ln_wavefunction(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
