@@ -122,9 +122,32 @@ def vmc_measure(o: OracleSystem, st: WalkerState, angles, eps_AS: float):
 
 
 # --------------------------------------------------------------------- LRDMC
-def lrdmc_terms(o: OracleSystem, st: WalkerState, R: np.ndarray, alat: float, Nv: int = 6):
-    """(diag, nondiag, p_list, kin_elements, V_nonlocal) at the walker's configuration
-    with rotation R (jqmc_gfmc.py:4806-5030 / 5361-5550, non_local_move='tmove')."""
+def _ecp_moves(o: OracleSystem, st: WalkerState, R: np.ndarray, Nv: int, non_local_move: str):
+    """(V_FN per mesh point, SP sum) of the non-local ECP.  'tmove': V with the full
+    psi ratio, FN = min(V, 0), SP = sum max(V, 0) (jqmc_gfmc.py:4941-4979).
+    'dltmove' (determinant locality): V with the determinant ratio alone, SP =
+    sum max(V, 0), FN = min(V, 0) times the Jastrow ratio of the same mesh point
+    (jqmc_gfmc.py:4980-5017, :920-946, :5553-5600)."""
+    if non_local_move == "tmove":
+        V, _ = o.ecp_nonlocal(st.r_up, st.r_dn, R.T, st.Ginv, Nv=Nv)
+        return np.minimum(V, 0.0), float(np.sum(np.maximum(V, 0.0)))
+    if non_local_move == "dltmove":
+        pts = []
+
+        def det_only(spin, i, rn):
+            pts.append((spin, i, rn.copy()))
+            return o.det_ratio_move(st.Ginv, st.r_up, st.r_dn, spin, i, rn)
+
+        V, _ = o.ecp_nonlocal(st.r_up, st.r_dn, R.T, st.Ginv, Nv=Nv, ratio_fn=det_only)
+        jr = np.array([o.jastrow_ratio_move(st.r_up, st.r_dn, s, i, rn) for s, i, rn in pts])
+        return np.minimum(V, 0.0) * jr, float(np.sum(np.maximum(V, 0.0)))
+    raise NotImplementedError(f"non_local_move={non_local_move!r}")
+
+
+def lrdmc_terms(o: OracleSystem, st: WalkerState, R: np.ndarray, alat: float, Nv: int = 6,
+                non_local_move: str = "tmove"):
+    """(diag, nondiag, p_list, kin_elements, V_nonlocal_FN) at the walker's configuration
+    with rotation R (jqmc_gfmc.py:4806-5030 / 5361-5550)."""
     N = o.n_up + o.n_dn
     tu, td = o.kinetic_elements(st.r_up, st.r_dn, st.Ginv)
     ke = np.concatenate([tu, td])
@@ -145,17 +168,15 @@ def lrdmc_terms(o: OracleSystem, st: WalkerState, R: np.ndarray, alat: float, Nv
     diag_kin = 3.0 / (2.0 * alat**2) * N
     if o.ecp:
         loc = o.ecp_local(st.r_up, st.r_dn)
-        V, _ = o.ecp_nonlocal(st.r_up, st.r_dn, R.T, st.Ginv, Nv=Nv)
-        vfn = np.minimum(V, 0.0)
-        sp_ecp = np.sum(np.maximum(V, 0.0))
+        vfn, sp_ecp = _ecp_moves(o, st, R, Nv, non_local_move)
         nondiag = nondiag + np.sum(vfn)
         diag = diag_kin + disc + loc + sp_kin + sp_ecp
         p = np.concatenate([fn.ravel(), vfn.ravel()])
     else:
         diag = diag_kin + disc + sp_kin
-        V = np.zeros(0)
+        vfn = np.zeros(0)
         p = fn.ravel()
-    return diag, nondiag, p, el, V
+    return diag, nondiag, p, el, vfn
 
 
 def choose_move(p: np.ndarray, u: float) -> int:
@@ -217,10 +238,11 @@ def sm_update(o: OracleSystem, st: WalkerState, spin: int, i: int, r_new):
     st.r_up, st.r_dn = ru, rd
 
 
-def lrdmc_step(o: OracleSystem, st: WalkerState, w: float, draw, alat: float, E_scf: float, Nv: int = 6):
+def lrdmc_step(o: OracleSystem, st: WalkerState, w: float, draw, alat: float, E_scf: float, Nv: int = 6,
+               non_local_move: str = "tmove"):
     """One GFMC_n projection; returns (w_new, diag, nondiag, k)."""
     R = rotation_matrix(draw[0], draw[1], draw[2])
-    diag, nondiag, p, _, _ = lrdmc_terms(o, st, R, alat, Nv)
+    diag, nondiag, p, _, _ = lrdmc_terms(o, st, R, alat, Nv, non_local_move)
     b_x = 1.0 / (diag - E_scf) * (-1.0 * nondiag)
     w = w * b_x
     k = choose_move(p, float(draw[3]))
@@ -229,12 +251,13 @@ def lrdmc_step(o: OracleSystem, st: WalkerState, w: float, draw, alat: float, E_
     return w, diag, nondiag, k
 
 
-def lrdmc_step_t(o: OracleSystem, st: WalkerState, w: float, tau_left: float, draw, alat: float, Nv: int = 6):
+def lrdmc_step_t(o: OracleSystem, st: WalkerState, w: float, tau_left: float, draw, alat: float, Nv: int = 6,
+                 non_local_move: str = "tmove"):
     """One GFMC_t projection (jqmc_gfmc.py:724-1107): draw = (alpha, beta, gamma, xi, u).
     tau_update = min(tau_left, ln(1 - xi) / V_nondiag); w *= exp(-tau_update e_L);
     the chosen move is made only while time is left.  Returns (w, tau_left, e_L, moved)."""
     R = rotation_matrix(draw[0], draw[1], draw[2])
-    diag, nondiag, p, _, _ = lrdmc_terms(o, st, R, alat, Nv)
+    diag, nondiag, p, _, _ = lrdmc_terms(o, st, R, alat, Nv, non_local_move)
     e_L = diag + nondiag
     tau_update = min(tau_left, np.log(1.0 - float(draw[3])) / nondiag)
     w = w * np.exp(-tau_update * e_L)
@@ -247,11 +270,12 @@ def lrdmc_step_t(o: OracleSystem, st: WalkerState, w: float, tau_left: float, dr
     return w, tau_left, e_L, True
 
 
-def lrdmc_energy(o: OracleSystem, st: WalkerState, last_draw, alat: float, Nv: int = 6):
+def lrdmc_energy(o: OracleSystem, st: WalkerState, last_draw, alat: float, Nv: int = 6,
+                 non_local_move: str = "tmove"):
     """(e_L, V_diag) at the walker's configuration with the last step's rotation
     (jqmc_gfmc.py:5361-5640, e_L = V_diag + V_nondiag)."""
     R = rotation_matrix(last_draw[0], last_draw[1], last_draw[2])
-    diag, nondiag, _, _, _ = lrdmc_terms(o, st, R, alat, Nv)
+    diag, nondiag, _, _, _ = lrdmc_terms(o, st, R, alat, Nv, non_local_move)
     return diag + nondiag, diag
 
 

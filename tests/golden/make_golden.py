@@ -164,6 +164,15 @@ def make(sysname: str, nwalk: int, seed: int):
     RT = lambda w: rotation(*angles[w]).T  # noqa: E731
     call("ecp_nonlocal", lambda w: r_cp.compute_ecp_non_local_parts_nearest_neighbors_fast_update(
         coul, wfd, r_up[w], r_dn[w], RT(w), ginv(w))[2:])
+    # determinant locality (non_local_move='dltmove', jqmc_gfmc.py:4980-5017): V with the
+    # determinant ratio only, and the Jastrow ratio at each of its mesh points
+    def dlt(w):
+        mu, md, V, _ = r_cp.compute_ecp_non_local_parts_nearest_neighbors_fast_update(
+            coul, wfd, r_up[w], r_dn[w], RT(w), ginv(w), flag_determinant_only=True)
+        jr = r_jas._compute_ratio_Jastrow_part_rank1_update(jas, r_up[w], r_dn[w], np.asarray(mu), np.asarray(md))
+        return np.asarray(V), np.asarray(jr)
+
+    call("ecp_nonlocal_det", dlt)
     call("local_energy", lambda w: r_ham.compute_local_energy_fast(H, r_up[w], r_dn[w], RT(w), ginv(w)))
     call("disc_kinetic", lambda w: r_wf.compute_discretized_kinetic_energy_fast_update(0.2, wfd, ginv(w), r_up[w], r_dn[w], RT(w).T)[2])
     path = os.path.join(HERE, f"{sysname}.npz")

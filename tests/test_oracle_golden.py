@@ -100,3 +100,27 @@ def test_as_factor_matches_reference(name, golden_dir):
     Gi = np.linalg.inv(G)
     got = as_factor(torch.as_tensor(G), torch.as_tensor(Gi)).numpy()
     assert rel(got, g["AS"]) < RTOL
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_oracle_determinant_locality_matches_reference(name, golden_dir):
+    """non_local_move='dltmove' (jqmc_gfmc.py:4980-5017): the reference's non-local
+    ECP with flag_determinant_only=True and the Jastrow ratios at its mesh
+    points pin the oracle's V_FN = min(V_det, 0) * J_ratio and SP = sum max(V_det, 0)."""
+    from oracle import drivers as D
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    o = OracleSystem(synthetic.SYSTEMS[name]().hamiltonian)
+    for w in range(g["r_up"].shape[0]):
+        st = D.init_state(o, g["r_up"][w], g["r_dn"][w])
+        R = rotation_matrix(*g["angles"][w])
+        V_det, jr = g["ecp_nonlocal_det.0"][w], g["ecp_nonlocal_det.1"][w]
+        fn, sp = D._ecp_moves(o, st, R, 6, "dltmove")
+        assert rel(fn, np.minimum(V_det, 0.0) * jr) < RTOL
+        assert rel(sp, np.sum(np.maximum(V_det, 0.0))) < RTOL
+        # with the full ratio (tmove) the same points give the reference's V
+        fn_t, sp_t = D._ecp_moves(o, st, R, 6, "tmove")
+        V = g["ecp_nonlocal.0"][w]
+        assert rel(fn_t, np.minimum(V, 0.0)) < RTOL and rel(sp_t, np.sum(np.maximum(V, 0.0))) < RTOL
+        assert np.any(jr != 1.0)
+    with pytest.raises(NotImplementedError):
+        D._ecp_moves(o, st, R, 6, "dla")
