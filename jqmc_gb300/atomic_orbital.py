@@ -1,4 +1,4 @@
-"""Contracted spherical Gaussian atomic orbitals.
+"""Contracted spherical Gaussian atomic orbitals (and the Cartesian data layout).
 
 Mirrors ``jqmc/atomic_orbital.py``: the data layout of ``AOs_sphe_data``
 (atomic_orbital.py:781-929) and the public calls ``compute_AOs``
@@ -103,6 +103,76 @@ class AOs_sphe_data:
                     continue
             shells.append({"atom": atom, "l": l, "exps": e, "coefs": c, "aos": [ao], "ms": [m]})
         return shells
+
+
+def cartesian_orders(l: int):
+    """(nx, ny, nz) of the Cartesian components of one shell in TREXIO order,
+    itertools.combinations_with_replacement("xyz", l) (trexio_wrapper.py:244-247):
+    xx, xy, xz, yy, yz, zz for l = 2."""
+    out = []
+    for nx in range(l, -1, -1):
+        for ny in range(l - nx, -1, -1):
+            out.append((nx, ny, l - nx - ny))
+    return out
+
+
+def cartesian_norm(l: int, Z: float, nx: int, ny: int, nz: int) -> float:
+    """sqrt((2Z/pi)^(3/2) (8Z)^l nx! ny! nz! / ((2nx)! (2ny)! (2nz)!)): the primitive
+    normalisation of a Cartesian Gaussian (atomic_orbital.py:1984-2030, :2198-2290)."""
+    ratio = factorial(nx) * factorial(ny) * factorial(nz) / (factorial(2 * nx) * factorial(2 * ny) * factorial(2 * nz))
+    return sqrt((2.0 * Z / pi) ** 1.5 * (8.0 * Z) ** l * ratio)
+
+
+@dataclass(frozen=True)
+class AOs_cart_data:
+    """Field-for-field mirror of jqmc's ``AOs_cart_data`` (atomic_orbital.py:88-330): an
+    AO is phi(r) = sum_p c_p N_p exp(-Z_p |r-R|^2) x^nx y^ny z^nz with N_p from
+    ``cartesian_norm``.  The oracle evaluates it; the walker kernels are
+    spherical, so a Cartesian basis on the GPU path raises."""
+
+    structure_data: Structure_data = field(default_factory=Structure_data)
+    nucleus_index: tuple = ()
+    num_ao: int = 0
+    num_ao_prim: int = 0
+    orbital_indices: tuple = ()
+    exponents: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    coefficients: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    angular_momentums: tuple = ()
+    polynominal_order_x: tuple = ()
+    polynominal_order_y: tuple = ()
+    polynominal_order_z: tuple = ()
+
+    def __post_init__(self):
+        object.__setattr__(self, "exponents", np.asarray(self.exponents, dtype=np.float64))
+        object.__setattr__(self, "coefficients", np.asarray(self.coefficients, dtype=np.float64))
+
+    def sanity_check(self) -> None:
+        """The checks of atomic_orbital.py:260-300, and nx + ny + nz = l."""
+        if len(self.nucleus_index) != self.num_ao:
+            raise ValueError("dim. of self.nucleus_index is wrong")
+        if len(np.unique(self.orbital_indices)) != self.num_ao:
+            raise ValueError(f"num_ao={self.num_ao} and/or num_ao_prim={self.num_ao_prim} is wrong")
+        if len(self.exponents) != self.num_ao_prim or len(self.coefficients) != self.num_ao_prim:
+            raise ValueError("dim. of self.exponents / self.coefficients is wrong")
+        for name in ("angular_momentums", "polynominal_order_x", "polynominal_order_y", "polynominal_order_z"):
+            if len(getattr(self, name)) != self.num_ao:
+                raise ValueError(f"dim. of self.{name} is wrong")
+        for l, nx, ny, nz in zip(self.angular_momentums, self.polynominal_order_x, self.polynominal_order_y,
+                                 self.polynominal_order_z):
+            if min(nx, ny, nz) < 0 or nx + ny + nz != l or not 0 <= l <= L_MAX:
+                raise ValueError(f"powers ({nx}, {ny}, {nz}) do not make l = {l} (l <= {L_MAX})")
+
+    @property
+    def orb_num(self) -> int:
+        return self.num_ao
+
+    @property
+    def _atomic_center_carts_np(self) -> np.ndarray:
+        return self.structure_data.positions[np.asarray(self.nucleus_index, dtype=np.int64)]
+
+    def primitives_of(self, ao: int):
+        idx = [i for i, v in enumerate(self.orbital_indices) if v == ao]
+        return self.exponents[idx], self.coefficients[idx]
 
 
 # ---------------------------------------------------------------- evaluation (GPU, jqmc_ao_vgl)

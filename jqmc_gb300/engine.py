@@ -31,6 +31,8 @@ def pack_basis(aos):
 
     A shell is a run of consecutive AOs on one nucleus with one l, one primitive
     list and consecutive m; each primitive row holds (Z, c N_p sqrt((2l+1)/4pi))."""
+    if hasattr(aos, "polynominal_order_x"):
+        raise NotImplementedError("Cartesian AOs: the walker kernels evaluate spherical AOs only")
     aos.sanity_check()
     oi = np.asarray(aos.orbital_indices, dtype=np.int64)
     ex = np.asarray(aos.exponents, dtype=np.float64)

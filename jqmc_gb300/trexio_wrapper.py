@@ -8,9 +8,14 @@ Coulomb/ECP data.  The conversions are the reference's:
   divided by the primitive normalisation, times the AO normalisation;
 - MOs with occupation >= 1e-6, lambda the identity over the paired
   orbitals (an unpaired block for N_up > N_dn);
-- ECP powers shifted by 2.
-Cartesian bases, periodic cells and complex orbitals raise NotImplementedError,
-as in the reference where noted and because the walker kernels are spherical.
+- ECP powers shifted by 2;
+- Cartesian shells (jqmc/trexio_wrapper.py:229-360) expand into their
+  (l+1)(l+2)/2 components in itertools.combinations_with_replacement order
+  with coefficients c shell_factor prim_factor / N_cart, N_cart the Cartesian
+  primitive normalisation of the component, times the AO normalisation; they
+  give AOs_cart_data (the oracle evaluates them; the walker kernels are
+  spherical).
+Periodic cells and complex orbitals raise NotImplementedError.
 """
 
 from __future__ import annotations
@@ -19,7 +24,7 @@ import math
 
 import numpy as np
 
-from .atomic_orbital import AOs_sphe_data
+from .atomic_orbital import AOs_cart_data, AOs_sphe_data, cartesian_norm, cartesian_orders
 from .coulomb_potential import Coulomb_potential_data
 from .determinant import Geminal_data
 from .hdf5_read import File
@@ -72,8 +77,7 @@ def read_trexio_file(trexio_file: str, store_tuple: bool = False):
     structure = Structure_data(positions=coords, pbc_flag=False, atomic_numbers=seq(_atomic_number(x) for x in labels),
                                element_symbols=seq(labels), atomic_labels=seq(labels))
 
-    if int(attr("ao", "ao_cartesian", 0)):
-        raise NotImplementedError("Cartesian AOs: the walker kernels evaluate spherical AOs only")
+    cartesian = bool(int(attr("ao", "ao_cartesian", 0)))
     shell_num = int(attr("basis", "basis_shell_num"))
     shell_index = data("basis/basis_shell_index")
     shell_nucleus = data("basis/basis_nucleus_index")
@@ -84,28 +88,42 @@ def read_trexio_file(trexio_file: str, store_tuple: bool = False):
     prim_factor = data("basis/basis_prim_factor")
     ao_num = int(attr("ao", "ao_num"))
     ao_norm = data("ao/ao_normalization")
-    nucleus_index, ang, mag, orb_idx, exps, coefs = [], [], [], [], [], []
+    nucleus_index, ang, mag, orb_idx, exps, coefs, powers = [], [], [], [], [], [], []
     ao = 0
     for s in range(shell_num):
         l = int(shell_l[s])
-        ms = [0] + [i * (-1) ** j for i in range(1, l + 1) for j in range(2)]
         prims = [k for k in range(len(shell_index)) if shell_index[k] == s]
-        pc = [shell_factor[s] * prim_factor[k] * math.sqrt(4.0 * math.pi) / math.sqrt(2 * l + 1)
-              / _primitive_normalization(l, expo[k]) * coef[k] for k in prims]
-        for j, m in enumerate(ms):
+        if cartesian:
+            comps = cartesian_orders(l)
+            pcs = [[shell_factor[s] * prim_factor[k] / cartesian_norm(l, expo[k], *pw) * coef[k] for k in prims]
+                   for pw in comps]
+        else:
+            comps = [0] + [i * (-1) ** j for i in range(1, l + 1) for j in range(2)]
+            pc = [shell_factor[s] * prim_factor[k] * math.sqrt(4.0 * math.pi) / math.sqrt(2 * l + 1)
+                  / _primitive_normalization(l, expo[k]) * coef[k] for k in prims]
+            pcs = [pc] * len(comps)
+        for j, comp in enumerate(comps):
             nucleus_index.append(int(shell_nucleus[s]))
             ang.append(l)
-            mag.append(m)
-            for k, c in zip(prims, pc):
+            (powers if cartesian else mag).append(comp)
+            for k, c in zip(prims, pcs[j]):
                 orb_idx.append(ao + j)
                 exps.append(float(expo[k]))
                 coefs.append(float(c * ao_norm[ao + j]))
-        ao += len(ms)
+        ao += len(comps)
     if ao != ao_num:
         raise ValueError(f"ao count {ao} is inconsistent with ao_num = {ao_num}")
-    aos = AOs_sphe_data(structure_data=structure, nucleus_index=seq(nucleus_index), num_ao=ao, num_ao_prim=len(exps),
-                        orbital_indices=seq(orb_idx), exponents=np.array(exps), coefficients=np.array(coefs),
-                        angular_momentums=seq(ang), magnetic_quantum_numbers=seq(mag))
+    if cartesian:
+        pw = np.array(powers, dtype=int).reshape(-1, 3)
+        aos = AOs_cart_data(structure_data=structure, nucleus_index=seq(nucleus_index), num_ao=ao, num_ao_prim=len(exps),
+                            orbital_indices=seq(orb_idx), exponents=np.array(exps), coefficients=np.array(coefs),
+                            angular_momentums=seq(ang), polynominal_order_x=seq(int(x) for x in pw[:, 0]),
+                            polynominal_order_y=seq(int(x) for x in pw[:, 1]),
+                            polynominal_order_z=seq(int(x) for x in pw[:, 2]))
+    else:
+        aos = AOs_sphe_data(structure_data=structure, nucleus_index=seq(nucleus_index), num_ao=ao, num_ao_prim=len(exps),
+                            orbital_indices=seq(orb_idx), exponents=np.array(exps), coefficients=np.array(coefs),
+                            angular_momentums=seq(ang), magnetic_quantum_numbers=seq(mag))
 
     if "mo_coefficient_im" in f["mo"]:
         raise NotImplementedError("complex molecular orbitals are not supported")

@@ -15,6 +15,12 @@ The solid harmonics are evaluated here from the closed form
 (the Racah-normalised real solid harmonics), which equals the reference's
 explicit table entry by entry (pinned by tests/golden).  lap S = 0 since solid
 harmonics are harmonic.
+
+Cartesian AOs (AOs_cart_data; _compute_AOs_cart_debug atomic_orbital.py:1984-2030,
+_compute_AOs_cart :2198-2290, _compute_AOs_value_grad_lap_cart :3378-3510) take
+the monomial P = x^nx y^ny z^nz in place of S, the primitive normalisation
+sqrt((2Z/pi)^(3/2) (8Z)^l nx!ny!nz!/((2nx)!(2ny)!(2nz)!)), and lap P (not zero)
+adds R lap P to the Laplacian.  Pinned by tests/golden/cart.npz.
 """
 
 from __future__ import annotations
@@ -77,15 +83,27 @@ def primitive_norm(l: int, Z):
     return np.sqrt(n2) * sqrt((2 * l + 1) / (4.0 * pi))
 
 
+def cartesian_norm(l: int, Z, nx: int, ny: int, nz: int):
+    """Primitive normalisation of a Cartesian Gaussian (atomic_orbital.py:2005-2016)."""
+    ratio = factorial(nx) * factorial(ny) * factorial(nz) / (factorial(2 * nx) * factorial(2 * ny) * factorial(2 * nz))
+    return np.sqrt((2.0 * Z / pi) ** 1.5 * (8.0 * Z) ** l * ratio)
+
+
 class AOTable:
     """Per-AO primitive tables (padded to the deepest contraction) extracted once
-    from an AOs_sphe_data-like object."""
+    from an AOs_sphe_data- or AOs_cart_data-like object."""
 
     def __init__(self, aos):
         self.num_ao = aos.num_ao
         self.centers = np.asarray(aos.structure_data.positions)[np.asarray(aos.nucleus_index, dtype=int)]
         self.l = np.asarray(aos.angular_momentums, dtype=int)
-        self.m = np.asarray(aos.magnetic_quantum_numbers, dtype=int)
+        self.cart = hasattr(aos, "polynominal_order_x")
+        if self.cart:
+            self.pw = np.stack([np.asarray(aos.polynominal_order_x, dtype=int), np.asarray(aos.polynominal_order_y, dtype=int),
+                                np.asarray(aos.polynominal_order_z, dtype=int)], axis=1)          # (A, 3)
+            self.m = np.zeros(self.num_ao, dtype=int)
+        else:
+            self.m = np.asarray(aos.magnetic_quantum_numbers, dtype=int)
         oi = np.asarray(aos.orbital_indices, dtype=int)
         ex = np.asarray(aos.exponents, dtype=np.float64)
         co = np.asarray(aos.coefficients, dtype=np.float64)
@@ -95,7 +113,10 @@ class AOTable:
         for a in range(self.num_ao):
             z, c = ex[oi == a], co[oi == a]
             self.Z[a, : len(z)] = z
-            self.cN[a, : len(z)] = c * primitive_norm(int(self.l[a]), z)
+            if self.cart:
+                self.cN[a, : len(z)] = c * cartesian_norm(int(self.l[a]), z, *(int(x) for x in self.pw[a]))
+            else:
+                self.cN[a, : len(z)] = c * primitive_norm(int(self.l[a]), z)
         self.by_l = {l: np.nonzero(self.l == l)[0] for l in np.unique(self.l)}
 
 
@@ -105,6 +126,8 @@ def _common(tab: AOTable, r, need_grad: bool):
     r2 = np.sum(d * d, axis=-1)                                      # (P, A)
     e = np.exp(-tab.Z[None, :, :] * r2[:, :, None])                  # (P, A, K)
     pref = tab.cN[None] * e                                          # (P, A, K)
+    if tab.cart:
+        return (d, r2, pref) + _monomials(tab.pw, d, need_grad)
     S = np.zeros(r2.shape)
     gS = np.zeros(d.shape) if need_grad else None
     for l, idx in tab.by_l.items():
@@ -114,22 +137,46 @@ def _common(tab: AOTable, r, need_grad: bool):
         S[:, idx] = Sl[sel, :, cols].T
         if need_grad:
             gS[:, idx] = np.transpose(Gl[sel, :, cols], (1, 0, 2))
-    return d, r2, pref, S, gS
+    return d, r2, pref, S, gS, None
+
+
+def _ipow(x, n):
+    """x^n elementwise for integer n >= 0 per column (0^0 = 1); n may be negative (-> 0)."""
+    n = np.asarray(n)
+    return np.where(n >= 0, np.power(x, np.maximum(n, 0)), 0.0)
+
+
+def _monomials(pw, d, need_grad):
+    """(P, grad P, lap P) of x^nx y^ny z^nz at displacements d (P, A, 3)."""
+    x, y, z = d[..., 0], d[..., 1], d[..., 2]
+    nx, ny, nz = pw[:, 0][None], pw[:, 1][None], pw[:, 2][None]
+    px, py, pz = _ipow(x, nx), _ipow(y, ny), _ipow(z, nz)
+    P = px * py * pz
+    if not need_grad:
+        return P, None, None
+    dx = nx * _ipow(x, nx - 1) * py * pz
+    dy = ny * px * _ipow(y, ny - 1) * pz
+    dz = nz * px * py * _ipow(z, nz - 1)
+    lap = (nx * (nx - 1) * _ipow(x, nx - 2) * py * pz + ny * (ny - 1) * px * _ipow(y, ny - 2) * pz
+           + nz * (nz - 1) * px * py * _ipow(z, nz - 2))
+    return P, np.stack([dx, dy, dz], axis=-1), lap
 
 
 def ao_value(tab: AOTable, r: np.ndarray) -> np.ndarray:
     """AO values (num_ao, P) at points r (P, 3)."""
-    d, r2, pref, S, _ = _common(tab, r, False)
+    d, r2, pref, S, _, _ = _common(tab, r, False)
     return (pref.sum(-1) * S).T
 
 
 def ao_vgl(tab: AOTable, r: np.ndarray):
     """(val, gx, gy, gz, lap), each (num_ao, P), following atomic_orbital.py:3560-3591."""
-    d, r2, pref, S, gS = _common(tab, r, True)
+    d, r2, pref, S, gS, lapS = _common(tab, r, True)
     Z = tab.Z[None]                                                  # (1, A, K)
     ao_p = pref * S[..., None]                                       # (P, A, K)
     g = (ao_p[..., None] * (-2.0 * Z[..., None] * d[:, :, None, :]) + pref[..., None] * gS[:, :, None, :]).sum(2)
     gSd = np.sum(gS * d, axis=-1)                                    # (P, A)
     lap = (ao_p * (4.0 * Z**2 * r2[..., None] - 6.0 * Z) - 4.0 * Z * pref * gSd[..., None]).sum(-1)
+    if lapS is not None:                                             # Cartesian: R lap P
+        lap = lap + pref.sum(-1) * lapS
     val = ao_p.sum(-1)
     return val.T, g[..., 0].T, g[..., 1].T, g[..., 2].T, lap.T

@@ -124,3 +124,33 @@ def test_oracle_determinant_locality_matches_reference(name, golden_dir):
         assert np.any(jr != 1.0)
     with pytest.raises(NotImplementedError):
         D._ecp_moves(o, st, R, 6, "dla")
+
+
+def _cart_aos(g):
+    from jqmc_gb300.atomic_orbital import AOs_cart_data
+    from jqmc_gb300.structure import Structure_data
+    st = Structure_data(positions=g["positions"], atomic_numbers=(0,) * len(g["positions"]))
+    return AOs_cart_data(structure_data=st, nucleus_index=tuple(int(x) for x in g["nucleus_index"]),
+                         num_ao=len(g["angular_momentums"]), num_ao_prim=len(g["exponents"]),
+                         orbital_indices=tuple(int(x) for x in g["orbital_indices"]), exponents=g["exponents"],
+                         coefficients=g["coefficients"], angular_momentums=tuple(int(x) for x in g["angular_momentums"]),
+                         polynominal_order_x=tuple(int(x) for x in g["polynominal_order_x"]),
+                         polynominal_order_y=tuple(int(x) for x in g["polynominal_order_y"]),
+                         polynominal_order_z=tuple(int(x) for x in g["polynominal_order_z"]))
+
+
+def test_oracle_cartesian_aos_match_reference(golden_dir):
+    """Cartesian AOs (s to g shells): values against the reference's debug and
+    production functions, gradients and Laplacians against its fused
+    value/grad/lap (tests/golden/make_cart_golden.py)."""
+    from oracle.ao import AOTable
+    g = np.load(os.path.join(golden_dir, "cart.npz"))
+    aos = _cart_aos(g)
+    aos.sanity_check()
+    tab = AOTable(aos)
+    assert rel(ao_value(tab, g["r"]), g["ao_debug"]) < RTOL
+    assert rel(ao_value(tab, g["r"]), g["ao"]) < RTOL
+    v = ao_vgl(tab, g["r"])
+    for k in range(5):
+        assert rel(v[k], g[f"ao_vgl.{k}"]) < RTOL, k
+    assert max(aos.angular_momentums) == 4

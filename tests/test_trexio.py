@@ -163,5 +163,33 @@ def test_reader_on_reference_files():
         st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, name))
         gem.sanity_check()
         assert (gem.num_electron_up, gem.num_electron_dn) == (nup, ndn)
+
+
+@pytest.mark.skipif(not os.path.isdir(TREXIO_DIR), reason="the reference's TREXIO files are not present")
+def test_cartesian_trexio_files():
+    """Cartesian files give AOs_cart_data with (l+1)(l+2)/2 components per shell.
+    H2 cc-pVDZ (s and p shells) in its Cartesian and spherical files spans one
+    space, so the occupied MO of the two files agrees up to sign at any point:
+    a check of the Cartesian conversion and normalisation (oracle AO values).
+    The walker kernels refuse a Cartesian basis."""
+    from jqmc_gb300.atomic_orbital import AOs_cart_data
+    from jqmc_gb300.engine import pack_basis
+    from jqmc_gb300.trexio_wrapper import read_trexio_file
+    from oracle.ao import AOTable, ao_value
+    for name in sorted(f for f in os.listdir(TREXIO_DIR) if f.endswith("_cart.h5")):
+        st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, name))
+        assert isinstance(aos, AOs_cart_data), name
+        aos.sanity_check()
+        gem.sanity_check()
+        assert all(nx + ny + nz == l for l, nx, ny, nz in zip(aos.angular_momentums, aos.polynominal_order_x,
+                                                               aos.polynominal_order_y, aos.polynominal_order_z))
+    r = np.random.default_rng(0).normal(scale=1.2, size=(40, 3))
+    mo = {}
+    for kind in ("cart", "sphe"):
+        st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, f"H2_ae_ccpvdz_{kind}.h5"))
+        mo[kind] = mu.mo_coefficients[0] @ ao_value(AOTable(aos), r)
+    np.testing.assert_allclose(np.abs(mo["cart"]), np.abs(mo["sphe"]), rtol=1e-12, atol=1e-14)
+    cart = read_trexio_file(os.path.join(TREXIO_DIR, "N_ae_ccpvdz_cart.h5"))[1]
+    assert max(cart.angular_momentums) == 2 and cart.num_ao == 15
     with pytest.raises(NotImplementedError):
-        read_trexio_file(os.path.join(TREXIO_DIR, "N2_ecp_ccpvtz_cart.h5"))
+        pack_basis(cart)
