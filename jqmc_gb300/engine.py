@@ -327,6 +327,11 @@ class WalkerSet:
                                                    self.sys.stream), "jqmc_lrdmc_project_t")
 
     def lrdmc_energy(self, last_draw: torch.Tensor, alat: float):
+        """(e_L, V_diag) with one rotation per walker: last_draw holds 4 doubles per
+        walker (three Euler angles and the unused move uniform of a GFMC_n draw)."""
+        last_draw = last_draw.contiguous()
+        if last_draw.dtype != torch.float64 or last_draw.numel() != 4 * self.nwalk:
+            raise ValueError(f"lrdmc_energy needs 4 float64 draws per walker; got {tuple(last_draw.shape)} {last_draw.dtype}")
         eL = torch.empty(self.nwalk, dtype=torch.float64, device=self.sys.device)
         vd = torch.empty_like(eL)
         d = self.desc()

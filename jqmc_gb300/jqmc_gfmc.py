@@ -225,7 +225,7 @@ class GFMC_t:
         w, total = self.project(draw_source)
         ws = self.walkers
         ws.rebuild()
-        ang = self.draws(1)[:, 0].contiguous()
+        ang = self.draws(1)[:, 0, :4].contiguous()   # the energy reads 4 doubles per walker
         eL, _ = ws.lrdmc_energy(ang, self.alat)
         sums = torch.stack([w.sum(), (w * eL).sum(), (w * eL * eL).sum(), total.double().mean()])
         branch_comb(w, zeta, self._chosen, self._cum)
