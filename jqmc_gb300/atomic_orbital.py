@@ -19,7 +19,7 @@ takes electron positions with a leading walker axis.
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from math import factorial, pi, sqrt
+from math import comb, factorial, pi, sqrt
 
 import numpy as np
 
@@ -121,6 +121,103 @@ def cartesian_norm(l: int, Z: float, nx: int, ny: int, nz: int) -> float:
     normalisation of a Cartesian Gaussian (atomic_orbital.py:1984-2030, :2198-2290)."""
     ratio = factorial(nx) * factorial(ny) * factorial(nz) / (factorial(2 * nx) * factorial(2 * ny) * factorial(2 * nz))
     return sqrt((2.0 * Z / pi) ** 1.5 * (8.0 * Z) ** l * ratio)
+
+
+def _poly_mul(a: dict, b: dict) -> dict:
+    out = {}
+    for ka, va in a.items():
+        for kb, vb in b.items():
+            k = (ka[0] + kb[0], ka[1] + kb[1], ka[2] + kb[2])
+            out[k] = out.get(k, 0.0) + va * vb
+    return out
+
+
+def solid_harmonic_monomials(l: int, m: int) -> dict:
+    """{(a, b, c): coefficient} of S_lm = sum coef x^a y^b z^c, the real solid
+    harmonic scaled by sqrt(4pi/(2l+1)) (the convention of atomic_orbital.py:2353-2585),
+    expanded from the closed form Pi_l^|m|(z, r^2) times Re/Im (x + iy)^|m|."""
+    am = abs(m)
+    pi = {}
+    for k in range((l - am) // 2 + 1):
+        ck = ((-1) ** k * 2.0 ** -l * comb(l, k) * comb(2 * l - 2 * k, l) * factorial(l - 2 * k)
+              / factorial(l - 2 * k - am))
+        for i in range(k + 1):
+            for j in range(k - i + 1):
+                q = k - i - j
+                key = (2 * i, 2 * j, 2 * q + l - 2 * k - am)
+                pi[key] = pi.get(key, 0.0) + ck * factorial(k) / (factorial(i) * factorial(j) * factorial(q))
+    scale = sqrt(factorial(l - am) / factorial(l + am))
+    if m == 0:
+        return {k: v * scale for k, v in pi.items() if v != 0.0}
+    part = {}
+    for t in range(am + 1):   # (x + i y)^|m| = sum C(|m|, t) x^(|m|-t) (i y)^t
+        if (t % 2 == 0) == (m > 0):
+            sign = (-1) ** (t // 2)
+            part[(am - t, t, 0)] = sign * comb(am, t)
+    out = _poly_mul(pi, part)
+    return {k: v * scale * sqrt(2.0) for k, v in out.items() if v != 0.0}
+
+
+def spherical_to_cartesian_matrix(l: int) -> np.ndarray:
+    """(2l+1, (l+1)(l+2)/2): row m + l expresses the spherical AO of m as a
+    combination of the Cartesian AOs of the same shell (same exponents and
+    contraction coefficients, each with its own primitive normalisation), in
+    TREXIO component order.  The factor N_sph / N_cart does not depend on Z."""
+    orders = cartesian_orders(l)
+    T = np.zeros((2 * l + 1, len(orders)))
+    for m in range(-l, l + 1):
+        for key, c in solid_harmonic_monomials(l, m).items():
+            T[m + l, orders.index(key)] = c * primitive_norm(l, 1.0) / cartesian_norm(l, 1.0, *key)
+    return T
+
+
+def aos_cart_to_sphe(aos_data):
+    """(AOs_sphe_data, transform_pinv (num_ao_cart, num_ao_sph)) of a Cartesian
+    basis (atomic_orbital.py:1574-1690): Cartesian AOs on one nucleus with one l
+    and the same primitives form a shell, which must be complete; each shell
+    gives 2l+1 spherical AOs with those primitives, m = -l..l; MO coefficients
+    map by C_sph = C_cart transform_pinv, the least-squares projection (exact
+    for l <= 1; higher shells drop their r^2 components)."""
+    if isinstance(aos_data, AOs_sphe_data):
+        return aos_data, np.eye(aos_data.num_ao)
+    if not isinstance(aos_data, AOs_cart_data):
+        raise ValueError("Spherical conversion is only available from Cartesian AOs.")
+    shells = []
+    for a in range(aos_data.num_ao):
+        e, c = aos_data.primitives_of(a)
+        atom, l = int(aos_data.nucleus_index[a]), int(aos_data.angular_momentums[a])
+        pw = (int(aos_data.polynominal_order_x[a]), int(aos_data.polynominal_order_y[a]), int(aos_data.polynominal_order_z[a]))
+        for sh in shells:
+            if (sh["atom"] == atom and sh["l"] == l and len(sh["exps"]) == len(e) and np.allclose(sh["exps"], e)
+                    and np.allclose(sh["coefs"], c) and pw not in sh["aos"]):
+                sh["aos"][pw] = a
+                break
+        else:
+            shells.append({"atom": atom, "l": l, "exps": e, "coefs": c, "aos": {pw: a}})
+    n_sph = sum(2 * sh["l"] + 1 for sh in shells)
+    T = np.zeros((n_sph, aos_data.num_ao))
+    nuc, ls, ms, oi, ex, co = [], [], [], [], [], []
+    row = 0
+    for sh in shells:
+        l = sh["l"]
+        orders = cartesian_orders(l)
+        if set(sh["aos"]) != set(orders):
+            raise ValueError(f"Shell with l={l} at nucleus {sh['atom']} is incomplete: {len(sh['aos'])} Cartesian AOs found.")
+        cols = [sh["aos"][o] for o in orders]
+        T[np.ix_(range(row, row + 2 * l + 1), cols)] = spherical_to_cartesian_matrix(l)
+        for m in range(-l, l + 1):
+            a = len(nuc)
+            nuc.append(sh["atom"])
+            ls.append(l)
+            ms.append(m)
+            oi += [a] * len(sh["exps"])
+            ex += list(sh["exps"])
+            co += list(sh["coefs"])
+        row += 2 * l + 1
+    sph = AOs_sphe_data(structure_data=aos_data.structure_data, nucleus_index=tuple(nuc), num_ao=n_sph, num_ao_prim=len(ex),
+                        orbital_indices=tuple(oi), exponents=np.array(ex), coefficients=np.array(co),
+                        angular_momentums=tuple(ls), magnetic_quantum_numbers=tuple(ms))
+    return sph, np.linalg.pinv(T)
 
 
 @dataclass(frozen=True)

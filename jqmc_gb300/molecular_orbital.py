@@ -36,6 +36,17 @@ class MOs_data:
             raise ValueError(f"mo_coefficients.shape={self.mo_coefficients.shape} != ({self.num_mo}, {self.aos_data.num_ao})")
         self.aos_data.sanity_check()
 
+    def to_spherical(self) -> "MOs_data":
+        """The MOs over spherical AOs (molecular_orbital.py:214-236): a Cartesian
+        basis becomes its spherical shells and C_sph = C_cart transform_pinv
+        (atomic_orbital.aos_cart_to_sphe); a spherical set is returned as it is.
+        This is how a Cartesian TREXIO wavefunction reaches the walker kernels."""
+        from .atomic_orbital import aos_cart_to_sphe
+        if isinstance(self.aos_data, AOs_sphe_data):
+            return self
+        sph, pinv = aos_cart_to_sphe(self.aos_data)
+        return MOs_data(num_mo=self.num_mo, aos_data=sph, mo_coefficients=self.mo_coefficients @ pinv)
+
 
 # ---------------------------------------------------------------- evaluation (GPU: AO tables, then C x AO)
 def compute_MOs(mos_data: MOs_data, r_carts) -> np.ndarray:

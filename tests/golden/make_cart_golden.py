@@ -11,7 +11,9 @@ the shells of water_like's geminal basis (l <= 2) with their exponents and
 contraction coefficients, every shell expanded into its (l+1)(l+2)/2 Cartesian
 components in TREXIO order, plus an f and a g shell on the first nucleus.  The
 reference's _compute_AOs_cart_debug, compute_AOs and compute_AOs_value_grad_lap
-are evaluated at seeded points; inputs and outputs go to tests/golden/cart.npz.
+are evaluated at seeded points, and its Cartesian -> spherical conversion
+(_aos_cart_to_sphe, MOs_data.to_spherical) is applied to the basis and to
+seeded MO coefficients; inputs and outputs go to tests/golden/cart.npz.
 """
 
 from __future__ import annotations
@@ -29,6 +31,7 @@ sys.path.insert(0, REFERENCE)
 sys.path.insert(0, ROOT)
 
 import jqmc.atomic_orbital as r_ao  # noqa: E402
+import jqmc.molecular_orbital as r_mo  # noqa: E402
 import jqmc.structure as r_st  # noqa: E402
 
 from jqmc_gb300 import synthetic  # noqa: E402
@@ -78,6 +81,19 @@ def main():
     out["ao"] = np.asarray(r_ao.compute_AOs(aos, r), dtype=np.float64)
     for k, v in enumerate(r_ao.compute_AOs_value_grad_lap(aos, r)):
         out[f"ao_vgl.{k}"] = np.asarray(v, dtype=np.float64)
+    # the reference's Cartesian -> spherical conversion (atomic_orbital.py:1574-1690,
+    # molecular_orbital.py:214-236) of the same basis and of seeded MO coefficients
+    sph, pinv = r_ao._aos_cart_to_sphe(aos)
+    out["to_sphe_pinv"] = np.asarray(pinv, dtype=np.float64)
+    out["to_sphe_l"] = np.asarray(sph.angular_momentums)
+    out["to_sphe_m"] = np.asarray(sph.magnetic_quantum_numbers)
+    out["to_sphe_nucleus_index"] = np.asarray(sph.nucleus_index)
+    out["to_sphe_exponents"] = np.asarray(sph.exponents, dtype=np.float64)
+    out["to_sphe_coefficients"] = np.asarray(sph.coefficients, dtype=np.float64)
+    c_cart = np.random.default_rng(32).normal(size=(3, aos.num_ao))
+    mos = r_mo.MOs_data(num_mo=3, aos_data=aos, mo_coefficients=c_cart).to_spherical()
+    out["mo_cart_coefficients"] = c_cart
+    out["mo_sphe_coefficients"] = np.asarray(mos.mo_coefficients, dtype=np.float64)
     path = os.path.join(HERE, "cart.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {len(out)} arrays to {path}; {aos.num_ao} AOs")

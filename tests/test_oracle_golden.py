@@ -154,3 +154,30 @@ def test_oracle_cartesian_aos_match_reference(golden_dir):
     for k in range(5):
         assert rel(v[k], g[f"ao_vgl.{k}"]) < RTOL, k
     assert max(aos.angular_momentums) == 4
+
+
+def test_cartesian_to_spherical_matches_reference(golden_dir):
+    """MOs_data.to_spherical (molecular_orbital.py:214-236) and the basis
+    conversion behind it (atomic_orbital.py:1574-1690) against the reference's
+    on the s-g Cartesian basis of tests/golden/cart.npz; MOs that lie in the
+    spherical span come back unchanged in value."""
+    from jqmc_gb300.atomic_orbital import aos_cart_to_sphe, spherical_to_cartesian_matrix
+    from jqmc_gb300.molecular_orbital import MOs_data
+    from oracle.ao import AOTable
+    g = np.load(os.path.join(golden_dir, "cart.npz"))
+    aos = _cart_aos(g)
+    sph, pinv = aos_cart_to_sphe(aos)
+    assert rel(pinv, g["to_sphe_pinv"]) < RTOL
+    assert tuple(sph.angular_momentums) == tuple(g["to_sphe_l"]) and tuple(sph.magnetic_quantum_numbers) == tuple(g["to_sphe_m"])
+    assert tuple(sph.nucleus_index) == tuple(g["to_sphe_nucleus_index"])
+    assert np.array_equal(sph.exponents, g["to_sphe_exponents"]) and np.array_equal(sph.coefficients, g["to_sphe_coefficients"])
+    mo = MOs_data(num_mo=3, aos_data=aos, mo_coefficients=g["mo_cart_coefficients"]).to_spherical()
+    assert rel(mo.mo_coefficients, g["mo_sphe_coefficients"]) < RTOL
+    # spherical span: C_cart = C_sph T reproduces the MO values exactly after the conversion
+    T = np.linalg.pinv(pinv)
+    c_sph = np.random.default_rng(5).normal(size=(2, sph.num_ao))
+    back = MOs_data(num_mo=2, aos_data=aos, mo_coefficients=c_sph @ T).to_spherical()
+    assert rel(back.mo_coefficients, c_sph) < 1e-10
+    assert rel(back.mo_coefficients @ ao_value(AOTable(sph), g["r"]), (c_sph @ T) @ ao_value(AOTable(aos), g["r"])) < 1e-10
+    for l in range(5):
+        assert spherical_to_cartesian_matrix(l).shape == (2 * l + 1, (l + 1) * (l + 2) // 2)

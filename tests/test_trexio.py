@@ -189,6 +189,11 @@ def test_cartesian_trexio_files():
         st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, f"H2_ae_ccpvdz_{kind}.h5"))
         mo[kind] = mu.mo_coefficients[0] @ ao_value(AOTable(aos), r)
     np.testing.assert_allclose(np.abs(mo["cart"]), np.abs(mo["sphe"]), rtol=1e-12, atol=1e-14)
+    # s and p shells: to_spherical is exact, and gives a basis the walker kernels take
+    st, aos, mu, md, gem, coul = read_trexio_file(os.path.join(TREXIO_DIR, "H2_ae_ccpvdz_cart.h5"))
+    ms = mu.to_spherical()
+    np.testing.assert_allclose(ms.mo_coefficients[0] @ ao_value(AOTable(ms.aos_data), r), mo["cart"], rtol=1e-12, atol=1e-14)
+    pack_basis(ms.aos_data)
     cart = read_trexio_file(os.path.join(TREXIO_DIR, "N_ae_ccpvdz_cart.h5"))[1]
     assert max(cart.angular_momentums) == 2 and cart.num_ao == 15
     with pytest.raises(NotImplementedError):
