@@ -54,6 +54,53 @@ class Geminal_data:
         if self.num_electron_up < self.num_electron_dn:
             raise ValueError("Number of up electrons must not be smaller than dn electrons.")
 
+    @property
+    def is_mo_representation(self) -> bool:
+        return isinstance(self.orb_data_up_spin, MOs_data) and isinstance(self.orb_data_dn_spin, MOs_data)
+
+    @property
+    def is_ao_representation(self) -> bool:
+        return not isinstance(self.orb_data_up_spin, MOs_data) and not isinstance(self.orb_data_dn_spin, MOs_data)
+
+    def symmetrize_lambda(self, mat):
+        """(A + A^T)/2 on the paired block when the current lambda's paired block is
+        symmetric (atol 1e-8, rtol 1e-6), else mat unchanged (determinant.py:332-380)."""
+        from .variational import _lambda_paired_columns, _symmetrize_leading_square
+        mat = np.asarray(mat, dtype=np.float64)
+        return _symmetrize_leading_square(mat.shape, _lambda_paired_columns(self.lambda_matrix))(mat)
+
+    def to_spherical(self) -> "Geminal_data":
+        """Spherical orbitals (determinant.py:587-626): MOs through
+        MOs_data.to_spherical with lambda unchanged; Cartesian AOs through the
+        basis conversion, lambda_paired -> P_up^T lambda P_dn and lambda_unpaired ->
+        P_up^T lambda (P the pseudo-inverse maps of aos_cart_to_sphe)."""
+        from .atomic_orbital import aos_cart_to_sphe
+        up, dn = self.orb_data_up_spin, self.orb_data_dn_spin
+        if isinstance(up, MOs_data) or isinstance(dn, MOs_data):
+            if not self.is_mo_representation:
+                raise ValueError("Spherical conversion requires both spin channels to use MOs or both to use AOs.")
+            return Geminal_data(self.num_electron_up, self.num_electron_dn, up.to_spherical(), dn.to_spherical(),
+                                self.lambda_matrix)
+        if isinstance(up, AOs_sphe_data) and isinstance(dn, AOs_sphe_data):
+            return self
+        sph_up, p_up = aos_cart_to_sphe(up)
+        sph_dn, p_dn = aos_cart_to_sphe(dn)
+        lp, lu = self.lambda_matrix[:, : self.orb_num_dn], self.lambda_matrix[:, self.orb_num_dn:]
+        lam = np.hstack([p_up.T @ lp @ p_dn, p_up.T @ lu])
+        return Geminal_data(self.num_electron_up, self.num_electron_dn, sph_up, sph_dn, lam)
+
+    @classmethod
+    def convert_from_MOs_to_AOs(cls, geminal_data: "Geminal_data") -> "Geminal_data":
+        """The same geminal over the AOs: lambda_AO = C_up^T lambda C_dn (paired) and
+        C_up^T lambda (unpaired) (determinant.py:687-722); AO geminals are returned as they are."""
+        if geminal_data.is_ao_representation:
+            return geminal_data
+        if not geminal_data.is_mo_representation:
+            raise NotImplementedError("mixed MO/AO geminals")
+        aos, lp, lu = geminal_data.ao_basis_lambda()
+        return cls(geminal_data.num_electron_up, geminal_data.num_electron_dn, aos,
+                   geminal_data.orb_data_dn_spin.aos_data, np.hstack([lp, lu]))
+
     def ao_basis_lambda(self):
         """(aos_data, lambda_paired_AO, lambda_unpaired_AO) with any MO layer folded
         into the pairing matrix: lambda_AO = C_up^T lambda C_dn."""

@@ -181,3 +181,43 @@ def test_cartesian_to_spherical_matches_reference(golden_dir):
     assert rel(back.mo_coefficients @ ao_value(AOTable(sph), g["r"]), (c_sph @ T) @ ao_value(AOTable(aos), g["r"])) < 1e-10
     for l in range(5):
         assert spherical_to_cartesian_matrix(l).shape == (2 * l + 1, (l + 1) * (l + 2) // 2)
+
+
+def test_geminal_conversions_keep_the_geminal():
+    """Geminal_data.convert_from_MOs_to_AOs (determinant.py:687-722) and
+    to_spherical (:587-626) give the same geminal matrix (oracle values): the
+    MO geminal of water_like over its AOs, and a Cartesian-AO geminal whose
+    lambda lies in the spherical span (lambda_cart = T^T lambda_sph T) over the
+    spherical shells, where lambda comes back exactly."""
+    import dataclasses
+
+    from cart_system import cartesian_from_spherical
+    from jqmc_gb300.atomic_orbital import aos_cart_to_sphe
+    from jqmc_gb300.determinant import Geminal_data
+    syn = synthetic.water_like()
+    ham = syn.hamiltonian
+    gem = ham.wavefunction_data.geminal_data
+    assert gem.is_mo_representation and not gem.is_ao_representation
+    r_up, r_dn = syn.initial_electrons(2, seed=9)
+
+    def geminal(g):
+        o = OracleSystem(dataclasses.replace(ham, wavefunction_data=dataclasses.replace(ham.wavefunction_data, geminal_data=g)))
+        return [o.geminal(r_up[w], r_dn[w]) for w in range(2)]
+
+    ao = Geminal_data.convert_from_MOs_to_AOs(gem)
+    assert ao.is_ao_representation and Geminal_data.convert_from_MOs_to_AOs(ao) is ao
+    for a, b in zip(geminal(ao), geminal(gem)):
+        assert rel(a, b) < 1e-12
+    sph = ao.orb_data_up_spin
+    cart = cartesian_from_spherical(sph)
+    _, pinv = aos_cart_to_sphe(cart)
+    T = np.linalg.pinv(pinv)
+    lam_sph = ao.lambda_matrix
+    gc = Geminal_data(gem.num_electron_up, gem.num_electron_dn, cart, cart, T.T @ lam_sph @ T)
+    gs = gc.to_spherical()
+    assert rel(gs.lambda_matrix, lam_sph) < 1e-10
+    for a, b in zip(geminal(gs), geminal(gc)):
+        assert rel(a, b) < 1e-10
+    assert gem.to_spherical().lambda_matrix is gem.lambda_matrix
+    sym = gs.symmetrize_lambda(gs.lambda_matrix + np.triu(np.ones_like(gs.lambda_matrix), 1))
+    assert np.array_equal(sym, sym.T)
