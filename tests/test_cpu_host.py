@@ -392,3 +392,29 @@ def test_as_factor_matches_the_oracle():
     want = np.array([OracleSystem.as_factor(g, gi) for g, gi in zip(G, Gi)])
     assert np.allclose(got, want, rtol=1e-14, atol=0.0), (got, want)
     assert got[3] == 0.0
+
+
+def test_initial_electrons_follow_the_reference_assignment(golden_dir):
+    """The nucleus of every initial electron equals the reference's
+    _generate_init_electron_configurations on nine charge/spin cases
+    (tests/golden/init_owners.npz); up electrons past the total charge go to
+    random nuclei (per walker) in both; offsets lie between 0.1 and 1 bohr."""
+    from jqmc_gb300._init_config import electron_owners, initial_electrons
+    g = np.load(os.path.join(golden_dir, "init_owners.npz"))
+    for name in g["cases"]:
+        z, c, (nu, nd) = g[f"{name}.charges"], g[f"{name}.coords"], (int(x) for x in g[f"{name}.n"])
+        up, dn, nr, order = electron_owners(z, c, nu, nd)
+        ru, rd = g[f"{name}.up_owner"], g[f"{name}.dn_owner"]
+        assert np.all(rd == dn[None]), name
+        assert np.all(ru[:, :nu - nr] == up[None, :nu - nr]), name
+        assert nr == 0 or not np.all(ru[:, nu - nr:] == ru[0, nu - nr:]), name    # random in the reference too
+        r_up, r_dn = initial_electrons(c, z, nu, nd, 64, seed=3)
+        assert r_up.shape == (64, nu, 3) and r_dn.shape == (64, nd, 3)
+        d_dn = np.linalg.norm(r_dn - c[dn][None], axis=-1)
+        assert np.all((d_dn >= 0.1) & (d_dn <= 1.0)), name
+        near = np.min(np.linalg.norm(r_up[:, :, None, :] - c[None, None], axis=-1), axis=-1)
+        assert np.all(near <= 1.0), name
+        again = initial_electrons(c, z, nu, nd, 64, seed=3)
+        assert np.array_equal(again[0], r_up) and np.array_equal(again[1], r_dn)
+    with pytest.raises(ValueError):
+        electron_owners(np.array([1.0]), np.zeros((1, 3)), 0, 2)
