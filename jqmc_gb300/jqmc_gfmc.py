@@ -22,6 +22,7 @@ threefry stream of the reference is not reproduced.
 from __future__ import annotations
 
 import math
+import time
 
 import numpy as np
 import torch
@@ -107,7 +108,11 @@ class GFMC_n:
         return sums
 
     def run(self, num_mcmc_steps: int = 50, max_time: int = 86400) -> None:
+        """num_mcmc_steps branching cycles, stopping early once max_time seconds have passed."""
+        t0 = time.perf_counter()
         for _ in range(num_mcmc_steps):
+            if time.perf_counter() - t0 > max_time:
+                break
             zeta = float(self._np_rng.random())
             sums = self.run_block(self.draws(), zeta).cpu().numpy()
             w_avg = sums[0] / self.num_walkers
@@ -234,7 +239,11 @@ class GFMC_t:
         return sums
 
     def run(self, num_mcmc_steps: int = 50, max_time: int = 86400) -> None:
+        """num_mcmc_steps branching cycles, stopping early once max_time seconds have passed."""
+        t0 = time.perf_counter()
         for _ in range(num_mcmc_steps):
+            if time.perf_counter() - t0 > max_time:
+                break
             zeta = float(self._np_rng.random())
             sums = self.run_block(zeta).cpu().numpy()
             self._w_L.append(sums[0] / self.num_walkers)

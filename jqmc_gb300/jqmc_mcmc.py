@@ -124,7 +124,12 @@ class MCMC:
         return self.walkers.vmc_measure(angles, self.epsilon_AS)
 
     def run(self, num_mcmc_steps: int = 0, max_time: int = 86400) -> None:
+        """num_mcmc_steps measurements, stopping early once max_time seconds have
+        passed (jqmc_mcmc.py:448, :940-947)."""
+        t0 = time.perf_counter()
         for _ in range(num_mcmc_steps):
+            if time.perf_counter() - t0 > max_time:
+                break
             idraw, fdraw, angles = self.draws()
             eL, wL = self.run_block(idraw, fdraw, angles)
             self._e_L.append(eL.cpu().numpy())
@@ -255,7 +260,7 @@ class MCMC:
         t0 = time.perf_counter()
         try:
             for _ in range(num_opt_steps):
-                self.run(num_mcmc_steps=num_mcmc_steps)
+                self.run(num_mcmc_steps=num_mcmc_steps, max_time=max_time)
                 E, E_std, _, _ = self.get_E(num_mcmc_warmup_steps, num_mcmc_bin_blocks)
                 if not np.isfinite(E):
                     break
