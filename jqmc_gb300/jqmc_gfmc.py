@@ -128,6 +128,11 @@ class GFMC_n:
         return gfmc_G_L(np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1), self.num_gfmc_collect_steps)
 
     @property
+    def bare_w_L(self) -> np.ndarray:
+        """The per-step mean walker weights before the G_L products (jqmc_gfmc.py:4599-4601)."""
+        return np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1)
+
+    @property
     def e_L(self) -> np.ndarray:
         return np.asarray(self._e_L, dtype=np.float64).reshape(-1, 1)[self.num_gfmc_collect_steps:]
 
@@ -255,6 +260,11 @@ class GFMC_t:
     @property
     def w_L(self) -> np.ndarray:
         return gfmc_G_L(np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1), self.num_gfmc_collect_steps)
+
+    @property
+    def bare_w_L(self) -> np.ndarray:
+        """The per-step mean walker weights before the G_L products (jqmc_gfmc.py:4599-4601)."""
+        return np.asarray(self._w_L, dtype=np.float64).reshape(-1, 1)
 
     @property
     def e_L(self) -> np.ndarray:
