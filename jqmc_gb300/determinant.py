@@ -137,6 +137,40 @@ def compute_det_geminal_all_elements(geminal_data: Geminal_data, r_up_carts, r_d
     return surface.scalar_or_array(sg * ld.exp(), single)
 
 
+def _geminal_ao_parts(geminal_data: Geminal_data):
+    """(up AOs, down AOs, lambda paired, lambda unpaired) with any MO layer folded into lambda."""
+    aos_up, lp, lu = geminal_data.ao_basis_lambda()
+    dn = geminal_data.orb_data_dn_spin
+    return aos_up, (dn.aos_data if isinstance(dn, MOs_data) else dn), lp, lu
+
+
+def compute_geminal_up_one_row_elements(geminal_data: Geminal_data, r_up_cart, r_dn_carts) -> np.ndarray:
+    """Row of G for one up electron at r_up_cart (1, 3): phi_up(r)^T lambda_paired
+    phi_dn(r_dn) followed by phi_up(r)^T lambda_unpaired, shape (N_dn + N_unpaired,)
+    (jqmc/determinant.py:1430-1478); AO values from the GPU (jqmc_ao_vgl)."""
+    import torch
+
+    from . import surface
+    aos_up, aos_dn, lp, lu = _geminal_ao_parts(geminal_data)
+    pu = surface.ao_vgl(aos_up, np.asarray(r_up_cart, dtype=np.float64).reshape(1, 3))[0][:, 0]
+    t = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=pu.device)   # noqa: E731
+    r_dn = np.asarray(r_dn_carts, dtype=np.float64).reshape(-1, 3)
+    paired = pu @ t(lp) @ surface.ao_vgl(aos_dn, r_dn)[0] if len(r_dn) else pu.new_zeros(0)
+    return surface.as_numpy(torch.cat([paired, pu @ t(lu)]))
+
+
+def compute_geminal_dn_one_column_elements(geminal_data: Geminal_data, r_up_carts, r_dn_cart) -> np.ndarray:
+    """Column of G for one down electron at r_dn_cart (1, 3): phi_up(r_up)^T
+    lambda_paired phi_dn(r), shape (N_up,) (jqmc/determinant.py:1482-1526)."""
+    import torch
+
+    from . import surface
+    aos_up, aos_dn, lp, _ = _geminal_ao_parts(geminal_data)
+    pd = surface.ao_vgl(aos_dn, np.asarray(r_dn_cart, dtype=np.float64).reshape(1, 3))[0][:, 0]
+    pu = surface.ao_vgl(aos_up, np.asarray(r_up_carts, dtype=np.float64).reshape(-1, 3))[0]
+    return surface.as_numpy(pu.T @ torch.as_tensor(np.asarray(lp, dtype=np.float64), device=pd.device) @ pd)
+
+
 def compute_AS_regularization_factor(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
     """Attaccalite-Sorella regularization factor (jqmc/determinant.py:1291)."""
     from . import surface

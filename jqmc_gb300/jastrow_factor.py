@@ -88,6 +88,23 @@ class Jastrow_data:
 
 
 # ---------------------------------------------------------------- evaluation (GPU: jqmc_log_psi's Jastrow output)
+def _compute_ratio_Jastrow_part_rank1_update(jastrow_data: Jastrow_data, old_r_up_carts, old_r_dn_carts,
+                                             new_r_up_carts_arr, new_r_dn_carts_arr, j3_state=None) -> np.ndarray:
+    """exp(J(r') - J(r)) for G configurations r' (G, n, 3) against r
+    (jqmc/jastrow_factor.py:2230-2693): J of all G + 1 configurations in one GPU
+    evaluation.  j3_state (the reference's streaming cache) is accepted and not
+    needed."""
+    import torch
+
+    from . import surface
+    ou, od = np.asarray(old_r_up_carts, dtype=np.float64), np.asarray(old_r_dn_carts, dtype=np.float64)
+    nu, nd = np.asarray(new_r_up_carts_arr, dtype=np.float64), np.asarray(new_r_dn_carts_arr, dtype=np.float64)
+    if nu.ndim != 3 or nd.ndim != 3 or nu.shape[0] != nd.shape[0] or nu.shape[1:] != ou.shape or nd.shape[1:] != od.shape:
+        raise ValueError(f"new configurations {nu.shape}, {nd.shape} do not match the old ones {ou.shape}, {od.shape}")
+    jj, _ = surface.jastrow_value(jastrow_data, np.concatenate([ou[None], nu]), np.concatenate([od[None], nd]))
+    return surface.as_numpy(torch.exp(jj[1:] - jj[0]))
+
+
 def compute_Jastrow_part(jastrow_data: Jastrow_data, r_up_carts, r_dn_carts):
     """J = J1 + J2 + J3, without exp (jqmc/jastrow_factor.py:2127)."""
     from . import surface

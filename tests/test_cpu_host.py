@@ -295,8 +295,12 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
         determinant: {**{n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
                          ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
                           "compute_det_geminal_all_elements", "compute_AS_regularization_factor")},
-                      "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"]},
+                      "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"],
+                      "compute_geminal_up_one_row_elements": ["geminal_data", "r_up_cart", "r_dn_carts"],
+                      "compute_geminal_dn_one_column_elements": ["geminal_data", "r_up_carts", "r_dn_cart"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
+                         "_compute_ratio_Jastrow_part_rank1_update": ["jastrow_data", "old_r_up_carts", "old_r_dn_carts",
+                                                                      "new_r_up_carts_arr", "new_r_dn_carts_arr", "j3_state"],
                          "compute_Jastrow_one_body": ["jastrow_one_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_two_body": ["jastrow_two_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"]},

@@ -117,3 +117,33 @@ def test_local_energy(setup):
     batch = H.compute_local_energy(ham, r_up, r_dn, RT)
     assert batch.shape == (3,)
     assert rel(batch, ref) < RTOL
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_geminal_rows_columns_and_jastrow_ratios_match_reference(name, golden_dir):
+    """compute_geminal_up_one_row_elements / _dn_one_column_elements rebuild the
+    reference's geminal matrix row by row and column by column, and
+    _compute_ratio_Jastrow_part_rank1_update reproduces the reference's ratios for
+    its single-electron moves (tests/golden/<system>.npz, made by the reference)."""
+    import os
+
+    from jqmc_gb300 import determinant as D
+    from jqmc_gb300 import jastrow_factor as J
+    from jqmc_gb300 import synthetic
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    wf = synthetic.SYSTEMS[name]().hamiltonian.wavefunction_data
+    gem, jd = wf.geminal_data, wf.jastrow_data
+    for w in range(g["r_up"].shape[0]):
+        ru, rd = g["r_up"][w], g["r_dn"][w]
+        G = g["geminal"][w]
+        rows = np.stack([D.compute_geminal_up_one_row_elements(gem, ru[i:i + 1], rd) for i in range(len(ru))])
+        cols = np.stack([D.compute_geminal_dn_one_column_elements(gem, ru, rd[j:j + 1]) for j in range(len(rd))], axis=1)
+        assert rel(rows, G) < RTOL and rel(cols, G) < RTOL
+        nu, nd = [], []
+        for k in range(g["moves_spin"].shape[1]):
+            u, d = ru.copy(), rd.copy()
+            (u if g["moves_spin"][w, k] == 0 else d)[g["moves_idx"][w, k]] += g["moves_d"][w, k]
+            nu.append(u)
+            nd.append(d)
+        ratio = J._compute_ratio_Jastrow_part_rank1_update(jd, ru, rd, np.stack(nu), np.stack(nd))
+        assert rel(ratio, g["J_ratio"][w]) < RTOL
