@@ -171,6 +171,50 @@ def compute_geminal_dn_one_column_elements(geminal_data: Geminal_data, r_up_cart
     return surface.as_numpy(pu.T @ torch.as_tensor(np.asarray(lp, dtype=np.float64), device=pd.device) @ pd)
 
 
+def _compute_ratio_determinant_part_rank1_update(geminal_data: Geminal_data, A_old_inv, old_r_up_carts, old_r_dn_carts,
+                                                 new_r_up_carts_arr, new_r_dn_carts_arr) -> np.ndarray:
+    """det G(r')/det G(r) for G configurations r' (G, n, 3) that each move one
+    electron (determinant.py:1530-1662): the new row (up move) or column (down
+    move) times the matching column or row of A_old_inv = G(r)^-1.  The AO
+    values of all moved electrons come from two GPU calls; a configuration that
+    moves no electron has ratio 1."""
+    import torch
+
+    from . import surface
+    aos_up, aos_dn, lp, lu = _geminal_ao_parts(geminal_data)
+    ou, od = np.asarray(old_r_up_carts, dtype=np.float64), np.asarray(old_r_dn_carts, dtype=np.float64)
+    nu, nd = np.asarray(new_r_up_carts_arr, dtype=np.float64), np.asarray(new_r_dn_carts_arr, dtype=np.float64)
+    if nu.ndim != 3 or nd.ndim != 3 or nu.shape[0] != nd.shape[0] or nu.shape[1:] != ou.shape or nd.shape[1:] != od.shape:
+        raise ValueError(f"new configurations {nu.shape}, {nd.shape} do not match the old ones {ou.shape}, {od.shape}")
+    G = nu.shape[0]
+    mu = np.any(nu != ou[None], axis=-1)             # (G, n_up) moved up electrons
+    md = np.any(nd != od[None], axis=-1)
+    if np.any(mu.sum(1) + md.sum(1) > 1):
+        raise ValueError("each new configuration must move one electron")
+    gu, iu = np.nonzero(mu)
+    gd, jd = np.nonzero(md)
+    out = np.ones(G)
+    if len(gu) == 0 and len(gd) == 0:
+        return out
+    dev = None
+    if len(gu):
+        pu = surface.ao_vgl(aos_up, nu[gu, iu])[0]                      # (A, K_up)
+        dev = pu.device
+    if len(gd):
+        pdn = surface.ao_vgl(aos_dn, nd[gd, jd])[0]                     # (A, K_dn)
+        dev = pdn.device
+    t = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=dev)   # noqa: E731
+    Ginv = t(A_old_inv)
+    if len(gu):
+        paired = pu.T @ t(lp) @ surface.ao_vgl(aos_dn, od)[0] if len(od) else pu.new_zeros((pu.shape[1], 0))
+        rows = torch.cat([paired, pu.T @ t(lu)], dim=1)                 # (K_up, n_up)
+        out[gu] = surface.as_numpy((rows * Ginv[:, torch.as_tensor(iu, device=dev)].T).sum(1))
+    if len(gd):
+        cols = surface.ao_vgl(aos_up, ou)[0].T @ t(lp) @ pdn            # (n_up, K_dn)
+        out[gd] = surface.as_numpy((Ginv[torch.as_tensor(jd, device=dev), :] * cols.T).sum(1))
+    return out
+
+
 def compute_AS_regularization_factor(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
     """Attaccalite-Sorella regularization factor (jqmc/determinant.py:1291)."""
     from . import surface

@@ -297,7 +297,10 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                           "compute_det_geminal_all_elements", "compute_AS_regularization_factor")},
                       "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"],
                       "compute_geminal_up_one_row_elements": ["geminal_data", "r_up_cart", "r_dn_carts"],
-                      "compute_geminal_dn_one_column_elements": ["geminal_data", "r_up_carts", "r_dn_cart"]},
+                      "compute_geminal_dn_one_column_elements": ["geminal_data", "r_up_carts", "r_dn_cart"],
+                      "_compute_ratio_determinant_part_rank1_update": ["geminal_data", "A_old_inv", "old_r_up_carts",
+                                                                       "old_r_dn_carts", "new_r_up_carts_arr",
+                                                                       "new_r_dn_carts_arr"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
                          "_compute_ratio_Jastrow_part_rank1_update": ["jastrow_data", "old_r_up_carts", "old_r_dn_carts",
                                                                       "new_r_up_carts_arr", "new_r_dn_carts_arr", "j3_state"],
@@ -422,3 +425,38 @@ def test_initial_electrons_follow_the_reference_assignment(golden_dir):
         assert np.array_equal(again[0], r_up) and np.array_equal(again[1], r_dn)
     with pytest.raises(ValueError):
         electron_owners(np.array([1.0]), np.zeros((1, 3)), 0, 2)
+
+
+def test_rank1_row_column_and_ratio_algebra(golden_dir, monkeypatch):
+    """The host algebra of compute_geminal_up_one_row_elements /
+    _dn_one_column_elements and _compute_ratio_determinant_part_rank1_update
+    (lambda folding, row/column assembly, rank-1 ratios) reproduces the
+    reference's G and determinant ratios (tests/golden/water_like.npz) when the
+    oracle's AO values stand in for the GPU AO call."""
+    import torch
+
+    from jqmc_gb300 import determinant as D
+    from jqmc_gb300 import surface, synthetic
+    from oracle.ao import AOTable, ao_value
+    monkeypatch.setattr(surface, "ao_vgl",
+                        lambda aos, r: torch.as_tensor(ao_value(AOTable(aos), np.asarray(r).reshape(-1, 3)))[None])
+    g = np.load(os.path.join(golden_dir, "water_like.npz"))
+    gem = synthetic.water_like().hamiltonian.wavefunction_data.geminal_data
+    for w in range(g["r_up"].shape[0]):
+        ru, rd, G = g["r_up"][w], g["r_dn"][w], g["geminal"][w]
+        rows = np.stack([D.compute_geminal_up_one_row_elements(gem, ru[i:i + 1], rd) for i in range(len(ru))])
+        cols = np.stack([D.compute_geminal_dn_one_column_elements(gem, ru, rd[j:j + 1]) for j in range(len(rd))], axis=1)
+        np.testing.assert_allclose(rows, G, rtol=1e-12, atol=1e-14 * np.abs(G).max())
+        np.testing.assert_allclose(cols, G, rtol=1e-12, atol=1e-14 * np.abs(G).max())
+        nu, nd = [ru.copy()], [rd.copy()]       # the first configuration moves nothing: ratio 1
+        for k in range(g["moves_spin"].shape[1]):
+            u, d = ru.copy(), rd.copy()
+            (u if g["moves_spin"][w, k] == 0 else d)[g["moves_idx"][w, k]] += g["moves_d"][w, k]
+            nu.append(u)
+            nd.append(d)
+        r = D._compute_ratio_determinant_part_rank1_update(gem, np.linalg.inv(G), ru, rd, np.stack(nu), np.stack(nd))
+        assert r[0] == 1.0
+        np.testing.assert_allclose(r[1:], g["det_ratio"][w], rtol=1e-11)
+    u2 = np.stack([ru + 0.1])
+    with pytest.raises(ValueError):
+        D._compute_ratio_determinant_part_rank1_update(gem, np.linalg.inv(G), ru, rd, u2, rd[None])

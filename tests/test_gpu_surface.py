@@ -147,3 +147,5 @@ def test_geminal_rows_columns_and_jastrow_ratios_match_reference(name, golden_di
             nd.append(d)
         ratio = J._compute_ratio_Jastrow_part_rank1_update(jd, ru, rd, np.stack(nu), np.stack(nd))
         assert rel(ratio, g["J_ratio"][w]) < RTOL
+        dr = D._compute_ratio_determinant_part_rank1_update(gem, np.linalg.inv(G), ru, rd, np.stack(nu), np.stack(nd))
+        assert rel(dr, g["det_ratio"][w]) < RTOL
