@@ -72,3 +72,52 @@ class Coulomb_potential_data:
         return z
 
     _effective_charges = effective_charges
+
+
+# ---------------------------------------------------------------- evaluation (GPU: the walker initialisation's energy cache)
+def compute_bare_coulomb_potential_el_ion_element_wise(coulomb_potential_data: Coulomb_potential_data, r_up_carts,
+                                                       r_dn_carts):
+    """(per up electron, per down electron) electron-ion Coulomb energies with the
+    effective charges (jqmc/coulomb_potential.py:2285)."""
+    from . import surface
+    ei, _, _, _, single = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
+    n = np.asarray(r_up_carts).shape[-2]
+    up, dn = surface.as_numpy(ei[:, :n]), surface.as_numpy(ei[:, n:])
+    return (up[0], dn[0]) if single else (up, dn)
+
+
+def compute_bare_coulomb_potential_el_ion(coulomb_potential_data: Coulomb_potential_data, r_up_carts, r_dn_carts):
+    """Total electron-ion Coulomb energy (jqmc/coulomb_potential.py:2575)."""
+    from . import surface
+    ei, _, _, _, single = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(ei.sum(dim=1), single)
+
+
+def compute_bare_coulomb_potential_el_el(r_up_carts, r_dn_carts):
+    """Electron-electron Coulomb energy (jqmc/coulomb_potential.py:2465)."""
+    from . import surface
+    _, _, ee, _, single = surface.coulomb_terms(None, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(ee, single)
+
+
+def compute_bare_coulomb_potential_ion_ion(coulomb_potential_data: Coulomb_potential_data) -> float:
+    """Ion-ion Coulomb energy with the effective charges (jqmc/coulomb_potential.py:2522)."""
+    from .engine import _ion_ion
+    return float(_ion_ion(np.asarray(coulomb_potential_data.structure_data.positions, dtype=np.float64),
+                          np.asarray(coulomb_potential_data.effective_charges, dtype=np.float64)))
+
+
+def compute_bare_coulomb_potential(coulomb_potential_data: Coulomb_potential_data, r_up_carts, r_dn_carts):
+    """Ion-ion + electron-ion + electron-electron (jqmc/coulomb_potential.py:2253)."""
+    from . import surface
+    ei, _, ee, ion_ion, single = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(ei.sum(dim=1) + ee + ion_ion, single)
+
+
+def compute_ecp_local_parts_all_pairs(coulomb_potential_data: Coulomb_potential_data, r_up_carts, r_dn_carts):
+    """Local ECP channel summed over all electron-nucleus pairs (jqmc/coulomb_potential.py:1145)."""
+    from . import surface
+    if not coulomb_potential_data.ecp_flag:
+        raise ValueError("the Coulomb data carry no ECP")
+    _, eloc, _, _, single = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(eloc.sum(dim=1), single)

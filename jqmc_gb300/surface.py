@@ -101,6 +101,44 @@ def _ham_for_jastrow(jd: Jastrow_data, n_up: int, n_dn: int) -> Hamiltonian_data
                             wavefunction_data=Wavefunction_data(jastrow_data=jd, geminal_data=gem))
 
 
+def _ham_for_coulomb(coul, n_up: int, n_dn: int) -> Hamiltonian_data:
+    """The given Coulomb/ECP data (None: no nuclear charges) with the Jastrow
+    stand-in's geminal (n_up s functions on nucleus 0) and no Jastrow.  The walker
+    initialisation fills the energy cache (electron-ion and local ECP terms per
+    electron, the electron-electron total), which is all that is read."""
+    if coul is None:
+        return _ham_for_jastrow(Jastrow_data(), n_up, n_dn)
+    st = coul.structure_data
+    s_set = AOs_sphe_data(structure_data=st, nucleus_index=(0,) * n_up, num_ao=n_up, num_ao_prim=n_up,
+                          orbital_indices=tuple(range(n_up)), exponents=np.ones(n_up), coefficients=np.ones(n_up),
+                          angular_momentums=(0,) * n_up, magnetic_quantum_numbers=(0,) * n_up)
+    gem = Geminal_data(num_electron_up=n_up, num_electron_dn=n_dn, orb_data_up_spin=s_set, orb_data_dn_spin=s_set,
+                       lambda_matrix=np.eye(n_up, 2 * n_up - n_dn))
+    return Hamiltonian_data(structure_data=st, coulomb_potential_data=coul,
+                            wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=gem))
+
+
+def coulomb_terms(coul, r_up_carts, r_dn_carts):
+    """(electron-ion per electron (W, N), local ECP per electron (W, N), electron-
+    electron (W,), ion-ion, single) from the energy cache of the walker
+    initialisation; coul None: no nuclear charges (electron-electron only)."""
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    n_up, n_dn = r_up.shape[1], r_dn.shape[1]
+    key = ("coulomb", id(coul), n_up, n_dn)
+    hit = _cache.get(key)
+    if hit is not None and hit[0] is coul:
+        _cache.move_to_end(key)
+        gs = hit[1]
+    else:
+        gs = GpuSystem(_ham_for_coulomb(coul, n_up, n_dn))
+        _cache[key] = (coul, gs)
+        while len(_cache) > _CACHE_SIZE:
+            _cache.popitem(last=False)
+    ec = _walkers(gs, r_up, r_dn).ecache          # (W, N + 1, stride)
+    N = n_up + n_dn
+    return ec[:, :N, 0], ec[:, :N, 1], ec[:, N, 0], float(gs.ion_ion), single
+
+
 def _configs(r_up_carts, r_dn_carts):
     """(r_up (W, n_up, 3), r_dn (W, n_dn, 3), single configuration?)"""
     r_up = np.asarray(r_up_carts, dtype=np.float64)

@@ -283,7 +283,8 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
     compute_local_energy reproduces the rotation; without a GPU they raise."""
     import inspect
 
-    from jqmc_gb300 import atomic_orbital, determinant, hamiltonians, jastrow_factor, molecular_orbital, wavefunction
+    from jqmc_gb300 import (atomic_orbital, coulomb_potential, determinant, hamiltonians, jastrow_factor,
+                            molecular_orbital, wavefunction)
     from jqmc_gb300._lib import JqmcError
     from jqmc_gb300.surface import angles_from_RT
     from oracle.wf import rotation_matrix
@@ -301,6 +302,12 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                       "_compute_ratio_determinant_part_rank1_update": ["geminal_data", "A_old_inv", "old_r_up_carts",
                                                                        "old_r_dn_carts", "new_r_up_carts_arr",
                                                                        "new_r_dn_carts_arr"]},
+        coulomb_potential: {**{n: ["coulomb_potential_data", "r_up_carts", "r_dn_carts"] for n in
+                               ("compute_bare_coulomb_potential", "compute_bare_coulomb_potential_el_ion",
+                                "compute_bare_coulomb_potential_el_ion_element_wise",
+                                "compute_ecp_local_parts_all_pairs")},
+                            "compute_bare_coulomb_potential_el_el": ["r_up_carts", "r_dn_carts"],
+                            "compute_bare_coulomb_potential_ion_ion": ["coulomb_potential_data"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
                          "_compute_ratio_Jastrow_part_rank1_update": ["jastrow_data", "old_r_up_carts", "old_r_dn_carts",
                                                                       "new_r_up_carts_arr", "new_r_dn_carts_arr", "j3_state"],

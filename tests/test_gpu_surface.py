@@ -149,3 +149,28 @@ def test_geminal_rows_columns_and_jastrow_ratios_match_reference(name, golden_di
         assert rel(ratio, g["J_ratio"][w]) < RTOL
         dr = D._compute_ratio_determinant_part_rank1_update(gem, np.linalg.inv(G), ru, rd, np.stack(nu), np.stack(nd))
         assert rel(dr, g["det_ratio"][w]) < RTOL
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_coulomb_module_functions_match_reference(name, golden_dir):
+    """compute_bare_coulomb_potential(_el_ion, _el_el, _ion_ion, _el_ion_element_wise)
+    and compute_ecp_local_parts_all_pairs from the walker initialisation's energy
+    cache, against the reference's bare Coulomb and local ECP values
+    (tests/golden/<system>.npz), batched and single."""
+    import os
+
+    from jqmc_gb300 import coulomb_potential as CP
+    from jqmc_gb300 import synthetic
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    coul = synthetic.SYSTEMS[name]().hamiltonian.coulomb_potential_data
+    ru, rd = g["r_up"], g["r_dn"]
+    v = CP.compute_bare_coulomb_potential(coul, ru, rd)
+    assert rel(v, g["bare_coulomb"]) < RTOL
+    parts = (CP.compute_bare_coulomb_potential_el_ion(coul, ru, rd) + CP.compute_bare_coulomb_potential_el_el(ru, rd)
+             + CP.compute_bare_coulomb_potential_ion_ion(coul))
+    assert rel(parts, g["bare_coulomb"]) < RTOL
+    up, dn = CP.compute_bare_coulomb_potential_el_ion_element_wise(coul, ru, rd)
+    assert rel(up.sum(1) + dn.sum(1), CP.compute_bare_coulomb_potential_el_ion(coul, ru, rd)) < RTOL
+    assert rel(CP.compute_ecp_local_parts_all_pairs(coul, ru, rd), g["ecp_local"]) < RTOL
+    single = CP.compute_bare_coulomb_potential(coul, ru[0], rd[0])
+    assert isinstance(single, float) and abs(single - g["bare_coulomb"][0]) < RTOL * abs(g["bare_coulomb"][0])
