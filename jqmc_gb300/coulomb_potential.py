@@ -121,3 +121,34 @@ def compute_ecp_local_parts_all_pairs(coulomb_potential_data: Coulomb_potential_
         raise ValueError("the Coulomb data carry no ECP")
     _, eloc, _, _, single = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
     return surface.scalar_or_array(eloc.sum(dim=1), single)
+
+
+def compute_coulomb_potential(coulomb_potential_data: Coulomb_potential_data, r_up_carts, r_dn_carts, RT, NN: int = 1,
+                              Nv: int = 6, wavefunction_data=None):
+    """Bare Coulomb plus the local and non-local ECP, the quadrature rotated by RT
+    (jqmc/coulomb_potential.py:2643): E_L - T of the walker kernels.  Without ECP
+    the bare Coulomb alone; the non-local part needs wavefunction_data.  One
+    nearest nucleus (NN = 1) on the walker path."""
+    from . import surface
+    if NN != 1:
+        raise NotImplementedError("the walker path evaluates the non-local ECP at the nearest nucleus (NN = 1)")
+    if not coulomb_potential_data.ecp_flag:
+        return compute_bare_coulomb_potential(coulomb_potential_data, r_up_carts, r_dn_carts)
+    if wavefunction_data is None:
+        raise ValueError("the non-local ECP needs wavefunction_data")
+    v, single = surface.potential_energy(coulomb_potential_data, wavefunction_data, r_up_carts, r_dn_carts, RT, Nv)
+    return surface.scalar_or_array(v, single)
+
+
+def compute_ecp_coulomb_potential(coulomb_potential_data: Coulomb_potential_data, wavefunction_data, r_up_carts,
+                                  r_dn_carts, RT, NN: int = 1, Nv: int = 6):
+    """Local plus non-local ECP energy (jqmc/coulomb_potential.py:2103): the total
+    potential less the bare Coulomb energy."""
+    from . import surface
+    if not coulomb_potential_data.ecp_flag:
+        raise ValueError("the Coulomb data carry no ECP")
+    if NN != 1:
+        raise NotImplementedError("the walker path evaluates the non-local ECP at the nearest nucleus (NN = 1)")
+    v, single = surface.potential_energy(coulomb_potential_data, wavefunction_data, r_up_carts, r_dn_carts, RT, Nv)
+    ei, _, ee, ion_ion, _ = surface.coulomb_terms(coulomb_potential_data, r_up_carts, r_dn_carts)
+    return surface.scalar_or_array(v - (ei.sum(dim=1) + ee + ion_ion), single)

@@ -275,9 +275,29 @@ def angles_from_RT(RT) -> np.ndarray:
     return np.stack([alpha, beta, gamma], axis=-1)
 
 
-def local_energy(ham: Hamiltonian_data, r_up_carts, r_dn_carts, RT):
+def potential_energy(coul, wf: Wavefunction_data, r_up_carts, r_dn_carts, RT, Nv: int = 6):
+    """(V = E_L - T for each configuration, single): bare Coulomb plus the local and
+    non-local ECP with the quadrature rotated by RT, on the system of (coul, wf)
+    (cached on both objects)."""
+    key = ("potential", id(coul), id(wf), Nv)
+    hit = _cache.get(key)
+    if hit is not None and hit[0][0] is coul and hit[0][1] is wf:
+        _cache.move_to_end(key)
+        gs = hit[1]
+    else:
+        ham = Hamiltonian_data(structure_data=coul.structure_data, coulomb_potential_data=coul, wavefunction_data=wf)
+        gs = GpuSystem(ham, Nv=Nv)
+        _cache[key] = ((coul, wf), gs)
+        while len(_cache) > _CACHE_SIZE:
+            _cache.popitem(last=False)
+    eL, single = local_energy(None, r_up_carts, r_dn_carts, RT, system=gs)
+    t, _ = kinetic_energy(wf, r_up_carts, r_dn_carts)
+    return eL - t, single
+
+
+def local_energy(ham: Hamiltonian_data, r_up_carts, r_dn_carts, RT, system: GpuSystem | None = None):
     """E_L for each configuration, non-local ECP quadrature rotated by RT."""
-    gs = _system(ham, lambda: ham)
+    gs = system if system is not None else _system(ham, lambda: ham)
     r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
     ang = angles_from_RT(RT).reshape(-1, 3)
     W = r_up.shape[0]

@@ -307,7 +307,11 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                                 "compute_bare_coulomb_potential_el_ion_element_wise",
                                 "compute_ecp_local_parts_all_pairs")},
                             "compute_bare_coulomb_potential_el_el": ["r_up_carts", "r_dn_carts"],
-                            "compute_bare_coulomb_potential_ion_ion": ["coulomb_potential_data"]},
+                            "compute_bare_coulomb_potential_ion_ion": ["coulomb_potential_data"],
+                            "compute_coulomb_potential": ["coulomb_potential_data", "r_up_carts", "r_dn_carts", "RT",
+                                                          "NN", "Nv", "wavefunction_data"],
+                            "compute_ecp_coulomb_potential": ["coulomb_potential_data", "wavefunction_data", "r_up_carts",
+                                                              "r_dn_carts", "RT", "NN", "Nv"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
                          "_compute_ratio_Jastrow_part_rank1_update": ["jastrow_data", "old_r_up_carts", "old_r_dn_carts",
                                                                       "new_r_up_carts_arr", "new_r_dn_carts_arr", "j3_state"],

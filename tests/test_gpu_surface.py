@@ -174,3 +174,23 @@ def test_coulomb_module_functions_match_reference(name, golden_dir):
     assert rel(CP.compute_ecp_local_parts_all_pairs(coul, ru, rd), g["ecp_local"]) < RTOL
     single = CP.compute_bare_coulomb_potential(coul, ru[0], rd[0])
     assert isinstance(single, float) and abs(single - g["bare_coulomb"][0]) < RTOL * abs(g["bare_coulomb"][0])
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_total_and_ecp_potential_match_reference(name, golden_dir):
+    """compute_coulomb_potential and compute_ecp_coulomb_potential (E_L - T of the
+    walker kernels) against the reference's bare Coulomb + local + non-local ECP
+    with the same quadrature rotations (tests/golden/<system>.npz)."""
+    import os
+
+    from jqmc_gb300 import coulomb_potential as CP
+    from jqmc_gb300 import synthetic
+    from oracle.wf import rotation_matrix
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    ham = synthetic.SYSTEMS[name]().hamiltonian
+    coul, wf = ham.coulomb_potential_data, ham.wavefunction_data
+    RT = np.stack([rotation_matrix(*a).T for a in g["angles"]])
+    ecp = g["ecp_local"] + g["ecp_nonlocal.1"]
+    v = CP.compute_coulomb_potential(coul, g["r_up"], g["r_dn"], RT, wavefunction_data=wf)
+    assert rel(v, g["bare_coulomb"] + ecp) < RTOL
+    assert rel(CP.compute_ecp_coulomb_potential(coul, wf, g["r_up"], g["r_dn"], RT), ecp) < 1e-9
