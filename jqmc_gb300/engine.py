@@ -292,6 +292,15 @@ class WalkerSet:
                                            C.c_void_p(jj.data_ptr()), self.sys.stream), "jqmc_log_psi")
         return ld, sg, jj
 
+    def electron_terms(self) -> torch.Tensor:
+        """(W, N, 9) per electron: grad ln|det| (3), lap ln|det|, grad J (3), lap J,
+        kinetic element T_e (FP64 walkers; jqmc_electron_terms)."""
+        out = torch.empty((self.nwalk, self.sys.N, 9), dtype=torch.float64, device=self.sys.device)
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_electron_terms(self.sys.handle, C.byref(d), C.c_void_p(out.data_ptr()), self.sys.stream),
+                   "jqmc_electron_terms")
+        return out
+
     def vmc_sweep(self, idraw: torch.Tensor, fdraw: torch.Tensor, Dt: float, eps_AS: float, accept: torch.Tensor):
         K = idraw.shape[1]
         d = self.desc()

@@ -58,3 +58,11 @@ def evaluate_ln_wavefunction_fast(wavefunction_data: Wavefunction_data, r_up_car
     """ln|psi| with a precomputed geminal inverse (jqmc/wavefunction.py:723): the same value as
     ``evaluate_ln_wavefunction``; ``geminal_inv`` is accepted and not read."""
     return evaluate_ln_wavefunction(wavefunction_data, r_up_carts, r_dn_carts)
+
+
+def compute_kinetic_energy_all_elements(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """Per-electron kinetic energies (T up (n_up,), T down (n_dn,)) (jqmc/wavefunction.py:1081),
+    from the walker kernels (jqmc_electron_terms)."""
+    from . import surface
+    a, n = surface.electron_tables(surface.wavefunction_system(wavefunction_data), r_up_carts, r_dn_carts)
+    return a[..., :n, 8], a[..., n:, 8]

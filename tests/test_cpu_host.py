@@ -216,6 +216,7 @@ def test_entry_points_reject_invalid_arguments():
         "jqmc_log_psi(sys=NULL)": L.jqmc_log_psi(None, wp, fake, fake, fake, None),
         "jqmc_dlnpsi_dparam(sys=NULL)": L.jqmc_dlnpsi_dparam(None, wp, fake, fake, fake, None, None, None),
         "jqmc_dlnpsi_dR(sys=NULL)": L.jqmc_dlnpsi_dR(None, wp, fake, None),
+        "jqmc_electron_terms(sys=NULL)": L.jqmc_electron_terms(None, wp, fake, None),
         "jqmc_vmc_sweep(sys=NULL)": L.jqmc_vmc_sweep(None, wp, 4, fake, fake, 0.4, 0.0, fake, None),
         "jqmc_vmc_measure(sys=NULL)": L.jqmc_vmc_measure(None, wp, fake, 0.0, fake, fake, None),
         "jqmc_lrdmc_project(sys=NULL)": L.jqmc_lrdmc_project(None, wp, 4, fake, 0.2, 0.0, fake, None),
@@ -294,15 +295,17 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                             ("compute_MOs", "compute_MOs_grad", "compute_MOs_laplacian", "compute_MOs_value_grad_lap")},
         determinant: {**{n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
                          ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
-                          "compute_det_geminal_all_elements", "compute_AS_regularization_factor")},
+                          "compute_det_geminal_all_elements", "compute_AS_regularization_factor",
+                          "compute_grads_and_laplacian_ln_Det")},
                       "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"]},
         jastrow_factor: {"compute_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_one_body": ["jastrow_one_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_two_body": ["jastrow_two_body_data", "r_up_carts", "r_dn_carts"],
-                         "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"]},
+                         "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"],
+                         "compute_grads_and_laplacian_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"]},
         wavefunction: {**{n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
                           ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow",
-                           "evaluate_determinant", "compute_kinetic_energy")},
+                           "evaluate_determinant", "compute_kinetic_energy", "compute_kinetic_energy_all_elements")},
                        "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"]},
         hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"],
                        "compute_local_energy_fast": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT",

@@ -117,3 +117,26 @@ def test_local_energy(setup):
     batch = H.compute_local_energy(ham, r_up, r_dn, RT)
     assert batch.shape == (3,)
     assert rel(batch, ref) < RTOL
+
+
+def test_per_electron_tables(setup):
+    """grad / lap of ln|det| and of J per electron, and the kinetic elements."""
+    from jqmc_gb300 import determinant as D
+    from jqmc_gb300 import jastrow_factor as JF
+    from jqmc_gb300 import wavefunction as WF
+    syn, o, r_up, r_dn = setup
+    wf = syn.hamiltonian.wavefunction_data
+    n = r_up.shape[1]
+    for w in range(2):
+        Ginv = np.linalg.inv(o.geminal(r_up[w], r_dn[w]))
+        gu, gd, lu, ld = o.det_grad_lap(r_up[w], r_dn[w], Ginv)
+        got = D.compute_grads_and_laplacian_ln_Det(wf.geminal_data, r_up[w], r_dn[w])
+        for a, b in zip(got, (gu, gd, lu, ld)):
+            assert a.shape == np.shape(b) and rel(a, b) < RTOL
+        gJ, lJ = o.jastrow_grad_lap(r_up[w], r_dn[w])
+        got = JF.compute_grads_and_laplacian_Jastrow_part(wf.jastrow_data, r_up[w], r_dn[w])
+        for a, b in zip(got, (gJ[:n], gJ[n:], lJ[:n], lJ[n:])):
+            assert a.shape == np.shape(b) and rel(a, b) < RTOL
+        tu, td = o.kinetic_elements(r_up[w], r_dn[w], Ginv)
+        Tu, Td = WF.compute_kinetic_energy_all_elements(wf, r_up[w], r_dn[w])
+        assert rel(Tu, tu) < RTOL and rel(Td, td) < RTOL
