@@ -167,6 +167,14 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
  * compute_kinetic_energy_all_elements (jqmc/wavefunction.py:1081). */
 int jqmc_electron_terms(const jqmc_system* sys, const jqmc_walkers* w, double* d_out, void* stream);
 
+/* Discretised kinetic elements, FP64 walkers: d_el (nwalk, N, 6) =
+ * -psi(r_e + alat s_k)/psi(r) / (2 alat^2) for every electron e (up spin
+ * first) and the moves s_k = +x, -x, +y, -y, +z, -z of the rotation
+ * R(d_angles[w]) (Euler angles as in jqmc_vmc_measure), i.e. the rows of
+ * R^T.  Replaces compute_discretized_kinetic_energy (jqmc/wavefunction.py:1620). */
+int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double alat, double* d_el,
+                      void* stream);
+
 /* Per-walker derivatives of ln|psi| with respect to the variational parameters,
  * FP64 walkers only, from the positions and G^-1 (AO values are recomputed, not
  * stored).  Replaces the per-walker grad(evaluate_ln_wavefunction) of

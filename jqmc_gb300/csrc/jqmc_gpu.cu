@@ -2488,6 +2488,24 @@ __global__ void k_electron_terms(KParams P, double* out) {
   }
 }
 
+// Discretised kinetic elements of every electron's six rotated lattice moves
+// (FP64 walkers): out[(w N + e) 6 + k] = -psi(r_e + a s_k)/psi / (2 a^2), with
+// s_k = +-column k/2 of R(angles[w]) in the order +x, -x, +y, -y, +z, -z
+// (wavefunction.py:1620-1740).
+__global__ void k_kinetic_mesh(KParams P, const double* __restrict__ angles, double alat, double* out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
+  Terms t = make_terms(P.ml, smem, nullptr, s);
+  load_walker(k, P.ws, w);
+  if (threadIdx.x == 0) rotation(angles[3 * w], angles[3 * w + 1], angles[3 * w + 2], t.R);
+  __syncthreads();
+  electron_terms<double, double>(k, t, alat);
+  mesh_terms<double, double, double>(k, t, alat, true);
+  for (int q = threadIdx.x; q < 6 * k.N; q += blockDim.x) out[(size_t)w * 6 * k.N + q] = t.el[q];
+}
+
 __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
@@ -3469,6 +3487,17 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
   int rc = launch_check((const void*)k_log_psi, smem);
   if (rc) return rc;
   k_log_psi<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, d_logdet, d_sign, d_jastrow);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double alat, double* d_el,
+                      void* stream) {
+  if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_angles || !d_el || !(alat > 0.0)) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  int rc = launch_check((const void*)k_kinetic_mesh, smem);
+  if (rc) return rc;
+  k_kinetic_mesh<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, alat, d_el);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 

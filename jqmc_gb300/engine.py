@@ -301,6 +301,16 @@ class WalkerSet:
                    "jqmc_electron_terms")
         return out
 
+    def kinetic_mesh(self, angles: torch.Tensor, alat: float) -> torch.Tensor:
+        """(W, N, 6) discretised kinetic elements of the six rotated lattice moves of
+        every electron (FP64 walkers; jqmc_kinetic_mesh)."""
+        out = torch.empty((self.nwalk, self.sys.N, 6), dtype=torch.float64, device=self.sys.device)
+        ang = angles.to(self.sys.device, torch.float64).contiguous()
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_kinetic_mesh(self.sys.handle, C.byref(d), C.c_void_p(ang.data_ptr()), float(alat),
+                                                C.c_void_p(out.data_ptr()), self.sys.stream), "jqmc_kinetic_mesh")
+        return out
+
     def vmc_sweep(self, idraw: torch.Tensor, fdraw: torch.Tensor, Dt: float, eps_AS: float, accept: torch.Tensor):
         K = idraw.shape[1]
         d = self.desc()

@@ -193,6 +193,39 @@ def electron_tables(gs: GpuSystem, r_up_carts, r_dn_carts):
     return (a[0] if single else a), gs.n_up
 
 
+def discretized_kinetic(alat: float, wf: Wavefunction_data, r_up_carts, r_dn_carts, RT):
+    """(r_up configurations (6N, n_up, 3), r_dn configurations (6N, n_dn, 3),
+    elements (6N,)) of the six moves +-alat along the rows of RT for every
+    electron, up electrons first; with a leading walker axis for (W, n, 3) inputs."""
+    gs = wavefunction_system(wf)
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    W, nu, nd = r_up.shape[0], r_up.shape[1], r_dn.shape[1]
+    ang = angles_from_RT(RT).reshape(-1, 3)
+    if ang.shape[0] == 1 and W > 1:
+        ang = np.repeat(ang, W, axis=0)
+    if ang.shape[0] != W:
+        raise ValueError(f"{ang.shape[0]} rotations for {W} configurations")
+    el = as_numpy(_walkers(gs, r_up, r_dn).kinetic_mesh(torch.as_tensor(ang), alat)).reshape(W, -1)
+    rt = np.asarray(RT, dtype=np.float64).reshape(-1, 3, 3)
+    if rt.shape[0] == 1:
+        rt = np.repeat(rt, W, axis=0)
+    shifts = alat * np.einsum("kc,wcd->wkd", np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]],
+                                                      dtype=np.float64), rt)           # (W, 6, 3): rows of RT
+    N = nu + nd
+    cu = np.repeat(r_up[:, None], 6 * N, axis=1)
+    cd = np.repeat(r_dn[:, None], 6 * N, axis=1)
+    for e in range(N):
+        for k in range(6):
+            g = 6 * e + k
+            if e < nu:
+                cu[:, g, e] += shifts[:, k]
+            else:
+                cd[:, g, e - nu] += shifts[:, k]
+    if single:
+        return cu[0], cd[0], el[0]
+    return cu, cd, el
+
+
 def wavefunction_system(wf: Wavefunction_data) -> GpuSystem:
     return _system(wf, lambda: _ham_for_wavefunction(wf))
 

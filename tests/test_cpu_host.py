@@ -217,6 +217,7 @@ def test_entry_points_reject_invalid_arguments():
         "jqmc_dlnpsi_dparam(sys=NULL)": L.jqmc_dlnpsi_dparam(None, wp, fake, fake, fake, None, None, None),
         "jqmc_dlnpsi_dR(sys=NULL)": L.jqmc_dlnpsi_dR(None, wp, fake, None),
         "jqmc_electron_terms(sys=NULL)": L.jqmc_electron_terms(None, wp, fake, None),
+        "jqmc_kinetic_mesh(sys=NULL)": L.jqmc_kinetic_mesh(None, wp, fake, 0.2, fake, None),
         "jqmc_vmc_sweep(sys=NULL)": L.jqmc_vmc_sweep(None, wp, 4, fake, fake, 0.4, 0.0, fake, None),
         "jqmc_vmc_measure(sys=NULL)": L.jqmc_vmc_measure(None, wp, fake, 0.0, fake, fake, None),
         "jqmc_lrdmc_project(sys=NULL)": L.jqmc_lrdmc_project(None, wp, 4, fake, 0.2, 0.0, fake, None),
@@ -306,7 +307,8 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
         wavefunction: {**{n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
                           ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow",
                            "evaluate_determinant", "compute_kinetic_energy", "compute_kinetic_energy_all_elements")},
-                       "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"]},
+                       "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"],
+                       "compute_discretized_kinetic_energy": ["alat", "wavefunction_data", "r_up_carts", "r_dn_carts", "RT"]},
         hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"],
                        "compute_local_energy_fast": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT",
                                                      "geminal_inverse"]},
