@@ -159,6 +159,22 @@ int jqmc_lu_rebuild_refine(const jqmc_system* sys, const jqmc_walkers* w, void* 
  * plus the Jastrow value J (jastrow_factor.py:2127-2178).  JQMC_PREC_FP64 only. */
 int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet, double* d_sign, double* d_jastrow, void* stream);
 
+/* Per-electron derivatives of ln|psi| and kinetic elements, FP64 walkers:
+ * d_out (nwalk, N, 9) = (grad ln|det| (3), lap ln|det|, grad J (3), lap J,
+ * T_e = -1/2 (lap ln psi + |grad ln psi|^2)) for every electron, up spin first.
+ * Replaces compute_grads_and_laplacian_ln_Det (jqmc/determinant.py:1809),
+ * compute_grads_and_laplacian_Jastrow_part (jqmc/jastrow_factor.py:2983) and
+ * compute_kinetic_energy_all_elements (jqmc/wavefunction.py:1081). */
+int jqmc_electron_terms(const jqmc_system* sys, const jqmc_walkers* w, double* d_out, void* stream);
+
+/* Discretised kinetic elements, FP64 walkers: d_el (nwalk, N, 6) =
+ * -psi(r_e + alat s_k)/psi(r) / (2 alat^2) for every electron e (up spin
+ * first) and the moves s_k = +x, -x, +y, -y, +z, -z of the rotation
+ * R(d_angles[w]) (Euler angles as in jqmc_vmc_measure), i.e. the rows of
+ * R^T.  Replaces compute_discretized_kinetic_energy (jqmc/wavefunction.py:1620). */
+int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double alat, double* d_el,
+                      void* stream);
+
 /* Per-walker derivatives of ln|psi| with respect to the variational parameters,
  * FP64 walkers only, from the positions and G^-1 (AO values are recomputed, not
  * stored).  Replaces the per-walker grad(evaluate_ln_wavefunction) of

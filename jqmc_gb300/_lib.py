@@ -81,6 +81,8 @@ def lib():
         L.jqmc_vmc_sweep_batch.argtypes = [vp, i32, vp, vp, f64, f64, vp, i32, i32, vp]
         L.jqmc_batch_rebuild.argtypes = [vp, i32, vp]
         L.jqmc_dlnpsi_dR.argtypes = [vp, C.POINTER(Walkers), vp, vp]
+        L.jqmc_electron_terms.argtypes = [vp, C.POINTER(Walkers), vp, vp]
+        L.jqmc_kinetic_mesh.argtypes = [vp, C.POINTER(Walkers), vp, f64, vp, vp]
         L.jqmc_log_psi.argtypes = [vp, C.POINTER(Walkers), vp, vp, vp, vp]
         L.jqmc_vmc_sweep.argtypes = [vp, C.POINTER(Walkers), i32, vp, vp, f64, f64, vp, vp]
         L.jqmc_vmc_measure.argtypes = [vp, C.POINTER(Walkers), vp, f64, vp, vp, vp]
@@ -96,7 +98,7 @@ def lib():
                      "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
                      "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
                      "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild",
-                     "jqmc_dlnpsi_dR"):
+                     "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -112,4 +114,4 @@ EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "j
             "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
             "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
             "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild",
-            "jqmc_dlnpsi_dR")
+            "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh")

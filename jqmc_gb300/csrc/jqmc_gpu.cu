@@ -2432,6 +2432,80 @@ __global__ void k_dlnpsi_dR(KParams P, int off_acc, double* out) {
 }
 
 // ln|det G|, sign (LU with partial pivoting on a copy of G) and J   (FP64 form)
+// Per-electron derivatives of ln|psi| and kinetic elements (FP64 walkers), from
+// the AO derivative tables, the T rows, the J3 field and the energy cache:
+// out[(w N + e) 9 + (0..2)] d ln|det| / dr_e, [3] lap_e ln|det|, [4..6] dJ / dr_e,
+// [7] lap_e J, [8] T_e = -1/2 (lap_e ln psi + |grad_e ln psi|^2)
+// (determinant.py:1809-1900, jastrow_factor.py:2983-3060, wavefunction.py:1081-1140).
+// One warp per electron.
+__global__ void k_electron_terms(KParams P, double* out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
+  load_walker(k, P.ws, w);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int A = k.A, A3 = k.A3;
+  for (int e = wid; e < k.N; e += nw) {
+    const bool up = e < s.n_up;
+    const int i = up ? e : e - s.n_up;
+    const double* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * A;
+    const double* dp = k.dphi + (size_t)e * 4 * A;
+    double gx = 0.0, gy = 0.0, gz = 0.0, lp = 0.0, hx = 0.0, hy = 0.0, hz = 0.0, hl = 0.0;
+    for (int a = lane; a < A; a += 32) {
+      const double tv = Trow[a];
+      gx += dp[a] * tv;
+      gy += dp[A + a] * tv;
+      gz += dp[2 * A + a] * tv;
+      lp += dp[3 * A + a] * tv;
+    }
+    if (s.has_j3) {
+      const double* h = k.h3 + (size_t)e * A3;
+      const double* q = k.dphi3 + (size_t)e * 5 * A3;
+      for (int a = lane; a < A3; a += 32) {
+        const double hv = h[a];
+        hx += q[A3 + a] * hv;
+        hy += q[2 * A3 + a] * hv;
+        hz += q[3 * A3 + a] * hv;
+        hl += q[4 * A3 + a] * hv;
+      }
+    }
+    gx = warp_sum(gx); gy = warp_sum(gy); gz = warp_sum(gz); lp = warp_sum(lp);
+    hx = warp_sum(hx); hy = warp_sum(hy); hz = warp_sum(hz); hl = warp_sum(hl);
+    if (lane == 0) {
+      const double* row = k.ec + (size_t)e * kEC;
+      const double jx = hx + row[EC_J1G] + row[EC_J2G];
+      const double jy = hy + row[EC_J1G + 1] + row[EC_J2G + 1];
+      const double jz = hz + row[EC_J1G + 2] + row[EC_J2G + 2];
+      const double jl = hl + row[EC_J1L] + row[EC_J2L];
+      const double dl = lp - (gx * gx + gy * gy + gz * gz);
+      const double Gx = gx + jx, Gy = gy + jy, Gz = gz + jz;
+      double* o = out + ((size_t)w * k.N + e) * 9;
+      o[0] = gx; o[1] = gy; o[2] = gz; o[3] = dl;
+      o[4] = jx; o[5] = jy; o[6] = jz; o[7] = jl;
+      o[8] = -0.5 * (dl + jl + Gx * Gx + Gy * Gy + Gz * Gz);
+    }
+  }
+}
+
+// Discretised kinetic elements of every electron's six rotated lattice moves
+// (FP64 walkers): out[(w N + e) 6 + k] = -psi(r_e + a s_k)/psi / (2 a^2), with
+// s_k = +-column k/2 of R(angles[w]) in the order +x, -x, +y, -y, +z, -z
+// (wavefunction.py:1620-1740).
+__global__ void k_kinetic_mesh(KParams P, const double* __restrict__ angles, double alat, double* out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = blockIdx.x;
+  const Sys s = stage_tables(P.s, P.tl, smem);
+  Work<double> k = make_work<double>(s, P.wl, smem, P.ws, w);
+  Terms t = make_terms(P.ml, smem, nullptr, s);
+  load_walker(k, P.ws, w);
+  if (threadIdx.x == 0) rotation(angles[3 * w], angles[3 * w + 1], angles[3 * w + 2], t.R);
+  __syncthreads();
+  electron_terms<double, double>(k, t, alat);
+  mesh_terms<double, double, double>(k, t, alat, true);
+  for (int q = threadIdx.x; q < 6 * k.N; q += blockDim.x) out[(size_t)w * 6 * k.N + q] = t.el[q];
+}
+
 __global__ void k_log_psi(KParams P, int off_aug, double* logdet, double* sign, double* jas) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
@@ -3413,6 +3487,27 @@ int jqmc_log_psi(const jqmc_system* sys, const jqmc_walkers* w, double* d_logdet
   int rc = launch_check((const void*)k_log_psi, smem);
   if (rc) return rc;
   k_log_psi<<<w->nwalk, 128, smem, S(stream)>>>(P, off_aug, d_logdet, d_sign, d_jastrow);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const double* d_angles, double alat, double* d_el,
+                      void* stream) {
+  if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_angles || !d_el || !(alat > 0.0)) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int smem = P.ml.bytes;
+  int rc = launch_check((const void*)k_kinetic_mesh, smem);
+  if (rc) return rc;
+  k_kinetic_mesh<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, alat, d_el);
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
+int jqmc_electron_terms(const jqmc_system* sys, const jqmc_walkers* w, double* d_out, void* stream) {
+  if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_out) return JQMC_E_ARG;
+  KParams P = make_params(sys, w);
+  const int smem = P.wl.bytes;
+  int rc = launch_check((const void*)k_electron_terms, smem);
+  if (rc) return rc;
+  k_electron_terms<<<w->nwalk, 128, smem, S(stream)>>>(P, d_out);
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
 

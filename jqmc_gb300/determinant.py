@@ -236,3 +236,11 @@ def compute_AS_regularization_factor_fast_update(geminal, geminal_inv):
     if single:
         G, Gi = G[None], Gi[None]
     return surface.scalar_or_array(surface.as_factor(G, Gi), single)
+
+
+def compute_grads_and_laplacian_ln_Det(geminal_data: Geminal_data, r_up_carts, r_dn_carts):
+    """(grad ln|det| up (n_up, 3), down (n_dn, 3), lap ln|det| up (n_up,), down (n_dn,))
+    (jqmc/determinant.py:1809), from the walker kernels (jqmc_electron_terms)."""
+    from . import surface
+    a, n = surface.electron_tables(surface.geminal_system(geminal_data), r_up_carts, r_dn_carts)
+    return a[..., :n, 0:3], a[..., n:, 0:3], a[..., :n, 3], a[..., n:, 3]

@@ -294,6 +294,25 @@ class WalkerSet:
                                            C.c_void_p(jj.data_ptr()), self.sys.stream), "jqmc_log_psi")
         return ld, sg, jj
 
+    def electron_terms(self) -> torch.Tensor:
+        """(W, N, 9) per electron: grad ln|det| (3), lap ln|det|, grad J (3), lap J,
+        kinetic element T_e (FP64 walkers; jqmc_electron_terms)."""
+        out = torch.empty((self.nwalk, self.sys.N, 9), dtype=torch.float64, device=self.sys.device)
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_electron_terms(self.sys.handle, C.byref(d), C.c_void_p(out.data_ptr()), self.sys.stream),
+                   "jqmc_electron_terms")
+        return out
+
+    def kinetic_mesh(self, angles: torch.Tensor, alat: float) -> torch.Tensor:
+        """(W, N, 6) discretised kinetic elements of the six rotated lattice moves of
+        every electron (FP64 walkers; jqmc_kinetic_mesh)."""
+        out = torch.empty((self.nwalk, self.sys.N, 6), dtype=torch.float64, device=self.sys.device)
+        ang = angles.to(self.sys.device, torch.float64).contiguous()
+        d = self.desc()
+        _lib.check(_lib.lib().jqmc_kinetic_mesh(self.sys.handle, C.byref(d), C.c_void_p(ang.data_ptr()), float(alat),
+                                                C.c_void_p(out.data_ptr()), self.sys.stream), "jqmc_kinetic_mesh")
+        return out
+
     def vmc_sweep(self, idraw: torch.Tensor, fdraw: torch.Tensor, Dt: float, eps_AS: float, accept: torch.Tensor):
         K = idraw.shape[1]
         d = self.desc()

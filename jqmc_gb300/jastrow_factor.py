@@ -134,3 +134,12 @@ def compute_Jastrow_three_body(jastrow_three_body_data: Jastrow_three_body_data,
     jj, single = surface.jastrow_value(Jastrow_data(jastrow_three_body_data=jastrow_three_body_data), r_up_carts,
                                        r_dn_carts, key_obj=jastrow_three_body_data)
     return surface.scalar_or_array(jj, single)
+
+
+def compute_grads_and_laplacian_Jastrow_part(jastrow_data: Jastrow_data, r_up_carts, r_dn_carts):
+    """(grad J up (n_up, 3), down (n_dn, 3), lap J up (n_up,), down (n_dn,))
+    (jqmc/jastrow_factor.py:2983), from the walker kernels (jqmc_electron_terms)."""
+    from . import surface
+    n_up, n_dn = np.shape(r_up_carts)[-2], np.shape(r_dn_carts)[-2]
+    a, n = surface.electron_tables(surface.jastrow_system(jastrow_data, n_up, n_dn), r_up_carts, r_dn_carts)
+    return a[..., :n, 4:7], a[..., n:, 4:7], a[..., :n, 7], a[..., n:, 7]

@@ -222,22 +222,77 @@ def wavefunction_parts(wf: Wavefunction_data, r_up_carts, r_dn_carts):
     return ld, sg, jj, single
 
 
-def jastrow_value(jd: Jastrow_data, r_up_carts, r_dn_carts, key_obj=None):
-    """J (without exp) for each configuration; the device copy is cached on
-    ``key_obj`` (the caller's data object; default ``jd``)."""
+def electron_tables(gs: GpuSystem, r_up_carts, r_dn_carts):
+    """Per-electron derivatives of ln|psi| and kinetic elements as NumPy, (N, 9) for
+    one configuration or (W, N, 9): grad ln|det| (3), lap ln|det|, grad J (3),
+    lap J, T_e; and n_up (jqmc_electron_terms)."""
     r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
-    n_up, n_dn = r_up.shape[1], r_dn.shape[1]
+    a = as_numpy(_walkers(gs, r_up, r_dn).electron_terms())
+    return (a[0] if single else a), gs.n_up
+
+
+def discretized_kinetic(alat: float, wf: Wavefunction_data, r_up_carts, r_dn_carts, RT):
+    """(r_up configurations (6N, n_up, 3), r_dn configurations (6N, n_dn, 3),
+    elements (6N,)) of the six moves +-alat along the rows of RT for every
+    electron, up electrons first; with a leading walker axis for (W, n, 3) inputs."""
+    gs = wavefunction_system(wf)
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    W, nu, nd = r_up.shape[0], r_up.shape[1], r_dn.shape[1]
+    ang = angles_from_RT(RT).reshape(-1, 3)
+    if ang.shape[0] == 1 and W > 1:
+        ang = np.repeat(ang, W, axis=0)
+    if ang.shape[0] != W:
+        raise ValueError(f"{ang.shape[0]} rotations for {W} configurations")
+    el = as_numpy(_walkers(gs, r_up, r_dn).kinetic_mesh(torch.as_tensor(ang), alat)).reshape(W, -1)
+    rt = np.asarray(RT, dtype=np.float64).reshape(-1, 3, 3)
+    if rt.shape[0] == 1:
+        rt = np.repeat(rt, W, axis=0)
+    shifts = alat * np.einsum("kc,wcd->wkd", np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]],
+                                                      dtype=np.float64), rt)           # (W, 6, 3): rows of RT
+    N = nu + nd
+    cu = np.repeat(r_up[:, None], 6 * N, axis=1)
+    cd = np.repeat(r_dn[:, None], 6 * N, axis=1)
+    for e in range(N):
+        for k in range(6):
+            g = 6 * e + k
+            if e < nu:
+                cu[:, g, e] += shifts[:, k]
+            else:
+                cd[:, g, e - nu] += shifts[:, k]
+    if single:
+        return cu[0], cd[0], el[0]
+    return cu, cd, el
+
+
+def wavefunction_system(wf: Wavefunction_data) -> GpuSystem:
+    return _system(wf, lambda: _ham_for_wavefunction(wf))
+
+
+def geminal_system(geminal: Geminal_data) -> GpuSystem:
+    wf = Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=geminal)
+    return _system(geminal, lambda: _ham_for_wavefunction(wf))
+
+
+def jastrow_system(jd: Jastrow_data, n_up: int, n_dn: int, key_obj=None) -> GpuSystem:
+    """The stand-in system of a Jastrow factor, cached on ``key_obj`` (default ``jd``)."""
     owner = jd if key_obj is None else key_obj
     key = (id(owner), n_up, n_dn)
     hit = _cache.get(key)
     if hit is not None and hit[0] is owner:
         _cache.move_to_end(key)
-        gs = hit[1]
-    else:
-        gs = GpuSystem(_ham_for_jastrow(jd, n_up, n_dn))
-        _cache[key] = (owner, gs)
-        while len(_cache) > _CACHE_SIZE:
-            _cache.popitem(last=False)
+        return hit[1]
+    gs = GpuSystem(_ham_for_jastrow(jd, n_up, n_dn))
+    _cache[key] = (owner, gs)
+    while len(_cache) > _CACHE_SIZE:
+        _cache.popitem(last=False)
+    return gs
+
+
+def jastrow_value(jd: Jastrow_data, r_up_carts, r_dn_carts, key_obj=None):
+    """J (without exp) for each configuration; the device copy is cached on
+    ``key_obj`` (the caller's data object; default ``jd``)."""
+    r_up, r_dn, single = _configs(r_up_carts, r_dn_carts)
+    gs = jastrow_system(jd, r_up.shape[1], r_dn.shape[1], key_obj)
     _, _, jj = _walkers(gs, r_up, r_dn).log_psi()
     return jj, single
 

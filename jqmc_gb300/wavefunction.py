@@ -70,3 +70,20 @@ def evaluate_ln_wavefunction_fast(wavefunction_data: Wavefunction_data, r_up_car
     """ln|psi| with a precomputed geminal inverse (jqmc/wavefunction.py:723): the same value as
     ``evaluate_ln_wavefunction``; ``geminal_inv`` is accepted and not read."""
     return evaluate_ln_wavefunction(wavefunction_data, r_up_carts, r_dn_carts)
+
+
+def compute_kinetic_energy_all_elements(wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts):
+    """Per-electron kinetic energies (T up (n_up,), T down (n_dn,)) (jqmc/wavefunction.py:1081),
+    from the walker kernels (jqmc_electron_terms)."""
+    from . import surface
+    a, n = surface.electron_tables(surface.wavefunction_system(wavefunction_data), r_up_carts, r_dn_carts)
+    return a[..., :n, 8], a[..., n:, 8]
+
+
+def compute_discretized_kinetic_energy(alat: float, wavefunction_data: Wavefunction_data, r_up_carts, r_dn_carts, RT):
+    """(r_up configurations (6N, n_up, 3), r_dn configurations (6N, n_dn, 3), elements
+    (6N,)) of the six moves +-alat along the rows of RT for every electron, up
+    electrons first; elements -psi(r')/psi(r) / (2 alat^2) (jqmc/wavefunction.py:1620),
+    from the walker kernels (jqmc_kinetic_mesh)."""
+    from . import surface
+    return surface.discretized_kinetic(alat, wavefunction_data, r_up_carts, r_dn_carts, RT)

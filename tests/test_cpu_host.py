@@ -216,6 +216,8 @@ def test_entry_points_reject_invalid_arguments():
         "jqmc_log_psi(sys=NULL)": L.jqmc_log_psi(None, wp, fake, fake, fake, None),
         "jqmc_dlnpsi_dparam(sys=NULL)": L.jqmc_dlnpsi_dparam(None, wp, fake, fake, fake, None, None, None),
         "jqmc_dlnpsi_dR(sys=NULL)": L.jqmc_dlnpsi_dR(None, wp, fake, None),
+        "jqmc_electron_terms(sys=NULL)": L.jqmc_electron_terms(None, wp, fake, None),
+        "jqmc_kinetic_mesh(sys=NULL)": L.jqmc_kinetic_mesh(None, wp, fake, 0.2, fake, None),
         "jqmc_vmc_sweep(sys=NULL)": L.jqmc_vmc_sweep(None, wp, 4, fake, fake, 0.4, 0.0, fake, None),
         "jqmc_vmc_measure(sys=NULL)": L.jqmc_vmc_measure(None, wp, fake, 0.0, fake, fake, None),
         "jqmc_lrdmc_project(sys=NULL)": L.jqmc_lrdmc_project(None, wp, 4, fake, 0.2, 0.0, fake, None),
@@ -295,7 +297,8 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                             ("compute_MOs", "compute_MOs_grad", "compute_MOs_laplacian", "compute_MOs_value_grad_lap")},
         determinant: {**{n: ["geminal_data", "r_up_carts", "r_dn_carts"] for n in
                          ("compute_geminal_all_elements", "compute_ln_det_geminal_all_elements",
-                          "compute_det_geminal_all_elements", "compute_AS_regularization_factor")},
+                          "compute_det_geminal_all_elements", "compute_AS_regularization_factor",
+                          "compute_grads_and_laplacian_ln_Det")},
                       "compute_AS_regularization_factor_fast_update": ["geminal", "geminal_inv"],
                       "compute_geminal_up_one_row_elements": ["geminal_data", "r_up_cart", "r_dn_carts"],
                       "compute_geminal_dn_one_column_elements": ["geminal_data", "r_up_carts", "r_dn_cart"],
@@ -317,11 +320,13 @@ def test_module_functions_keep_the_reference_names_and_need_a_gpu():
                                                                       "new_r_up_carts_arr", "new_r_dn_carts_arr", "j3_state"],
                          "compute_Jastrow_one_body": ["jastrow_one_body_data", "r_up_carts", "r_dn_carts"],
                          "compute_Jastrow_two_body": ["jastrow_two_body_data", "r_up_carts", "r_dn_carts"],
-                         "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"]},
+                         "compute_Jastrow_three_body": ["jastrow_three_body_data", "r_up_carts", "r_dn_carts"],
+                         "compute_grads_and_laplacian_Jastrow_part": ["jastrow_data", "r_up_carts", "r_dn_carts"]},
         wavefunction: {**{n: ["wavefunction_data", "r_up_carts", "r_dn_carts"] for n in
                           ("evaluate_ln_wavefunction", "evaluate_wavefunction", "evaluate_jastrow",
-                           "evaluate_determinant", "compute_kinetic_energy")},
-                       "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"]},
+                           "evaluate_determinant", "compute_kinetic_energy", "compute_kinetic_energy_all_elements")},
+                       "evaluate_ln_wavefunction_fast": ["wavefunction_data", "r_up_carts", "r_dn_carts", "geminal_inv"],
+                       "compute_discretized_kinetic_energy": ["alat", "wavefunction_data", "r_up_carts", "r_dn_carts", "RT"]},
         hamiltonians: {"compute_local_energy": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT"],
                        "compute_local_energy_fast": ["hamiltonian_data", "r_up_carts", "r_dn_carts", "RT",
                                                      "geminal_inverse"]},

@@ -194,3 +194,46 @@ def test_total_and_ecp_potential_match_reference(name, golden_dir):
     v = CP.compute_coulomb_potential(coul, g["r_up"], g["r_dn"], RT, wavefunction_data=wf)
     assert rel(v, g["bare_coulomb"] + ecp) < RTOL
     assert rel(CP.compute_ecp_coulomb_potential(coul, wf, g["r_up"], g["r_dn"], RT), ecp) < 1e-9
+
+
+def test_per_electron_tables(setup):
+    """grad / lap of ln|det| and of J per electron, and the kinetic elements."""
+    from jqmc_gb300 import determinant as D
+    from jqmc_gb300 import jastrow_factor as JF
+    from jqmc_gb300 import wavefunction as WF
+    syn, o, r_up, r_dn = setup
+    wf = syn.hamiltonian.wavefunction_data
+    n = r_up.shape[1]
+    for w in range(2):
+        Ginv = np.linalg.inv(o.geminal(r_up[w], r_dn[w]))
+        gu, gd, lu, ld = o.det_grad_lap(r_up[w], r_dn[w], Ginv)
+        got = D.compute_grads_and_laplacian_ln_Det(wf.geminal_data, r_up[w], r_dn[w])
+        for a, b in zip(got, (gu, gd, lu, ld)):
+            assert a.shape == np.shape(b) and rel(a, b) < RTOL
+        gJ, lJ = o.jastrow_grad_lap(r_up[w], r_dn[w])
+        got = JF.compute_grads_and_laplacian_Jastrow_part(wf.jastrow_data, r_up[w], r_dn[w])
+        for a, b in zip(got, (gJ[:n], gJ[n:], lJ[:n], lJ[n:])):
+            assert a.shape == np.shape(b) and rel(a, b) < RTOL
+        tu, td = o.kinetic_elements(r_up[w], r_dn[w], Ginv)
+        Tu, Td = WF.compute_kinetic_energy_all_elements(wf, r_up[w], r_dn[w])
+        assert rel(Tu, tu) < RTOL and rel(Td, td) < RTOL
+
+
+def test_discretized_kinetic(setup):
+    """The six rotated lattice moves of every electron: configurations and elements."""
+    from jqmc_gb300 import wavefunction as WF
+    from oracle.wf import rotation_matrix
+    syn, o, r_up, r_dn = setup
+    wf = syn.hamiltonian.wavefunction_data
+    n = r_up.shape[1]
+    ang = np.random.default_rng(12).uniform(-2 * np.pi, 2 * np.pi, size=3)
+    RT = rotation_matrix(*ang).T
+    Ginv = np.linalg.inv(o.geminal(r_up[0], r_dn[0]))
+    cu, cd, el = WF.compute_discretized_kinetic_energy(0.2, wf, r_up[0], r_dn[0], RT)
+    ref = o.discretized_kinetic(0.2, r_up[0], r_dn[0], RT, Ginv)
+    assert el.shape == ref.shape and rel(el, ref) < RTOL
+    N = 2 * n
+    assert cu.shape == (6 * N, n, 3) and cd.shape == (6 * N, n, 3)
+    shifts = 0.2 * np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], float) @ RT
+    e, k = n + 1, 4          # a down electron's +z move
+    assert np.allclose(cd[6 * e + k, e - n], r_dn[0][e - n] + shifts[k]) and np.array_equal(cu[6 * e + k], r_up[0])
