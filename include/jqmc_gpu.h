@@ -82,7 +82,8 @@ typedef struct {
                               /* and rank-1 updates float; AO gradients/Laplacians,*/
                               /* energy cache, weights and the table rebuild double;*/
                               /* block energy (jqmc_lrdmc_energy): float values     */
-                              /* with compensated float-float sums; the walkers     */
+                              /* with compensated float-float sums over the FP64-   */
+                              /* accurate tables (jqmc_walkers.tlo); the walkers    */
                               /* whose mesh ratios cancel strongly (factor above    */
                               /* JQMC_FAST_ENERGY_CANCEL) recomputed in FP64        */
 #define JQMC_PREC_MIXED_FASTE 2 /* as JQMC_PREC_MIXED, the compensated energy alone */
@@ -121,6 +122,15 @@ typedef struct {
                       /* displacements, required when that exceeds 64 KiB per    */
                       /* walker (else kept in shared memory); may be NULL below  */
   int32_t* status;    /* nwalk JQMC_ST_* bits                                    */
+  float* tlo;         /* JQMC_PREC_MIXED, optional: nwalk*2*n*A floats, the low  */
+                      /* parts of the FP64-accurate T tables (T_up rows, then    */
+                      /* T_dn rows): written by jqmc_walker_init and             */
+                      /* jqmc_lu_rebuild_refine when non-NULL; read by           */
+                      /* jqmc_lrdmc_energy when non-NULL, which the caller may   */
+                      /* pass only while no move has changed the tables since    */
+                      /* that build.  With it the block energy is computed from  */
+                      /* T_hi + T_lo and AO gradients/Laplacians re-evaluated in */
+                      /* FP64 at the electrons instead of the float tables.      */
 } jqmc_walkers;
 
 /* Copy the tables to the current device.  Replaces the per-call packing of

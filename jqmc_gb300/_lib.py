@@ -44,7 +44,8 @@ class SystemDesc(C.Structure):
 
 class Walkers(C.Structure):
     _fields_ = [("nwalk", i32), ("precision", i32), ("r", vp), ("G", vp), ("Ginv", vp), ("Tup", vp), ("Tdn", vp), ("h3", vp),
-                ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("dcache", vp), ("status", vp)]
+                ("dphi", vp), ("dphi3", vp), ("ecache", vp), ("scratch", vp), ("dcache", vp), ("status", vp),
+                ("tlo", vp)]
 
 
 PREC_FP64, PREC_MIXED, PREC_MIXED_FASTE = 0, 1, 2

@@ -37,6 +37,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <type_traits>
 #include <algorithm>
 #include <vector>
 
@@ -242,6 +243,7 @@ struct WS {
   float* dcache;
   double* scratch;
   int* status;
+  float* tlo;   // mixed form, optional: low parts of the FP64-accurate T tables
 };
 
 // Shared-memory table layout (byte offsets), identical for every walker kernel.
@@ -436,14 +438,18 @@ __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R
 // P points at once: sum_{a in shell} phi_a(d_p) v[a] into acc[p].  The points
 // share the shell's primitive table and the v entries (loaded once); the P
 // evaluations are independent, which gives each lane P chains of work.
-template <int L, int P, class R, class V, class Acc>
+// LO: the table also has low parts vlo (v + vlo is the FP64-accurate value);
+// their products are added as a correction.
+template <int L, int P, class R, class V, class Acc, bool LO = false>
 __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* dz, const R* rad, int ao0, int jlo, int nm,
-                                             const V* v, Acc* acc) {
+                                             const V* v, Acc* acc, const float* vlo = nullptr) {
   R vv[2 * L + 1];
+  R vl[LO ? 2 * L + 1 : 1];
 #pragma unroll
   for (int j = 0; j < 2 * L + 1; ++j) {
     const int k = j - jlo;
     vv[j] = (k >= 0 && k < nm) ? (R)v[ao0 + k] : R(0);
+    if constexpr (LO) vl[j] = (k >= 0 && k < nm) ? (R)vlo[ao0 + k] : R(0);
   }
 #pragma unroll
   for (int p = 0; p < P; ++p) {
@@ -453,6 +459,12 @@ __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* 
 #pragma unroll
     for (int j = 0; j < 2 * L + 1; ++j) part += S[j] * vv[j];
     acc_fma(acc[p], rad[p], part);
+    if constexpr (LO) {
+      R plo = R(0);
+#pragma unroll
+      for (int j = 0; j < 2 * L + 1; ++j) plo += S[j] * vl[j];
+      acc_add(acc[p], rad[p] * plo);
+    }
     if constexpr (AccTraits<Acc>::accurate) {
       R pabs = R(0);
 #pragma unroll
@@ -462,8 +474,9 @@ __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* 
   }
 }
 
-template <int P, class R, class V, class Acc>
-__device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, Acc* acc) {
+template <int P, class R, class V, class Acc, bool LO = false>
+__device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, Acc* acc,
+                                              const float* vlo = nullptr) {
   const int* sh = b.shells + 8 * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const R* pr = prims_of<R>(b) + 2 * p0;
@@ -479,22 +492,23 @@ __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx
     for (int p = 0; p < P; ++p) rad[p] += c * MeshExp<R, AccTraits<Acc>::accurate>::ex(-Z * r2[p]);
   }
   switch (l) {
-    case 0: emit_dot_pts<0, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 1: emit_dot_pts<1, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 2: emit_dot_pts<2, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 3: emit_dot_pts<3, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 4: emit_dot_pts<4, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 5: emit_dot_pts<5, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    default: emit_dot_pts<6, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 0: emit_dot_pts<0, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 1: emit_dot_pts<1, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 2: emit_dot_pts<2, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 3: emit_dot_pts<3, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 4: emit_dot_pts<4, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 5: emit_dot_pts<5, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    default: emit_dot_pts<6, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
   }
 }
 
 // shell_dot_pts with the squared distances given as float-float pairs
 // (r2h + r2l): exp(-Z (r2h + r2l)) = expf(-Z r2h) (1 - Z r2l) to second order,
 // so that the float AO values carry only the rounding of their own evaluation.
-template <int P, class V, class Acc>
+template <int P, class V, class Acc, bool LO = false>
 __device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const float* dx, const float* dy, const float* dz,
-                                                 const float* r2h, const float* r2l, const V* v, Acc* acc) {
+                                                 const float* r2h, const float* r2l, const V* v, Acc* acc,
+                                                 const float* vlo = nullptr) {
   const int* sh = b.shells + 8 * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const float* pr = b.primsf + 2 * p0;
@@ -507,13 +521,13 @@ __device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const fl
     for (int p = 0; p < P; ++p) rad[p] += c * expf(-Z * r2h[p]) * (1.f - Z * r2l[p]);
   }
   switch (l) {
-    case 0: emit_dot_pts<0, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 1: emit_dot_pts<1, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 2: emit_dot_pts<2, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 3: emit_dot_pts<3, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 4: emit_dot_pts<4, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    case 5: emit_dot_pts<5, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
-    default: emit_dot_pts<6, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
+    case 0: emit_dot_pts<0, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 1: emit_dot_pts<1, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 2: emit_dot_pts<2, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 3: emit_dot_pts<3, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 4: emit_dot_pts<4, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    case 5: emit_dot_pts<5, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
+    default: emit_dot_pts<6, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
   }
 }
 
@@ -964,6 +978,8 @@ struct Work {
   Tab* vn3;
   double* red;   // kRed
   double* sc;    // 32 scalars
+  const float* tlo_up;   // mixed form: low parts of T_up / T_dn from the last build
+  const float* tlo_dn;   // (nullptr when the tables have moved since, or not kept)
 };
 
 struct WorkLayout {
@@ -1020,6 +1036,8 @@ __device__ Work<Tab> make_work(const Sys& s, const WorkLayout& L, unsigned char*
   k.dphi = static_cast<Tab*>(ws.dphi) + (size_t)w * k.N * 4 * k.A;
   k.dphi3 = s.has_j3 ? static_cast<Tab*>(ws.dphi3) + (size_t)w * k.N * 5 * k.A3 : nullptr;
   k.ec = ws.ecache + (size_t)w * (k.N + 1) * kEC;
+  k.tlo_up = ws.tlo ? ws.tlo + (size_t)w * 2 * k.n * k.A : nullptr;
+  k.tlo_dn = ws.tlo ? k.tlo_up + (size_t)k.n * k.A : nullptr;
   return k;
 }
 
@@ -1351,6 +1369,31 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
   __syncthreads();
 }
 
+// The determinant part of electron e's derivatives at FP64 accuracy, for the
+// block energy of the mixed form right after a build: the AO gradients and
+// Laplacians re-evaluated in FP64 at r_e (the float tables hold them rounded,
+// which alone moves E_L by about 1e-5 Ha on the 30-electron ring) dotted with
+// the FP64-accurate T row T_hi + T_lo.  One warp; the lanes split the shells;
+// every lane returns (grad x, y, z, Laplacian) of phi . T.
+template <class Tab>
+__device__ void det_terms_fp64(const Work<Tab>& k, int e, const Tab* Trow, const float* Tlo, double* out) {
+  const Sys& s = k.s;
+  const int lane = threadIdx.x & 31;
+  const double px = k.r[3 * e], py = k.r[3 * e + 1], pz = k.r[3 * e + 2];
+  double ax = 0.0, ay = 0.0, az = 0.0, al = 0.0;
+  auto f = [&](int a, double, double gx, double gy, double gz, double lap) {
+    const double t = (double)Trow[a] + (double)Tlo[a];
+    ax += gx * t; ay += gy * t; az += gz * t; al += lap * t;
+  };
+  for (int idx = lane; idx < s.det.nshell; idx += 32) {
+    const int sh = s.det.shells[8 * idx + 7];
+    double dx, dy, dz;
+    disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
+    shell_vgl_d<double>(s.det, sh, dx, dy, dz, f);
+  }
+  out[0] = warp_sum(ax); out[1] = warp_sum(ay); out[2] = warp_sum(az); out[3] = warp_sum(al);
+}
+
 // Phase A: per-electron continuum kinetic energy and the old-position values
 // the ratios need (wavefunction.py:1142-1207 with jastrow_factor.py:961-1034,
 // 3435-3558, 4077-4156).  One warp per electron: the cached AO derivative tables
@@ -1384,12 +1427,21 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     Acc tgx, tgy, tgz, tlp, tc3, thx, thy, thz, thl;
     acc_zero(tgx); acc_zero(tgy); acc_zero(tgz); acc_zero(tlp);
     acc_zero(tc3); acc_zero(thx); acc_zero(thy); acc_zero(thz); acc_zero(thl);
-    for (int a = lane; a < A; a += 32) {
-      const Ar tv = (Ar)Trow[a];
-      acc_fma(tgx, (Ar)dp[a], tv);
-      acc_fma(tgy, (Ar)dp[A + a], tv);
-      acc_fma(tgz, (Ar)dp[2 * A + a], tv);
-      acc_fma(tlp, (Ar)dp[3 * A + a], tv);
+    // the block energy of the mixed form on fresh tables: FP64-accurate
+    // determinant terms (the float projection keeps the table dots)
+    constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
+    const float* Tlo = kMayRefine ? (up ? k.tlo_up : k.tlo_dn) : nullptr;
+    double dt[4] = {0.0, 0.0, 0.0, 0.0};
+    if (kMayRefine && Tlo) {
+      det_terms_fp64(k, e, Trow, Tlo + (size_t)i * A, dt);
+    } else {
+      for (int a = lane; a < A; a += 32) {
+        const Ar tv = (Ar)Trow[a];
+        acc_fma(tgx, (Ar)dp[a], tv);
+        acc_fma(tgy, (Ar)dp[A + a], tv);
+        acc_fma(tgz, (Ar)dp[2 * A + a], tv);
+        acc_fma(tlp, (Ar)dp[3 * A + a], tv);
+      }
     }
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
@@ -1403,7 +1455,8 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
         acc_fma(thl, (Ar)q[4 * A3 + a], hv);
       }
     }
-    const Out v0 = acc_out(tgx), v1 = acc_out(tgy), v2 = acc_out(tgz), v3 = acc_out(tlp);
+    Out v0 = acc_out(tgx), v1 = acc_out(tgy), v2 = acc_out(tgz), v3 = acc_out(tlp);
+    if (kMayRefine && Tlo) { v0 = (Out)dt[0]; v1 = (Out)dt[1]; v2 = (Out)dt[2]; v3 = (Out)dt[3]; }
     const Out v4 = acc_out(tc3), v5 = acc_out(thx), v6 = acc_out(thy), v7 = acc_out(thz), v8 = acc_out(thl);
     if (lane == (it & 31)) {
       kp[0] = v0; kp[1] = v1; kp[2] = v2; kp[3] = v3; kp[4] = v4; kp[5] = v5; kp[6] = v6; kp[7] = v7; kp[8] = v8;
@@ -1476,6 +1529,10 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
   const bool up = e < s.n_up;
   const int i = up ? e : e - s.n_up;
   const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
+  // block energy on fresh tables (mixed form): the T row's low parts as well
+  constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
+  const float* Tlo = nullptr;
+  if constexpr (kMayRefine) Tlo = (up ? k.tlo_up : k.tlo_dn) ? (up ? k.tlo_up : k.tlo_dn) + (size_t)i * k.A : nullptr;
   const bool rel = sizeof(R) == sizeof(float) && t.dA != nullptr;
   const float* dAe = rel ? t.dA + (size_t)e * s.natom * 3 : nullptr;
   const float* dEe = rel ? t.dE + (size_t)e * k.N * 3 : nullptr;
@@ -1498,7 +1555,7 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     // compensated energy: displacements as float pairs (the low part from the
     // double positions), squared distances as float pairs
     float dxl[P], dyl[P], dzl[P], r2h[P], r2l[P];
-    auto shells = [&](const Basis& b, const Tab* v, Acc* acc) {
+    auto shells = [&](const Basis& b, const Tab* v, Acc* acc, const float* vlo) {
       for (int idx = lane; idx < b.nshell; idx += 32) {
         const int sh = b.shells[8 * idx + 7];
         const int atom = b.shells[8 * sh];
@@ -1514,11 +1571,12 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
           ff_add(z, zl + sl[2 * P + p], mz[p], dz[p], dzl[p]);
           ff_r2(dx[p], dxl[p], dy[p], dyl[p], dz[p], dzl[p], r2h[p], r2l[p]);
         }
-        shell_dot_pts_ff<P>(b, sh, dx, dy, dz, r2h, r2l, v, acc);
+        if (vlo) shell_dot_pts_ff<P, Tab, Acc, true>(b, sh, dx, dy, dz, r2h, r2l, v, acc, vlo);
+        else shell_dot_pts_ff<P>(b, sh, dx, dy, dz, r2h, r2l, v, acc);
       }
     };
-    shells(s.det, Trow, det);
-    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj);
+    shells(s.det, Trow, det, Tlo);
+    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, nullptr);
   } else {
     for (int idx = lane; idx < s.det.nshell; idx += 32) {
       const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
@@ -1526,7 +1584,12 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
       dnuc(s.det.shells[8 * sh], x, y, z);
 #pragma unroll
       for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
-      shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
+      if constexpr (kMayRefine) {
+        if (Tlo) shell_dot_pts<P, R, Tab, Acc, true>(s.det, sh, dx, dy, dz, Trow, det, Tlo);
+        else shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
+      } else {
+        shell_dot_pts<P, R>(s.det, sh, dx, dy, dz, Trow, det);
+      }
     }
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * k.A3;
@@ -2145,6 +2208,7 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
     __syncthreads();
     const float2* Mdn2 = reinterpret_cast<const float2*>(Mdn);
     const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
+    float* tlo = P.ws.tlo ? P.ws.tlo + (size_t)w * 2 * n * A : nullptr;
     constexpr int KB = 8;
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
       for (int k0 = 0; k0 < n; k0 += KB) {
@@ -2164,8 +2228,14 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
 #pragma unroll
         for (int u = 0; u < KB; ++u)
           if (k0 + u < n) {
-            Tup[(size_t)(k0 + u) * A + a] = (Tab)(us[u] + uc[u]);
-            Tdn[(size_t)(k0 + u) * A + a] = (Tab)(ds[u] + dc[u]);
+            // (s, c) -> (hi, lo) with hi the float nearest to s + c
+            const float uh = __fadd_rn(us[u], uc[u]), dh = __fadd_rn(ds[u], dc[u]);
+            Tup[(size_t)(k0 + u) * A + a] = (Tab)uh;
+            Tdn[(size_t)(k0 + u) * A + a] = (Tab)dh;
+            if (tlo) {
+              tlo[(size_t)(k0 + u) * A + a] = __fadd_rn(__fsub_rn(us[u], uh), uc[u]);
+              tlo[(size_t)(n + k0 + u) * A + a] = __fadd_rn(__fsub_rn(ds[u], dh), dc[u]);
+            }
           }
       }
     }
@@ -3134,7 +3204,7 @@ WS to_ws(const jqmc_walkers* w) {
   WS x;
   x.r = w->r; x.G = w->G; x.Ginv = w->Ginv; x.Tup = w->Tup; x.Tdn = w->Tdn; x.h3 = w->h3;
   x.dphi = w->dphi; x.dphi3 = w->dphi3; x.ecache = w->ecache; x.dcache = w->dcache;
-  x.scratch = w->scratch; x.status = w->status;
+  x.scratch = w->scratch; x.status = w->status; x.tlo = w->tlo;
   return x;
 }
 

@@ -223,9 +223,14 @@ class WalkerSet:
             M = len(system._keep["pos"])
             big = N * (M + N) * 3 * 4 > 64 * 1024
             self.dcache = torch.empty((W, N * (M + N) * 3), dtype=torch.float32, device=dev) if big else None
+            # low parts of the FP64-accurate T tables, written by every build and read
+            # by the block energy while no move has changed the tables (fresh)
+            self.tlo = torch.empty((W, 2, n, A), dtype=torch.float32, device=dev)
         else:
             self.scratch = None
             self.dcache = None
+            self.tlo = None
+        self.fresh = False
         self.init()
 
     @classmethod
@@ -238,9 +243,13 @@ class WalkerSet:
             setattr(obj, name, torch.empty_like(getattr(other, name)))
         obj.scratch = other.scratch   # the rebuild scratch is shared: it holds no state between calls
         obj.dcache = other.dcache     # so are the displacement caches (rebuilt every projection step)
+        obj.tlo = other.tlo           # and the low table parts (valid only from a build to the next move)
+        obj.fresh = False
         return obj
 
-    def desc(self) -> _lib.Walkers:
+    def desc(self, tlo: bool = False) -> _lib.Walkers:
+        """The C descriptor; ``tlo`` passes the low table parts (builds write them,
+        the block energy reads them while the tables are fresh)."""
         d = _lib.Walkers()
         d.nwalk = self.nwalk
         d.precision = PRECISIONS[self.precision]
@@ -248,6 +257,7 @@ class WalkerSet:
             setattr(d, name, C.c_void_p(getattr(self, name).data_ptr()))
         d.scratch = C.c_void_p(self.scratch.data_ptr()) if self.scratch is not None else None
         d.dcache = C.c_void_p(self.dcache.data_ptr()) if self.dcache is not None else None
+        d.tlo = C.c_void_p(self.tlo.data_ptr()) if (tlo and self.tlo is not None) else None
         return d
 
     @property
@@ -259,14 +269,16 @@ class WalkerSet:
         return self.r[:, self.sys.n_up:]
 
     def init(self):
-        d = self.desc()
+        d = self.desc(tlo=True)
         _lib.check(_lib.lib().jqmc_walker_init(self.sys.handle, C.byref(d), self.sys.stream), "jqmc_walker_init")
+        self.fresh = True
 
     def rebuild(self):
         """FP64 rebuild of G, G^-1 (+ one refinement step), T and the J3 field from
         the positions; the exact per-electron caches are kept."""
-        d = self.desc()
+        d = self.desc(tlo=True)
         _lib.check(_lib.lib().jqmc_lu_rebuild_refine(self.sys.handle, C.byref(d), self.sys.stream), "jqmc_lu_rebuild_refine")
+        self.fresh = True
 
     def dlnpsi_dparam(self, lam: bool = True):
         """Raw per-walker derivative blocks of ln|psi| (FP64 walkers): (d_j1 (W,),
@@ -315,6 +327,7 @@ class WalkerSet:
 
     def vmc_sweep(self, idraw: torch.Tensor, fdraw: torch.Tensor, Dt: float, eps_AS: float, accept: torch.Tensor):
         K = idraw.shape[1]
+        self.fresh = False
         d = self.desc()
         _lib.check(_lib.lib().jqmc_vmc_sweep(self.sys.handle, C.byref(d), K, C.c_void_p(idraw.data_ptr()),
                                              C.c_void_p(fdraw.data_ptr()), float(Dt), float(eps_AS),
@@ -331,6 +344,7 @@ class WalkerSet:
 
     def lrdmc_project(self, draws: torch.Tensor, alat: float, E_scf: float, w: torch.Tensor):
         K = draws.shape[1]
+        self.fresh = False
         d = self.desc()
         _lib.check(_lib.lib().jqmc_lrdmc_project(self.sys.handle, C.byref(d), K, C.c_void_p(draws.data_ptr()), float(alat),
                                                  float(E_scf), C.c_void_p(w.data_ptr()), self.sys.stream), "jqmc_lrdmc_project")
@@ -338,6 +352,7 @@ class WalkerSet:
     def lrdmc_project_t(self, draws: torch.Tensor, alat: float, w: torch.Tensor, tau_left: torch.Tensor,
                         nsteps: torch.Tensor, eL: torch.Tensor):
         """GFMC_t projections until tau_left is spent or the K draws (W, K, 5) are used."""
+        self.fresh = False
         K = draws.shape[1]
         d = self.desc()
         _lib.check(_lib.lib().jqmc_lrdmc_project_t(self.sys.handle, C.byref(d), K, C.c_void_p(draws.data_ptr()), float(alat),
@@ -353,7 +368,7 @@ class WalkerSet:
             raise ValueError(f"lrdmc_energy needs 4 float64 draws per walker; got {tuple(last_draw.shape)} {last_draw.dtype}")
         eL = torch.empty(self.nwalk, dtype=torch.float64, device=self.sys.device)
         vd = torch.empty_like(eL)
-        d = self.desc()
+        d = self.desc(tlo=self.fresh)
         _lib.check(_lib.lib().jqmc_lrdmc_energy(self.sys.handle, C.byref(d), C.c_void_p(last_draw.data_ptr()), float(alat),
                                                 C.c_void_p(eL.data_ptr()), C.c_void_p(vd.data_ptr()), self.sys.stream),
                    "jqmc_lrdmc_energy")
@@ -369,6 +384,7 @@ class WalkerSet:
         return self.scratch.view(self.nwalk, -1)[:, 0].clone()
 
     def gather_from(self, src: "WalkerSet", chosen: torch.Tensor):
+        self.fresh = False
         ds, dd = src.desc(), self.desc()
         _lib.check(_lib.lib().jqmc_walker_gather(self.sys.handle, C.byref(ds), C.byref(dd), C.c_void_p(chosen.data_ptr()),
                                                  self.sys.stream), "jqmc_walker_gather")
