@@ -5,7 +5,8 @@
  * descriptors are read during the call only.  Every entry point returns 0 on
  * success or a negative JQMC_E_* code; nothing throws across the ABI.  Calls
  * are asynchronous on the given CUDA stream (cudaStream_t passed as void*);
- * the library synchronises only inside jqmc_system_create/destroy.
+ * the library synchronises only inside jqmc_system_create/destroy and when a
+ * mixed-form rebuild first grows the system's tensor-core workspace.
  *
  * Each entry point names the reference interface (jQMC, Python/JAX) whose
  * per-walker computation it replaces, batched over a leading walker axis.
@@ -139,6 +140,18 @@ typedef struct {
  * jastrow_factor.py:561-1476, coulomb_potential.py:188-598). */
 int jqmc_system_create(const jqmc_system_desc* desc, jqmc_system** out);
 int jqmc_system_destroy(jqmc_system* sys);
+
+/* 1 when the mixed form's table rebuild (jqmc_walker_init, jqmc_lu_rebuild_refine)
+ * forms M = Phi lambda on the tensor cores (tcgen05, split-bf16 operands with
+ * exact FP32 sums, about 1e-14 relative) -- systems with at most 1024 geminal
+ * AOs -- and 0 when it uses the float-float CUDA-core kernel.  The tensor-core
+ * path keeps an operand workspace with the system (about 12 bytes per
+ * electron-row x AO for up to 65536 rows, allocated on the first rebuild); a
+ * rebuild that would have to allocate it inside a stream capture uses the
+ * CUDA-core kernel instead.  Rebuilds of one system must not overlap on
+ * different streams (they share the workspace).  Replaces the geminal assembly
+ * lambda . Phi of jqmc/determinant.py:1380-1402 in the rebuild. */
+int32_t jqmc_tensor_core_rebuild(const jqmc_system* sys);
 
 /* Bytes of walker state per walker (sum over the jqmc_walkers arrays) for a
  * JQMC_PREC_* precision. */

@@ -94,12 +94,13 @@ def lib():
         L.jqmc_probe_fp64.argtypes = [i64, i32, vp, pf64, vp]
         L.jqmc_branch_comb_noalloc.argtypes = [i32, vp, f64, vp, vp]
         L.jqmc_probe_fp32.argtypes = [i64, i32, vp, pf64, vp]
+        L.jqmc_tensor_core_rebuild.argtypes = [vp]
         for name in ("jqmc_probe_fp64", "jqmc_system_create", "jqmc_system_destroy", "jqmc_ao_vgl", "jqmc_walker_init", "jqmc_log_psi",
                      "jqmc_vmc_sweep", "jqmc_vmc_measure", "jqmc_lrdmc_project", "jqmc_lrdmc_energy",
                      "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
                      "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
                      "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild",
-                     "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh"):
+                     "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh", "jqmc_tensor_core_rebuild"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -115,4 +116,4 @@ EXPORTED = ("jqmc_system_create", "jqmc_system_destroy", "jqmc_walker_bytes", "j
             "jqmc_branch_comb", "jqmc_walker_gather", "jqmc_probe_fp64", "jqmc_branch_comb_noalloc", "jqmc_probe_fp32",
             "jqmc_lu_rebuild_refine", "jqmc_dlnpsi_dparam", "jqmc_lrdmc_project_t", "jqmc_batch_create",
             "jqmc_batch_destroy", "jqmc_batch_walkers", "jqmc_vmc_sweep_batch", "jqmc_batch_rebuild",
-            "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh")
+            "jqmc_dlnpsi_dR", "jqmc_electron_terms", "jqmc_kinetic_mesh", "jqmc_tensor_core_rebuild")

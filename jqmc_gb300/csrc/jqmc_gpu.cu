@@ -41,7 +41,10 @@
 #include <algorithm>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "jqmc_gpu.h"
+#include "jqmc_tc.h"
 #include "solid_harmonics.cuh"
 
 // CTAs per SM the projection kernel is compiled for (register budget)
@@ -1953,6 +1956,80 @@ __global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
   rebuild_m_body<ROWS>(P, blockIdx.x, blockIdx.y, smem);
 }
 
+// Operand A of the tensor-core lambda-GEMM (jqmc_tc.cu): the FP64 AO values of
+// 8 electrons of one spin (rows row0 + 8 blockIdx.x + rr of the chunk; row g is
+// electron g % n of walker g / n), each row scaled by 2^-e (max |phi| < 2^e) and
+// split into six 8-bit integer slices, written as bf16 in the tensor cores'
+// shared-memory layout: [row tile][K chunk][slice][128 x 32 canonical block].
+// Rows at or past rows_total are written as zeros.  Shared memory: 8 x K doubles.
+__global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long long row0, long long rows_total, int nk,
+                                                   uint8_t* __restrict__ a_sl, int* __restrict__ row_exp) {
+  using namespace jqmc_tc;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int ex[8];
+  const Sys& s = P.s;
+  const int n = s.n_up, K = nk * kKC;
+  double* phi = reinterpret_cast<double*>(smem);   // 8 x K
+  for (int t = threadIdx.x; t < 8 * K; t += blockDim.x) phi[t] = 0.0;
+  __syncthreads();
+  const long long g0 = row0 + 8ll * blockIdx.x;
+  for (int rr = 0; rr < 8 && g0 + rr < rows_total; ++rr) {
+    const long long g = g0 + rr;
+    const int w = (int)(g / n), i = (int)(g % n);
+    const double* r = P.ws.r + ((size_t)w * s.N + (size_t)spin * n + i) * 3;
+    const double px = r[0], py = r[1], pz = r[2];
+    double* out = phi + rr * K;
+    auto f = [&](int a, double v) { out[a] = v; };
+    for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
+      shell_val_d<double>(s.det, sh, dx, dy, dz, f);
+    }
+  }
+  __syncthreads();
+  {
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int rr = wid; rr < 8; rr += blockDim.x >> 5) {
+      double m = 0.0;
+      for (int a = lane; a < K; a += 32) m = fmax(m, fabs(phi[rr * K + a]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (lane == 0) {
+        int e = 0;
+        if (m > 0.0) frexp(m, &e);
+        ex[rr] = e;
+      }
+    }
+  }
+  __syncthreads();
+  const int lr0 = 8 * blockIdx.x;             // first local row of this CTA
+  const int tile = lr0 / kBM, rg = (lr0 % kBM) / 8;
+  if (threadIdx.x < 8) row_exp[lr0 + threadIdx.x] = ex[threadIdx.x];
+  // item (k group gk of 8 AOs, row rr): the 8 lanes of consecutive rows write one
+  // 128-byte core matrix per slice
+  for (int it = threadIdx.x; it < 8 * (K / 8); it += blockDim.x) {
+    const int rr = it & 7, gk = it >> 3;
+    const double sc = ldexp(1.0, -ex[rr]);
+    float q[8][kSlices];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) split8(phi[rr * K + 8 * gk + j] * sc, q[j]);
+    const int c = gk / 4;
+    uint8_t* base = a_sl + ((size_t)tile * nk + c) * kAStage + rg * 512 + (gk % 4) * 128 + rr * 16;
+#pragma unroll
+    for (int sl = 0; sl < kSlices; ++sl) {
+      unsigned short h[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) h[j] = __bfloat16_as_ushort(__float2bfloat16_rn(q[j][sl]));
+      uint4 v;
+      v.x = h[0] | ((unsigned)h[1] << 16);
+      v.y = h[2] | ((unsigned)h[3] << 16);
+      v.z = h[4] | ((unsigned)h[5] << 16);
+      v.w = h[6] | ((unsigned)h[7] << 16);
+      *reinterpret_cast<uint4*>(base + sl * kASliceBytes) = v;
+    }
+  }
+}
+
 // J3 field h_e = dJ3/dphi3(r_e) of every electron (the gradient of J3 with
 // respect to one electron's J3 AO vector, jastrow_factor.py:4077-4156), with
 // arithmetic type J and stored as Tab, in two passes over the electrons so that
@@ -3196,6 +3273,15 @@ inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
 struct jqmc_system {
   Sys s;
   void* blob;
+  // tensor-core lambda-GEMM of the mixed rebuild (jqmc_tc.cu), when A <= 1024:
+  // operand B = lambda (spin up) and lambda^T (spin down), split and laid out
+  // once; operand A and the row exponents in a workspace grown on first use
+  int tc_nk = 0, tc_ncol_tiles = 0;
+  uint16_t* tc_b = nullptr;     // [spin][col tile][k chunk][slice][64 x 32]
+  int* tc_col_exp = nullptr;    // [spin][col tile * 64]
+  uint16_t* tc_a = nullptr;     // [row tile][k chunk][slice][128 x 32]
+  int* tc_row_exp = nullptr;
+  long long tc_rows_cap = 0;    // rows the workspace holds
 };
 
 namespace {
@@ -3462,14 +3548,64 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.nv = nv; s.mesh_pts = dp(o_mp); s.mesh_w = dp(o_mw);
   s.ion_ion = d->ion_ion;
   sys->blob = blob;
+  if (A <= jqmc_tc::kMaxK) {
+    // operand B of the tensor-core lambda-GEMM: column b of L = lambda (spin up:
+    // M_up = Phi_up lambda) or lambda^T (spin down: M_dn rows = lambda phi_dn),
+    // scaled by 2^-e_b and split into six 8-bit slices (bf16), in the tensor
+    // cores' layout [spin][col tile][k chunk][slice][64 x 32 canonical block]
+    using namespace jqmc_tc;
+    const int nk = (A + kKC - 1) / kKC, nct = (A + kBN - 1) / kBN;
+    const size_t per_spin = (size_t)nct * nk * kBStage / 2;   // bf16 elements
+    std::vector<uint16_t> hb(2 * per_spin, 0);
+    std::vector<int> hexp((size_t)2 * nct * kBN, 0);
+    for (int spin = 0; spin < 2; ++spin)
+      for (int b = 0; b < A; ++b) {
+        auto L = [&](int a) { return spin == 0 ? d->lambda[(size_t)a * A + b] : d->lambda[(size_t)b * A + a]; };
+        double m = 0.0;
+        for (int a = 0; a < A; ++a) m = std::max(m, fabs(L(a)));
+        int e = 0;
+        if (m > 0.0) frexp(m, &e);
+        hexp[(size_t)spin * nct * kBN + b] = e;
+        const int ct = b / kBN, rb = b % kBN;
+        for (int a = 0; a < A; ++a) {
+          float q[kSlices];
+          split8(ldexp(L(a), -e), q);
+          const int c = a / kKC, kk = a % kKC;
+          for (int sl = 0; sl < kSlices; ++sl) {
+            uint32_t bits;
+            memcpy(&bits, &q[sl], 4);   // an integer of at most 8 bits: the high half is its exact bf16
+            const size_t off = ((size_t)ct * nk + c) * kBStage + (size_t)sl * kBSliceBytes + canon_offset(rb, kk);
+            hb[spin * per_spin + off / 2] = (uint16_t)(bits >> 16);
+          }
+        }
+      }
+    if (cudaMalloc(&sys->tc_b, hb.size() * 2) != cudaSuccess ||
+        cudaMalloc(&sys->tc_col_exp, hexp.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(sys->tc_b, hb.data(), hb.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sys->tc_col_exp, hexp.data(), hexp.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+      if (sys->tc_b) cudaFree(sys->tc_b);
+      if (sys->tc_col_exp) cudaFree(sys->tc_col_exp);
+      cudaFree(blob);
+      delete sys;
+      return JQMC_E_CUDA;
+    }
+    sys->tc_nk = nk;
+    sys->tc_ncol_tiles = nct;
+  }
   *out = sys;
   return JQMC_OK;
 }
+
+int32_t jqmc_tensor_core_rebuild(const jqmc_system* sys) { return sys ? (sys->tc_b ? 1 : 0) : JQMC_E_ARG; }
 
 int jqmc_system_destroy(jqmc_system* sys) {
   if (!sys) return JQMC_E_ARG;
   cudaDeviceSynchronize();
   if (sys->blob) cudaFree(sys->blob);
+  if (sys->tc_b) cudaFree(sys->tc_b);
+  if (sys->tc_col_exp) cudaFree(sys->tc_col_exp);
+  if (sys->tc_a) cudaFree(sys->tc_a);
+  if (sys->tc_row_exp) cudaFree(sys->tc_row_exp);
   delete sys;
   return JQMC_OK;
 }
@@ -3511,6 +3647,53 @@ static InitLayout init_layout(const Sys& s, const KParams&) {
   return L;
 }
 
+// M_up / M_dn of the mixed rebuild on the tensor cores (k_ao_slices +
+// jqmc_tc::ozaki_gemm) into the walkers' scratch, in chunks of at most 65536
+// electron rows per spin (the operand workspace, about 0.6 GB for A = 736, is
+// allocated on first use and kept with the system).  Returns kTcUnavailable
+// when the workspace would have to grow inside a stream capture; the caller
+// then uses the CUDA-core kernel.
+constexpr int kTcUnavailable = 1;
+static int tc_rebuild_m(const jqmc_system* csys, const jqmc_walkers* w, const KParams& P, void* stream) {
+  using namespace jqmc_tc;
+  jqmc_system* sys = const_cast<jqmc_system*>(csys);   // the workspace is a cache of the system
+  const Sys& s = sys->s;
+  const int n = s.n_up, A = s.det.nao, nk = sys->tc_nk, nct = sys->tc_ncol_tiles;
+  const long long rows_total = (long long)w->nwalk * n;
+  const long long want = ((std::min(rows_total, 65536ll) + kBM - 1) / kBM) * kBM;
+  if (sys->tc_rows_cap < want) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(S(stream), &cs) != cudaSuccess) return JQMC_E_CUDA;
+    if (cs != cudaStreamCaptureStatusNone) return kTcUnavailable;
+    if (cudaStreamSynchronize(S(stream)) != cudaSuccess) return JQMC_E_CUDA;   // the old workspace may be in use
+    if (sys->tc_a) cudaFree(sys->tc_a);
+    if (sys->tc_row_exp) cudaFree(sys->tc_row_exp);
+    sys->tc_a = nullptr;
+    sys->tc_row_exp = nullptr;
+    sys->tc_rows_cap = 0;
+    if (cudaMalloc(&sys->tc_a, (size_t)(want / kBM) * nk * kAStage) != cudaSuccess ||
+        cudaMalloc(&sys->tc_row_exp, (size_t)want * sizeof(int)) != cudaSuccess)
+      return JQMC_E_CUDA;
+    sys->tc_rows_cap = want;
+  }
+  const int smem_a = 8 * nk * kKC * 8;
+  int rc = launch_check((const void*)k_ao_slices, smem_a);
+  if (rc) return rc;
+  const size_t b_spin = (size_t)nct * nk * kBStage / 2;
+  for (int spin = 0; spin < 2; ++spin)
+    for (long long r0 = 0; r0 < rows_total; r0 += sys->tc_rows_cap) {
+      const long long rows = std::min(sys->tc_rows_cap, rows_total - r0);
+      const int tiles = (int)((rows + kBM - 1) / kBM);
+      k_ao_slices<<<tiles * (kBM / 8), 128, smem_a, S(stream)>>>(P, spin, r0, rows_total, nk,
+                                                                 reinterpret_cast<uint8_t*>(sys->tc_a), sys->tc_row_exp);
+      rc = ozaki_gemm(sys->tc_a, sys->tc_b + spin * b_spin, sys->tc_row_exp, sys->tc_col_exp + (size_t)spin * nct * kBN, nk,
+                      nct, tiles, r0, rows_total, n, A, spin == 0 ? 1 : 0, reinterpret_cast<float2*>(w->scratch), w->status,
+                      JQMC_ST_NAN, S(stream));
+      if (rc) return JQMC_E_CUDA;
+    }
+  return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
+}
+
 static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, void* stream, int mode) {
   if (!walkers_ok(sys, w)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
@@ -3519,15 +3702,21 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
   const InitLayout IL = init_layout(s, P);
   const int smem = IL.bytes;
   if (is_mixed(w->precision)) {
-    // M_up, M_dn by the float-float lam-GEMM into the scratch, then the rest in FP64
-    const int rows = s.det.nao <= 2048 ? 8 : 4;
-    const int smem_m = rows * s.det.nao * 8;
-    const void* fm = rows == 8 ? (const void*)k_rebuild_m<8> : (const void*)k_rebuild_m<4>;
-    int rc = launch_check(fm, smem_m);
-    if (rc) return rc;
-    const dim3 grid_m(w->nwalk, 2 * ((n + rows - 1) / rows));
-    if (rows == 8) k_rebuild_m<8><<<grid_m, 128, smem_m, S(stream)>>>(P);
-    else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
+    // M_up, M_dn into the scratch: by the split-bf16 tensor-core GEMM when the
+    // system has its operand (A <= 1024), else by the float-float CUDA-core
+    // kernel; then the rest in FP64
+    int rc = sys->tc_b ? tc_rebuild_m(sys, w, P, stream) : kTcUnavailable;
+    if (rc < 0) return rc;
+    if (rc == kTcUnavailable) {
+      const int rows = s.det.nao <= 2048 ? 8 : 4;
+      const int smem_m = rows * s.det.nao * 8;
+      const void* fm = rows == 8 ? (const void*)k_rebuild_m<8> : (const void*)k_rebuild_m<4>;
+      rc = launch_check(fm, smem_m);
+      if (rc) return rc;
+      const dim3 grid_m(w->nwalk, 2 * ((n + rows - 1) / rows));
+      if (rows == 8) k_rebuild_m<8><<<grid_m, 128, smem_m, S(stream)>>>(P);
+      else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
+    }
     rc = launch_check((const void*)k_walker_init<float>, smem);
     if (rc) return rc;
     k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, IL, mode | kInitMReady);

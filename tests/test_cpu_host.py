@@ -16,7 +16,7 @@ def _declared_symbols():
     for fn in os.listdir(os.path.join(ROOT, "include")):
         if fn.endswith(".h"):
             txt = open(os.path.join(ROOT, "include", fn)).read()
-            names += re.findall(r"^\s*(?:int|int64_t)\s+(jqmc_\w+)\s*\(", txt, flags=re.M)
+            names += re.findall(r"^\s*(?:int|int32_t|int64_t)\s+(jqmc_\w+)\s*\(", txt, flags=re.M)
     return sorted(set(names))
 
 
@@ -236,6 +236,7 @@ def test_entry_points_reject_invalid_arguments():
         "jqmc_vmc_sweep_batch(NULL)": L.jqmc_vmc_sweep_batch(None, 4, fake, fake, 0.4, 0.0, fake, 64, 0, None),
         "jqmc_vmc_sweep_batch(threads=33)": L.jqmc_vmc_sweep_batch(fake, 4, fake, fake, 0.4, 0.0, fake, 33, 0, None),
         "jqmc_batch_rebuild(NULL)": L.jqmc_batch_rebuild(None, 0, None),
+        "jqmc_tensor_core_rebuild(NULL)": L.jqmc_tensor_core_rebuild(None),
     }
     bad = {k: v for k, v in calls.items() if v != E_ARG}
     assert not bad, bad
