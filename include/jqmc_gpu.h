@@ -279,7 +279,9 @@ int jqmc_walker_gather(const jqmc_system* sys, const jqmc_walkers* src, const jq
  * that loads it until the process exits.  nwalk above that limit returns
  * JQMC_E_LIMIT; no cudaMalloc/cudaFree is called.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
+ * current; make that first call before any stream capture.  The look-up is
+ * repeated on the first call after the device's context was replaced (e.g. by
+ * cudaDeviceReset), which reloads the array.  All calls share
  * the one array, so calls that overlap on the GPU (other streams, other host
  * threads) race: serialise them. */
 #define JQMC_NOALLOC_MAX_WALKERS 262144

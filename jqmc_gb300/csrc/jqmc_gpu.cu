@@ -3907,7 +3907,41 @@ int jqmc_probe_fp32(int64_t iters, int32_t blocks, float* d_sink, double* flops,
 static __device__ __align__(256) double g_branch_scratch[JQMC_NOALLOC_MAX_WALKERS];
 
 static std::mutex g_noalloc_mu;
-static double* g_noalloc_ptr[64] = {nullptr};
+// Set-up done per device: the device address of g_branch_scratch and the unique
+// ID of the CUDA context it belongs to.  cudaDeviceReset (or any other end of the
+// primary context) reloads the module, possibly elsewhere; a new context has a
+// new ID, so the next call repeats the set-up instead of using a stale address.
+struct NoallocSetup {
+  unsigned long long ctx_id = 0;
+  double* ptr = nullptr;
+};
+static NoallocSetup g_noalloc[64];
+
+// ID of the current context (driver entry points found through the runtime, so
+// the library does not link libcuda); 0 when it cannot be read.
+static unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int32_t* d_chosen, void* stream) {
   if (nwalk <= 0 || !d_w || !d_chosen || !(zeta >= 0.0 && zeta < 1.0)) return JQMC_E_ARG;
@@ -3916,15 +3950,19 @@ int jqmc_branch_comb_noalloc(int32_t nwalk, const double* d_w, double zeta, int3
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return JQMC_E_CUDA;
   double* scratch = nullptr;
   {
-    // one-time set-up per device, with that device current: the host-side
-    // symbol is only a stand-in, so the kernels get the device address
+    // set-up once per device (and again after its context was replaced), with
+    // that device current: the host-side symbol is only a stand-in, so the
+    // kernels get the device address
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoallocSetup& su = g_noalloc[dev];
+    const unsigned long long id = current_context_id();
+    if (!su.ptr || id == 0 || id != su.ctx_id) {
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_branch_scratch) != cudaSuccess || !p) return JQMC_E_CUDA;
-      g_noalloc_ptr[dev] = static_cast<double*>(p);
+      su.ptr = static_cast<double*>(p);
+      su.ctx_id = id;
     }
-    scratch = g_noalloc_ptr[dev];
+    scratch = su.ptr;
   }
   // every scratch entry the search reads is written by the cumsum first, so
   // nothing needs clearing between calls

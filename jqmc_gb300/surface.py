@@ -83,6 +83,18 @@ def _ham_for_wavefunction(wf: Wavefunction_data) -> Hamiltonian_data:
     return Hamiltonian_data(structure_data=st, coulomb_potential_data=_no_charges(st), wavefunction_data=wf)
 
 
+def _stand_in_geminal(st, n_up: int, n_dn: int) -> Geminal_data:
+    """A geminal for quantities that do not depend on it: n_up s functions with
+    distinct exponents (0.3 to 3 bohr^-2) on nucleus 0 and a unit pairing matrix,
+    so that G is non-singular for electrons at distinct distances from that
+    nucleus and the walker initialisation runs through cleanly."""
+    s_set = AOs_sphe_data(structure_data=st, nucleus_index=(0,) * n_up, num_ao=n_up, num_ao_prim=n_up,
+                          orbital_indices=tuple(range(n_up)), exponents=np.geomspace(0.3, 3.0, n_up),
+                          coefficients=np.ones(n_up), angular_momentums=(0,) * n_up, magnetic_quantum_numbers=(0,) * n_up)
+    return Geminal_data(num_electron_up=n_up, num_electron_dn=n_dn, orb_data_up_spin=s_set, orb_data_dn_spin=s_set,
+                        lambda_matrix=np.eye(n_up, 2 * n_up - n_dn))
+
+
 def _ham_for_jastrow(jd: Jastrow_data, n_up: int, n_dn: int) -> Hamiltonian_data:
     if jd.jastrow_one_body_data is not None:
         st = jd.jastrow_one_body_data.structure_data
@@ -90,32 +102,22 @@ def _ham_for_jastrow(jd: Jastrow_data, n_up: int, n_dn: int) -> Hamiltonian_data
         st = jd.jastrow_three_body_data.orb_data.structure_data
     else:
         st = Structure_data(positions=np.zeros((1, 3)), atomic_numbers=(0,))
-    # n_up s functions on nucleus 0 (the geminal needs at least n_up AOs); its
-    # determinant outputs are not read, and the J outputs do not depend on it
-    s_set = AOs_sphe_data(structure_data=st, nucleus_index=(0,) * n_up, num_ao=n_up, num_ao_prim=n_up,
-                          orbital_indices=tuple(range(n_up)), exponents=np.ones(n_up), coefficients=np.ones(n_up),
-                          angular_momentums=(0,) * n_up, magnetic_quantum_numbers=(0,) * n_up)
-    gem = Geminal_data(num_electron_up=n_up, num_electron_dn=n_dn, orb_data_up_spin=s_set, orb_data_dn_spin=s_set,
-                       lambda_matrix=np.eye(n_up, 2 * n_up - n_dn))
+    # its determinant outputs are not read, and the J outputs do not depend on it
     return Hamiltonian_data(structure_data=st, coulomb_potential_data=_no_charges(st),
-                            wavefunction_data=Wavefunction_data(jastrow_data=jd, geminal_data=gem))
+                            wavefunction_data=Wavefunction_data(jastrow_data=jd, geminal_data=_stand_in_geminal(st, n_up, n_dn)))
 
 
 def _ham_for_coulomb(coul, n_up: int, n_dn: int) -> Hamiltonian_data:
-    """The given Coulomb/ECP data (None: no nuclear charges) with the Jastrow
-    stand-in's geminal (n_up s functions on nucleus 0) and no Jastrow.  The walker
-    initialisation fills the energy cache (electron-ion and local ECP terms per
-    electron, the electron-electron total), which is all that is read."""
+    """The given Coulomb/ECP data (None: no nuclear charges) with the stand-in
+    geminal and no Jastrow.  The walker initialisation fills the energy cache
+    (electron-ion and local ECP terms per electron, the electron-electron total),
+    which is all that is read."""
     if coul is None:
         return _ham_for_jastrow(Jastrow_data(), n_up, n_dn)
     st = coul.structure_data
-    s_set = AOs_sphe_data(structure_data=st, nucleus_index=(0,) * n_up, num_ao=n_up, num_ao_prim=n_up,
-                          orbital_indices=tuple(range(n_up)), exponents=np.ones(n_up), coefficients=np.ones(n_up),
-                          angular_momentums=(0,) * n_up, magnetic_quantum_numbers=(0,) * n_up)
-    gem = Geminal_data(num_electron_up=n_up, num_electron_dn=n_dn, orb_data_up_spin=s_set, orb_data_dn_spin=s_set,
-                       lambda_matrix=np.eye(n_up, 2 * n_up - n_dn))
     return Hamiltonian_data(structure_data=st, coulomb_potential_data=coul,
-                            wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(), geminal_data=gem))
+                            wavefunction_data=Wavefunction_data(jastrow_data=Jastrow_data(),
+                                                                geminal_data=_stand_in_geminal(st, n_up, n_dn)))
 
 
 def coulomb_terms(coul, r_up_carts, r_dn_carts):
@@ -136,7 +138,10 @@ def coulomb_terms(coul, r_up_carts, r_dn_carts):
             _cache.popitem(last=False)
     ec = _walkers(gs, r_up, r_dn).ecache          # (W, N + 1, stride)
     N = n_up + n_dn
-    return ec[:, :N, 0], ec[:, :N, 1], ec[:, N, 0], float(gs.ion_ion), single
+    ei, eloc, ee = ec[:, :N, 0], ec[:, :N, 1], ec[:, N, 0]
+    if not (bool(torch.isfinite(ei).all()) and bool(torch.isfinite(eloc).all()) and bool(torch.isfinite(ee).all())):
+        raise JqmcError("the energy cache of the Coulomb evaluation holds non-finite values")
+    return ei, eloc, ee, float(gs.ion_ion), single
 
 
 def _configs(r_up_carts, r_dn_carts):

@@ -1,10 +1,12 @@
 """Algorithmic work model of the walker kernels (for roofline accounting).
 
-FP64 operation counts per unit of work, counted from the algorithm the kernels
+Operation counts per unit of work, counted from the algorithm the kernels
 implement (not from profiler counters):  FMA = 2, add / sub / mul / div /
-sqrt / compare = 1, and one FP64 exponential = EXP_FLOPS (a range reduction
-plus a degree-10 polynomial in FP64 is about 20 operations; this is the
-convention, stated with every number that uses it).
+sqrt / compare = 1.  An exponential counts as the instructions that evaluate
+it: EXP_FLOPS = 20 in FP64 (a software range reduction and polynomial), and
+EXP_F32 = 2 in the float kernels (one multiply by log2 e and one SFU ex2: the
+float mesh uses the fast intrinsic).  The convention is stated with every
+number that uses it.
 
 Bytes per unit are the walker-state bytes a step must read and write in HBM.
 """
@@ -14,18 +16,19 @@ from __future__ import annotations
 import numpy as np
 
 EXP_FLOPS = 20.0
+EXP_F32 = 2.0
 
 
 def _sh_flops(l: int) -> float:
     return 0.0 if l < 2 else 4.0 * (2 * l + 1)
 
 
-def ao_point_flops(shells: np.ndarray) -> float:
+def ao_point_flops(shells: np.ndarray, exp_flops: float = EXP_FLOPS) -> float:
     """Value of every AO of a packed basis at one point, dotted with a vector."""
     f = 0.0
     for sh in shells:
         l, np_, nm = int(sh[1]), int(sh[2]), int(sh[5])
-        f += 8 + np_ * (3 + EXP_FLOPS) + _sh_flops(l) + nm * 3
+        f += 8 + np_ * (3 + exp_flops) + _sh_flops(l) + nm * 3
     return f
 
 
@@ -37,7 +40,7 @@ def ao_vgl_flops(shells: np.ndarray) -> float:
     return f
 
 
-def _step_parts(gs, ecp_fraction: float):
+def _step_parts(gs, ecp_fraction: float, exp_mesh: float = EXP_FLOPS):
     """Operation counts of one GFMC_n projection of one walker, by phase, as the
     walker kernels execute it (streaming caches: the AO derivative tables and the
     per-electron energy cache are read every step and recomputed only for the
@@ -45,13 +48,13 @@ def _step_parts(gs, ecp_fraction: float):
     keep = gs._keep
     N, n, A, M = gs.N, gs.n_up, gs.A, len(keep["pos"])
     A3 = gs.A3
-    det_p = ao_point_flops(keep["dsh"])
-    j3_p = ao_point_flops(keep["jsh"]) if A3 else 0.0
+    det_p = ao_point_flops(keep["dsh"], exp_mesh)
+    j3_p = ao_point_flops(keep["jsh"], exp_mesh) if A3 else 0.0
     det_v = ao_vgl_flops(keep["dsh"])
     j3_v = ao_vgl_flops(keep["jsh"]) if A3 else 0.0
     # psi(r')/psi(r) at one mesh point: AO values dotted with the T row / J3 field,
     # J1 over nuclei, J2 over electrons, the exponential of the Jastrow difference
-    ratio = det_p + j3_p + M * (12 + 2 * EXP_FLOPS) + N * 16 + EXP_FLOPS + 3
+    ratio = det_p + j3_p + M * (12 + 2 * exp_mesh) + N * 16 + exp_mesh + 3
     mesh = 6 * N * (ratio + 8) + gs.Nv * N * ecp_fraction * (ratio + 40)
     # electron terms: cached derivative tables dotted with T rows and J3 fields
     elec_dots = N * (2 * (4 * A + 5 * A3) + 40)
@@ -69,7 +72,7 @@ def lrdmc_step_split(gs, ecp_fraction: float):
     the mesh ratios, the electron-term dots and the rank-1 table updates run in
     float; the moved electron's derivative tables, the energy cache, the sums and
     the move choice stay in double."""
-    mesh, elec_dots, move, fp64 = _step_parts(gs, ecp_fraction)
+    mesh, elec_dots, move, fp64 = _step_parts(gs, ecp_fraction, EXP_F32)
     return mesh + elec_dots + move, fp64
 
 
@@ -78,11 +81,26 @@ def lrdmc_step_flops(gs, ecp_fraction: float) -> float:
     return sum(_step_parts(gs, ecp_fraction))
 
 
-def lrdmc_step_bytes(gs) -> float:
-    """HBM bytes of one projection of one walker: the rank-1 updates read and write
-    T_up, T_dn (2 n A doubles each way), the J3 field (N A3), and G, G^-1 once per
-    block (amortised, ignored)."""
-    return 8.0 * (2 * 2 * gs.n_up * gs.A + 2 * gs.N * max(gs.A3, 0))
+def lrdmc_step_bytes(gs, table_bytes: int = 8) -> float:
+    """HBM bytes of one projection of one walker with tables of `table_bytes`:
+    - read: the AO derivative tables of every electron (N 4 A + N 5 A3), the T
+      rows (2 n A) and J3 field (N A3) of the electron terms and the mesh, the
+      energy cache (8-byte rows of the stride);
+    - the rank-1 updates read and write T_up, T_dn (2 n A each way) and the J3
+      field (N A3 each way);
+    - written: the moved electron's derivative tables (4 A + 5 A3) and cache row.
+    G and G^-1 stay in shared memory for the whole block (read and written once
+    per block, amortised away)."""
+    n, N, A, A3 = gs.n_up, gs.N, gs.A, max(gs.A3, 0)
+    tables = (N * 4 * A + N * 5 * A3) + (2 * n * A + N * A3) + 2 * (2 * n * A + N * A3) + (4 * A + 5 * A3)
+    return float(table_bytes) * tables + 8.0 * (N + 2) * 24
+
+
+def rebuild_gemm_flops(gs) -> float:
+    """Operations of the rebuild's lambda-GEMM per walker: M_up = Phi_up lambda and
+    M_dn = Phi_dn lambda^T, 2 x 2 n A^2 (one product; the split form issues 21
+    bf16 slice products per product on the tensor cores)."""
+    return 2.0 * 2.0 * gs.n_up * gs.A * gs.A
 
 
 def dlnpsi_flops(gs, lam: bool = True) -> float:
