@@ -449,7 +449,7 @@ def gpu_arm(a):
     from jqmc_gb300.engine import WalkerSet
     from jqmc_gb300.jqmc_gfmc import GFMC_n
     from jqmc_gb300.replicas import max_over_ranks
-    from jqmc_gb300.workload import EXP_FLOPS, lrdmc_step_bytes, lrdmc_step_flops, lrdmc_step_split
+    from jqmc_gb300.workload import EXP_F32, EXP_FLOPS, lrdmc_step_bytes, lrdmc_step_flops, lrdmc_step_split
 
     syn = synthetic.SYSTEMS[a.workload]()
     W, K = a.walkers, a.nproj
@@ -601,12 +601,17 @@ def gpu_arm(a):
     adjoint = leg(lambda: adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")), a.no_adjoint)
     batching = leg(batching_leg, a.no_batching)
     vmc = leg(vmc_leg, a.no_vmc)
-    bytes_launch = lrdmc_step_bytes(gs) * W * K / 2.0   # float tables
+    bytes_launch = lrdmc_step_bytes(gs, 4) * W * K     # float tables
+    ach_hbm = bytes_launch / (mix_ms / 1e3) / 1e9
+    hbm_peak = peaks.get("hbm_gbs")
     per_call = {"jqmc_lrdmc_project": 1, "jqmc_lrdmc_energy": 2, "jqmc_branch_comb": 2, "jqmc_walker_gather": 10 if gs.A3 else 8,
                 "jqmc_lu_rebuild_refine": 2}   # k_rebuild_m + k_walker_init
     if rank == 0:
         line = {
-            "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "metric": METRIC, "value": mixed["value"], "unit": UNIT,
+            "accuracy": {"eL_rms_Ha": eL_rms, "dE_mean_Ha": float(np.mean(de)), "eL_max_Ha": float(np.max(np.abs(de))),
+                         "configs": int(len(de)), "bar": "eL_rms<=1e-5 Ha, |dE_mean|<=1e-4 Ha"},
+            "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": mixed["ms"] / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": f"lrdmc_{a.workload}", "form": "mixed precision (headline) vs plain FP64", "walkers": W,
@@ -631,7 +636,7 @@ def gpu_arm(a):
                                           "energy_ms": e_ms["fast"],
                                           "note": "precision mixed_fast_energy: the cycle with the compensated-float "
                                                   "energy alone, no FP64 recompute (accuracy under accuracy.fast_block_energy_variant)"},
-            "accuracy": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": int(len(de)),
+            "accuracy_detail": {"eL_rms_Ha": eL_rms, "eL_max_Ha": float(np.max(np.abs(de))), "configs": int(len(de)),
                          "same_path_fraction": same_frac, "block_weight_rel_diff_max": float(np.max(relw)),
                          "dE_mean_Ha": float(np.mean(de)), "dE_mean_stderr_Ha": float(np.std(de) / np.sqrt(len(de))),
                          "fp64_recomputed_fraction": float(flagged.mean()),
@@ -647,19 +652,24 @@ def gpu_arm(a):
                          "bar": "|dE_L| <= 1e-5 Ha rms per configuration; |d<E>| <= 1e-4 Ha"},
             "e2e": e2e,
             "gpu_launches": sum(per_call.values()) * a.steps,
-            "roofline": {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,
+            "roofline": {"bound": "hbm", "achieved": ach_hbm, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": ach_hbm / hbm_peak if hbm_peak else None,
                          "traffic": traffic, "traffic_unit": "bytes per launch (ncu, scaled from 912 walkers x 2 steps)",
                          "kernel": "k_lrdmc<float,float,float> (jqmc_lrdmc_project, mixed)",
-                         "flop_convention": f"FMA=2, add/mul/div/sqrt=1, exp={EXP_FLOPS:g}",
-                         "peak_source": "measured in this run by jqmc_probe_fp32 (8 independent FMA chains per thread)",
-                         "avg_launch_ms": mix_ms, "ecp_electron_fraction": ecp_frac,
-                         "fp64_part": {"achieved": ach64, "peak": peak64, "frac": ach64 / peak64,
-                                       "peak_source": "jqmc_probe_fp64, this run"},
-                         "hbm": {"algorithmic_bytes_per_launch": bytes_launch,
-                                 "achieved_gbs": bytes_launch / (mix_ms / 1e3) / 1e9, "peak_gbs": peaks.get("hbm_gbs"),
-                                 "peak_source": "MEASURED_PEAKS.json"},
+                         "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": mix_ms,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                         "bytes_model": "per walker-step: derivative tables of every electron, T rows and J3 field read, "
+                                        "rank-1 updates of T and the J3 field read and written, the moved electron's "
+                                        "tables and cache row written (jqmc_gb300.workload.lrdmc_step_bytes)",
+                         "compute_view": {"achieved": ach32, "peak": peak32, "unit": "GFLOP/s", "frac": ach32 / peak32,
+                                          "flop_convention": f"FMA=2, add/mul/div/sqrt=1, float exp={EXP_F32:g} "
+                                                             f"(mul + SFU ex2), FP64 exp={EXP_FLOPS:g}",
+                                          "peak_source": "measured in this run by jqmc_probe_fp32 (8 independent FMA chains per thread)",
+                                          "fp64_part": {"achieved": ach64, "peak": peak64, "frac": ach64 / peak64,
+                                                        "peak_source": "jqmc_probe_fp64, this run"}},
+                         "ecp_electron_fraction": ecp_frac,
                          "plain_fp64_kernel": {"bound": "fp64", "achieved": plain_ach, "peak": peak64, "frac": plain_ach / peak64,
-                                               "avg_launch_ms": plain_ms}},
+                                               "avg_launch_ms": plain_ms, "unit": "GFLOP/s"}},
             "adjoint": adjoint,
             "batching": batching,
             "vmc": vmc,

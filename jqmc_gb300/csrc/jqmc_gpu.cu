@@ -170,7 +170,12 @@ struct Basis {
   const int* shells;
   const double* prims;   // (Z, cN) double
   const float* primsf;   // (Z, cN) float copy
+  const float* rcut;     // per shell: beyond this distance from its nucleus every AO of the shell is below kScreenEps
 };
+
+// AO magnitude below which the float projection skips a shell at a mesh point
+// (the FP64 form and the block energy never skip).
+constexpr double kScreenEps = 1e-12;
 
 template <class R>
 __device__ __forceinline__ const R* prims_of(const Basis& b);
@@ -1272,14 +1277,19 @@ struct Terms {
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
+  int* slist;     // mixed form: per warp, the shells (geminal, then J3) within reach of its electron's mesh
+  int sl_stride;  // ints per warp in slist
+  int sl_nd, sl_nj;   // shells listed for the current electron (sl_nd < 0: no list, visit every shell)
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, off_sl, sl_stride,
+      bytes;
 };
 
-// rel: reserve the float displacement caches of the mixed form in shared memory
-TermsLayout terms_layout(const Sys& s, int base, bool rel) {
+// rel: reserve the float displacement caches of the mixed form in shared memory;
+// screen: reserve the per-warp shell lists of the float projection (4 warps)
+TermsLayout terms_layout(const Sys& s, int base, bool rel, bool screen = false) {
   TermsLayout L;
   const int N = s.N;
   int o = base;
@@ -1295,6 +1305,8 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
+  L.sl_stride = screen ? s.det.nshell + (s.has_j3 ? s.j3.nshell : 0) : 0;
+  L.off_sl = o; o = align16(o + 4 * L.sl_stride * 4);
   L.bytes = o;
   return L;
 }
@@ -1319,7 +1331,11 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
-  t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  t.dE = L.off_sl > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
+  t.slist = L.sl_stride > 0 ? reinterpret_cast<int*>(smem + L.off_sl) : nullptr;
+  t.sl_stride = L.sl_stride;
+  t.sl_nd = -1;
+  t.sl_nj = -1;
   if (gdcache) {
     t.dA = gdcache;
     t.dE = gdcache + (size_t)s.N * s.natom * 3;
@@ -1581,8 +1597,14 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     shells(s.det, Trow, det, Tlo);
     if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, nullptr);
   } else {
-    for (int idx = lane; idx < s.det.nshell; idx += 32) {
-      const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
+    // float projection: the shells listed within reach of the mesh (mesh_terms);
+    // otherwise every shell, in the (l, nprim)-sorted order
+    const int wid = threadIdx.x >> 5;
+    const bool listed = sizeof(R) == sizeof(float) && t.sl_nd >= 0;
+    const int* ld = listed ? t.slist + (size_t)wid * t.sl_stride : nullptr;
+    const int ndet = listed ? t.sl_nd : s.det.nshell;
+    for (int idx = lane; idx < ndet; idx += 32) {
+      const int sh = listed ? ld[idx] : s.det.shells[8 * idx + 7];
       R x, y, z;
       dnuc(s.det.shells[8 * sh], x, y, z);
 #pragma unroll
@@ -1596,8 +1618,9 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     }
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * k.A3;
-      for (int idx = lane; idx < s.j3.nshell; idx += 32) {
-        const int sh = s.j3.shells[8 * idx + 7];
+      const int nj3 = listed ? t.sl_nj : s.j3.nshell;
+      for (int idx = lane; idx < nj3; idx += 32) {
+        const int sh = listed ? ld[s.det.nshell + idx] : s.j3.shells[8 * idx + 7];
         R x, y, z;
         dnuc(s.j3.shells[8 * sh], x, y, z);
 #pragma unroll
@@ -1688,6 +1711,41 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
       if (sizeof(R) == sizeof(float) && t.dA && __isGlobal(t.dA)) {   // (a shared-memory cache needs none)
         prefetch_l2(t.dA + (size_t)en * s.natom * 3, (size_t)s.natom * 12, lane);
         prefetch_l2(t.dE + (size_t)en * N * 3, (size_t)N * 12, lane);
+      }
+    }
+    if constexpr (sizeof(R) == sizeof(float) && !kErr) {
+      // the shells within reach of this electron's mesh points (lattice moves of
+      // alat; quadrature points within 2 |r_e - R_I| of the electron), in the
+      // (l, nprim)-sorted order, compacted by ballots into the warp's list
+      if (t.slist && s.det.rcut) {
+        const float* dAe = t.dA + (size_t)e * s.natom * 3;
+        float reach = (float)alat;
+        if (ecp) {
+          const float* d = dAe + 3 * atom;
+          reach = fmaxf(reach, 2.f * sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        }
+        int* list = t.slist + (size_t)wid * t.sl_stride;
+        auto build = [&](const Basis& b, int* out) {
+          int cnt = 0;
+          for (int base = 0; base < b.nshell; base += 32) {
+            const int idx = base + lane;
+            int sh = 0;
+            bool need = false;
+            if (idx < b.nshell) {
+              sh = b.shells[8 * idx + 7];
+              const float* d = dAe + 3 * b.shells[8 * sh];
+              const float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+              need = dist - reach < b.rcut[sh];
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, need);
+            if (need) out[cnt + __popc(m & ((1u << lane) - 1u))] = sh;
+            cnt += __popc(m);
+          }
+          return cnt;
+        };
+        t.sl_nd = build(s.det, list);
+        t.sl_nj = s.has_j3 ? build(s.j3, list + s.det.nshell) : 0;
+        __syncwarp();
       }
     }
     for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
@@ -1792,6 +1850,42 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
   }
   __syncthreads();
   return cancel;
+}
+
+// Block energy of the mixed form: the lattice elements of an electron enter
+// E_L only through the fixed-node diagonal when one of its six moves crosses a
+// node of psi (ratio <= 0, jqmc_gfmc.py:5421-5500); elsewhere they cancel between
+// the diagonal and the non-diagonal sums.  The electrons with a lattice ratio
+// below kFlipMargin (crossing, or close enough that float rounding could decide
+// the sign) get their six ratios again in FP64 arithmetic on the FP64-accurate
+// tables, one warp per electron.
+constexpr double kFlipMargin = 0.05;
+template <class Tab>
+__device__ void refine_lattice(const Work<Tab>& k, Terms& t, double alat) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double kin = -1.0 / (2.0 * alat * alat);
+  for (int e = wid; e < k.N; e += nw) {
+    const bool near = lane < 6 && t.el[6 * e + lane] / kin < kFlipMargin;
+    if (!__any_sync(0xffffffffu, near)) continue;
+    for (int c = 0; c < 2; ++c) {
+      double mx = 0.0, my = 0.0, mz = 0.0;
+      if (lane < 3) {
+        const int kk = 3 * c + lane, ax = kk >> 1;
+        const double sg = (kk & 1) ? -alat : alat;
+        mx = sg * t.R[ax]; my = sg * t.R[3 + ax]; mz = sg * t.R[6 + ax];
+      }
+      double sx[3], sy[3], sz[3], rd[3];
+#pragma unroll
+      for (int p = 0; p < 3; ++p) {
+        sx[p] = __shfl_sync(0xffffffffu, mx, p);
+        sy[p] = __shfl_sync(0xffffffffu, my, p);
+        sz[p] = __shfl_sync(0xffffffffu, mz, p);
+      }
+      wf_ratio_pts<3, double, Tab, double>(k, t, e, sx, sy, sz, rd);
+      if (lane < 3) t.el[6 * e + 3 * c + lane] = kin * (lane == 0 ? rd[0] : lane == 1 ? rd[1] : rd[2]);
+    }
+  }
+  __syncthreads();
 }
 
 // Phase C of the GFMC_n step: (diag, nondiag) sums (jqmc_gfmc.py:4806-5030).
@@ -3085,6 +3179,8 @@ __global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K
     }
     electron_terms<Tab, Acc>(k, t, alat);
     const Cancellation mc = mesh_terms<R, Tab, Acc>(k, t, alat, true);
+    if constexpr (AccTraits<Acc>::accurate && sizeof(Tab) == sizeof(float))
+      if (K == 0 && k.tlo_up) refine_lattice(k, t, alat);
     double diag, nondiag;
     lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
@@ -3314,7 +3410,7 @@ KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   P.tl = table_layout(sys->s, !mixed);
   P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
   P.dcache_global = mixed && dcache_bytes(sys->s) > kDcacheSmemMax;
-  P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global);
+  P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global, mixed && sys->s.det.rcut != nullptr);
   P.nwalk = w->nwalk;
   return P;
 }
@@ -3483,6 +3579,29 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     for (int k = 0; k < b.nshell; ++k) rows[8 * k + 7] = ord[k];
     return rows;
   };
+  // per shell, the distance from its nucleus beyond which every AO of the shell
+  // is below kScreenEps: 4 r^l sum_p |c_p| e^{-Z_p r^2} (the solid harmonics of
+  // the normalisation used are at most about 1 on the unit sphere) scanned on a
+  // 0.02 bohr grid to 80 bohr; shells still above it there are never skipped
+  auto rcut_of = [](const jqmc_basis_desc& b) {
+    std::vector<float> rc(b.nshell);
+    for (int k = 0; k < b.nshell; ++k) {
+      const int* sh = b.shells + 8 * k;
+      const int l = sh[1], np = sh[2], p0 = sh[3];
+      auto f = [&](double r) {
+        double v = 0.0;
+        for (int q = 0; q < np; ++q) v += fabs(b.prims[2 * (p0 + q) + 1]) * exp(-b.prims[2 * (p0 + q)] * r * r);
+        return 4.0 * pow(r, l) * v;
+      };
+      double last = 0.0;
+      for (double r = 0.0; r <= 80.0; r += 0.02)
+        if (f(r) >= kScreenEps) last = r;
+      rc[k] = f(80.0) >= kScreenEps ? 1e30f : (float)(last + 0.05);
+    }
+    return rc;
+  };
+  const std::vector<float> drc = rcut_of(d->det);
+  const size_t o_drc = put(drc.data(), drc.size() * 4);
   const std::vector<int32_t> dsh_rows = with_order(d->det);
   const size_t o_dsh = put(dsh_rows.data(), (size_t)d->det.nshell * 32);
   const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
@@ -3494,9 +3613,11 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   const size_t o_laml = put(laml.data(), (size_t)A * A * 4);
   const size_t o_lamTl = put(lamTl.data(), (size_t)A * A * 4);
   const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
-  size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
+  size_t o_jrc = 0, o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
     const std::vector<int32_t> jsh_rows = with_order(d->j3);
+    const std::vector<float> jrc = rcut_of(d->j3);
+    o_jrc = put(jrc.data(), jrc.size() * 4);
     o_jsh = put(jsh_rows.data(), (size_t)d->j3.nshell * 32);
     o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
     o_jprf = put(jprf.data(), jprf.size() * 4);
@@ -3527,7 +3648,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.natom = M; s.n_up = d->n_up; s.n_dn = d->n_dn; s.N = d->n_up + d->n_dn;
   s.atom_pos = dp(o_apos); s.atom_zeff = dp(o_az);
   s.det.nshell = d->det.nshell; s.det.nao = A; s.det.nprim = d->det.nprim;
-  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf);
+  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf); s.det.rcut = fp(o_drc);
   s.lam = dp(o_lam); s.lamT = dp(o_lamT); s.lamf = fp(o_lamf); s.lamTf = fp(o_lamTf);
   s.laml = fp(o_laml); s.lamTl = fp(o_lamTl);
   s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_cA = dp(o_j1z);
@@ -3535,10 +3656,11 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.has_j3 = d->has_j3;
   if (d->has_j3) {
     s.j3.nshell = d->j3.nshell; s.j3.nao = A3; s.j3.nprim = d->j3.nprim;
-    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf);
+    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf); s.j3.rcut = fp(o_jrc);
     s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v); s.j3matf = fp(o_j3mf); s.j3matTf = fp(o_j3mTf);
   } else {
     s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr; s.j3.primsf = nullptr;
+    s.j3.rcut = nullptr;
     s.j3mat = s.j3matT = s.j3vec = nullptr;
     s.j3matf = s.j3matTf = nullptr;
   }
