@@ -170,12 +170,7 @@ struct Basis {
   const int* shells;
   const double* prims;   // (Z, cN) double
   const float* primsf;   // (Z, cN) float copy
-  const float* rcut;     // per shell: beyond this distance from its nucleus every AO of the shell is below kScreenEps
 };
-
-// AO magnitude below which the float projection skips a shell at a mesh point
-// (the FP64 form and the block energy never skip).
-constexpr double kScreenEps = 1e-12;
 
 template <class R>
 __device__ __forceinline__ const R* prims_of(const Basis& b);
@@ -1277,19 +1272,14 @@ struct Terms {
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
-  int* slist;     // mixed form: per warp, the shells (geminal, then J3) within reach of its electron's mesh
-  int sl_stride;  // ints per warp in slist
-  int sl_nd, sl_nj;   // shells listed for the current electron (sl_nd < 0: no list, visit every shell)
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, off_sl, sl_stride,
-      bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, bytes;
 };
 
-// rel: reserve the float displacement caches of the mixed form in shared memory;
-// screen: reserve the per-warp shell lists of the float projection (4 warps)
-TermsLayout terms_layout(const Sys& s, int base, bool rel, bool screen = false) {
+// rel: reserve the float displacement caches of the mixed form in shared memory
+TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   TermsLayout L;
   const int N = s.N;
   int o = base;
@@ -1305,8 +1295,6 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel, bool screen = false) 
   L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
-  L.sl_stride = screen ? s.det.nshell + (s.has_j3 ? s.j3.nshell : 0) : 0;
-  L.off_sl = o; o = align16(o + 4 * L.sl_stride * 4);
   L.bytes = o;
   return L;
 }
@@ -1331,11 +1319,7 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
-  t.dE = L.off_sl > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
-  t.slist = L.sl_stride > 0 ? reinterpret_cast<int*>(smem + L.off_sl) : nullptr;
-  t.sl_stride = L.sl_stride;
-  t.sl_nd = -1;
-  t.sl_nj = -1;
+  t.dE = L.bytes > L.off_dE ? reinterpret_cast<float*>(smem + L.off_dE) : nullptr;
   if (gdcache) {
     t.dA = gdcache;
     t.dE = gdcache + (size_t)s.N * s.natom * 3;
@@ -1597,14 +1581,8 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     shells(s.det, Trow, det, Tlo);
     if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, nullptr);
   } else {
-    // float projection: the shells listed within reach of the mesh (mesh_terms);
-    // otherwise every shell, in the (l, nprim)-sorted order
-    const int wid = threadIdx.x >> 5;
-    const bool listed = sizeof(R) == sizeof(float) && t.sl_nd >= 0;
-    const int* ld = listed ? t.slist + (size_t)wid * t.sl_stride : nullptr;
-    const int ndet = listed ? t.sl_nd : s.det.nshell;
-    for (int idx = lane; idx < ndet; idx += 32) {
-      const int sh = listed ? ld[idx] : s.det.shells[8 * idx + 7];
+    for (int idx = lane; idx < s.det.nshell; idx += 32) {
+      const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
       R x, y, z;
       dnuc(s.det.shells[8 * sh], x, y, z);
 #pragma unroll
@@ -1618,9 +1596,8 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     }
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * k.A3;
-      const int nj3 = listed ? t.sl_nj : s.j3.nshell;
-      for (int idx = lane; idx < nj3; idx += 32) {
-        const int sh = listed ? ld[s.det.nshell + idx] : s.j3.shells[8 * idx + 7];
+      for (int idx = lane; idx < s.j3.nshell; idx += 32) {
+        const int sh = s.j3.shells[8 * idx + 7];
         R x, y, z;
         dnuc(s.j3.shells[8 * sh], x, y, z);
 #pragma unroll
@@ -1711,41 +1688,6 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
       if (sizeof(R) == sizeof(float) && t.dA && __isGlobal(t.dA)) {   // (a shared-memory cache needs none)
         prefetch_l2(t.dA + (size_t)en * s.natom * 3, (size_t)s.natom * 12, lane);
         prefetch_l2(t.dE + (size_t)en * N * 3, (size_t)N * 12, lane);
-      }
-    }
-    if constexpr (sizeof(R) == sizeof(float) && !kErr) {
-      // the shells within reach of this electron's mesh points (lattice moves of
-      // alat; quadrature points within 2 |r_e - R_I| of the electron), in the
-      // (l, nprim)-sorted order, compacted by ballots into the warp's list
-      if (t.slist && s.det.rcut) {
-        const float* dAe = t.dA + (size_t)e * s.natom * 3;
-        float reach = (float)alat;
-        if (ecp) {
-          const float* d = dAe + 3 * atom;
-          reach = fmaxf(reach, 2.f * sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-        }
-        int* list = t.slist + (size_t)wid * t.sl_stride;
-        auto build = [&](const Basis& b, int* out) {
-          int cnt = 0;
-          for (int base = 0; base < b.nshell; base += 32) {
-            const int idx = base + lane;
-            int sh = 0;
-            bool need = false;
-            if (idx < b.nshell) {
-              sh = b.shells[8 * idx + 7];
-              const float* d = dAe + 3 * b.shells[8 * sh];
-              const float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-              need = dist - reach < b.rcut[sh];
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, need);
-            if (need) out[cnt + __popc(m & ((1u << lane) - 1u))] = sh;
-            cnt += __popc(m);
-          }
-          return cnt;
-        };
-        t.sl_nd = build(s.det, list);
-        t.sl_nj = s.has_j3 ? build(s.j3, list + s.det.nshell) : 0;
-        __syncwarp();
       }
     }
     for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
@@ -3410,7 +3352,7 @@ KParams make_params(const jqmc_system* sys, const jqmc_walkers* w) {
   P.tl = table_layout(sys->s, !mixed);
   P.wl = work_layout(sys->s, P.tl.bytes, tab_bytes(w));
   P.dcache_global = mixed && dcache_bytes(sys->s) > kDcacheSmemMax;
-  P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global, mixed && sys->s.det.rcut != nullptr);
+  P.ml = terms_layout(sys->s, P.wl.bytes, mixed && !P.dcache_global);
   P.nwalk = w->nwalk;
   return P;
 }
@@ -3579,29 +3521,6 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     for (int k = 0; k < b.nshell; ++k) rows[8 * k + 7] = ord[k];
     return rows;
   };
-  // per shell, the distance from its nucleus beyond which every AO of the shell
-  // is below kScreenEps: 4 r^l sum_p |c_p| e^{-Z_p r^2} (the solid harmonics of
-  // the normalisation used are at most about 1 on the unit sphere) scanned on a
-  // 0.02 bohr grid to 80 bohr; shells still above it there are never skipped
-  auto rcut_of = [](const jqmc_basis_desc& b) {
-    std::vector<float> rc(b.nshell);
-    for (int k = 0; k < b.nshell; ++k) {
-      const int* sh = b.shells + 8 * k;
-      const int l = sh[1], np = sh[2], p0 = sh[3];
-      auto f = [&](double r) {
-        double v = 0.0;
-        for (int q = 0; q < np; ++q) v += fabs(b.prims[2 * (p0 + q) + 1]) * exp(-b.prims[2 * (p0 + q)] * r * r);
-        return 4.0 * pow(r, l) * v;
-      };
-      double last = 0.0;
-      for (double r = 0.0; r <= 80.0; r += 0.02)
-        if (f(r) >= kScreenEps) last = r;
-      rc[k] = f(80.0) >= kScreenEps ? 1e30f : (float)(last + 0.05);
-    }
-    return rc;
-  };
-  const std::vector<float> drc = rcut_of(d->det);
-  const size_t o_drc = put(drc.data(), drc.size() * 4);
   const std::vector<int32_t> dsh_rows = with_order(d->det);
   const size_t o_dsh = put(dsh_rows.data(), (size_t)d->det.nshell * 32);
   const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
@@ -3613,11 +3532,9 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   const size_t o_laml = put(laml.data(), (size_t)A * A * 4);
   const size_t o_lamTl = put(lamTl.data(), (size_t)A * A * 4);
   const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
-  size_t o_jrc = 0, o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
+  size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
     const std::vector<int32_t> jsh_rows = with_order(d->j3);
-    const std::vector<float> jrc = rcut_of(d->j3);
-    o_jrc = put(jrc.data(), jrc.size() * 4);
     o_jsh = put(jsh_rows.data(), (size_t)d->j3.nshell * 32);
     o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
     o_jprf = put(jprf.data(), jprf.size() * 4);
@@ -3648,7 +3565,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.natom = M; s.n_up = d->n_up; s.n_dn = d->n_dn; s.N = d->n_up + d->n_dn;
   s.atom_pos = dp(o_apos); s.atom_zeff = dp(o_az);
   s.det.nshell = d->det.nshell; s.det.nao = A; s.det.nprim = d->det.nprim;
-  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf); s.det.rcut = fp(o_drc);
+  s.det.shells = ip(o_dsh); s.det.prims = dp(o_dpr); s.det.primsf = fp(o_dprf);
   s.lam = dp(o_lam); s.lamT = dp(o_lamT); s.lamf = fp(o_lamf); s.lamTf = fp(o_lamTf);
   s.laml = fp(o_laml); s.lamTl = fp(o_lamTl);
   s.has_j1 = d->has_j1; s.j1_type = d->j1_type; s.j1_param = d->j1_param; s.j1_cA = dp(o_j1z);
@@ -3656,11 +3573,10 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.has_j3 = d->has_j3;
   if (d->has_j3) {
     s.j3.nshell = d->j3.nshell; s.j3.nao = A3; s.j3.nprim = d->j3.nprim;
-    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf); s.j3.rcut = fp(o_jrc);
+    s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf);
     s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v); s.j3matf = fp(o_j3mf); s.j3matTf = fp(o_j3mTf);
   } else {
     s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr; s.j3.primsf = nullptr;
-    s.j3.rcut = nullptr;
     s.j3mat = s.j3matT = s.j3vec = nullptr;
     s.j3matf = s.j3matTf = nullptr;
   }
@@ -3695,7 +3611,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
           const int c = a / kKC, kk = a % kKC;
           for (int sl = 0; sl < kSlices; ++sl) {
             uint32_t bits;
-            memcpy(&bits, &q[sl], 4);   // an integer of at most 8 bits: the high half is its exact bf16
+            memcpy(&bits, &q[sl], 4);   // 8 significant bits at most: the high half is its exact bf16
             const size_t off = ((size_t)ct * nk + c) * kBStage + (size_t)sl * kBSliceBytes + canon_offset(rb, kk);
             hb[spin * per_spin + off / 2] = (uint16_t)(bits >> 16);
           }

@@ -8,15 +8,16 @@
 // six 8-bit integer slices (Ozaki's error-free splitting); a bf16 holds each slice
 // exactly, every slice product is an exact 16-bit integer, and sums of at most
 // 2^24 / 2^14 = 1024 such products are exact in the FP32 accumulators.  The
-// products of slice pairs (s, t) with s + t <= 5 are accumulated per level
-// d = s + t in tensor memory (TMEM):
+// products of slice pairs (s, t) with s + t <= 5 (slice s stored as its integer
+// times 2^-8s, so a product carries the scale of its level) are accumulated per
+// level d = s + t in tensor memory (TMEM):
 //   level 0           one accumulator over all of K (K <= 1024)
 //   level 1 (2 pairs) one accumulator per 512 of K
 //   level 2 (3 pairs) one accumulator per 256 of K
 //   levels 3..5       one accumulator (its FP32 rounding is 2^-48 of the total)
 // so eight 128 x 64 FP32 accumulators fill the 512 TMEM columns of the SM.  The
 // epilogue reads them back with tcgen05.ld, adds the levels as float-float pairs
-// (exact integers scaled by 2^-8d) and scales by the row and column exponents.
+// and scales by the row and column exponents.
 //
 // Data movement: the sliced operands are laid out in global memory exactly as the
 // tensor cores read them from shared memory (canonical K-major core matrices, no
@@ -274,14 +275,9 @@ __global__ void __launch_bounds__(128, 1)
     for (int x = 0; x < 16; ++x) {
       const int b = ct * kBN + q * 16 + x;
       if (b >= ncols) break;
-      float h = v[0][x], l = 0.f;
-      two_sum(h, l, v[1][x] * 0x1p-8f);
-      two_sum(h, l, v[2][x] * 0x1p-8f);
-      two_sum(h, l, v[3][x] * 0x1p-16f);
-      two_sum(h, l, v[4][x] * 0x1p-16f);
-      two_sum(h, l, v[5][x] * 0x1p-16f);
-      two_sum(h, l, v[6][x] * 0x1p-16f);
-      two_sum(h, l, v[7][x] * 0x1p-24f);
+      float h = v[0][x], l = 0.f;   // (the slices carry their levels' scales)
+#pragma unroll
+      for (int j = 1; j < kAcc; ++j) two_sum(h, l, v[j][x]);
       const float hs = __fadd_rn(h, l);   // renormalise the pair
       const float ls = __fadd_rn(__fsub_rn(h, hs), l);
       const float sc = ldexpf(1.0f, rexp + col_exp[b] - 14);

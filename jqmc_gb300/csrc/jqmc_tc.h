@@ -25,13 +25,16 @@ __host__ __device__ inline int canon_offset(int row, int k) {
   return (row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
 }
 
-// The split of x (|x| < 1) into kSlices integers q_s in [-128, 128] with
-// x = 2^-7 (q_0 + 2^-8 (q_1 + 2^-8 (q_2 + ...))) up to 2^-48.
+// The split of x (|x| < 1) into kSlices slices q_s = 2^-8s k_s with integers
+// k_s in [-128, 128] and x = 2^-7 (q_0 + q_1 + q_2 + ...) up to 2^-48.  Each
+// slice is exact in bf16 (8 significant bits, the exponent carries 2^-8s), so
+// a product of slices s and t carries its level's scale 2^-8(s+t) and the
+// levels merged into one accumulator add up correctly.
 __host__ __device__ inline void split8(double x, float* q) {
   double y = x * 128.0;
   for (int s = 0; s < kSlices; ++s) {
     const double r = rint(y);
-    q[s] = (float)r;
+    q[s] = (float)ldexp(r, -8 * s);
     y = (y - r) * 256.0;
   }
 }
