@@ -15,6 +15,9 @@ jackknife (``get_aF``, :1191-1380; here ``statistics.jackknife_force``).
   R through the AO centres, J1, the Coulomb and ECP terms and the ECP quadrature
   points (R_I + |r - R_I| R Omega); the differences follow all of them, as the
   reference's automatic differentiation of E_L does.
+* LRDMC forces (jqmc_gfmc.py:1900-2000, :5980-6040, without space warp): the
+  same terms with the LRDMC local energy (``LRDMCEnergyGradientFD``), averaged
+  over the walkers with the projection weights before the branching.
 """
 
 from __future__ import annotations
@@ -62,8 +65,13 @@ class ELGradientFD:
         self.systems = [[[GpuSystem(displaced(hamiltonian, I, k, o * h), Nv=Nv) for o, _ in STENCIL] for k in range(3)]
                         for I in range(self.M)]
 
-    def __call__(self, r_up, r_dn, angles: torch.Tensor, eps_AS: float = 0.0) -> torch.Tensor:
-        """(W, natom, 3) at the configurations (W, n, 3) with the rotations (W, 3)."""
+    def _energy(self, ws: WalkerSet, *args) -> torch.Tensor:
+        angles, eps_AS = args
+        return ws.vmc_measure(angles, eps_AS)[0]
+
+    def __call__(self, r_up, r_dn, *args) -> torch.Tensor:
+        """(W, natom, 3) at the configurations (W, n, 3); args: the rotations (W, 3)
+        and the AS cutoff."""
         r_up = np.asarray(r_up)
         r_dn = np.asarray(r_dn)
         W = r_up.shape[0]
@@ -73,8 +81,22 @@ class ELGradientFD:
                 acc = torch.zeros(W, dtype=torch.float64, device=out.device)
                 for gs, (_, wgt) in zip(self.systems[I][k], STENCIL):
                     ws = WalkerSet(gs, r_up, r_dn)
-                    eL, _ = ws.vmc_measure(angles, eps_AS)
-                    acc += wgt * eL
+                    acc += wgt * self._energy(ws, *args)
                     del ws
                 out[:, I, k] = acc / self.h
         return out
+
+
+class LRDMCEnergyGradientFD(ELGradientFD):
+    """d e_L/dR of the LRDMC local energy V_diag + V_nondiag of the lattice-
+    regularised Hamiltonian (jqmc_gfmc.py:5630-5650, the function whose gradient
+    the reference's LRDMC force takes, :5842-5870) by the same five-point
+    differences; call with the configurations and the energy's draws (W, 4)."""
+
+    def __init__(self, hamiltonian, alat: float, h: float = 5e-4, Nv: int = 6):
+        super().__init__(hamiltonian, h=h, Nv=Nv)
+        self.alat = alat
+
+    def _energy(self, ws: WalkerSet, *args) -> torch.Tensor:
+        (last_draw,) = args
+        return ws.lrdmc_energy(last_draw, self.alat)[0]

@@ -29,16 +29,46 @@ import torch
 
 from .engine import GpuSystem, WalkerSet, branch_comb
 from .hamiltonians import Hamiltonian_data
-from .statistics import gfmc_G_L, jackknife_energy
+from .forces import LRDMCEnergyGradientFD, dlnpsi_dR
+from .statistics import gfmc_G_L, jackknife_energy, jackknife_force
 from ._init_config import initial_electrons
 
 
-def _check_lrdmc_options(non_local_move: str, comput_position_deriv: bool) -> None:
+def _check_lrdmc_options(non_local_move: str, comput_position_deriv: bool, use_swct: bool = False,
+                         epsilon_PW: float = 0.0, precision: str = "fp64") -> None:
     if non_local_move != "tmove":
         raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
     if comput_position_deriv:
-        raise NotImplementedError("LRDMC forces (comput_position_deriv) are not on the GPU path; "
-                                  "MCMC(comput_position_deriv=True) gives VMC forces")
+        if use_swct:
+            raise NotImplementedError("the space-warp transformation of the LRDMC forces is not on the GPU path")
+        if epsilon_PW > 0.0:
+            raise NotImplementedError("the nodal regularisation of the LRDMC forces (epsilon_PW > 0) is not on the GPU path")
+        if precision != "fp64":
+            raise ValueError("LRDMC forces are computed on FP64 walkers (precision='fp64')")
+
+
+class _ForceTerms:
+    """Per-step LRDMC force observables (jqmc_gfmc.py:1940-2000, :5980-6040): the
+    walkers' d e_L/dR, d ln psi/dR and e_L d ln psi/dR averaged with weights f
+    (w for GFMC_t, w / (V_diag - E_scf) for GFMC_n) before the branching."""
+
+    def __init__(self, hamiltonian_data, alat: float, Nv: int, h: float):
+        self.grad = LRDMCEnergyGradientFD(hamiltonian_data, alat, h=h, Nv=Nv)
+        self.HF, self.PP, self.ELPP = [], [], []
+
+    def add(self, ws: WalkerSet, f: torch.Tensor, eL: torch.Tensor, last_draw: torch.Tensor) -> None:
+        fpp = dlnpsi_dR(ws)
+        r = ws.r.cpu().numpy()
+        n = ws.sys.n_up
+        fhf = self.grad(r[:, :n], r[:, n:], last_draw)
+        fs = f.sum()
+        avg = lambda x: (torch.einsum("w,wij->ij", f, x) / fs).cpu().numpy()[None]   # noqa: E731
+        self.HF.append(avg(fhf))
+        self.PP.append(avg(fpp))
+        self.ELPP.append(avg(eL[:, None, None] * fpp))
+
+    def arrays(self, skip: int):
+        return tuple(np.asarray(x)[skip:] for x in (self.HF, self.PP, self.ELPP))
 
 
 class GFMC_n:
@@ -46,12 +76,13 @@ class GFMC_n:
                  num_gfmc_collect_steps: int = 5, mcmc_seed: int = 34467, E_scf: float = 0.0, alat: float = 0.1,
                  random_discretized_mesh: bool = True, non_local_move: str = "tmove", comput_position_deriv: bool = False,
                  epsilon_PW: float = 0.0, use_swct: bool = False, Nv: int = 6, init_r_up=None, init_r_dn=None,
-                 rebuild_after_branching: bool = True, precision: str = "fp64"):
+                 rebuild_after_branching: bool = True, precision: str = "fp64", force_fd_step: float = 5e-4):
         """The reference's GFMC_n (jqmc_gfmc.py:4222-4236) on the GPU path, with the
         same arguments in the same order, then Nv, initial electrons, the rebuild
-        switch and the precision form.  LRDMC forces (comput_position_deriv) are
-        refused; epsilon_PW and use_swct only act on them."""
-        _check_lrdmc_options(non_local_move, comput_position_deriv)
+        switch, the precision form and the finite-difference step of d e_L/dR.
+        LRDMC forces (comput_position_deriv) run on FP64 walkers without space warp
+        (use_swct) and nodal regularisation (epsilon_PW > 0), which raise."""
+        _check_lrdmc_options(non_local_move, comput_position_deriv, use_swct, epsilon_PW, precision)
         hamiltonian_data.sanity_check()
         self.hamiltonian_data = hamiltonian_data
         self.num_walkers = num_walkers
@@ -78,6 +109,8 @@ class GFMC_n:
         self._cum = torch.empty(num_walkers, dtype=torch.float64, device=dev)
         self._e_L, self._e_L2, self._w_L = [], [], []
         self.mcmc_counter = 0
+        self.comput_position_deriv = comput_position_deriv
+        self._forces = _ForceTerms(hamiltonian_data, alat, Nv, force_fd_step) if comput_position_deriv else None
 
     # ------------------------------------------------------------------ draws
     def draws(self, K: int | None = None) -> torch.Tensor:
@@ -101,6 +134,8 @@ class GFMC_n:
         last = draws[:, -1].contiguous()
         eL, vd = ws.lrdmc_energy(last, self.alat)
         f = w / (vd - self.E_scf)
+        if self._forces is not None:   # at the configurations before the branching (jqmc_gfmc.py:5842-6040)
+            self._forces.add(ws, f, eL, last)
         sums = torch.stack([w.sum(), f.sum(), (f * eL).sum(), (f * eL * eL).sum()])
         branch_comb(w, zeta, self._chosen, self._cum)
         self._spare.gather_from(ws, self._chosen)
@@ -144,6 +179,19 @@ class GFMC_n:
         e, e2, w = self.e_L[num_mcmc_warmup_steps:], self.e_L2[num_mcmc_warmup_steps:], self.w_L[num_mcmc_warmup_steps:]
         return jackknife_energy(e, e2, w, num_mcmc_bin_blocks)
 
+    def get_aF(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
+        """(force_mean, force_std), (natom, 3) in Hartree/bohr: the jackknife of
+        jqmc_gfmc.py:6694-6800 over the G_L-weighted steps."""
+        return _gfmc_forces(self, num_mcmc_warmup_steps, num_mcmc_bin_blocks)
+
+
+def _gfmc_forces(drv, warmup: int, bins: int):
+    if drv._forces is None:
+        raise ValueError("construct the driver with comput_position_deriv=True to measure forces")
+    hf, pp, elpp = drv._forces.arrays(drv.num_gfmc_collect_steps)
+    k = warmup
+    return jackknife_force(drv.w_L[k:], drv.e_L[k:], hf[k:], pp[k:], elpp[k:], bins)
+
 
 class GFMC_t:
     """LRDMC driver with fixed projection time (GFMC_t), on one GPU.
@@ -167,11 +215,12 @@ class GFMC_t:
                  mcmc_seed: int = 34467, tau: float = 0.1, alat: float = 0.1, random_discretized_mesh: bool = True,
                  non_local_move: str = "tmove", comput_position_deriv: bool = False, epsilon_PW: float = 0.0,
                  use_swct: bool = False, Nv: int = 6, init_r_up=None, init_r_dn=None, precision: str = "fp64",
-                 draws_per_call: int = 64, max_calls: int = 10000):
+                 draws_per_call: int = 64, max_calls: int = 10000, force_fd_step: float = 5e-4):
         """The reference's GFMC_t (jqmc_gfmc.py:208-221) on the GPU path, with the
         same arguments in the same order, then Nv, initial electrons, the
-        precision form and the draw batching.  LRDMC forces are refused."""
-        _check_lrdmc_options(non_local_move, comput_position_deriv)
+        precision form, the draw batching and the finite-difference step of
+        d e_L/dR.  LRDMC forces as in GFMC_n."""
+        _check_lrdmc_options(non_local_move, comput_position_deriv, use_swct, epsilon_PW, precision)
         if not tau > 0.0:
             raise ValueError("tau must be positive")
         hamiltonian_data.sanity_check()
@@ -205,6 +254,8 @@ class GFMC_t:
         self._cum = torch.empty(W, dtype=torch.float64, device=dev)
         self._e_L, self._e_L2, self._w_L, self._proj = [], [], [], []
         self.mcmc_counter = 0
+        self.comput_position_deriv = comput_position_deriv
+        self._forces = _ForceTerms(hamiltonian_data, alat, Nv, force_fd_step) if comput_position_deriv else None
 
     def draws(self, K: int) -> torch.Tensor:
         """(W, K, 5): three rotation angles U(-2pi, 2pi), xi, and the move uniform."""
@@ -237,6 +288,8 @@ class GFMC_t:
         ws.rebuild()
         ang = self.draws(1)[:, 0, :4].contiguous()   # the energy reads 4 doubles per walker
         eL, _ = ws.lrdmc_energy(ang, self.alat)
+        if self._forces is not None:   # jqmc_gfmc.py:1810-2000, weights w
+            self._forces.add(ws, w, eL, ang)
         sums = torch.stack([w.sum(), (w * eL).sum(), (w * eL * eL).sum(), total.double().mean()])
         branch_comb(w, zeta, self._chosen, self._cum)
         self._spare.gather_from(ws, self._chosen)
@@ -281,3 +334,7 @@ class GFMC_t:
     def get_E(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
         e, e2, w = self.e_L[num_mcmc_warmup_steps:], self.e_L2[num_mcmc_warmup_steps:], self.w_L[num_mcmc_warmup_steps:]
         return jackknife_energy(e, e2, w, num_mcmc_bin_blocks)
+
+    def get_aF(self, num_mcmc_warmup_steps: int = 50, num_mcmc_bin_blocks: int = 10):
+        """(force_mean, force_std), (natom, 3) in Hartree/bohr (jqmc_gfmc.py:2587-2700)."""
+        return _gfmc_forces(self, num_mcmc_warmup_steps, num_mcmc_bin_blocks)

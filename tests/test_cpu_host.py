@@ -275,7 +275,11 @@ def test_drivers_keep_the_reference_signatures_and_refuse_unsupported_options():
     with pytest.raises(NotImplementedError):
         MCMC(h, comput_position_deriv=True, use_swct=True)
     with pytest.raises(NotImplementedError):
-        GFMC_n(h, comput_position_deriv=True)
+        GFMC_n(h, comput_position_deriv=True, use_swct=True)
+    with pytest.raises(NotImplementedError):
+        GFMC_t(h, comput_position_deriv=True, epsilon_PW=0.1)
+    with pytest.raises(ValueError):
+        GFMC_n(h, comput_position_deriv=True, precision="mixed")
     with pytest.raises(NotImplementedError):
         GFMC_t(h, non_local_move="dltmove")
 
