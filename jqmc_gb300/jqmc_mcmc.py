@@ -23,7 +23,7 @@ import torch
 
 from .adjoint import dlnpsi_dparams
 from .engine import GpuSystem, WalkerSet
-from .forces import ELGradientFD, dlnpsi_dR
+from .forces import ELGradientFD, dlnpsi_dR, swct_domega, warped_dlnpsi
 from .hamiltonians import Hamiltonian_data
 from .statistics import jackknife_energy, jackknife_force
 from ._init_config import initial_electrons
@@ -33,15 +33,12 @@ class MCMC:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, mcmc_seed: int = 34467, num_walkers: int = 40,
                  num_mcmc_per_measurement: int = 16, Dt: float = 2.0, epsilon_AS: float = 1e-1,
                  comput_log_WF_param_deriv: bool = False, comput_e_L_param_deriv: bool = False,
-                 comput_position_deriv: bool = False, random_discretized_mesh: bool = True, use_swct: bool = False,
+                 comput_position_deriv: bool = False, random_discretized_mesh: bool = True, use_swct: bool = True,
                  Nv: int = 6, init_r_up=None, init_r_dn=None, force_fd_step: float = 5e-4):
         """The reference's MCMC driver (jqmc_mcmc.py:129-143) on the GPU path, with
-        the same arguments in the same order, then Nv (quadrature points), initial
-        electrons and the finite-difference step of dE_L/dR.  Differences: use_swct
-        defaults to False and True is refused with forces (the space-warp
-        transformation is not built); comput_e_L_param_deriv=True is refused."""
-        if comput_position_deriv and use_swct:
-            raise NotImplementedError("the space-warp coordinate transformation of the forces is not on the GPU path")
+        the same arguments in the same order and defaults, then Nv (quadrature
+        points), initial electrons and the finite-difference step of the force
+        terms.  comput_e_L_param_deriv=True is refused."""
         if comput_e_L_param_deriv:
             raise NotImplementedError("d e_L / d c (comput_e_L_param_deriv) is not on the GPU path")
         hamiltonian_data.sanity_check()
@@ -70,7 +67,9 @@ class MCMC:
         self.comput_position_deriv = comput_position_deriv
         self._param_grads = {}
         self._force_HF, self._force_PP, self._E_L_force_PP = [], [], []
-        self._el_grad = ELGradientFD(hamiltonian_data, h=force_fd_step, Nv=Nv) if comput_position_deriv else None
+        self.use_swct = use_swct
+        self._fd_step = force_fd_step
+        self._el_grad = ELGradientFD(hamiltonian_data, h=force_fd_step, Nv=Nv, warp=use_swct) if comput_position_deriv else None
 
     def draws(self, K: int | None = None):
         K = self.num_mcmc_per_measurement if K is None else K
@@ -107,7 +106,11 @@ class MCMC:
                 fpp = dlnpsi_dR(self.walkers)
                 r = self.walkers.r.cpu().numpy()
                 n = self.sys.n_up
-                fhf = self._el_grad(r[:, :n], r[:, n:], angles, self.epsilon_AS)
+                fhf = self._el_grad(r[:, :n], r[:, n:], angles, self.epsilon_AS)   # warped with use_swct
+                if self.use_swct:   # jqmc_mcmc.py:836-842
+                    R = torch.as_tensor(self.sys._keep["pos"], device=self.walkers.r.device)
+                    fpp = (fpp + warped_dlnpsi(self.sys, r[:, :n], r[:, n:], self._fd_step)
+                           + 0.5 * swct_domega(R, self.walkers.r))
                 self._force_HF.append(fhf.cpu().numpy())
                 self._force_PP.append(fpp.cpu().numpy())
                 self._E_L_force_PP.append((eL[:, None, None] * fpp).cpu().numpy())
