@@ -15,6 +15,14 @@ jackknife (``get_aF``, :1191-1380; here ``statistics.jackknife_force``).
   R through the AO centres, J1, the Coulomb and ECP terms and the ECP quadrature
   points (R_I + |r - R_I| R Omega); the differences follow all of them, as the
   reference's automatic differentiation of E_L does.
+* Space warp (use_swct, jqmc_mcmc.py:795-845, swct.py): with the weights
+  omega_{I i} = |r_i - R_I|^-4 / sum_J |r_i - R_J|^-4 the reference adds
+  sum_i omega_{I i} dE_L/dr_i to force_HF and sum_i omega_{I i} d ln psi/dr_i
+  + 1/2 sum_i grad_{r_i} omega_{I i} to force_PP.  The first sums are
+  directional derivatives: moving nucleus I by delta together with every
+  electron i by omega_{I i} delta gives dE_L/dR_I + sum_i omega_{I i} dE_L/dr_i,
+  so the same five-point differences give force_HF with the electrons warped
+  along; moving only the electrons gives the ln psi sum.
 * LRDMC forces (jqmc_gfmc.py:1900-2000, :5980-6040, without space warp): the
   same terms with the LRDMC local energy (``LRDMCEnergyGradientFD``), averaged
   over the walkers with the projection weights before the branching.
@@ -55,15 +63,68 @@ def displaced(hamiltonian, atom: int, axis: int, delta: float):
 STENCIL = ((2.0, -1.0 / 12.0), (1.0, 8.0 / 12.0), (-1.0, -8.0 / 12.0), (-2.0, 1.0 / 12.0))   # (offset / h, weight)
 
 
+def swct_omega(R: torch.Tensor, r: torch.Tensor) -> torch.Tensor:
+    """(W, M, Ne) space-warp weights omega_{I i} for nuclei R (M, 3) and
+    electrons r (W, Ne, 3) (jqmc/swct.py:20-60)."""
+    d = r[:, None, :, :] - R[None, :, None, :]
+    k = (d * d).sum(dim=-1) ** -2
+    return k / k.sum(dim=1, keepdim=True)
+
+
+def swct_domega(R: torch.Tensor, r: torch.Tensor) -> torch.Tensor:
+    """(W, M, 3) sum_i grad_{r_i} omega_{I i} (jqmc/swct.py:90-110), in closed form:
+    grad omega_I = omega_I (g_I - sum_J omega_J g_J), g_J = -4 (r - R_J) / |r - R_J|^2."""
+    d = r[:, None, :, :] - R[None, :, None, :]
+    d2 = (d * d).sum(dim=-1)
+    k = d2 ** -2
+    w = k / k.sum(dim=1, keepdim=True)
+    g = -4.0 * d / d2[..., None]
+    gbar = (w[..., None] * g).sum(dim=1, keepdim=True)
+    return (w[..., None] * (g - gbar)).sum(dim=2)
+
+
+def _warped(r: np.ndarray, omega_I: np.ndarray, axis: int, delta: float) -> np.ndarray:
+    """r (W, Ne, 3) with every electron moved by omega_I (W, Ne) delta along axis."""
+    out = r.copy()
+    out[:, :, axis] += delta * omega_I
+    return out
+
+
+def warped_dlnpsi(system: GpuSystem, r_up, r_dn, h: float = 5e-4) -> torch.Tensor:
+    """(W, natom, 3) sum_i omega_{I i} d ln|psi| / dr_i by five-point differences of
+    the GPU ln|psi| with the electrons moved by omega_{I i} delta (nuclei fixed)."""
+    r_up = np.asarray(r_up, dtype=np.float64)
+    r_dn = np.asarray(r_dn, dtype=np.float64)
+    n = r_up.shape[1]
+    r = np.concatenate([r_up, r_dn], axis=1)
+    R = np.asarray(system._keep["pos"], dtype=np.float64)
+    om = swct_omega(torch.as_tensor(R), torch.as_tensor(r)).numpy()
+    W, M = r.shape[0], R.shape[0]
+    out = torch.empty((W, M, 3), dtype=torch.float64, device=system.device)
+    for I in range(M):
+        for k in range(3):
+            acc = torch.zeros(W, dtype=torch.float64, device=system.device)
+            for o, wgt in STENCIL:
+                rw = _warped(r, om[:, I], k, o * h)
+                ld, _, jj = WalkerSet(system, rw[:, :n], rw[:, n:]).log_psi()
+                acc += wgt * (ld + jj)
+            out[:, I, k] = acc / h
+    return out
+
+
 class ELGradientFD:
     """dE_L/dR by five-point central differences of the GPU FP64 local energy;
-    the 12 natom displaced systems are built once and reused."""
+    the 12 natom displaced systems are built once and reused.  With ``warp`` the
+    electrons move with each displaced nucleus by omega_{I i} delta, which gives
+    dE_L/dR_I + sum_i omega_{I i} dE_L/dr_i (the space-warp force_HF)."""
 
-    def __init__(self, hamiltonian, h: float = 5e-4, Nv: int = 6):
+    def __init__(self, hamiltonian, h: float = 5e-4, Nv: int = 6, warp: bool = False, non_local_move: str = "tmove"):
         self.h = h
+        self.warp = warp
+        self.R = np.asarray(hamiltonian.structure_data.positions, dtype=np.float64).copy()
         self.M = hamiltonian.structure_data.natom
-        self.systems = [[[GpuSystem(displaced(hamiltonian, I, k, o * h), Nv=Nv) for o, _ in STENCIL] for k in range(3)]
-                        for I in range(self.M)]
+        self.systems = [[[GpuSystem(displaced(hamiltonian, I, k, o * h), Nv=Nv, non_local_move=non_local_move)
+                          for o, _ in STENCIL] for k in range(3)] for I in range(self.M)]
 
     def _energy(self, ws: WalkerSet, *args) -> torch.Tensor:
         angles, eps_AS = args
@@ -71,16 +132,22 @@ class ELGradientFD:
 
     def __call__(self, r_up, r_dn, *args) -> torch.Tensor:
         """(W, natom, 3) at the configurations (W, n, 3); args: the rotations (W, 3)
-        and the AS cutoff."""
-        r_up = np.asarray(r_up)
-        r_dn = np.asarray(r_dn)
-        W = r_up.shape[0]
+        and the AS cutoff (the LRDMC form: the energy's draws)."""
+        r_up = np.asarray(r_up, dtype=np.float64)
+        r_dn = np.asarray(r_dn, dtype=np.float64)
+        W, n = r_up.shape[0], r_up.shape[1]
+        r = np.concatenate([r_up, r_dn], axis=1)
+        om = swct_omega(torch.as_tensor(self.R), torch.as_tensor(r)).numpy() if self.warp else None
         out = torch.empty((W, self.M, 3), dtype=torch.float64, device=self.systems[0][0][0].device)
         for I in range(self.M):
             for k in range(3):
                 acc = torch.zeros(W, dtype=torch.float64, device=out.device)
-                for gs, (_, wgt) in zip(self.systems[I][k], STENCIL):
-                    ws = WalkerSet(gs, r_up, r_dn)
+                for gs, (o, wgt) in zip(self.systems[I][k], STENCIL):
+                    if self.warp:
+                        rw = _warped(r, om[:, I], k, o * self.h)
+                        ws = WalkerSet(gs, rw[:, :n], rw[:, n:])
+                    else:
+                        ws = WalkerSet(gs, r_up, r_dn)
                     acc += wgt * self._energy(ws, *args)
                     del ws
                 out[:, I, k] = acc / self.h
@@ -93,8 +160,8 @@ class LRDMCEnergyGradientFD(ELGradientFD):
     the reference's LRDMC force takes, :5842-5870) by the same five-point
     differences; call with the configurations and the energy's draws (W, 4)."""
 
-    def __init__(self, hamiltonian, alat: float, h: float = 5e-4, Nv: int = 6):
-        super().__init__(hamiltonian, h=h, Nv=Nv)
+    def __init__(self, hamiltonian, alat: float, h: float = 5e-4, Nv: int = 6, non_local_move: str = "tmove"):
+        super().__init__(hamiltonian, h=h, Nv=Nv, non_local_move=non_local_move)
         self.alat = alat
 
     def _energy(self, ws: WalkerSet, *args) -> torch.Tensor:

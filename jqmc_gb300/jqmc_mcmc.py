@@ -31,7 +31,7 @@ import torch
 
 from .adjoint import dlnpsi_dparams
 from .engine import GpuSystem, WalkerSet
-from .forces import ELGradientFD, dlnpsi_dR
+from .forces import ELGradientFD, dlnpsi_dR, swct_domega, warped_dlnpsi
 from .hamiltonians import Hamiltonian_data
 from .statistics import jackknife_energy, jackknife_force, jackknife_generalized_force
 from .variational import apply_block_updates, get_variational_blocks, sr_direction
@@ -42,15 +42,12 @@ class MCMC:
     def __init__(self, hamiltonian_data: Hamiltonian_data = None, mcmc_seed: int = 34467, num_walkers: int = 40,
                  num_mcmc_per_measurement: int = 16, Dt: float = 2.0, epsilon_AS: float = 1e-1,
                  comput_log_WF_param_deriv: bool = False, comput_e_L_param_deriv: bool = False,
-                 comput_position_deriv: bool = False, random_discretized_mesh: bool = True, use_swct: bool = False,
+                 comput_position_deriv: bool = False, random_discretized_mesh: bool = True, use_swct: bool = True,
                  Nv: int = 6, init_r_up=None, init_r_dn=None, force_fd_step: float = 5e-4):
         """The reference's MCMC driver (jqmc_mcmc.py:129-143) on the GPU path, with
-        the same arguments in the same order, then Nv (quadrature points), initial
-        electrons and the finite-difference step of dE_L/dR.  Differences: use_swct
-        defaults to False and True is refused with forces (the space-warp
-        transformation is not built); comput_e_L_param_deriv=True is refused."""
-        if comput_position_deriv and use_swct:
-            raise NotImplementedError("the space-warp coordinate transformation of the forces is not on the GPU path")
+        the same arguments in the same order and defaults, then Nv (quadrature
+        points), initial electrons and the finite-difference step of the force
+        terms.  comput_e_L_param_deriv=True is refused."""
         if comput_e_L_param_deriv:
             raise NotImplementedError("d e_L / d c (comput_e_L_param_deriv) is not on the GPU path")
         self.num_walkers = num_walkers
@@ -62,6 +59,7 @@ class MCMC:
         self.force_fd_step = force_fd_step
         self.comput_log_WF_param_deriv = comput_log_WF_param_deriv
         self.comput_position_deriv = comput_position_deriv
+        self.use_swct = use_swct
         self._opt_lambda = True
         self._build(hamiltonian_data, init_r_up, init_r_dn, mcmc_seed)
         self.gen = torch.Generator(device=self.sys.device)
@@ -86,7 +84,7 @@ class MCMC:
         # per-measurement derivative observables (jqmc_mcmc.py:756-876)
         self._param_grads = {}
         self._force_HF, self._force_PP, self._E_L_force_PP = [], [], []
-        self._el_grad = (ELGradientFD(hamiltonian_data, h=self.force_fd_step, Nv=self.Nv)
+        self._el_grad = (ELGradientFD(hamiltonian_data, h=self.force_fd_step, Nv=self.Nv, warp=self.use_swct)
                          if self.comput_position_deriv else None)
 
     @property
@@ -141,7 +139,11 @@ class MCMC:
                 fpp = dlnpsi_dR(self.walkers)
                 r = self.walkers.r.cpu().numpy()
                 n = self.sys.n_up
-                fhf = self._el_grad(r[:, :n], r[:, n:], angles, self.epsilon_AS)
+                fhf = self._el_grad(r[:, :n], r[:, n:], angles, self.epsilon_AS)   # warped with use_swct
+                if self.use_swct:   # jqmc_mcmc.py:836-842
+                    R = torch.as_tensor(self.sys._keep["pos"], device=self.walkers.r.device)
+                    fpp = (fpp + warped_dlnpsi(self.sys, r[:, :n], r[:, n:], self.force_fd_step)
+                           + 0.5 * swct_domega(R, self.walkers.r))
                 self._force_HF.append(fhf.cpu().numpy())
                 self._force_PP.append(fpp.cpu().numpy())
                 self._E_L_force_PP.append((eL[:, None, None] * fpp).cpu().numpy())

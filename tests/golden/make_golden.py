@@ -36,6 +36,7 @@ import jqmc.hamiltonians as r_ham  # noqa: E402
 import jqmc.jastrow_factor as r_jas  # noqa: E402
 import jqmc.molecular_orbital as r_mo  # noqa: E402
 import jqmc.structure as r_st  # noqa: E402
+import jqmc.swct as r_swct  # noqa: E402
 import jqmc.wavefunction as r_wf  # noqa: E402
 
 from jqmc_gb300 import synthetic  # noqa: E402
@@ -133,6 +134,8 @@ def make(sysname: str, nwalk: int, seed: int):
     call("geminal", lambda w: r_det.compute_geminal_all_elements(gem, r_up[w], r_dn[w]))
     call("det_debug", lambda w: r_det._compute_det_geminal_all_elements_debug(gem, r_up[w], r_dn[w]))
     call("AS", lambda w: r_det.compute_AS_regularization_factor(gem, r_up[w], r_dn[w]))
+    call("swct_omega", lambda w: r_swct._evaluate_swct_omega_debug(H.structure_data, rall(w)))
+    call("swct_domega", lambda w: r_swct._evaluate_swct_domega_debug(H.structure_data, rall(w)))
     call("J1", lambda w: r_jas.compute_Jastrow_one_body(jas.jastrow_one_body_data, r_up[w], r_dn[w]))
     call("J2", lambda w: r_jas.compute_Jastrow_two_body(jas.jastrow_two_body_data, r_up[w], r_dn[w]))
     call("J3", lambda w: r_jas.compute_Jastrow_three_body(jas.jastrow_three_body_data, r_up[w], r_dn[w]))

@@ -273,8 +273,6 @@ def test_drivers_keep_the_reference_signatures_and_refuse_unsupported_options():
     with pytest.raises(NotImplementedError):
         MCMC(h, comput_e_L_param_deriv=True)
     with pytest.raises(NotImplementedError):
-        MCMC(h, comput_position_deriv=True, use_swct=True)
-    with pytest.raises(NotImplementedError):
         GFMC_n(h, comput_position_deriv=True, use_swct=True)
     with pytest.raises(NotImplementedError):
         GFMC_t(h, comput_position_deriv=True, epsilon_PW=0.1)

@@ -14,6 +14,7 @@ import pytest
 
 from jqmc_gb300 import synthetic
 from oracle.ao import ao_value, ao_vgl
+from oracle import swct
 from oracle.wf import OracleSystem, rotation_matrix
 
 RTOL = 1e-10
@@ -45,6 +46,10 @@ def test_oracle_matches_reference_functions(name, golden_dir):
         assert rel(J1 + J2 + J3, g["J"][w]) < RTOL
         Gi = np.linalg.inv(G)
         assert rel(o.as_factor(G, Gi), g["AS"][w]) < RTOL and rel(o.as_factor(G, Gi), g["AS_fast"][w]) < RTOL
+        R = synthetic.SYSTEMS[name]().hamiltonian.structure_data.positions
+        assert rel(swct.omega(R, r), g["swct_omega"][w]) < RTOL
+        # the reference's debug form of sum_i grad omega is a central difference (h = 1e-5)
+        assert rel(swct.domega(R, r), g["swct_domega"][w]) < 1e-8
         gu, gd, lu, ld = o.det_grad_lap(ru, rd, Gi)
         for k, x in enumerate((gu, gd, lu, ld)):
             assert rel(x, g[f"det_grad_lap.{k}"][w]) < RTOL
@@ -100,6 +105,20 @@ def test_as_factor_matches_reference(name, golden_dir):
     Gi = np.linalg.inv(G)
     got = as_factor(torch.as_tensor(G), torch.as_tensor(Gi)).numpy()
     assert rel(got, g["AS"]) < RTOL
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_swct_weights_match_reference(name, golden_dir):
+    """The space-warp weights and their electron gradients of the force estimator
+    (torch, evaluated here on CPU tensors) against the reference's."""
+    import torch
+
+    from jqmc_gb300.forces import swct_domega, swct_omega
+    g = np.load(os.path.join(golden_dir, f"{name}.npz"))
+    R = torch.as_tensor(synthetic.SYSTEMS[name]().hamiltonian.structure_data.positions)
+    r = torch.as_tensor(np.concatenate([g["r_up"], g["r_dn"]], axis=1))
+    assert rel(swct_omega(R, r).numpy(), g["swct_omega"]) < RTOL
+    assert rel(swct_domega(R, r).numpy(), g["swct_domega"]) < 1e-8
 
 
 @pytest.mark.parametrize("name", ["water_like", "ring12"])
