@@ -75,7 +75,16 @@ typedef struct {
   const double* mesh_points;     /* nv*3 unit vectors                        */
   const double* mesh_weights;    /* nv                                       */
   double ion_ion;                /* constant ion-ion Coulomb energy          */
+  int32_t nonlocal_move;         /* LRDMC non-local ECP moves (jqmc_gfmc.py:4941-5017):
+                                  * JQMC_NONLOCAL_TMOVE or JQMC_NONLOCAL_DLTMOVE */
 } jqmc_system_desc;
+
+/* Non-local ECP moves of the LRDMC projections and energies.  T-move: the
+ * element V = w_q V_l P_l psi(r')/psi(r); dltmove (determinant locality):
+ * V_det with the determinant ratio alone, SP part max(V_det, 0), move weight
+ * min(V_det, 0) times the Jastrow ratio.  The VMC energy always uses psi. */
+#define JQMC_NONLOCAL_TMOVE 0
+#define JQMC_NONLOCAL_DLTMOVE 1
 
 /* Walker-table precision. */
 #define JQMC_PREC_FP64 0      /* every table and every operation in double       */

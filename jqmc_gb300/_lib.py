@@ -38,7 +38,7 @@ class SystemDesc(C.Structure):
         ("has_j3", i32), ("j3", BasisDesc), ("j3_matrix", pf64),
         ("ecp_flag", i32), ("ecp_maxl1", pi32), ("ecp_chan", pi32), ("ecp_nterm", i32), ("ecp_terms", pf64),
         ("nv", i32), ("mesh_points", pf64), ("mesh_weights", pf64),
-        ("ion_ion", f64),
+        ("ion_ion", f64), ("nonlocal_move", i32),
     ]
 
 
@@ -49,6 +49,7 @@ class Walkers(C.Structure):
 
 
 PREC_FP64, PREC_MIXED, PREC_MIXED_FASTE = 0, 1, 2
+NONLOCAL_MOVES = {"tmove": 0, "dltmove": 1}   # JQMC_NONLOCAL_TMOVE, JQMC_NONLOCAL_DLTMOVE
 FAST_ENERGY_CANCEL = 10.0   # JQMC_FAST_ENERGY_CANCEL: cancellation factor above which a block energy is recomputed in FP64
 
 

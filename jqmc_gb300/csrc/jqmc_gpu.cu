@@ -211,6 +211,7 @@ struct Sys {
   const double* mesh_pts;
   const double* mesh_w;
   double ion_ion;
+  int dlt;   // LRDMC non-local moves: 0 T-move, 1 determinant locality (dltmove)
 };
 
 template <class T>
@@ -1525,7 +1526,8 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 // caches t.dA / t.dE; otherwise from the positions in double.
 template <int P, class R, class Tab, class Acc>
 __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz,
-                             typename AccTraits<Acc>::out* ratio, float* mag = nullptr, const float* sl = nullptr) {
+                             typename AccTraits<Acc>::out* ratio, float* mag = nullptr, const float* sl = nullptr,
+                             bool dlt = false, unsigned vneg = 0u) {
   using Out = typename AccTraits<Acc>::out;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
@@ -1637,6 +1639,10 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     const Out jsum = acc_out(dj[p]);
     const Out jf = Num<Out>::ex(jsum - c3);
     ratio[p] = dsum * jf;
+    if (dlt) {   // determinant locality: the Jastrow factor only where w_p det'/det < 0 (bit p of vneg: w_p < 0)
+      const bool neg = ((vneg >> p) & 1u) ? (dsum > Out(0)) : (dsum < Out(0));
+      if (!neg) ratio[p] = dsum;
+    }
     if constexpr (AccTraits<Acc>::accurate) {
       if (mag) mag[p] = acc_mag_out(det[p]) * (float)jf;   // sum |phi_a T_a| on the ratio's scale
     }
@@ -1754,6 +1760,23 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
       }
       Out ratio[P];
       float mag[P];
+      // determinant locality (jqmc_gfmc.py:4980-5017): an ECP element's sign and
+      // its positive (SP) value come from the determinant ratio alone, so the
+      // ratio routine needs the sign of each point's weight (bit p of vneg)
+      const bool dlt = kinetic && s.dlt && c >= nkc;
+      unsigned vneg = 0u;
+      if (dlt) {
+        bool neg = false;
+        if (lane < np) {
+          const Out cto = (Out)ct;
+          const double* vl = k.ec + (size_t)e * kEC + EC_VL;
+          const Out wv = (Out)s.mesh_w[v0 + lane];
+          Out vw = Out(0);
+          for (int l = 0; l < s.ecp_maxl1[atom]; ++l) vw += (Out)vl[l] * (Out(2 * l + 1) * legendre_t<Out>(l, cto) * wv);
+          neg = vw < Out(0);
+        }
+        vneg = __ballot_sync(0xffffffffu, neg);
+      }
       if constexpr (kErr) {
         float sl[3 * P];
 #pragma unroll
@@ -1762,9 +1785,9 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
           sl[P + p] = __shfl_sync(0xffffffffu, myl, p);
           sl[2 * P + p] = __shfl_sync(0xffffffffu, mzl, p);
         }
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg);
       } else {
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg);
       }
       if (lane < np) {
         Out rr = Out(0);
@@ -1784,6 +1807,9 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
           const Out cto = (Out)ct;
           Out vw = Out(0);   // the element's weight: V = vw * ratio
           for (int l = 0; l < lmax; ++l) vw += (Out)vl[l] * (Out(2 * l + 1) * legendre_t<Out>(l, cto) * wv);
+          // T-move: V = vw psi'/psi.  dltmove: rr is det'/det where V_det = vw det'/det
+          // >= 0 and psi'/psi (the Jastrow factor, > 0, keeps the sign) elsewhere,
+          // so min(V, 0) and max(V, 0) are the FN move weight and the SP part
           t.V[e * nv + v] = (double)(vw * rr);
           if (kErr) cancel.add(fabsf((float)vw), mg, (float)(vw * rr));
         }
@@ -3435,6 +3461,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   if (d->has_j1 && !d->j1_zeff) return JQMC_E_ARG;
   if (d->ecp_flag && (!d->ecp_maxl1 || !d->ecp_chan || !d->ecp_terms || !d->mesh_points || !d->mesh_weights)) return JQMC_E_ARG;
   if (d->ecp_flag && !(d->nv == 4 || d->nv == 6 || d->nv == 12 || d->nv == 18)) return JQMC_E_ARG;
+  if (d->nonlocal_move != JQMC_NONLOCAL_TMOVE && d->nonlocal_move != JQMC_NONLOCAL_DLTMOVE) return JQMC_E_ARG;
   auto check_basis = [M](const jqmc_basis_desc& b) {
     int prev_atom = -1;
     for (int s = 0; s < b.nshell; ++s) {
@@ -3585,6 +3612,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   s.ecp_nterm = d->ecp_flag ? d->ecp_nterm : 0; s.ecp_terms = dp(o_terms);
   s.nv = nv; s.mesh_pts = dp(o_mp); s.mesh_w = dp(o_mw);
   s.ion_ion = d->ion_ion;
+  s.dlt = d->nonlocal_move == JQMC_NONLOCAL_DLTMOVE;
   sys->blob = blob;
   if (A <= jqmc_tc::kMaxK) {
     // operand B of the tensor-core lambda-GEMM: column b of L = lambda (spin up:

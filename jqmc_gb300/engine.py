@@ -64,7 +64,7 @@ def _ion_ion(pos, z):
     return e
 
 
-def system_desc(ham: Hamiltonian_data, Nv: int = 6):
+def system_desc(ham: Hamiltonian_data, Nv: int = 6, non_local_move: str = "tmove"):
     """(jqmc_system_desc, arrays it points into, sizes) for one Hamiltonian_data
     (jqmc/hamiltonians.py:83); the arrays must outlive the descriptor."""
     ham.sanity_check()
@@ -131,19 +131,23 @@ def system_desc(ham: Hamiltonian_data, Nv: int = 6):
         d.mesh_points = _ptr(keep["mp"], C.c_double)
         d.mesh_weights = _ptr(keep["mw"], C.c_double)
     d.ion_ion = _ion_ion(keep["pos"], keep["zeff"])
+    if non_local_move not in _lib.NONLOCAL_MOVES:
+        raise NotImplementedError(f"non_local_move={non_local_move!r}: 'tmove' or 'dltmove'")
+    d.nonlocal_move = _lib.NONLOCAL_MOVES[non_local_move]
     return d, keep, {"n_up": n_up, "n_dn": n_dn, "A": A, "A3": A3}
 
 
 class GpuSystem:
     """Device copy of one Hamiltonian_data (jqmc/hamiltonians.py:83) for the walker kernels."""
 
-    def __init__(self, ham: Hamiltonian_data, Nv: int = 6, device: int | None = None):
+    def __init__(self, ham: Hamiltonian_data, Nv: int = 6, device: int | None = None, non_local_move: str = "tmove"):
         if not torch.cuda.is_available():
             raise _lib.JqmcError("no CUDA device: the walker path runs only on the GPU")
         self.ham = ham
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         L = _lib.lib()
-        d, keep, info = system_desc(ham, Nv)
+        d, keep, info = system_desc(ham, Nv, non_local_move)
+        self.non_local_move = non_local_move
         self.n_up, self.n_dn = info["n_up"], info["n_dn"]
         self.N = self.n_up + self.n_dn
         self.A, self.A3 = info["A"], info["A3"]

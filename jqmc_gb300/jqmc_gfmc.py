@@ -36,8 +36,8 @@ from ._init_config import initial_electrons
 
 def _check_lrdmc_options(non_local_move: str, comput_position_deriv: bool, use_swct: bool = False,
                          epsilon_PW: float = 0.0, precision: str = "fp64") -> None:
-    if non_local_move != "tmove":
-        raise NotImplementedError(f"non_local_move={non_local_move!r}: only 'tmove' is on the GPU path")
+    if non_local_move not in ("tmove", "dltmove"):
+        raise NotImplementedError(f"non_local_move={non_local_move!r}: 'tmove' or 'dltmove'")
     if comput_position_deriv:
         if use_swct:
             raise NotImplementedError("the space-warp transformation of the LRDMC forces is not on the GPU path")
@@ -92,7 +92,7 @@ class GFMC_n:
         self.random_discretized_mesh = random_discretized_mesh
         self.num_gfmc_collect_steps = num_gfmc_collect_steps
         self.rebuild_after_branching = rebuild_after_branching
-        self.sys = GpuSystem(hamiltonian_data, Nv=Nv)
+        self.sys = GpuSystem(hamiltonian_data, Nv=Nv, non_local_move=non_local_move)
         if init_r_up is None:
             st = hamiltonian_data.structure_data
             coul = hamiltonian_data.coulomb_potential_data
@@ -232,7 +232,7 @@ class GFMC_t:
         self.random_discretized_mesh = random_discretized_mesh
         self.draws_per_call = draws_per_call
         self.max_calls = max_calls
-        self.sys = GpuSystem(hamiltonian_data, Nv=Nv)
+        self.sys = GpuSystem(hamiltonian_data, Nv=Nv, non_local_move=non_local_move)
         if init_r_up is None:
             st = hamiltonian_data.structure_data
             coul = hamiltonian_data.coulomb_potential_data

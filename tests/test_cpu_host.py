@@ -279,7 +279,7 @@ def test_drivers_keep_the_reference_signatures_and_refuse_unsupported_options():
     with pytest.raises(ValueError):
         GFMC_n(h, comput_position_deriv=True, precision="mixed")
     with pytest.raises(NotImplementedError):
-        GFMC_t(h, non_local_move="dltmove")
+        GFMC_t(h, non_local_move="dla")
 
 
 def test_module_functions_keep_the_reference_names_and_need_a_gpu():
@@ -479,3 +479,32 @@ def test_rank1_row_column_and_ratio_algebra(golden_dir, monkeypatch):
     u2 = np.stack([ru + 0.1])
     with pytest.raises(ValueError):
         D._compute_ratio_determinant_part_rank1_update(gem, np.linalg.inv(G), ru, rd, u2, rd[None])
+
+
+def test_nonlocal_move_option():
+    """non_local_move reaches the system descriptor (T-move 0, dltmove 1); the
+    library refuses any other code before touching the device, and the drivers
+    accept both names."""
+    import ctypes as C
+
+    from jqmc_gb300 import _lib, synthetic
+    from jqmc_gb300.build import build
+    from jqmc_gb300.engine import system_desc
+    from jqmc_gb300.jqmc_gfmc import _check_lrdmc_options
+    build()
+    L = _lib.lib()
+    ham = synthetic.SYSTEMS["water_like"]().hamiltonian
+    for name, code in (("tmove", 0), ("dltmove", 1)):
+        d, keep, _ = system_desc(ham, 6, name)
+        assert d.nonlocal_move == code
+        h = C.c_void_p()
+        assert L.jqmc_system_create(C.byref(d), C.byref(h)) in (0, -3)
+        _check_lrdmc_options(name, False)
+    d, keep, _ = system_desc(ham)
+    d.nonlocal_move = 2
+    h = C.c_void_p()
+    assert L.jqmc_system_create(C.byref(d), C.byref(h)) == -1
+    with pytest.raises(NotImplementedError):
+        system_desc(ham, 6, "dla")
+    with pytest.raises(NotImplementedError):
+        _check_lrdmc_options("dla", False)
