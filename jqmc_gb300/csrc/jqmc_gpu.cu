@@ -381,6 +381,39 @@ __device__ __forceinline__ void emit_vgl(R dx, R dy, R dz, R r2, R rad, R radZ, 
   }
 }
 
+// Cartesian shells (shell field 7 = 1) hold one AO, x^nx y^ny z^nz times the
+// contracted Gaussian: component sh[6] of the (l+1)(l+2)/2 in TREXIO order
+// (nx from l down, then ny from l - nx down; itertools.combinations_with_replacement).
+__device__ __forceinline__ void cart_powers(int l, int j, int& nx, int& ny, int& nz) {
+  nx = l;
+  while (nx > 0 && j >= l - nx + 1) {
+    j -= l - nx + 1;
+    --nx;
+  }
+  ny = l - nx - j;
+  nz = j;
+}
+
+// P = x^nx y^ny z^nz, its gradient G and Laplacian (not zero: P is not harmonic)
+template <class R>
+__device__ __forceinline__ R cart_mono(R x, R y, R z, int nx, int ny, int nz) {
+  return jq_pow(x, nx) * jq_pow(y, ny) * jq_pow(z, nz);
+}
+
+template <class R>
+__device__ __forceinline__ void cart_mono_gl(R x, R y, R z, int nx, int ny, int nz, R& P, R* G, R& lap) {
+  const R px = jq_pow(x, nx), py = jq_pow(y, ny), pz = jq_pow(z, nz);
+  const R d1x = nx > 0 ? R(nx) * jq_pow(x, nx - 1) : R(0), d1y = ny > 0 ? R(ny) * jq_pow(y, ny - 1) : R(0);
+  const R d1z = nz > 0 ? R(nz) * jq_pow(z, nz - 1) : R(0);
+  const R d2x = nx > 1 ? R(nx * (nx - 1)) * jq_pow(x, nx - 2) : R(0), d2y = ny > 1 ? R(ny * (ny - 1)) * jq_pow(y, ny - 2) : R(0);
+  const R d2z = nz > 1 ? R(nz * (nz - 1)) * jq_pow(z, nz - 2) : R(0);
+  P = px * py * pz;
+  G[0] = d1x * py * pz;
+  G[1] = px * d1y * pz;
+  G[2] = px * py * d1z;
+  lap = d2x * py * pz + px * d2y * pz + px * py * d2z;
+}
+
 // d = p - R_atom in double (no cancellation), then rounded to R
 template <class R>
 __device__ __forceinline__ void disp(const double* apos, int atom, double px, double py, double pz, R& dx, R& dy, R& dz) {
@@ -397,6 +430,12 @@ __device__ __forceinline__ void shell_val_d(const Basis& b, int s, R dx, R dy, R
   const R* pr = prims_of<R>(b) + 2 * p0;
   R rad = R(0);
   for (int p = 0; p < np; ++p) rad += pr[2 * p + 1] * Num<R>::ex(-pr[2 * p] * r2);
+  if (sh[7]) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6], nx, ny, nz);
+    f(ao0, rad * cart_mono(dx, dy, dz, nx, ny, nz));
+    return;
+  }
   switch (l) {
     case 0: emit_val<0, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
     case 1: emit_val<1, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
@@ -421,6 +460,16 @@ __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R
     rad += e;
     radZ += Z * e;
     radZ2 += Z * Z * e;
+  }
+  if (sh[7]) {   // grad = rad grad P - 2 radZ P d; lap = P (4 r^2 radZ2 - (4l+6) radZ) + rad lap P (d . grad P = l P)
+    int nx, ny, nz;
+    cart_powers(l, sh[6], nx, ny, nz);
+    R P, G[3], lp;
+    cart_mono_gl(dx, dy, dz, nx, ny, nz, P, G, lp);
+    const R t = R(-2) * radZ * P;
+    f(ao0, rad * P, rad * G[0] + t * dx, rad * G[1] + t * dy, rad * G[2] + t * dz,
+      P * (R(4) * r2 * radZ2 - (R(4 * l) + R(6)) * radZ) + rad * lp);
+    return;
   }
   switch (l) {
     case 0: emit_vgl<0, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
@@ -478,6 +527,18 @@ __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx
 #pragma unroll
     for (int p = 0; p < P; ++p) rad[p] += c * MeshExp<R, AccTraits<Acc>::accurate>::ex(-Z * r2[p]);
   }
+  if (sh[7]) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6], nx, ny, nz);
+    const R vv = (R)v[ao0];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const R t = cart_mono(dx[p], dy[p], dz[p], nx, ny, nz) * vv;
+      acc_fma(acc[p], rad[p], t);
+      if constexpr (AccTraits<Acc>::accurate) acc_mag(acc[p], fabs(rad[p]) * fabs(t));
+    }
+    return;
+  }
   switch (l) {
     case 0: emit_dot_pts<0, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
     case 1: emit_dot_pts<1, P, R, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
@@ -505,6 +566,18 @@ __device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const fl
     const float Z = pr[2 * q], c = pr[2 * q + 1];
 #pragma unroll
     for (int p = 0; p < P; ++p) rad[p] += c * expf(-Z * r2h[p]) * (1.f - Z * r2l[p]);
+  }
+  if (sh[7]) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6], nx, ny, nz);
+    const float vv = (float)v[ao0];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const float t = cart_mono(dx[p], dy[p], dz[p], nx, ny, nz) * vv;
+      acc_fma(acc[p], rad[p], t);
+      if constexpr (AccTraits<Acc>::accurate) acc_mag(acc[p], fabs(rad[p]) * fabs(t));
+    }
+    return;
   }
   switch (l) {
     case 0: emit_dot_pts<0, P, float, V, Acc>(dx, dy, dz, rad, ao0, jlo, nm, v, acc); break;
@@ -3174,7 +3247,12 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       if (sh[0] < 0 || sh[0] >= M || sh[0] < prev_atom) return false;  // shells grouped by nucleus
       prev_atom = sh[0];
       if (sh[1] < 0 || sh[1] > JQMC_LMAX || sh[2] <= 0 || sh[3] < 0 || sh[3] + sh[2] > b.nprim) return false;
-      if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) return false;
+      if (sh[7] != 0 && sh[7] != 1) return false;
+      if (sh[7] == 1) {   // Cartesian: one AO, component index below (l+1)(l+2)/2
+        if (sh[5] != 1 || sh[6] < 0 || sh[6] >= (sh[1] + 1) * (sh[1] + 2) / 2 || sh[4] < 0 || sh[4] >= b.nao) return false;
+      } else if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) {
+        return false;
+      }
     }
     return true;
   };
