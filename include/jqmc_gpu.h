@@ -42,10 +42,15 @@ extern "C" {
 typedef struct jqmc_system jqmc_system; /* opaque: device copy of the tables */
 
 /* One contracted-GTO basis.  shells: nshell rows of 8 int32
- *   {atom, l, nprim, prim0, ao0, nm, mfirst, 0}
- * (AO ao0+k of the shell carries m = mfirst+k, k < nm; 1 <= nm <= 2l+1);
- * prims: nprim rows of {Z, c*N_p*sqrt((2l+1)/4pi)} with N_p the primitive
- * normalisation of jqmc/atomic_orbital.py:2316-2323. */
+ *   {atom, l, nprim, prim0, ao0, nm, mfirst, kind}
+ * kind 0, spherical: AO ao0+k of the shell carries m = mfirst+k, k < nm,
+ * 1 <= nm <= 2l+1; prims: nprim rows of {Z, c*N_p*sqrt((2l+1)/4pi)} with N_p the
+ * primitive normalisation of jqmc/atomic_orbital.py:2316-2323.
+ * kind 1, Cartesian (jqmc/atomic_orbital.py:1984-2290): one AO (nm = 1),
+ * x^nx y^ny z^nz with (nx, ny, nz) component mfirst of the shell's
+ * (l+1)(l+2)/2 in TREXIO order; prims {Z, c*N_cart} with
+ * N_cart = sqrt((2Z/pi)^(3/2) (8Z)^l nx!ny!nz!/((2nx)!(2ny)!(2nz)!)).
+ * Shells are grouped by nucleus (atom non-decreasing). */
 typedef struct {
   int32_t nshell, nao, nprim;
   const int32_t* shells;
@@ -152,8 +157,8 @@ int jqmc_system_destroy(jqmc_system* sys);
 
 /* 1 when the mixed form's table rebuild (jqmc_walker_init, jqmc_lu_rebuild_refine)
  * forms M = Phi lambda on the tensor cores (tcgen05, split-bf16 operands with
- * exact FP32 sums, about 1e-14 relative) -- systems with at most 1024 geminal
- * AOs -- and 0 when it uses the float-float CUDA-core kernel.  The tensor-core
+ * exact FP32 sums, about 1e-12 of sum |Phi| |lambda|) -- systems with at most
+ * 768 geminal AOs -- and 0 when it uses the float-float CUDA-core kernel.  The tensor-core
  * path keeps an operand workspace with the system (about 12 bytes per
  * electron-row x AO for up to 65536 rows, allocated on the first rebuild); a
  * rebuild that would have to allocate it inside a stream capture uses the

@@ -387,6 +387,42 @@ __device__ __forceinline__ void emit_vgl(R dx, R dy, R dz, R r2, R rad, R radZ, 
   }
 }
 
+// Cartesian shells hold one AO, x^nx y^ny z^nz times the contracted Gaussian:
+// component sh[6] - kCartBase of the (l+1)(l+2)/2 in TREXIO order (nx from l
+// down, then ny from l - nx down; itertools.combinations_with_replacement).  The
+// device shell rows carry the Cartesian kind in field 6 (component + kCartBase,
+// outside the spherical m range): field 7 holds the (l, nprim) sort order.
+constexpr int kCartBase = 1000;
+__device__ __forceinline__ void cart_powers(int l, int j, int& nx, int& ny, int& nz) {
+  nx = l;
+  while (nx > 0 && j >= l - nx + 1) {
+    j -= l - nx + 1;
+    --nx;
+  }
+  ny = l - nx - j;
+  nz = j;
+}
+
+// P = x^nx y^ny z^nz, its gradient G and Laplacian (not zero: P is not harmonic)
+template <class R>
+__device__ __forceinline__ R cart_mono(R x, R y, R z, int nx, int ny, int nz) {
+  return jq_pow(x, nx) * jq_pow(y, ny) * jq_pow(z, nz);
+}
+
+template <class R>
+__device__ __forceinline__ void cart_mono_gl(R x, R y, R z, int nx, int ny, int nz, R& P, R* G, R& lap) {
+  const R px = jq_pow(x, nx), py = jq_pow(y, ny), pz = jq_pow(z, nz);
+  const R d1x = nx > 0 ? R(nx) * jq_pow(x, nx - 1) : R(0), d1y = ny > 0 ? R(ny) * jq_pow(y, ny - 1) : R(0);
+  const R d1z = nz > 0 ? R(nz) * jq_pow(z, nz - 1) : R(0);
+  const R d2x = nx > 1 ? R(nx * (nx - 1)) * jq_pow(x, nx - 2) : R(0), d2y = ny > 1 ? R(ny * (ny - 1)) * jq_pow(y, ny - 2) : R(0);
+  const R d2z = nz > 1 ? R(nz * (nz - 1)) * jq_pow(z, nz - 2) : R(0);
+  P = px * py * pz;
+  G[0] = d1x * py * pz;
+  G[1] = px * d1y * pz;
+  G[2] = px * py * d1z;
+  lap = d2x * py * pz + px * d2y * pz + px * py * d2z;
+}
+
 // d = p - R_atom in double (no cancellation), then rounded to R
 template <class R>
 __device__ __forceinline__ void disp(const double* apos, int atom, double px, double py, double pz, R& dx, R& dy, R& dz) {
@@ -403,6 +439,12 @@ __device__ __forceinline__ void shell_val_d(const Basis& b, int s, R dx, R dy, R
   const R* pr = prims_of<R>(b) + 2 * p0;
   R rad = R(0);
   for (int p = 0; p < np; ++p) rad += pr[2 * p + 1] * Num<R>::ex(-pr[2 * p] * r2);
+  if (sh[6] >= kCartBase) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6] - kCartBase, nx, ny, nz);
+    f(ao0, rad * cart_mono(dx, dy, dz, nx, ny, nz));
+    return;
+  }
   switch (l) {
     case 0: emit_val<0, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
     case 1: emit_val<1, R>(dx, dy, dz, rad, ao0, jlo, nm, f); break;
@@ -427,6 +469,16 @@ __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R
     rad += e;
     radZ += Z * e;
     radZ2 += Z * Z * e;
+  }
+  if (sh[6] >= kCartBase) {   // grad = rad grad P - 2 radZ P d; lap = P (4 r^2 radZ2 - (4l+6) radZ) + rad lap P (d . grad P = l P)
+    int nx, ny, nz;
+    cart_powers(l, sh[6] - kCartBase, nx, ny, nz);
+    R P, G[3], lp;
+    cart_mono_gl(dx, dy, dz, nx, ny, nz, P, G, lp);
+    const R t = R(-2) * radZ * P;
+    f(ao0, rad * P, rad * G[0] + t * dx, rad * G[1] + t * dy, rad * G[2] + t * dz,
+      P * (R(4) * r2 * radZ2 - (R(4 * l) + R(6)) * radZ) + rad * lp);
+    return;
   }
   switch (l) {
     case 0: emit_vgl<0, R>(dx, dy, dz, r2, rad, radZ, radZ2, ao0, jlo, nm, f); break;
@@ -495,6 +547,18 @@ __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx
 #pragma unroll
     for (int p = 0; p < P; ++p) rad[p] += c * MeshExp<R, AccTraits<Acc>::accurate>::ex(-Z * r2[p]);
   }
+  if (sh[6] >= kCartBase) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6] - kCartBase, nx, ny, nz);
+    const R vv = (R)v[ao0];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const R t = cart_mono(dx[p], dy[p], dz[p], nx, ny, nz) * vv;
+      acc_fma(acc[p], rad[p], t);
+      if constexpr (AccTraits<Acc>::accurate) acc_mag(acc[p], fabs(rad[p]) * fabs(t));
+    }
+    return;
+  }
   switch (l) {
     case 0: emit_dot_pts<0, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
     case 1: emit_dot_pts<1, P, R, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
@@ -523,6 +587,18 @@ __device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const fl
     const float Z = pr[2 * q], c = pr[2 * q + 1];
 #pragma unroll
     for (int p = 0; p < P; ++p) rad[p] += c * expf(-Z * r2h[p]) * (1.f - Z * r2l[p]);
+  }
+  if (sh[6] >= kCartBase) {
+    int nx, ny, nz;
+    cart_powers(l, sh[6] - kCartBase, nx, ny, nz);
+    const float vv = (float)v[ao0];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const float t = cart_mono(dx[p], dy[p], dz[p], nx, ny, nz) * vv;
+      acc_fma(acc[p], rad[p], t);
+      if constexpr (AccTraits<Acc>::accurate) acc_mag(acc[p], fabs(rad[p]) * fabs(t));
+    }
+    return;
   }
   switch (l) {
     case 0: emit_dot_pts<0, P, float, V, Acc, LO>(dx, dy, dz, rad, ao0, jlo, nm, v, acc, vlo); break;
@@ -1820,21 +1896,30 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
   return cancel;
 }
 
-// Block energy of the mixed form: the lattice elements of an electron enter
-// E_L only through the fixed-node diagonal when one of its six moves crosses a
-// node of psi (ratio <= 0, jqmc_gfmc.py:5421-5500); elsewhere they cancel between
-// the diagonal and the non-diagonal sums.  The electrons with a lattice ratio
-// below kFlipMargin (crossing, or close enough that float rounding could decide
-// the sign) get their six ratios again in FP64 arithmetic on the FP64-accurate
+// Block energy of the mixed form: the lattice elements x_k of an electron cancel
+// between the diagonal and the non-diagonal sums of E_L unless one of its six
+// moves crosses a node of psi (x_k >= 0, jqmc_gfmc.py:5421-5500) and the
+// fixed-node diagonal takes eu over zv = e_ion + T_e - sum_k (x_k + 1/(4a^2)).
+// Only then do the float ratios reach E_L, so those electrons (a ratio below
+// kFlipMargin, i.e. crossing or close enough that float rounding could decide
+// the sign, and eu above zv - kFlipEnergyMargin Ha with zv from the float
+// elements) get their six ratios again in FP64 arithmetic on the FP64-accurate
 // tables, one warp per electron.
-constexpr double kFlipMargin = 0.05;
+constexpr double kFlipMargin = 1e-3;
+constexpr double kFlipEnergyMargin = 1e-2;
 template <class Tab>
 __device__ void refine_lattice(const Work<Tab>& k, Terms& t, double alat) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const double kin = -1.0 / (2.0 * alat * alat);
+  const Sys& s = k.s;
   for (int e = wid; e < k.N; e += nw) {
-    const bool near = lane < 6 && t.el[6 * e + lane] / kin < kFlipMargin;
+    const double x = lane < 6 ? t.el[6 * e + lane] : 0.0;
+    const bool near = lane < 6 && x / kin < kFlipMargin;
     if (!__any_sync(0xffffffffu, near)) continue;
+    const double nd = warp_sum(lane < 6 ? x + 1.0 / (4.0 * alat * alat) : 0.0);
+    const double zv = t.ei[e] + t.ke[e] - nd;
+    const double eu = s.ecp_flag ? t.ei[e] : t.eid[e];
+    if (!(eu > zv - kFlipEnergyMargin)) continue;   // (warp-uniform)
     for (int c = 0; c < 2; ++c) {
       double mx = 0.0, my = 0.0, mz = 0.0;
       if (lane < 3) {
@@ -3337,7 +3422,7 @@ inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
 struct jqmc_system {
   Sys s;
   void* blob;
-  // tensor-core lambda-GEMM of the mixed rebuild (jqmc_tc.cu), when A <= 1024:
+  // tensor-core lambda-GEMM of the mixed rebuild (jqmc_tc.cu), when A <= 768:
   // operand B = lambda (spin up) and lambda^T (spin down), split and laid out
   // once; operand A and the row exponents in a workspace grown on first use
   int tc_nk = 0, tc_ncol_tiles = 0;
@@ -3469,7 +3554,12 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       if (sh[0] < 0 || sh[0] >= M || sh[0] < prev_atom) return false;  // shells grouped by nucleus
       prev_atom = sh[0];
       if (sh[1] < 0 || sh[1] > JQMC_LMAX || sh[2] <= 0 || sh[3] < 0 || sh[3] + sh[2] > b.nprim) return false;
-      if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) return false;
+      if (sh[7] != 0 && sh[7] != 1) return false;
+      if (sh[7] == 1) {   // Cartesian: one AO, component index below (l+1)(l+2)/2
+        if (sh[5] != 1 || sh[6] < 0 || sh[6] >= (sh[1] + 1) * (sh[1] + 2) / 2 || sh[4] < 0 || sh[4] >= b.nao) return false;
+      } else if (sh[5] <= 0 || sh[6] < -sh[1] || sh[6] + sh[5] - 1 > sh[1] || sh[4] < 0 || sh[4] + sh[5] > b.nao) {
+        return false;
+      }
     }
     return true;
   };
@@ -3545,7 +3635,10 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       const int lx = rows[8 * x + 1], ly = rows[8 * y + 1];
       return lx != ly ? lx < ly : rows[8 * x + 2] < rows[8 * y + 2];
     });
-    for (int k = 0; k < b.nshell; ++k) rows[8 * k + 7] = ord[k];
+    for (int k = 0; k < b.nshell; ++k) {
+      if (rows[8 * k + 7] == 1) rows[8 * k + 6] += kCartBase;   // the Cartesian kind moves to field 6
+      rows[8 * k + 7] = ord[k];
+    }
     return rows;
   };
   const std::vector<int32_t> dsh_rows = with_order(d->det);
@@ -3769,7 +3862,7 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
   const int smem = IL.bytes;
   if (is_mixed(w->precision)) {
     // M_up, M_dn into the scratch: by the split-bf16 tensor-core GEMM when the
-    // system has its operand (A <= 1024), else by the float-float CUDA-core
+    // system has its operand (A <= 768), else by the float-float CUDA-core
     // kernel; then the rest in FP64
     int rc = sys->tc_b ? tc_rebuild_m(sys, w, P, stream) : kTcUnavailable;
     if (rc < 0) return rc;

@@ -11,10 +11,12 @@
 // products of slice pairs (s, t) with s + t <= 5 (slice s stored as its integer
 // times 2^-8s, so a product carries the scale of its level) are accumulated per
 // level d = s + t in tensor memory (TMEM):
-//   level 0           one accumulator over all of K (K <= 1024)
+//   level 0           one accumulator over all of K (K <= 768)
 //   level 1 (2 pairs) one accumulator per 512 of K
 //   level 2 (3 pairs) one accumulator per 256 of K
-//   levels 3..5       one accumulator (its FP32 rounding is 2^-48 of the total)
+//   level 3 (4 pairs) one accumulator; levels 4, 5 one more (the accumulators
+//                     round toward zero once a sum passes 2^24: about 2^-40 of
+//                     the total for level 3, far less for 4 and 5)
 // so eight 128 x 64 FP32 accumulators fill the 512 TMEM columns of the SM.  The
 // epilogue reads them back with tcgen05.ld, adds the levels as float-float pairs
 // and scales by the row and column exponents.
@@ -155,6 +157,7 @@ __device__ __forceinline__ int acc_of(int d, int c) {
   if (d == 0) return 0;
   if (d == 1) return 1 + (c >= 16 ? 1 : 0);
   if (d == 2) return 3 + (c >> 3);
+  if (d == 3) return 6;
   return 7;
 }
 
@@ -303,9 +306,9 @@ int ozaki_gemm(const uint16_t* a_slices, const uint16_t* b_slices, const int* ro
     if (cudaFuncSetAttribute(k_ozaki_m, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) != cudaSuccess) return -3;
     attr_set[dev] = true;
   }
-  unsigned used = 1u | (1u << 1) | (1u << 7);
+  unsigned used = 1u | (1u << 1) | (1u << 6) | (1u << 7);
   if (nk_chunks > 16) used |= 1u << 2;
-  for (int q = 0; q < 4; ++q)
+  for (int q = 0; q < 3; ++q)
     if (nk_chunks > 8 * q) used |= 1u << (3 + q);
   const dim3 grid(n_col_tiles, row_tiles);
   k_ozaki_m<<<grid, 128, kSmemBytes, stream>>>(reinterpret_cast<const uint8_t*>(a_slices),

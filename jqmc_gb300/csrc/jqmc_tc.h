@@ -15,7 +15,7 @@ constexpr int kASliceBytes = kBM * kKC * 2;        // one slice of an A stage (b
 constexpr int kBSliceBytes = kBN * kKC * 2;
 constexpr int kAStage = kSlices * kASliceBytes;    // 48 KiB
 constexpr int kBStage = kSlices * kBSliceBytes;    // 24 KiB
-constexpr int kMaxK = 1024;                        // exact FP32 sums need K <= 1024
+constexpr int kMaxK = 768;                         // K <= 768: level 0 and levels 1, 2 by ranges exact
 constexpr int kSmemBytes = kStages * (kAStage + kBStage) + 256;
 
 // Byte offset of element (row, k) inside one slice block of `rows` x kKC bf16 in

@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .atomic_orbital import primitive_norm
+from .atomic_orbital import cartesian_norm, cartesian_orders, primitive_norm
 from .coulomb_potential import ECP_MESHES
 from .hamiltonians import Hamiltonian_data
 
@@ -32,7 +32,7 @@ def pack_basis(aos):
     A shell is a run of consecutive AOs on one nucleus with one l, one primitive
     list and consecutive m; each primitive row holds (Z, c N_p sqrt((2l+1)/4pi))."""
     if hasattr(aos, "polynominal_order_x"):
-        raise NotImplementedError("Cartesian AOs: the walker kernels evaluate spherical AOs only")
+        return _pack_cartesian(aos)
     aos.sanity_check()
     oi = np.asarray(aos.orbital_indices, dtype=np.int64)
     ex = np.asarray(aos.exponents, dtype=np.float64)
@@ -53,6 +53,28 @@ def pack_basis(aos):
             prims.append((zz, cc * primitive_norm(l, zz)))
         shells.append((atom, l, len(z), p0, a, b - a, m, 0))
         a = b
+    return np.ascontiguousarray(np.array(shells, dtype=np.int32)), np.ascontiguousarray(np.array(prims, dtype=np.float64))
+
+
+def _pack_cartesian(aos):
+    """Shell table of an AOs_cart_data: one shell per AO, {atom, l, nprim, prim0, ao,
+    1, component, 1} with the component's index in TREXIO order and primitive
+    rows (Z, c N_cart)."""
+    aos.sanity_check()
+    oi = np.asarray(aos.orbital_indices, dtype=np.int64)
+    ex = np.asarray(aos.exponents, dtype=np.float64)
+    co = np.asarray(aos.coefficients, dtype=np.float64)
+    shells, prims = [], []
+    for a in range(aos.num_ao):
+        atom, l = int(aos.nucleus_index[a]), int(aos.angular_momentums[a])
+        pw = (int(aos.polynominal_order_x[a]), int(aos.polynominal_order_y[a]), int(aos.polynominal_order_z[a]))
+        idx = np.nonzero(oi == a)[0]
+        p0 = len(prims)
+        for zz, cc in zip(ex[idx], co[idx]):
+            prims.append((zz, cc * cartesian_norm(l, zz, *pw)))
+        shells.append((atom, l, len(idx), p0, a, 1, cartesian_orders(l).index(pw), 1))
+    if any(shells[i][0] > shells[i + 1][0] for i in range(len(shells) - 1)):
+        raise ValueError("the AOs must be grouped by nucleus")
     return np.ascontiguousarray(np.array(shells, dtype=np.int32)), np.ascontiguousarray(np.array(prims, dtype=np.float64))
 
 

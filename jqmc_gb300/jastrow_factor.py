@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .atomic_orbital import AOs_sphe_data
+from .atomic_orbital import AOs_cart_data, AOs_sphe_data
 from .structure import Structure_data
 
 
@@ -68,8 +68,8 @@ class Jastrow_three_body_data:
     def sanity_check(self) -> None:
         if self.j_matrix.shape != (self.orb_num, self.orb_num + 1):
             raise ValueError(f"dim. of j_matrix = {self.j_matrix.shape} is incompatible with ({self.orb_num}, {self.orb_num + 1})")
-        if not isinstance(self.orb_data, AOs_sphe_data):
-            raise NotImplementedError("the J3 basis must be a spherical AO set on the walker path")
+        if not isinstance(self.orb_data, (AOs_sphe_data, AOs_cart_data)):
+            raise NotImplementedError("the J3 basis must be an AO set (spherical or Cartesian) on the walker path")
 
 
 @dataclass(frozen=True)

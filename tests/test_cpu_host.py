@@ -508,3 +508,36 @@ def test_nonlocal_move_option():
         system_desc(ham, 6, "dla")
     with pytest.raises(NotImplementedError):
         _check_lrdmc_options("dla", False)
+
+
+def test_cartesian_shell_table():
+    """A Cartesian basis packs one shell per AO, {atom, l, nprim, prim0, ao, 1,
+    component, 1}, with (Z, c N_cart) primitives; the library accepts it and
+    refuses a bad kind or component index before touching the device."""
+    import ctypes as C
+
+    from cart_system import water_like_cartesian
+
+    from jqmc_gb300 import _lib
+    from jqmc_gb300.atomic_orbital import cartesian_norm, cartesian_orders
+    from jqmc_gb300.build import build
+    from jqmc_gb300.engine import pack_basis, system_desc
+    build()
+    L = _lib.lib()
+    syn, ham = water_like_cartesian()
+    aos = ham.wavefunction_data.geminal_data.orb_data_up_spin
+    sh, pr = pack_basis(aos)
+    assert sh.shape == (aos.num_ao, 8) and np.all(sh[:, 5] == 1) and np.all(sh[:, 7] == 1)
+    for a in range(aos.num_ao):
+        pw = (aos.polynominal_order_x[a], aos.polynominal_order_y[a], aos.polynominal_order_z[a])
+        assert sh[a, 4] == a and cartesian_orders(int(sh[a, 1]))[sh[a, 6]] == pw
+        z, c = aos.primitives_of(a)
+        np.testing.assert_allclose(pr[sh[a, 3]:sh[a, 3] + sh[a, 2]],
+                                   np.stack([z, c * np.array([cartesian_norm(int(sh[a, 1]), zz, *pw) for zz in z])], 1))
+    d, keep, _ = system_desc(ham)
+    h = C.c_void_p()
+    assert L.jqmc_system_create(C.byref(d), C.byref(h)) in (0, -3)
+    for col, bad in ((7, 2), (6, 99)):
+        d, keep, _ = system_desc(ham)
+        keep["dsh"][0, col] = bad
+        assert L.jqmc_system_create(C.byref(d), C.byref(h)) == -1, (col, bad)

@@ -171,7 +171,7 @@ def test_cartesian_trexio_files():
     H2 cc-pVDZ (s and p shells) in its Cartesian and spherical files spans one
     space, so the occupied MO of the two files agrees up to sign at any point:
     a check of the Cartesian conversion and normalisation (oracle AO values).
-    The walker kernels refuse a Cartesian basis."""
+    The walker kernels take a Cartesian basis as one shell per AO."""
     from jqmc_gb300.atomic_orbital import AOs_cart_data
     from jqmc_gb300.engine import pack_basis
     from jqmc_gb300.trexio_wrapper import read_trexio_file
@@ -196,5 +196,5 @@ def test_cartesian_trexio_files():
     pack_basis(ms.aos_data)
     cart = read_trexio_file(os.path.join(TREXIO_DIR, "N_ae_ccpvdz_cart.h5"))[1]
     assert max(cart.angular_momentums) == 2 and cart.num_ao == 15
-    with pytest.raises(NotImplementedError):
-        pack_basis(cart)
+    sh, _ = pack_basis(cart)   # one Cartesian shell (kind 1) per AO for the walker kernels
+    assert sh.shape == (15, 8) and np.all(sh[:, 7] == 1)
