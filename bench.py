@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true", help="skip the parameter-derivative leg")
     p.add_argument("--no-batching", action="store_true", help="skip the many-molecule leg")
     p.add_argument("--no-vmc", action="store_true", help="skip the chain32 VMC leg (mixed vs plain FP64)")
+    p.add_argument("--no-configs", action="store_true", help="skip the config 0 (VMC water) and config 1 (LRDMC ring12) legs")
     a = p.parse_args()
     if a.walkers is None:
         a.walkers = 16384 if a.workload == "chain32" else 8192
@@ -426,6 +427,76 @@ def vmc_leg(walkers: int = 16384, K: int = 32, rounds: int = 3):
                     "rebuild of the float tables; draws resident in HBM"}
 
 
+def config0_leg(walkers: int = 1024, K: int = 40, blocks: int = 5):
+    """Config 0: plain FP64 VMC on the JSD water-like molecule, 1024 walkers,
+    single-electron Metropolis proposals (step 0.4 bohr) with E_L every K = 40
+    proposals, through MCMC.run_block (jqmc_mcmc.py:4278-4533, :725-747).
+    walker-steps/s counts proposals; the energy's share of the time is reported."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.jqmc_mcmc import MCMC
+    syn = synthetic.water_like()
+    m = MCMC(syn.hamiltonian, mcmc_seed=3, num_walkers=walkers, num_mcmc_per_measurement=K, Dt=0.4, epsilon_AS=0.0)
+    draws = [m.draws() for _ in range(blocks + 2)]
+    for d in draws[:2]:
+        m.run_block(*d)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record()
+    for d in draws[2:]:
+        m.run_block(*d)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    e0.record()
+    for d in draws[2:]:
+        m.walkers.vmc_measure(d[2], 0.0)
+    e2.record()
+    torch.cuda.synchronize()
+    ms_e = e0.elapsed_time(e2)
+    acc = m.accepted_moves / max(1, m.accepted_moves + m.rejected_moves)
+    out = {"workload": f"VMC FP64, JSD water-like (8 electrons, {m.sys.A} AOs), {walkers} walkers, {blocks} x {K} proposals "
+                       f"+ E_L per block", "walker_steps_per_s": walkers * K * blocks / (ms / 1e3), "ms": ms,
+           "energy_share": ms_e / ms, "accept_ratio": acc,
+           "note": "CUDA events around MCMC.run_block (sweep + E_L); draws resident in HBM"}
+    del m, draws
+    torch.cuda.empty_cache()
+    return out
+
+
+def config1_leg(walkers: int = 8192, K: int = 40, cycles: int = 2):
+    """Config 1: plain FP64 LRDMC (GFMC_n) on the 12-nucleus ring (30 electrons,
+    JAGP), 8192 walkers, a = 0.2 bohr, 40 projections per branching: the GPU
+    drop-in baseline; the mixed form on the same cycle beside it."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.jqmc_gfmc import GFMC_n
+    syn = synthetic.ring12()
+    out = {"workload": f"LRDMC GFMC_n, 12-nucleus ring (30 electrons), {walkers} walkers, {K} projections per branching, "
+                       f"a = 0.2 bohr"}
+    for form in ("fp64", "mixed"):
+        g = GFMC_n(syn.hamiltonian, num_walkers=walkers, num_mcmc_per_measurement=K, mcmc_seed=9, alat=0.2,
+                   precision=form)
+        draws = [g.draws() for _ in range(cycles + 1)]
+        g.run_block(draws[0], 0.5)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for d in draws[1:]:
+            g.run_block(d, 0.5)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[form] = {"walker_steps_per_s": walkers * K * cycles / (ms / 1e3), "ms_per_cycle": ms / cycles}
+        del g, draws
+        torch.cuda.empty_cache()
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["walker_steps_per_s"] / out["fp64"]["walker_steps_per_s"]
+    out["note"] = "CUDA events around GFMC_n.run_block (projections, rebuild, energy, comb, gather); draws resident in HBM"
+    return out
+
+
 def gpu_arm(a):
     import ctypes
 
@@ -601,6 +672,8 @@ def gpu_arm(a):
     adjoint = leg(lambda: adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")), a.no_adjoint)
     batching = leg(batching_leg, a.no_batching)
     vmc = leg(vmc_leg, a.no_vmc)
+    config0 = leg(config0_leg, a.no_configs)
+    config1 = leg(config1_leg, a.no_configs)
     bytes_launch = lrdmc_step_bytes(gs, 4) * W * K     # float tables
     ach_hbm = bytes_launch / (mix_ms / 1e3) / 1e9
     hbm_peak = peaks.get("hbm_gbs")
@@ -673,6 +746,8 @@ def gpu_arm(a):
             "adjoint": adjoint,
             "batching": batching,
             "vmc": vmc,
+            "config0_vmc_water": config0,
+            "config1_lrdmc_ring12": config1,
             "cpu_baseline": cpu_base,
             "clocks": mixed["clocks"],
         }

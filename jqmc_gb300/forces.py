@@ -127,7 +127,9 @@ class ELGradientFD:
                           for o, _ in STENCIL] for k in range(3)] for I in range(self.M)]
 
     def _energy(self, ws: WalkerSet, *args) -> torch.Tensor:
-        angles, eps_AS = args
+        """args: the rotations (W, 3) and, optionally, the AS cutoff (default 0)."""
+        angles = args[0]
+        eps_AS = args[1] if len(args) > 1 else 0.0
         return ws.vmc_measure(angles, eps_AS)[0]
 
     def __call__(self, r_up, r_dn, *args) -> torch.Tensor:
