@@ -47,7 +47,11 @@
 #include "jqmc_tc.h"
 #include "solid_harmonics.cuh"
 
-// CTAs per SM the projection kernel is compiled for (register budget)
+// Threads per CTA of the LRDMC kernels (one walker per CTA) and the CTAs per SM
+// their register budget is sized for.
+#ifndef JQMC_LRDMC_THREADS
+#define JQMC_LRDMC_THREADS 128
+#endif
 #ifndef JQMC_LRDMC_MINB
 #define JQMC_LRDMC_MINB 3
 #endif
@@ -3192,7 +3196,7 @@ __device__ __forceinline__ double* energy_bound(const KParams& P, int w) {
 }
 
 template <class R, class Tab, class Acc = R>
-__global__ void __launch_bounds__(128, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
+__global__ void __launch_bounds__(JQMC_LRDMC_THREADS, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
                         double* eL, double* vdiag, TauArgs ta, int emode) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
@@ -3504,26 +3508,26 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
       auto fn = k_lrdmc<float, float, float>;
       int rc = launch_check((const void*)fn, smem);
       if (rc) return rc;
-      fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+      fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
     } else {
       const bool gate = w->precision == JQMC_PREC_MIXED;
       auto fn = k_lrdmc<float, float, F2>;
       int rc = launch_check((const void*)fn, smem);
       if (rc) return rc;
-      fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
+      fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
                                              gate ? kEnergyBound : kEnergyPlain);
       if (gate) {
         auto fd = k_lrdmc<double, float, double>;
         rc = launch_check((const void*)fd, smem);
         if (rc) return rc;
-        fd<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyGate);
+        fd<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyGate);
       }
     }
   } else {
     auto fn = k_lrdmc<double, double>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
-    fn<<<w->nwalk, 128, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+    fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
