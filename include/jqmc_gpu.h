@@ -137,15 +137,19 @@ typedef struct {
                       /* displacements, required when that exceeds 64 KiB per    */
                       /* walker (else kept in shared memory); may be NULL below  */
   int32_t* status;    /* nwalk JQMC_ST_* bits                                    */
-  float* tlo;         /* JQMC_PREC_MIXED, optional: nwalk*2*n*A floats, the low  */
-                      /* parts of the FP64-accurate T tables (T_up rows, then    */
-                      /* T_dn rows): written by jqmc_walker_init and             */
-                      /* jqmc_lu_rebuild_refine when non-NULL; read by           */
-                      /* jqmc_lrdmc_energy when non-NULL, which the caller may   */
-                      /* pass only while no move has changed the tables since    */
-                      /* that build.  With it the block energy is computed from  */
-                      /* T_hi + T_lo and AO gradients/Laplacians re-evaluated in */
-                      /* FP64 at the electrons instead of the float tables.      */
+  float* tlo;         /* JQMC_PREC_MIXED, optional: per walker 2*n*A + N*A3      */
+                      /* floats, the low parts of the FP64-accurate T tables     */
+                      /* (T_up rows, then T_dn rows) followed by those of the J3 */
+                      /* field (N rows of A3; A3 = 0 without J3): written by     */
+                      /* jqmc_walker_init and jqmc_lu_rebuild_refine when        */
+                      /* non-NULL; read by jqmc_lrdmc_energy when non-NULL,      */
+                      /* which the caller may pass only while no move has        */
+                      /* changed the tables since that build.  With it the block */
+                      /* energy is computed from T_hi + T_lo, h_hi + h_lo and AO */
+                      /* values, gradients and Laplacians re-evaluated in FP64   */
+                      /* at the electrons instead of the float tables, and the   */
+                      /* non-local ECP ratios of the electrons whose elements    */
+                      /* weigh most are recomputed in FP64.                      */
 } jqmc_walkers;
 
 /* Copy the tables to the current device.  Replaces the per-call packing of

@@ -169,6 +169,11 @@ struct MeshExp<float, true> {
   static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
 };
 
+// Device shell records: the 8 ints of jqmc_basis_desc plus one of padding, so
+// that lanes reading one field of consecutive shells hit distinct shared-memory
+// banks (a stride of 9 words is coprime with the 32 banks).
+constexpr int kSh = 9;
+
 struct Basis {
   int nshell, nao, nprim;
   const int* shells;
@@ -264,15 +269,21 @@ struct TableLayout {
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
+// Floats per walker of the low-part buffer (jqmc_walkers.tlo): T_up and T_dn
+// rows, then the J3 field's N rows.
+__host__ __device__ inline size_t tlo_stride(const Sys& s) {
+  return (size_t)2 * s.n_up * s.det.nao + (s.has_j3 ? (size_t)s.N * s.j3.nao : 0);
+}
+
 TableLayout table_layout(const Sys& s, bool f64prims = true) {
   TableLayout L;
   int o = 0;
   const int jsh = s.has_j3 ? s.j3.nshell : 0, jpr = s.has_j3 ? s.j3.nprim : 0;
   L.f64prims = f64prims ? 1 : 0;
-  L.off_dsh = o; o = align16(o + s.det.nshell * 8 * 4);
+  L.off_dsh = o; o = align16(o + s.det.nshell * kSh * 4);
   L.off_dpr = o; o = align16(o + (f64prims ? s.det.nprim * 2 * 8 : 0));
   L.off_dprf = o; o = align16(o + s.det.nprim * 2 * 4);
-  L.off_jsh = o; o = align16(o + jsh * 8 * 4);
+  L.off_jsh = o; o = align16(o + jsh * kSh * 4);
   L.off_jpr = o; o = align16(o + (f64prims ? jpr * 2 * 8 : 0));
   L.off_jprf = o; o = align16(o + jpr * 2 * 4);
   L.off_apos = o; o = align16(o + s.natom * 3 * 8);
@@ -299,7 +310,7 @@ __device__ void copy_words(void* dst, const void* src, int bytes) {
 // refer to the shared copies.  Ends with __syncthreads().
 __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* smem) {
   Sys s = g;
-  copy_words(smem + L.off_dsh, g.det.shells, g.det.nshell * 32);
+  copy_words(smem + L.off_dsh, g.det.shells, g.det.nshell * kSh * 4);
   copy_words(smem + L.off_dprf, g.det.primsf, g.det.nprim * 8);
   s.det.shells = reinterpret_cast<const int*>(smem + L.off_dsh);
   s.det.primsf = reinterpret_cast<const float*>(smem + L.off_dprf);
@@ -308,7 +319,7 @@ __device__ Sys stage_tables(const Sys& g, const TableLayout& L, unsigned char* s
     s.det.prims = reinterpret_cast<const double*>(smem + L.off_dpr);
   }
   if (g.has_j3) {
-    copy_words(smem + L.off_jsh, g.j3.shells, g.j3.nshell * 32);
+    copy_words(smem + L.off_jsh, g.j3.shells, g.j3.nshell * kSh * 4);
     copy_words(smem + L.off_jprf, g.j3.primsf, g.j3.nprim * 8);
     s.j3.shells = reinterpret_cast<const int*>(smem + L.off_jsh);
     s.j3.primsf = reinterpret_cast<const float*>(smem + L.off_jprf);
@@ -437,7 +448,7 @@ __device__ __forceinline__ void disp(const double* apos, int atom, double px, do
 
 template <class R, class F>
 __device__ __forceinline__ void shell_val_d(const Basis& b, int s, R dx, R dy, R dz, F& f) {
-  const int* sh = b.shells + 8 * s;
+  const int* sh = b.shells + kSh * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const R r2 = dx * dx + dy * dy + dz * dz;
   const R* pr = prims_of<R>(b) + 2 * p0;
@@ -462,7 +473,7 @@ __device__ __forceinline__ void shell_val_d(const Basis& b, int s, R dx, R dy, R
 
 template <class R, class F>
 __device__ __forceinline__ void shell_vgl_d(const Basis& b, int s, R dx, R dy, R dz, F& f) {
-  const int* sh = b.shells + 8 * s;
+  const int* sh = b.shells + kSh * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const R r2 = dx * dx + dy * dy + dz * dz;
   const R* pr = prims_of<R>(b) + 2 * p0;
@@ -537,7 +548,7 @@ __device__ __forceinline__ void emit_dot_pts(const R* dx, const R* dy, const R* 
 template <int P, class R, class V, class Acc, bool LO = false>
 __device__ __forceinline__ void shell_dot_pts(const Basis& b, int s, const R* dx, const R* dy, const R* dz, const V* v, Acc* acc,
                                               const float* vlo = nullptr) {
-  const int* sh = b.shells + 8 * s;
+  const int* sh = b.shells + kSh * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const R* pr = prims_of<R>(b) + 2 * p0;
   R r2[P], rad[P];
@@ -581,7 +592,7 @@ template <int P, class V, class Acc, bool LO = false>
 __device__ __forceinline__ void shell_dot_pts_ff(const Basis& b, int s, const float* dx, const float* dy, const float* dz,
                                                  const float* r2h, const float* r2l, const V* v, Acc* acc,
                                                  const float* vlo = nullptr) {
-  const int* sh = b.shells + 8 * s;
+  const int* sh = b.shells + kSh * s;
   const int l = sh[1], np = sh[2], p0 = sh[3], ao0 = sh[4], nm = sh[5], jlo = sh[6] + sh[1];
   const float* pr = b.primsf + 2 * p0;
   float rad[P];
@@ -646,7 +657,7 @@ __device__ __forceinline__ void ao_visit(const Basis& b, const double* apos, dou
   int last = -1;
   R dx = R(0), dy = R(0), dz = R(0);
   for (int s = 0; s < b.nshell; ++s) {
-    const int atom = b.shells[8 * s];
+    const int atom = b.shells[kSh * s];
     if (atom != last) {
       disp<R>(apos, atom, px, py, pz, dx, dy, dz);
       last = atom;
@@ -660,7 +671,7 @@ __device__ __forceinline__ void ao_visit_vgl(const Basis& b, const double* apos,
   int last = -1;
   R dx = R(0), dy = R(0), dz = R(0);
   for (int s = 0; s < b.nshell; ++s) {
-    const int atom = b.shells[8 * s];
+    const int atom = b.shells[kSh * s];
     if (atom != last) {
       disp<R>(apos, atom, px, py, pz, dx, dy, dz);
       last = atom;
@@ -675,7 +686,7 @@ __device__ void ao_fill_block(const Basis& b, const double* apos, double px, dou
   auto f = [&](int a, R val) { out[a] = (V)val; };
   for (int s = threadIdx.x; s < b.nshell; s += blockDim.x) {
     R dx, dy, dz;
-    disp<R>(apos, b.shells[8 * s], px, py, pz, dx, dy, dz);
+    disp<R>(apos, b.shells[kSh * s], px, py, pz, dx, dy, dz);
     shell_val_d<R>(b, s, dx, dy, dz, f);
   }
 }
@@ -884,7 +895,7 @@ __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp
   const int A = s.det.nao;
   for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
     double dx, dy, dz;
-    disp<double>(s.atom_pos, s.det.shells[8 * sh], x, y, z, dx, dy, dz);
+    disp<double>(s.atom_pos, s.det.shells[kSh * sh], x, y, z, dx, dy, dz);
     auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
       dp[a] = (Tab)gx; dp[A + a] = (Tab)gy; dp[2 * A + a] = (Tab)gz; dp[3 * A + a] = (Tab)lp;
     };
@@ -894,7 +905,7 @@ __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp
     const int A3 = s.j3.nao;
     for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
       double dx, dy, dz;
-      disp<double>(s.atom_pos, s.j3.shells[8 * sh], x, y, z, dx, dy, dz);
+      disp<double>(s.atom_pos, s.j3.shells[kSh * sh], x, y, z, dx, dy, dz);
       auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
         dp3[a] = (Tab)v; dp3[A3 + a] = (Tab)gx; dp3[2 * A3 + a] = (Tab)gy; dp3[3 * A3 + a] = (Tab)gz; dp3[4 * A3 + a] = (Tab)lp;
       };
@@ -1062,8 +1073,9 @@ struct Work {
   Tab* vn3;
   double* red;   // kRed
   double* sc;    // 32 scalars
-  const float* tlo_up;   // mixed form: low parts of T_up / T_dn from the last build
-  const float* tlo_dn;   // (nullptr when the tables have moved since, or not kept)
+  const float* tlo_up;   // mixed form: low parts of T_up / T_dn and of the J3 field
+  const float* tlo_dn;   // from the last build (nullptr when the tables have moved
+  const float* h3lo;     // since, or are not kept); h3lo is nullptr without J3
 };
 
 struct WorkLayout {
@@ -1120,8 +1132,9 @@ __device__ Work<Tab> make_work(const Sys& s, const WorkLayout& L, unsigned char*
   k.dphi = static_cast<Tab*>(ws.dphi) + (size_t)w * k.N * 4 * k.A;
   k.dphi3 = s.has_j3 ? static_cast<Tab*>(ws.dphi3) + (size_t)w * k.N * 5 * k.A3 : nullptr;
   k.ec = ws.ecache + (size_t)w * (k.N + 1) * kEC;
-  k.tlo_up = ws.tlo ? ws.tlo + (size_t)w * 2 * k.n * k.A : nullptr;
+  k.tlo_up = ws.tlo ? ws.tlo + (size_t)w * tlo_stride(s) : nullptr;
   k.tlo_dn = ws.tlo ? k.tlo_up + (size_t)k.n * k.A : nullptr;
+  k.h3lo = ws.tlo && s.has_j3 ? k.tlo_up + (size_t)2 * k.n * k.A : nullptr;
   return k;
 }
 
@@ -1349,6 +1362,7 @@ struct Terms {
   int* eatom;     // N  nearest nucleus
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
+  float* vm;      // N  compensated energy: sum over the electron's ECP points of |w_v| M_v
   double* R;      // 9 rotation
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
@@ -1356,7 +1370,7 @@ struct Terms {
 };
 
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_R, off_Rf, off_dA, off_dE, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form in shared memory
@@ -1372,6 +1386,7 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_ea = o; o = align16(o + N * 4);
   L.off_el = o; o = align16(o + 6 * N * 8);
   L.off_V = o; o = align16(o + (s.nv > 0 ? s.nv : 1) * N * 8);
+  L.off_vm = o; o = align16(o + N * 4);
   L.off_R = o; o = align16(o + 9 * 8);
   L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
@@ -1397,6 +1412,7 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.eatom = reinterpret_cast<int*>(smem + L.off_ea);
   t.el = reinterpret_cast<double*>(smem + L.off_el);
   t.V = reinterpret_cast<double*>(smem + L.off_V);
+  t.vm = reinterpret_cast<float*>(smem + L.off_vm);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
@@ -1454,28 +1470,27 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
 }
 
 // The determinant part of electron e's derivatives at FP64 accuracy, for the
-// block energy of the mixed form right after a build: the AO gradients and
-// Laplacians re-evaluated in FP64 at r_e (the float tables hold them rounded,
-// which alone moves E_L by about 1e-5 Ha on the 30-electron ring) dotted with
-// the FP64-accurate T row T_hi + T_lo.  One warp; the lanes split the shells;
-// every lane returns (grad x, y, z, Laplacian) of phi . T.
+// block energy of the mixed form right after a build: the AO values, gradients
+// and Laplacians of basis b re-evaluated in FP64 at r_e (the float tables hold
+// them rounded, which alone moves E_L by about 1e-5 Ha on the 30-electron ring)
+// dotted with the FP64-accurate row v_hi + v_lo (a T row, or a J3 field row).
+// One warp; the lanes split the shells; every lane returns (value, grad x, y, z,
+// Laplacian) of phi . v.
 template <class Tab>
-__device__ void det_terms_fp64(const Work<Tab>& k, int e, const Tab* Trow, const float* Tlo, double* out) {
-  const Sys& s = k.s;
+__device__ void dot_vgl_fp64(const Sys& s, const Basis& b, const double* re, const Tab* v, const float* vlo, double* out) {
   const int lane = threadIdx.x & 31;
-  const double px = k.r[3 * e], py = k.r[3 * e + 1], pz = k.r[3 * e + 2];
-  double ax = 0.0, ay = 0.0, az = 0.0, al = 0.0;
-  auto f = [&](int a, double, double gx, double gy, double gz, double lap) {
-    const double t = (double)Trow[a] + (double)Tlo[a];
-    ax += gx * t; ay += gy * t; az += gz * t; al += lap * t;
+  double a0 = 0.0, ax = 0.0, ay = 0.0, az = 0.0, al = 0.0;
+  auto f = [&](int a, double val, double gx, double gy, double gz, double lap) {
+    const double t = (double)v[a] + (double)vlo[a];
+    a0 += val * t; ax += gx * t; ay += gy * t; az += gz * t; al += lap * t;
   };
-  for (int idx = lane; idx < s.det.nshell; idx += 32) {
-    const int sh = s.det.shells[8 * idx + 7];
+  for (int idx = lane; idx < b.nshell; idx += 32) {
+    const int sh = b.shells[kSh * idx + 7];
     double dx, dy, dz;
-    disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
-    shell_vgl_d<double>(s.det, sh, dx, dy, dz, f);
+    disp<double>(s.atom_pos, b.shells[kSh * sh], re[0], re[1], re[2], dx, dy, dz);
+    shell_vgl_d<double>(b, sh, dx, dy, dz, f);
   }
-  out[0] = warp_sum(ax); out[1] = warp_sum(ay); out[2] = warp_sum(az); out[3] = warp_sum(al);
+  out[0] = warp_sum(a0); out[1] = warp_sum(ax); out[2] = warp_sum(ay); out[3] = warp_sum(az); out[4] = warp_sum(al);
 }
 
 // Phase A: per-electron continuum kinetic energy and the old-position values
@@ -1515,9 +1530,9 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     // determinant terms (the float projection keeps the table dots)
     constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
     const float* Tlo = kMayRefine ? (up ? k.tlo_up : k.tlo_dn) : nullptr;
-    double dt[4] = {0.0, 0.0, 0.0, 0.0};
+    double dt[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, d3[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     if (kMayRefine && Tlo) {
-      det_terms_fp64(k, e, Trow, Tlo + (size_t)i * A, dt);
+      dot_vgl_fp64(s, s.det, k.r + 3 * e, Trow, Tlo + (size_t)i * A, dt);
     } else {
       for (int a = lane; a < A; a += 32) {
         const Ar tv = (Ar)Trow[a];
@@ -1527,7 +1542,9 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
         acc_fma(tlp, (Ar)dp[3 * A + a], tv);
       }
     }
-    if (s.has_j3) {
+    if (kMayRefine && Tlo && k.h3lo) {
+      dot_vgl_fp64(s, s.j3, k.r + 3 * e, k.h3 + (size_t)e * A3, k.h3lo + (size_t)e * A3, d3);
+    } else if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
       for (int a = lane; a < A3; a += 32) {
@@ -1540,8 +1557,9 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
       }
     }
     Out v0 = acc_out(tgx), v1 = acc_out(tgy), v2 = acc_out(tgz), v3 = acc_out(tlp);
-    if (kMayRefine && Tlo) { v0 = (Out)dt[0]; v1 = (Out)dt[1]; v2 = (Out)dt[2]; v3 = (Out)dt[3]; }
-    const Out v4 = acc_out(tc3), v5 = acc_out(thx), v6 = acc_out(thy), v7 = acc_out(thz), v8 = acc_out(thl);
+    if (kMayRefine && Tlo) { v0 = (Out)dt[1]; v1 = (Out)dt[2]; v2 = (Out)dt[3]; v3 = (Out)dt[4]; }
+    Out v4 = acc_out(tc3), v5 = acc_out(thx), v6 = acc_out(thy), v7 = acc_out(thz), v8 = acc_out(thl);
+    if (kMayRefine && Tlo && k.h3lo) { v4 = (Out)d3[0]; v5 = (Out)d3[1]; v6 = (Out)d3[2]; v7 = (Out)d3[3]; v8 = (Out)d3[4]; }
     if (lane == (it & 31)) {
       kp[0] = v0; kp[1] = v1; kp[2] = v2; kp[3] = v3; kp[4] = v4; kp[5] = v5; kp[6] = v6; kp[7] = v7; kp[8] = v8;
       mine = e;
@@ -1617,7 +1635,11 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
   // block energy on fresh tables (mixed form): the T row's low parts as well
   constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
   const float* Tlo = nullptr;
-  if constexpr (kMayRefine) Tlo = (up ? k.tlo_up : k.tlo_dn) ? (up ? k.tlo_up : k.tlo_dn) + (size_t)i * k.A : nullptr;
+  const float* hlo = nullptr;   // the J3 field row's low parts
+  if constexpr (kMayRefine) {
+    Tlo = (up ? k.tlo_up : k.tlo_dn) ? (up ? k.tlo_up : k.tlo_dn) + (size_t)i * k.A : nullptr;
+    hlo = Tlo && k.h3lo ? k.h3lo + (size_t)e * k.A3 : nullptr;
+  }
   const bool rel = sizeof(R) == sizeof(float) && t.dA != nullptr;
   const float* dAe = rel ? t.dA + (size_t)e * s.natom * 3 : nullptr;
   const float* dEe = rel ? t.dE + (size_t)e * k.N * 3 : nullptr;
@@ -1642,8 +1664,8 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     float dxl[P], dyl[P], dzl[P], r2h[P], r2l[P];
     auto shells = [&](const Basis& b, const Tab* v, Acc* acc, const float* vlo) {
       for (int idx = lane; idx < b.nshell; idx += 32) {
-        const int sh = b.shells[8 * idx + 7];
-        const int atom = b.shells[8 * sh];
+        const int sh = b.shells[kSh * idx + 7];
+        const int atom = b.shells[kSh * sh];
         R x, y, z;
         dnuc(atom, x, y, z);
         const float xl = (float)((ex - s.atom_pos[3 * atom]) - (double)x);
@@ -1661,12 +1683,12 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
       }
     };
     shells(s.det, Trow, det, Tlo);
-    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, nullptr);
+    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, hlo);
   } else {
     for (int idx = lane; idx < s.det.nshell; idx += 32) {
-      const int sh = s.det.shells[8 * idx + 7];   // (l, nprim)-sorted order
+      const int sh = s.det.shells[kSh * idx + 7];   // (l, nprim)-sorted order
       R x, y, z;
-      dnuc(s.det.shells[8 * sh], x, y, z);
+      dnuc(s.det.shells[kSh * sh], x, y, z);
 #pragma unroll
       for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
       if constexpr (kMayRefine) {
@@ -1679,12 +1701,17 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * k.A3;
       for (int idx = lane; idx < s.j3.nshell; idx += 32) {
-        const int sh = s.j3.shells[8 * idx + 7];
+        const int sh = s.j3.shells[kSh * idx + 7];
         R x, y, z;
-        dnuc(s.j3.shells[8 * sh], x, y, z);
+        dnuc(s.j3.shells[kSh * sh], x, y, z);
 #pragma unroll
         for (int p = 0; p < P; ++p) { dx[p] = x + mx[p]; dy[p] = y + my[p]; dz[p] = z + mz[p]; }
-        shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
+        if constexpr (kMayRefine) {
+          if (hlo) shell_dot_pts<P, R, Tab, Acc, true>(s.j3, sh, dx, dy, dz, h, dj, hlo);
+          else shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
+        } else {
+          shell_dot_pts<P, R>(s.j3, sh, dx, dy, dz, h, dj);
+        }
       }
     }
   }
@@ -1749,10 +1776,23 @@ struct Cancellation {
   }
 };
 
+// Electrons whose ECP points have sum_v |w_v| M_v above this get their non-local
+// elements again in FP64 in the block energy of the mixed form: with the float
+// AO values off by a few 1e-8 relative, what the others leave is below about
+// 3e-7 Ha per electron.
+#ifndef JQMC_ECP_REFINE_MAG
+#define JQMC_ECP_REFINE_MAG 8.0
+#endif
+constexpr double kEcpRefineMag = JQMC_ECP_REFINE_MAG;
+
 // Returns this thread's shares of the walker's cancellation factor (compensated
-// mode; zero otherwise).
+// mode; zero otherwise).  The compensated mode also leaves per electron in t.vm
+// the sum over its ECP points of |w_v| M_v (w_v the element's weight, M_v as in
+// the cancellation factor): the float AO values' rounding moves the electron's
+// non-local energy by a few 1e-8 of it.  With `refine` set, only the ECP points
+// of the electrons with refine[e] > kEcpRefineMag are computed (again).
 template <class R, class Tab, class Acc = R>
-__device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic) {
+__device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bool kinetic, const float* refine = nullptr) {
   using Out = typename AccTraits<Acc>::out;
   constexpr bool kErr = AccTraits<Acc>::accurate;
   Cancellation cancel;
@@ -1763,9 +1803,11 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
   const int N = k.N, nv = s.nv;
   const double kin = -1.0 / (2.0 * alat * alat);
   for (int e = wid; e < N; e += nw) {
+    if (refine && !(refine[e] > (float)kEcpRefineMag)) continue;   // (warp-uniform)
     const int atom = t.eatom[e];
     const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
     const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
+    float vmag = 0.f;
     if (e + nw < N) {   // this warp's next electron: its T row, J3 field and displacements
       const int en = e + nw;
       const Tab* Tn = (en < s.n_up ? k.Tup + (size_t)en * k.A : k.Tdn + (size_t)(en - s.n_up) * k.A);
@@ -1776,7 +1818,7 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
         prefetch_l2(t.dE + (size_t)en * N * 3, (size_t)N * 12, lane);
       }
     }
-    for (int c = kinetic ? 0 : nkc; c < nchunk; ++c) {
+    for (int c = kinetic && !refine ? 0 : nkc; c < nchunk; ++c) {
       // lane p < P sets up point p, then every lane receives all P moves.  The
       // float form builds them from the float rotation, quadrature directions
       // and displacement cache, so that the chunk issues no FP64 instruction.
@@ -1891,9 +1933,16 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
           // >= 0 and psi'/psi (the Jastrow factor, > 0, keeps the sign) elsewhere,
           // so min(V, 0) and max(V, 0) are the FN move weight and the SP part
           t.V[e * nv + v] = (double)(vw * rr);
-          if (kErr) cancel.add(fabsf((float)vw), mg, (float)(vw * rr));
+          if (kErr) {
+            cancel.add(fabsf((float)vw), mg, (float)(vw * rr));
+            vmag += fabsf((float)vw) * mg;
+          }
         }
       }
+    }
+    if constexpr (kErr) {
+      vmag = warp_sum(vmag);
+      if (lane == 0) t.vm[e] = vmag;
     }
   }
   __syncthreads();
@@ -2069,7 +2118,7 @@ __device__ void rebuild_m_body(const KParams& P, int w, int by, unsigned char* s
       };
       for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
         double dx, dy, dz;
-        disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
+        disp<double>(s.atom_pos, s.det.shells[kSh * sh], px, py, pz, dx, dy, dz);
         shell_val_d<double>(s.det, sh, dx, dy, dz, f);
       }
     } else {
@@ -2133,7 +2182,7 @@ __global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long lon
     auto f = [&](int a, double v) { out[a] = v; };
     for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
       double dx, dy, dz;
-      disp<double>(s.atom_pos, s.det.shells[8 * sh], px, py, pz, dx, dy, dz);
+      disp<double>(s.atom_pos, s.det.shells[kSh * sh], px, py, pz, dx, dy, dz);
       shell_val_d<double>(s.det, sh, dx, dy, dz, f);
     }
   }
@@ -2188,7 +2237,7 @@ __global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long lon
 // the running prefix (the electron's J3 AO values are evaluated again).
 // buf: 4 A3 values of type J.  Block-cooperative.
 template <class J, class Tab>
-__device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J* jm, const J* jmT) {
+__device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J* jm, const J* jmT, float* hlo = nullptr) {
   const int N = s.N, A3 = s.j3.nao;
   J* tot_up = buf;
   J* tot_dn = buf + A3;
@@ -2198,7 +2247,7 @@ __device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J*
     auto f = [&](int a, J v) { pe[a] = v; };
     for (int sh = threadIdx.x; sh < s.j3.nshell; sh += blockDim.x) {
       J dx, dy, dz;
-      disp<J>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      disp<J>(s.atom_pos, s.j3.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
       shell_val_d<J>(s.j3, sh, dx, dy, dz, f);
     }
   };
@@ -2234,6 +2283,7 @@ __device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J*
         acc += up ? Jccp * tot_dn[cp] : Jcpc * tot_up[cp];
       }
       h[(size_t)e * A3 + c] = (Tab)acc;
+      if (hlo) hlo[(size_t)e * A3 + c] = (float)((double)acc - (double)(Tab)acc);
     }
     __syncthreads();
     for (int c = threadIdx.x; c < A3; c += blockDim.x) pfx[c] += pe[c];
@@ -2436,7 +2486,7 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
     __syncthreads();
     const float2* Mdn2 = reinterpret_cast<const float2*>(Mdn);
     const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
-    float* tlo = P.ws.tlo ? P.ws.tlo + (size_t)w * 2 * n * A : nullptr;
+    float* tlo = P.ws.tlo ? P.ws.tlo + (size_t)w * tlo_stride(s) : nullptr;
     constexpr int KB = 8;
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
       for (int k0 = 0; k0 < n; k0 += KB) {
@@ -2500,10 +2550,15 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
   // energy), or in the table type with kInitJ3Table.
   if (s.has_j3) {
     Tab* h = static_cast<Tab*>(P.ws.h3) + (size_t)w * N * A3;
-    if (sizeof(Tab) == sizeof(float) && (mode & kInitJ3Table))
+    // the low parts of an FP64 field go behind the T tables' in the low-part buffer
+    float* hlo = sizeof(Tab) == sizeof(float) && P.ws.tlo ? P.ws.tlo + (size_t)w * tlo_stride(s) + (size_t)2 * n * A : nullptr;
+    if (sizeof(Tab) == sizeof(float) && (mode & kInitJ3Table)) {
       j3_field<Tab, Tab>(s, h, r, reinterpret_cast<Tab*>(vec), j3m_of<Tab>(s), j3mT_of<Tab>(s));
-    else
-      j3_field<double, Tab>(s, h, r, vec, s.j3mat, s.j3matT);
+      if (hlo)
+        for (int c = threadIdx.x; c < N * A3; c += blockDim.x) hlo[c] = 0.f;
+    } else {
+      j3_field<double, Tab>(s, h, r, vec, s.j3mat, s.j3matT, hlo);
+    }
   }
 }
 
@@ -2590,7 +2645,7 @@ __global__ void k_dlnpsi_dparam(KParams P, int off_red, int off_su, int off_sd, 
       double* out = phi3 + (size_t)e * A3;
       auto f = [&](int a, double v) { out[a] = v; };
       double dx, dy, dz;
-      disp<double>(s.atom_pos, s.j3.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      disp<double>(s.atom_pos, s.j3.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
       shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
     }
     __syncthreads();
@@ -2627,7 +2682,7 @@ __global__ void k_dlnpsi_dparam(KParams P, int off_red, int off_su, int off_sd, 
       double* out = e < n ? Phi + (size_t)e * A : X + (size_t)(e - n) * A;
       auto f = [&](int a, double v) { out[a] = v; };
       double dx, dy, dz;
-      disp<double>(s.atom_pos, s.det.shells[8 * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      disp<double>(s.atom_pos, s.det.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
       shell_val_d<double>(s.det, sh, dx, dy, dz, f);
     }
     __syncthreads();
@@ -2672,7 +2727,7 @@ __global__ void k_dlnpsi_dR(KParams P, int off_acc, double* out) {
   const int nsh = s.det.nshell;
   for (int p = threadIdx.x; p < N * nsh; p += blockDim.x) {
     const int e = p / nsh, sh = p % nsh;
-    const int* row = s.det.shells + 8 * sh;
+    const int* row = s.det.shells + kSh * sh;
     const int atom = row[0], ao0 = row[4], nm = row[5];
     const double* T = (e < n ? k.Tup + (size_t)e * A : k.Tdn + (size_t)(e - n) * A);
     const double* dp = k.dphi + (size_t)e * 4 * A;
@@ -2690,7 +2745,7 @@ __global__ void k_dlnpsi_dR(KParams P, int off_acc, double* out) {
     const int A3 = k.A3, nsh3 = s.j3.nshell;
     for (int p = threadIdx.x; p < N * nsh3; p += blockDim.x) {
       const int e = p / nsh3, sh = p % nsh3;
-      const int* row = s.j3.shells + 8 * sh;
+      const int* row = s.j3.shells + kSh * sh;
       const int atom = row[0], ao0 = row[4], nm = row[5];
       const double* h = k.h3 + (size_t)e * A3;
       const double* q = k.dphi3 + (size_t)e * 5 * A3;
@@ -3237,7 +3292,10 @@ __global__ void __launch_bounds__(JQMC_LRDMC_THREADS, JQMC_LRDMC_MINB) k_lrdmc(K
     electron_terms<Tab, Acc>(k, t, alat);
     const Cancellation mc = mesh_terms<R, Tab, Acc>(k, t, alat, true);
     if constexpr (AccTraits<Acc>::accurate && sizeof(Tab) == sizeof(float))
-      if (K == 0 && k.tlo_up) refine_lattice(k, t, alat);
+      if (K == 0 && k.tlo_up) {
+        refine_lattice(k, t, alat);
+        if (s.ecp_flag) mesh_terms<double, Tab, double>(k, t, alat, true, t.vm);   // ECP elements of the heavy electrons
+      }
     double diag, nondiag;
     lrdmc_sums(s, k.ec, N, k.red, t, alat, &diag, &nondiag);
     if (K == 0) {
@@ -3628,7 +3686,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     }
   const size_t o_apos = put(d->atom_pos, (size_t)M * 24);
   const size_t o_az = put(d->atom_zeff, (size_t)M * 8);
-  // Shell rows are copied with their 8th int set to a permutation of the shells
+  // Shell rows are copied at the device stride kSh with their 8th int set to a permutation of the shells
   // sorted by (l, nprim): the warp-cooperative mesh evaluation walks the shells
   // in that order, so the 32 lanes of an iteration take the same code path.
   auto with_order = [](const jqmc_basis_desc& b) {
@@ -3639,14 +3697,16 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       const int lx = rows[8 * x + 1], ly = rows[8 * y + 1];
       return lx != ly ? lx < ly : rows[8 * x + 2] < rows[8 * y + 2];
     });
+    std::vector<int32_t> dev((size_t)b.nshell * kSh, 0);   // padded to the device stride
     for (int k = 0; k < b.nshell; ++k) {
-      if (rows[8 * k + 7] == 1) rows[8 * k + 6] += kCartBase;   // the Cartesian kind moves to field 6
-      rows[8 * k + 7] = ord[k];
+      for (int f = 0; f < 8; ++f) dev[(size_t)kSh * k + f] = rows[8 * k + f];
+      if (rows[8 * k + 7] == 1) dev[(size_t)kSh * k + 6] += kCartBase;   // the Cartesian kind moves to field 6
+      dev[(size_t)kSh * k + 7] = ord[k];
     }
-    return rows;
+    return dev;
   };
   const std::vector<int32_t> dsh_rows = with_order(d->det);
-  const size_t o_dsh = put(dsh_rows.data(), (size_t)d->det.nshell * 32);
+  const size_t o_dsh = put(dsh_rows.data(), dsh_rows.size() * 4);
   const size_t o_dpr = put(d->det.prims, (size_t)d->det.nprim * 16);
   const size_t o_dprf = put(dprf.data(), dprf.size() * 4);
   const size_t o_lam = put(d->lambda, (size_t)A * A * 8);
@@ -3659,7 +3719,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
   if (d->has_j3) {
     const std::vector<int32_t> jsh_rows = with_order(d->j3);
-    o_jsh = put(jsh_rows.data(), (size_t)d->j3.nshell * 32);
+    o_jsh = put(jsh_rows.data(), jsh_rows.size() * 4);
     o_jpr = put(d->j3.prims, (size_t)d->j3.nprim * 16);
     o_jprf = put(jprf.data(), jprf.size() * 4);
     o_j3m = put(j3m.data(), j3m.size() * 8);

@@ -249,9 +249,10 @@ class WalkerSet:
             M = len(system._keep["pos"])
             big = N * (M + N) * 3 * 4 > 64 * 1024
             self.dcache = torch.empty((W, N * (M + N) * 3), dtype=torch.float32, device=dev) if big else None
-            # low parts of the FP64-accurate T tables, written by every build and read
-            # by the block energy while no move has changed the tables (fresh)
-            self.tlo = torch.empty((W, 2, n, A), dtype=torch.float32, device=dev)
+            # low parts of the FP64-accurate T tables and J3 field, written by every
+            # build and read by the block energy while no move has changed the
+            # tables (fresh)
+            self.tlo = torch.empty((W, 2 * n * A + N * A3), dtype=torch.float32, device=dev)
         else:
             self.scratch = None
             self.dcache = None
