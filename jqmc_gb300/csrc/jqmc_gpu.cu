@@ -47,16 +47,21 @@
 #include "jqmc_tc.h"
 #include "solid_harmonics.cuh"
 
-// Threads per CTA of the LRDMC kernels (one walker per CTA) and the CTAs per SM
-// their register budget is sized for.
-#ifndef JQMC_LRDMC_THREADS
-#define JQMC_LRDMC_THREADS 128
-#endif
-#ifndef JQMC_LRDMC_MINB
-#define JQMC_LRDMC_MINB 3
-#endif
-
 namespace {
+
+// Threads per CTA of the LRDMC kernels (one walker per CTA) and the CTAs per SM
+// their register budget is sized for.  The float projection runs 8 warps per
+// walker at 2 CTAs per SM (16 warps per SM; 12 % faster on the chain than 4
+// warps at 3 CTAs); the FP64 and block-energy kernels keep 4 warps at 3 CTAs
+// (170 registers, which their FP64 paths need).
+template <class R, class Acc>
+struct LrdmcShape {
+  static constexpr int threads = 128, min_ctas = 3;
+};
+template <>
+struct LrdmcShape<float, float> {
+  static constexpr int threads = 256, min_ctas = 2;
+};
 
 constexpr int kSlots = JQMC_ECP_SLOTS;
 constexpr int kRed = 64;  // doubles of reduction scratch
@@ -1781,7 +1786,7 @@ struct Cancellation {
 // AO values off by a few 1e-8 relative, what the others leave is below about
 // 3e-7 Ha per electron.
 #ifndef JQMC_ECP_REFINE_MAG
-#define JQMC_ECP_REFINE_MAG 8.0
+#define JQMC_ECP_REFINE_MAG 16.0
 #endif
 constexpr double kEcpRefineMag = JQMC_ECP_REFINE_MAG;
 
@@ -3251,7 +3256,7 @@ __device__ __forceinline__ double* energy_bound(const KParams& P, int w) {
 }
 
 template <class R, class Tab, class Acc = R>
-__global__ void __launch_bounds__(JQMC_LRDMC_THREADS, JQMC_LRDMC_MINB) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
+__global__ void __launch_bounds__(LrdmcShape<R, Acc>::threads, LrdmcShape<R, Acc>::min_ctas) k_lrdmc(KParams P, int K, const double* __restrict__ draw, double alat, double E_scf, double* wgt,
                         double* eL, double* vdiag, TauArgs ta, int emode) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = blockIdx.x;
@@ -3566,26 +3571,27 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
       auto fn = k_lrdmc<float, float, float>;
       int rc = launch_check((const void*)fn, smem);
       if (rc) return rc;
-      fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+      fn<<<w->nwalk, LrdmcShape<float, float>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
     } else {
       const bool gate = w->precision == JQMC_PREC_MIXED;
       auto fn = k_lrdmc<float, float, F2>;
       int rc = launch_check((const void*)fn, smem);
       if (rc) return rc;
-      fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
-                                             gate ? kEnergyBound : kEnergyPlain);
+      fn<<<w->nwalk, LrdmcShape<float, F2>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
+                                                                         gate ? kEnergyBound : kEnergyPlain);
       if (gate) {
         auto fd = k_lrdmc<double, float, double>;
         rc = launch_check((const void*)fd, smem);
         if (rc) return rc;
-        fd<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyGate);
+        fd<<<w->nwalk, LrdmcShape<double, double>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyGate);
       }
     }
   } else {
     auto fn = k_lrdmc<double, double>;
     int rc = launch_check((const void*)fn, smem);
     if (rc) return rc;
-    fn<<<w->nwalk, JQMC_LRDMC_THREADS, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+    fn<<<w->nwalk, LrdmcShape<double, double>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
+                                                                           kEnergyPlain);
   }
   return cudaGetLastError() == cudaSuccess ? JQMC_OK : JQMC_E_CUDA;
 }
