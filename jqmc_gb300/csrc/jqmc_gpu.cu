@@ -39,6 +39,8 @@
 #include <mutex>
 #include <type_traits>
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -174,10 +176,16 @@ struct MeshExp<float, true> {
   static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
 };
 
-// Device shell records: the 8 ints of jqmc_basis_desc plus one of padding, so
-// that lanes reading one field of consecutive shells hit distinct shared-memory
-// banks (a stride of 9 words is coprime with the 32 banks).
-constexpr int kSh = 9;
+// Device shell records: the 8 ints of jqmc_basis_desc, then the squares of the
+// shell's two reach radii as float bits (field 8: float mesh ratios, field 9:
+// FP64 and compensated ones), then one int of padding, so that lanes reading one
+// field of consecutive shells hit distinct shared-memory banks (a stride of 11
+// words is coprime with the 32 banks).  Beyond its reach radius from the shell's
+// nucleus, every AO of the shell is below e^-kReachFloat (e^-kReachFp64) in
+// magnitude for unit table entries: sum_q |c_q| max(r, 1)^l e^(-Z_q r^2).
+constexpr int kSh = 11;
+constexpr int kShReachF = 8, kShReach64 = 9;
+constexpr double kReachFloat = 25.0, kReachFp64 = 40.0;
 
 struct Basis {
   int nshell, nao, nprim;
@@ -1368,14 +1376,20 @@ struct Terms {
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
   float* vm;      // N  compensated energy: sum over the electron's ECP points of |w_v| M_v
+  uint16_t* act;  // 8 warps x (det + J3 shells): each warp's list of shells within reach
   double* R;      // 9 rotation
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
 };
 
+constexpr int kMaxWarps = 8;   // warps per CTA of the walker kernels that use the terms layout
+static_assert(LrdmcShape<float, float>::threads / 32 <= kMaxWarps && LrdmcShape<double, double>::threads / 32 <= kMaxWarps,
+              "shell-list slots for every warp");
+
 struct TermsLayout {
-  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, bytes;
+  int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, off_act,
+      act_warp, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form in shared memory
@@ -1396,9 +1410,15 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
+  // last, so that a kernel of fewer warps launches with less of it
+  L.act_warp = align16((s.det.nshell + (s.has_j3 ? s.j3.nshell : 0)) * 2);
+  L.off_act = o; o += kMaxWarps * L.act_warp;
   L.bytes = o;
   return L;
 }
+
+// Dynamic shared memory of a walker kernel of `threads` threads per CTA.
+int terms_smem(const TermsLayout& L, int threads) { return L.bytes - (kMaxWarps - threads / 32) * L.act_warp; }
 
 // Displacement caches bigger than this live in global memory (per walker).
 constexpr int kDcacheSmemMax = 64 * 1024;
@@ -1418,6 +1438,7 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.el = reinterpret_cast<double*>(smem + L.off_el);
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.vm = reinterpret_cast<float*>(smem + L.off_vm);
+  t.act = reinterpret_cast<uint16_t*>(smem + L.off_act);
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
@@ -1475,6 +1496,61 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
 }
 
 // The determinant part of electron e's derivatives at FP64 accuracy, for the
+// The shells (positions in the (l, nprim)-sorted order) whose reach radius
+// extends to within `margin` of electron e: every mesh point p of the electron
+// with |p - r_e| <= margin is then beyond the reach of every other shell, whose
+// AOs are below e^-kReachFloat (field kShReachF) or e^-kReachFp64 (kShReach64)
+// there and are left out of the ratio.  One warp; the list goes to the warp's
+// slot of t.act.
+struct ShellList {
+  const uint16_t* det;
+  int ndet;
+  const uint16_t* j3;
+  int nj3;
+};
+
+template <class Tab>
+__device__ ShellList shell_list(const Work<Tab>& k, const Terms& t, int e, float margin, int field, bool rel) {
+  const Sys& s = k.s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint16_t* buf = t.act + (size_t)wid * (s.det.nshell + (s.has_j3 ? s.j3.nshell : 0));
+  const float* dAe = rel ? t.dA + (size_t)e * s.natom * 3 : nullptr;
+  auto build = [&](const Basis& b, uint16_t* out) -> int {
+    int cnt = 0;
+    for (int base = 0; base < b.nshell; base += 32) {
+      const int idx = base + lane;
+      bool keep = false;
+      if (idx < b.nshell) {
+        const int sh = b.shells[kSh * idx + 7];
+        const int atom = b.shells[kSh * sh];
+        float d2;
+        if (rel) {
+          const float x = dAe[3 * atom], y = dAe[3 * atom + 1], z = dAe[3 * atom + 2];
+          d2 = x * x + y * y + z * z;
+        } else {
+          const double x = k.r[3 * e] - s.atom_pos[3 * atom], y = k.r[3 * e + 1] - s.atom_pos[3 * atom + 1];
+          const double z = k.r[3 * e + 2] - s.atom_pos[3 * atom + 2];
+          d2 = (float)(x * x + y * y + z * z);
+        }
+        const float dd = fmaxf(sqrtf(d2) - margin, 0.f);
+        keep = dd * dd < __int_as_float(b.shells[kSh * sh + field]);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (keep) out[cnt + __popc(m & ((1u << lane) - 1u))] = (uint16_t)idx;
+      cnt += __popc(m);
+    }
+    return cnt;
+  };
+  __syncwarp();   // the previous list is no longer read
+  ShellList L;
+  L.det = buf;
+  L.ndet = build(s.det, buf);
+  L.j3 = buf + s.det.nshell;
+  L.nj3 = s.has_j3 ? build(s.j3, buf + s.det.nshell) : 0;
+  __syncwarp();
+  return L;
+}
+
 // block energy of the mixed form right after a build: the AO values, gradients
 // and Laplacians of basis b re-evaluated in FP64 at r_e (the float tables hold
 // them rounded, which alone moves E_L by about 1e-5 Ha on the 30-electron ring)
@@ -1482,15 +1558,16 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
 // One warp; the lanes split the shells; every lane returns (value, grad x, y, z,
 // Laplacian) of phi . v.
 template <class Tab>
-__device__ void dot_vgl_fp64(const Sys& s, const Basis& b, const double* re, const Tab* v, const float* vlo, double* out) {
+__device__ void dot_vgl_fp64(const Sys& s, const Basis& b, const double* re, const Tab* v, const float* vlo, double* out,
+                             const uint16_t* lst, int nl) {
   const int lane = threadIdx.x & 31;
   double a0 = 0.0, ax = 0.0, ay = 0.0, az = 0.0, al = 0.0;
   auto f = [&](int a, double val, double gx, double gy, double gz, double lap) {
     const double t = (double)v[a] + (double)vlo[a];
     a0 += val * t; ax += gx * t; ay += gy * t; az += gz * t; al += lap * t;
   };
-  for (int idx = lane; idx < b.nshell; idx += 32) {
-    const int sh = b.shells[kSh * idx + 7];
+  for (int q = lane; q < nl; q += 32) {   // the shells within reach of r_e
+    const int sh = b.shells[kSh * lst[q] + 7];
     double dx, dy, dz;
     disp<double>(s.atom_pos, b.shells[kSh * sh], re[0], re[1], re[2], dx, dy, dz);
     shell_vgl_d<double>(b, sh, dx, dy, dz, f);
@@ -1536,8 +1613,10 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
     const float* Tlo = kMayRefine ? (up ? k.tlo_up : k.tlo_dn) : nullptr;
     double dt[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, d3[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    ShellList lst{nullptr, 0, nullptr, 0};
     if (kMayRefine && Tlo) {
-      dot_vgl_fp64(s, s.det, k.r + 3 * e, Trow, Tlo + (size_t)i * A, dt);
+      lst = shell_list(k, t, e, 1e-3f, kShReach64, false);
+      dot_vgl_fp64(s, s.det, k.r + 3 * e, Trow, Tlo + (size_t)i * A, dt, lst.det, lst.ndet);
     } else {
       for (int a = lane; a < A; a += 32) {
         const Ar tv = (Ar)Trow[a];
@@ -1548,7 +1627,7 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
       }
     }
     if (kMayRefine && Tlo && k.h3lo) {
-      dot_vgl_fp64(s, s.j3, k.r + 3 * e, k.h3 + (size_t)e * A3, k.h3lo + (size_t)e * A3, d3);
+      dot_vgl_fp64(s, s.j3, k.r + 3 * e, k.h3 + (size_t)e * A3, k.h3lo + (size_t)e * A3, d3, lst.j3, lst.nj3);
     } else if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
@@ -1630,11 +1709,15 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 template <int P, class R, class Tab, class Acc>
 __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz,
                              typename AccTraits<Acc>::out* ratio, float* mag = nullptr, const float* sl = nullptr,
-                             bool dlt = false, unsigned vneg = 0u) {
+                             bool dlt = false, unsigned vneg = 0u, const ShellList* lst = nullptr) {
   using Out = typename AccTraits<Acc>::out;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
   const bool up = e < s.n_up;
+  // the shells walked: those in the list, else all
+  const int ndet = lst ? lst->ndet : s.det.nshell, nj3 = lst ? lst->nj3 : (s.has_j3 ? s.j3.nshell : 0);
+  auto det_at = [&](int q) { return lst ? (int)lst->det[q] : q; };
+  auto j3_at = [&](int q) { return lst ? (int)lst->j3[q] : q; };
   const int i = up ? e : e - s.n_up;
   const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
   // block energy on fresh tables (mixed form): the T row's low parts as well
@@ -1667,8 +1750,10 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     // compensated energy: displacements as float pairs (the low part from the
     // double positions), squared distances as float pairs
     float dxl[P], dyl[P], dzl[P], r2h[P], r2l[P];
-    auto shells = [&](const Basis& b, const Tab* v, Acc* acc, const float* vlo) {
-      for (int idx = lane; idx < b.nshell; idx += 32) {
+    auto shells = [&](const Basis& b, const Tab* v, Acc* acc, const float* vlo, bool isj3) {
+      const int nsh = isj3 ? nj3 : ndet;
+      for (int q = lane; q < nsh; q += 32) {
+        const int idx = isj3 ? j3_at(q) : det_at(q);
         const int sh = b.shells[kSh * idx + 7];
         const int atom = b.shells[kSh * sh];
         R x, y, z;
@@ -1687,11 +1772,11 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
         else shell_dot_pts_ff<P>(b, sh, dx, dy, dz, r2h, r2l, v, acc);
       }
     };
-    shells(s.det, Trow, det, Tlo);
-    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, hlo);
+    shells(s.det, Trow, det, Tlo, false);
+    if (s.has_j3) shells(s.j3, k.h3 + (size_t)e * k.A3, dj, hlo, true);
   } else {
-    for (int idx = lane; idx < s.det.nshell; idx += 32) {
-      const int sh = s.det.shells[kSh * idx + 7];   // (l, nprim)-sorted order
+    for (int q = lane; q < ndet; q += 32) {
+      const int sh = s.det.shells[kSh * det_at(q) + 7];   // (l, nprim)-sorted order
       R x, y, z;
       dnuc(s.det.shells[kSh * sh], x, y, z);
 #pragma unroll
@@ -1705,8 +1790,8 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
     }
     if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * k.A3;
-      for (int idx = lane; idx < s.j3.nshell; idx += 32) {
-        const int sh = s.j3.shells[kSh * idx + 7];
+      for (int q = lane; q < nj3; q += 32) {
+        const int sh = s.j3.shells[kSh * j3_at(q) + 7];
         R x, y, z;
         dnuc(s.j3.shells[kSh * sh], x, y, z);
 #pragma unroll
@@ -1786,7 +1871,7 @@ struct Cancellation {
 // AO values off by a few 1e-8 relative, what the others leave is below about
 // 3e-7 Ha per electron.
 #ifndef JQMC_ECP_REFINE_MAG
-#define JQMC_ECP_REFINE_MAG 16.0
+#define JQMC_ECP_REFINE_MAG 32.0
 #endif
 constexpr double kEcpRefineMag = JQMC_ECP_REFINE_MAG;
 
@@ -1813,6 +1898,12 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
     const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
     const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
     float vmag = 0.f;
+    // the electron's mesh points lie within alat (lattice) and 2 |r_e - R_I|
+    // (quadrature sphere around its nearest nucleus I) of r_e
+    const bool lattice = kinetic && !refine;
+    const float margin = fmaxf(lattice ? (float)alat : 0.f, ecp ? 2.f * (float)t.edist[e] : 0.f) + 1e-3f;
+    const ShellList lst = shell_list(k, t, e, margin, sizeof(R) == sizeof(float) && !kErr ? kShReachF : kShReach64,
+                                     sizeof(R) == sizeof(float) && t.dA != nullptr);
     if (e + nw < N) {   // this warp's next electron: its T row, J3 field and displacements
       const int en = e + nw;
       const Tab* Tn = (en < s.n_up ? k.Tup + (size_t)en * k.A : k.Tdn + (size_t)(en - s.n_up) * k.A);
@@ -1823,7 +1914,7 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
         prefetch_l2(t.dE + (size_t)en * N * 3, (size_t)N * 12, lane);
       }
     }
-    for (int c = kinetic && !refine ? 0 : nkc; c < nchunk; ++c) {
+    for (int c = lattice ? 0 : nkc; c < nchunk; ++c) {
       // lane p < P sets up point p, then every lane receives all P moves.  The
       // float form builds them from the float rotation, quadrature directions
       // and displacement cache, so that the chunk issues no FP64 instruction.
@@ -1912,9 +2003,9 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
           sl[P + p] = __shfl_sync(0xffffffffu, myl, p);
           sl[2 * P + p] = __shfl_sync(0xffffffffu, mzl, p);
         }
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg, &lst);
       } else {
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg, &lst);
       }
       if (lane < np) {
         Out rr = Out(0);
@@ -3557,10 +3648,31 @@ int launch_check(const void* fn, int smem) {
   return JQMC_OK;
 }
 
+// Square of the radius beyond which sum_q |c_q| max(r, 1)^l exp(-Z_q r^2), a
+// bound on every AO of shell k (|solid harmonic| <= r^l with the prefactor in
+// c_q; Cartesian monomials likewise), stays below e^-C.  The bound decreases
+// for r past its last crossing, found on a 0.05-bohr grid out to 100 bohr; the
+// radius is rounded up by one grid step.
+double shell_reach2(const jqmc_basis_desc& b, int k, double C) {
+  const int32_t* sh = b.shells + 8 * (size_t)k;
+  const int l = sh[1], np = sh[2], p0 = sh[3];
+  const double lim = std::exp(-C);
+  double last = 0.0;
+  for (int i = 0; i <= 2000; ++i) {
+    const double r = 0.05 * i;
+    double f = 0.0;
+    for (int q = 0; q < np; ++q) f += std::fabs(b.prims[2 * (p0 + q) + 1]) * std::exp(-b.prims[2 * (p0 + q)] * r * r);
+    f *= std::pow(r > 1.0 ? r : 1.0, l);
+    if (f >= lim) last = r;
+  }
+  const double R = last + 0.05;
+  return R * R;
+}
+
 int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const double* d_draw, double alat, double E_scf,
                  double* d_w, double* d_eL, double* d_vd, void* stream, TauArgs ta = TauArgs{nullptr, nullptr, nullptr}) {
   KParams P = make_params(sys, w);
-  const int smem = P.ml.bytes;
+  const int smem = terms_smem(P.ml, LrdmcShape<double, double>::threads);   // 4-warp kernels
   if (is_mixed(w->precision)) {
     // projections: float arithmetic on the float tables.  The local energy of a
     // block (K == 0): float values with compensated float-float sums, then FP64
@@ -3569,9 +3681,10 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
     // (JQMC_PREC_MIXED_FASTE)
     if (K > 0) {
       auto fn = k_lrdmc<float, float, float>;
-      int rc = launch_check((const void*)fn, smem);
+      const int smem_p = terms_smem(P.ml, LrdmcShape<float, float>::threads);
+      int rc = launch_check((const void*)fn, smem_p);
       if (rc) return rc;
-      fn<<<w->nwalk, LrdmcShape<float, float>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
+      fn<<<w->nwalk, LrdmcShape<float, float>::threads, smem_p, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
     } else {
       const bool gate = w->precision == JQMC_PREC_MIXED;
       auto fn = k_lrdmc<float, float, F2>;
@@ -3708,6 +3821,9 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       for (int f = 0; f < 8; ++f) dev[(size_t)kSh * k + f] = rows[8 * k + f];
       if (rows[8 * k + 7] == 1) dev[(size_t)kSh * k + 6] += kCartBase;   // the Cartesian kind moves to field 6
       dev[(size_t)kSh * k + 7] = ord[k];
+      const float rf = (float)shell_reach2(b, k, kReachFloat), r64 = (float)shell_reach2(b, k, kReachFp64);
+      std::memcpy(&dev[(size_t)kSh * k + kShReachF], &rf, 4);
+      std::memcpy(&dev[(size_t)kSh * k + kShReach64], &r64, 4);
     }
     return dev;
   };
@@ -3982,7 +4098,7 @@ int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const doubl
                       void* stream) {
   if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_angles || !d_el || !(alat > 0.0)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
-  const int smem = P.ml.bytes;
+  const int smem = terms_smem(P.ml, 128);
   int rc = launch_check((const void*)k_kinetic_mesh, smem);
   if (rc) return rc;
   k_kinetic_mesh<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, alat, d_el);
@@ -4048,7 +4164,7 @@ int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double
   if (!walkers_ok(sys, w) || !d_angles || !d_eL || !d_wL) return JQMC_E_ARG;
   if (w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
-  const int smem = P.ml.bytes;
+  const int smem = terms_smem(P.ml, 128);
   int rc = launch_check((const void*)k_vmc_measure, smem);
   if (rc) return rc;
   k_vmc_measure<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, eps_AS, d_eL, d_wL);
