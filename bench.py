@@ -284,6 +284,47 @@ def adjoint_leg(stream, dev, peak64, hbm_peak, walkers: int = 8192, reps: int = 
     return out
 
 
+def forces_leg(stream, walkers: int = 8192):
+    """Config 3's forces on the 12-nucleus ring with 8192 walkers: d ln psi/dR
+    (one jqmc_dlnpsi_dR launch) and dE_L/dR by five-point differences of the
+    FP64 VMC local energy (12 natom displaced systems, built once, each a walker
+    initialisation and an E_L launch per call)."""
+    import torch
+
+    from jqmc_gb300 import synthetic
+    from jqmc_gb300.engine import GpuSystem, WalkerSet
+    from jqmc_gb300.forces import ELGradientFD, dlnpsi_dR
+    syn = synthetic.ring12()
+    gs = GpuSystem(syn.hamiltonian)
+    r_up, r_dn = syn.initial_electrons(walkers, seed=78)
+    ws = WalkerSet(gs, r_up, r_dn)
+    angles = torch.as_tensor(np.random.default_rng(5).uniform(-np.pi, np.pi, (walkers, 3)), device=gs.device)
+    fd = ELGradientFD(syn.hamiltonian)
+    dlnpsi_dR(ws)
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    ms_psi, _ = timed(lambda: dlnpsi_dR(ws))
+    ms_el, g = timed(lambda: fd(r_up, r_dn, angles))
+    finite = bool(torch.isfinite(g).all())
+    out = {"workload": "ring12 forces (12 nuclei, 30 electrons), FP64", "walkers": walkers,
+           "dlnpsi_dR_ms": ms_psi, "dEL_dR_ms": ms_el, "el_evaluations_per_walker": 12 * int(fd.M),
+           "walker_forces_per_s": walkers / ((ms_psi + ms_el) / 1e3), "finite": finite,
+           "note": "CUDA events; dE_L/dR by differences of the GPU E_L (4 displaced systems per nucleus and axis), "
+                   "d ln psi/dR analytic (one launch); the displaced systems are created before timing"}
+    del ws, gs, fd
+    torch.cuda.empty_cache()
+    return out
+
+
 def batching_leg(nmol: int = 64, steps: int = 500, K: int = 50, fp64_steps: int = 50):
     """64 independent molecules (1-20 nuclei, Z_eff in {1, 4, 6}), walkers in
     proportion to the electron count (256-4096), VMC in the mixed precision:
@@ -670,6 +711,7 @@ def gpu_arm(a):
             return {"error": repr(ex)}
 
     adjoint = leg(lambda: adjoint_leg(stream, dev, peak64, peaks.get("hbm_gbs")), a.no_adjoint)
+    forces = leg(lambda: forces_leg(stream), a.no_adjoint)
     batching = leg(batching_leg, a.no_batching)
     vmc = leg(vmc_leg, a.no_vmc)
     config0 = leg(config0_leg, a.no_configs)
@@ -744,6 +786,7 @@ def gpu_arm(a):
                          "plain_fp64_kernel": {"bound": "fp64", "achieved": plain_ach, "peak": peak64, "frac": plain_ach / peak64,
                                                "avg_launch_ms": plain_ms, "unit": "GFLOP/s"}},
             "adjoint": adjoint,
+            "forces": forces,
             "batching": batching,
             "vmc": vmc,
             "config0_vmc_water": config0,

@@ -176,16 +176,15 @@ struct MeshExp<float, true> {
   static __device__ __forceinline__ float em1(float x) { return expm1f(x); }
 };
 
-// Device shell records: the 8 ints of jqmc_basis_desc, then the squares of the
-// shell's two reach radii as float bits (field 8: float mesh ratios, field 9:
-// FP64 and compensated ones), then one int of padding, so that lanes reading one
-// field of consecutive shells hit distinct shared-memory banks (a stride of 11
-// words is coprime with the 32 banks).  Beyond its reach radius from the shell's
-// nucleus, every AO of the shell is below e^-kReachFloat (e^-kReachFp64) in
-// magnitude for unit table entries: sum_q |c_q| max(r, 1)^l e^(-Z_q r^2).
-constexpr int kSh = 11;
-constexpr int kShReachF = 8, kShReach64 = 9;
-constexpr double kReachFloat = 25.0, kReachFp64 = 40.0;
+// Device shell records: the 8 ints of jqmc_basis_desc, then the square of the
+// shell's reach radius as float bits (field 8), so that lanes reading one field
+// of consecutive shells hit distinct shared-memory banks (a stride of 9 words is
+// coprime with the 32 banks).  Beyond its reach radius from the shell's nucleus,
+// every AO of the shell is below e^-kReach in magnitude for unit table entries:
+// sum_q |c_q| max(r, 1)^l e^(-Z_q r^2).
+constexpr int kSh = 9;
+constexpr int kShReach = 8;
+constexpr double kReach = 40.0;
 
 struct Basis {
   int nshell, nao, nprim;
@@ -693,13 +692,18 @@ __device__ __forceinline__ void ao_visit_vgl(const Basis& b, const double* apos,
   }
 }
 
-// all AO values at one point into out[] (block-cooperative, split by shell; no sync)
+// all AO values at one point into out[] (block-cooperative, split by shell; no
+// sync).  Shells whose reach (e^-40) ends short of the point write zeros.
 template <class R, class V>
 __device__ void ao_fill_block(const Basis& b, const double* apos, double px, double py, double pz, V* out) {
   auto f = [&](int a, R val) { out[a] = (V)val; };
   for (int s = threadIdx.x; s < b.nshell; s += blockDim.x) {
     R dx, dy, dz;
     disp<R>(apos, b.shells[kSh * s], px, py, pz, dx, dy, dz);
+    if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(b.shells[kSh * s + kShReach])) {
+      for (int a = 0; a < b.shells[kSh * s + 5]; ++a) out[b.shells[kSh * s + 4] + a] = (V)0;
+      continue;
+    }
     shell_val_d<R>(b, s, dx, dy, dz, f);
   }
 }
@@ -903,6 +907,7 @@ __device__ void rotation(double a, double b, double g, double* R) {
 // Derivative tables of one electron at (x, y, z), computed in double and stored
 // in Tab: dp[c*A + a] = (grad x, y, z, lap)_c of geminal AO a; dp3[c*A3 + a] =
 // (value, grad x, y, z, lap)_c of J3 AO a.  Block-cooperative over shells, no sync.
+// Shells whose reach (e^-40 for the values) ends short of the point write zeros.
 template <class Tab>
 __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp, Tab* dp3) {
   const int A = s.det.nao;
@@ -912,6 +917,10 @@ __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp
     auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
       dp[a] = (Tab)gx; dp[A + a] = (Tab)gy; dp[2 * A + a] = (Tab)gz; dp[3 * A + a] = (Tab)lp;
     };
+    if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.det.shells[kSh * sh + kShReach])) {
+      for (int a = 0; a < s.det.shells[kSh * sh + 5]; ++a) f(s.det.shells[kSh * sh + 4] + a, 0.0, 0.0, 0.0, 0.0, 0.0);
+      continue;
+    }
     shell_vgl_d<double>(s.det, sh, dx, dy, dz, f);
   }
   if (s.has_j3) {
@@ -922,6 +931,10 @@ __device__ void fill_dtables(const Sys& s, double x, double y, double z, Tab* dp
       auto f = [&](int a, double v, double gx, double gy, double gz, double lp) {
         dp3[a] = (Tab)v; dp3[A3 + a] = (Tab)gx; dp3[2 * A3 + a] = (Tab)gy; dp3[3 * A3 + a] = (Tab)gz; dp3[4 * A3 + a] = (Tab)lp;
       };
+      if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.j3.shells[kSh * sh + kShReach])) {
+        for (int a = 0; a < s.j3.shells[kSh * sh + 5]; ++a) f(s.j3.shells[kSh * sh + 4] + a, 0.0, 0.0, 0.0, 0.0, 0.0);
+        continue;
+      }
       shell_vgl_d<double>(s.j3, sh, dx, dy, dz, f);
     }
   }
@@ -1376,16 +1389,17 @@ struct Terms {
   double* el;     // 6N kinetic lattice elements
   double* V;      // nv*N non-local ECP elements
   float* vm;      // N  compensated energy: sum over the electron's ECP points of |w_v| M_v
-  uint16_t* act;  // 8 warps x (det + J3 shells): each warp's list of shells within reach
+  uint16_t* act;  // kMaxWarps x (det + J3 shells): each warp's list of shells within reach
   double* R;      // 9 rotation
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
 };
 
-constexpr int kMaxWarps = 8;   // warps per CTA of the walker kernels that use the terms layout
-static_assert(LrdmcShape<float, float>::threads / 32 <= kMaxWarps && LrdmcShape<double, double>::threads / 32 <= kMaxWarps,
-              "shell-list slots for every warp");
+// Warps per CTA of the walker kernels with FP64 mesh ratios (the only ones that
+// keep shell lists); the float projection launches without the list slots.
+constexpr int kMaxWarps = 4;
+static_assert(LrdmcShape<double, double>::threads / 32 <= kMaxWarps, "shell-list slots for every warp");
 
 struct TermsLayout {
   int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, off_act,
@@ -1417,7 +1431,8 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   return L;
 }
 
-// Dynamic shared memory of a walker kernel of `threads` threads per CTA.
+// Dynamic shared memory of a walker kernel whose FP64 mesh ratios run in
+// `threads` threads per CTA (0: no FP64 mesh ratios, no shell lists).
 int terms_smem(const TermsLayout& L, int threads) { return L.bytes - (kMaxWarps - threads / 32) * L.act_warp; }
 
 // Displacement caches bigger than this live in global memory (per walker).
@@ -1499,9 +1514,8 @@ __device__ void dcache_update(const Work<Tab>& k, Terms& t, int e) {
 // The shells (positions in the (l, nprim)-sorted order) whose reach radius
 // extends to within `margin` of electron e: every mesh point p of the electron
 // with |p - r_e| <= margin is then beyond the reach of every other shell, whose
-// AOs are below e^-kReachFloat (field kShReachF) or e^-kReachFp64 (kShReach64)
-// there and are left out of the ratio.  One warp; the list goes to the warp's
-// slot of t.act.
+// AOs are below e^-kReach there and are left out of the ratio.  One warp; the
+// list goes to the warp's slot of t.act.
 struct ShellList {
   const uint16_t* det;
   int ndet;
@@ -1510,11 +1524,10 @@ struct ShellList {
 };
 
 template <class Tab>
-__device__ ShellList shell_list(const Work<Tab>& k, const Terms& t, int e, float margin, int field, bool rel) {
+__device__ ShellList shell_list(const Work<Tab>& k, const Terms& t, int e, float margin) {
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint16_t* buf = t.act + (size_t)wid * (s.det.nshell + (s.has_j3 ? s.j3.nshell : 0));
-  const float* dAe = rel ? t.dA + (size_t)e * s.natom * 3 : nullptr;
   auto build = [&](const Basis& b, uint16_t* out) -> int {
     int cnt = 0;
     for (int base = 0; base < b.nshell; base += 32) {
@@ -1523,17 +1536,10 @@ __device__ ShellList shell_list(const Work<Tab>& k, const Terms& t, int e, float
       if (idx < b.nshell) {
         const int sh = b.shells[kSh * idx + 7];
         const int atom = b.shells[kSh * sh];
-        float d2;
-        if (rel) {
-          const float x = dAe[3 * atom], y = dAe[3 * atom + 1], z = dAe[3 * atom + 2];
-          d2 = x * x + y * y + z * z;
-        } else {
-          const double x = k.r[3 * e] - s.atom_pos[3 * atom], y = k.r[3 * e + 1] - s.atom_pos[3 * atom + 1];
-          const double z = k.r[3 * e + 2] - s.atom_pos[3 * atom + 2];
-          d2 = (float)(x * x + y * y + z * z);
-        }
-        const float dd = fmaxf(sqrtf(d2) - margin, 0.f);
-        keep = dd * dd < __int_as_float(b.shells[kSh * sh + field]);
+        const double x = k.r[3 * e] - s.atom_pos[3 * atom], y = k.r[3 * e + 1] - s.atom_pos[3 * atom + 1];
+        const double z = k.r[3 * e + 2] - s.atom_pos[3 * atom + 2];
+        const float dd = fmaxf(sqrtf((float)(x * x + y * y + z * z)) - margin, 0.f);
+        keep = dd * dd < __int_as_float(b.shells[kSh * sh + kShReach]);
       }
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (keep) out[cnt + __popc(m & ((1u << lane) - 1u))] = (uint16_t)idx;
@@ -1558,16 +1564,15 @@ __device__ ShellList shell_list(const Work<Tab>& k, const Terms& t, int e, float
 // One warp; the lanes split the shells; every lane returns (value, grad x, y, z,
 // Laplacian) of phi . v.
 template <class Tab>
-__device__ void dot_vgl_fp64(const Sys& s, const Basis& b, const double* re, const Tab* v, const float* vlo, double* out,
-                             const uint16_t* lst, int nl) {
+__device__ void dot_vgl_fp64(const Sys& s, const Basis& b, const double* re, const Tab* v, const float* vlo, double* out) {
   const int lane = threadIdx.x & 31;
   double a0 = 0.0, ax = 0.0, ay = 0.0, az = 0.0, al = 0.0;
   auto f = [&](int a, double val, double gx, double gy, double gz, double lap) {
     const double t = (double)v[a] + (double)vlo[a];
     a0 += val * t; ax += gx * t; ay += gy * t; az += gz * t; al += lap * t;
   };
-  for (int q = lane; q < nl; q += 32) {   // the shells within reach of r_e
-    const int sh = b.shells[kSh * lst[q] + 7];
+  for (int idx = lane; idx < b.nshell; idx += 32) {
+    const int sh = b.shells[kSh * idx + 7];
     double dx, dy, dz;
     disp<double>(s.atom_pos, b.shells[kSh * sh], re[0], re[1], re[2], dx, dy, dz);
     shell_vgl_d<double>(b, sh, dx, dy, dz, f);
@@ -1613,10 +1618,8 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
     constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
     const float* Tlo = kMayRefine ? (up ? k.tlo_up : k.tlo_dn) : nullptr;
     double dt[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, d3[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    ShellList lst{nullptr, 0, nullptr, 0};
     if (kMayRefine && Tlo) {
-      lst = shell_list(k, t, e, 1e-3f, kShReach64, false);
-      dot_vgl_fp64(s, s.det, k.r + 3 * e, Trow, Tlo + (size_t)i * A, dt, lst.det, lst.ndet);
+      dot_vgl_fp64(s, s.det, k.r + 3 * e, Trow, Tlo + (size_t)i * A, dt);
     } else {
       for (int a = lane; a < A; a += 32) {
         const Ar tv = (Ar)Trow[a];
@@ -1627,7 +1630,7 @@ __device__ void electron_terms(Work<Tab>& k, Terms& t, double alat) {
       }
     }
     if (kMayRefine && Tlo && k.h3lo) {
-      dot_vgl_fp64(s, s.j3, k.r + 3 * e, k.h3 + (size_t)e * A3, k.h3lo + (size_t)e * A3, d3, lst.j3, lst.nj3);
+      dot_vgl_fp64(s, s.j3, k.r + 3 * e, k.h3 + (size_t)e * A3, k.h3lo + (size_t)e * A3, d3);
     } else if (s.has_j3) {
       const Tab* h = k.h3 + (size_t)e * A3;
       const Tab* q = k.dphi3 + (size_t)e * 5 * A3;
@@ -1898,12 +1901,19 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
     const bool ecp = s.ecp_flag && s.ecp_maxl1[atom] > 0;
     const int nchunk = nkc + (ecp ? (nv + P - 1) / P : 0);
     float vmag = 0.f;
-    // the electron's mesh points lie within alat (lattice) and 2 |r_e - R_I|
-    // (quadrature sphere around its nearest nucleus I) of r_e
     const bool lattice = kinetic && !refine;
-    const float margin = fmaxf(lattice ? (float)alat : 0.f, ecp ? 2.f * (float)t.edist[e] : 0.f) + 1e-3f;
-    const ShellList lst = shell_list(k, t, e, margin, sizeof(R) == sizeof(float) && !kErr ? kShReachF : kShReach64,
-                                     sizeof(R) == sizeof(float) && t.dA != nullptr);
+    // FP64 ratios walk only the shells within reach of the electron's mesh
+    // points, which lie within alat (lattice) and 2 |r_e - R_I| (quadrature
+    // sphere around its nearest nucleus I) of r_e.  The float ratios walk every
+    // shell: there the list costs more than the AO work it saves (measured on
+    // the chain: 582 ms with lists against 486 ms without for 40 projections of
+    // 4096 walkers; the FP64 projection gains 18 %).
+    ShellList lst{nullptr, 0, nullptr, 0};
+    if constexpr (sizeof(R) == sizeof(double)) {
+      const float margin = fmaxf(lattice ? (float)alat : 0.f, ecp ? 2.f * (float)t.edist[e] : 0.f) + 1e-3f;
+      lst = shell_list(k, t, e, margin);
+    }
+    const ShellList* lstp = sizeof(R) == sizeof(double) ? &lst : nullptr;
     if (e + nw < N) {   // this warp's next electron: its T row, J3 field and displacements
       const int en = e + nw;
       const Tab* Tn = (en < s.n_up ? k.Tup + (size_t)en * k.A : k.Tdn + (size_t)(en - s.n_up) * k.A);
@@ -2003,9 +2013,9 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
           sl[P + p] = __shfl_sync(0xffffffffu, myl, p);
           sl[2 * P + p] = __shfl_sync(0xffffffffu, mzl, p);
         }
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg, &lst);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg, lstp);
       } else {
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg, &lst);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg, lstp);
       }
       if (lane < np) {
         Out rr = Out(0);
@@ -2279,6 +2289,8 @@ __global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long lon
     for (int sh = threadIdx.x; sh < s.det.nshell; sh += blockDim.x) {
       double dx, dy, dz;
       disp<double>(s.atom_pos, s.det.shells[kSh * sh], px, py, pz, dx, dy, dz);
+      // beyond the shell's reach (e^-40) its AOs stay zero
+      if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.det.shells[kSh * sh + kShReach])) continue;
       shell_val_d<double>(s.det, sh, dx, dy, dz, f);
     }
   }
@@ -3681,7 +3693,7 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
     // (JQMC_PREC_MIXED_FASTE)
     if (K > 0) {
       auto fn = k_lrdmc<float, float, float>;
-      const int smem_p = terms_smem(P.ml, LrdmcShape<float, float>::threads);
+      const int smem_p = terms_smem(P.ml, 0);   // float mesh ratios only
       int rc = launch_check((const void*)fn, smem_p);
       if (rc) return rc;
       fn<<<w->nwalk, LrdmcShape<float, float>::threads, smem_p, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
@@ -3821,9 +3833,8 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       for (int f = 0; f < 8; ++f) dev[(size_t)kSh * k + f] = rows[8 * k + f];
       if (rows[8 * k + 7] == 1) dev[(size_t)kSh * k + 6] += kCartBase;   // the Cartesian kind moves to field 6
       dev[(size_t)kSh * k + 7] = ord[k];
-      const float rf = (float)shell_reach2(b, k, kReachFloat), r64 = (float)shell_reach2(b, k, kReachFp64);
-      std::memcpy(&dev[(size_t)kSh * k + kShReachF], &rf, 4);
-      std::memcpy(&dev[(size_t)kSh * k + kShReach64], &r64, 4);
+      const float r2 = (float)shell_reach2(b, k, kReach);
+      std::memcpy(&dev[(size_t)kSh * k + kShReach], &r2, 4);
     }
     return dev;
   };
