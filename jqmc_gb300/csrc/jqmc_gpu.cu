@@ -2398,6 +2398,58 @@ __device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J*
   }
 }
 
+// The J3 field of the mixed rebuild with the walker's rebuild scratch (free
+// after the T phase) as work space, all electrons at once (same result as
+// j3_field up to the order of the FP64 sums):
+//   1. phi3(r_e) of every electron into U (N x A3), all (electron, shell) items;
+//   2. per column c, over the electrons in order: u_e = prefix_e (+ tot_up for a
+//      down electron), v_e = tot_same - prefix_e - phi3_e (+ tot_dn for an up
+//      electron), prefix_e the sum of phi3 over the same-spin electrons before e;
+//   3. h_e[c] = j[c] + sum_cp J[cp][c] u_e[cp] + J[c][cp] v_e[cp] for all (e, c),
+//      a warp over 32 consecutive c of one e.
+// Written in Tab with the low parts in hlo (when given).  Needs 2 N A3 doubles.
+template <class Tab>
+__device__ void j3_field_rows(const Sys& s, Tab* h, float* hlo, const double* r, double* U) {
+  const int N = s.N, A3 = s.j3.nao, nsh = s.j3.nshell, nu = s.n_up;
+  double* V = U + (size_t)N * A3;
+  for (int it = threadIdx.x; it < N * nsh; it += blockDim.x) {
+    const int e = it / nsh, sh = it - e * nsh;
+    double* row = U + (size_t)e * A3;
+    double dx, dy, dz;
+    disp<double>(s.atom_pos, s.j3.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+    if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.j3.shells[kSh * sh + kShReach])) {
+      for (int a = 0; a < s.j3.shells[kSh * sh + 5]; ++a) row[s.j3.shells[kSh * sh + 4] + a] = 0.0;
+      continue;
+    }
+    auto f = [&](int a, double v) { row[a] = v; };
+    shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < A3; c += blockDim.x) {
+    double tu = 0.0, td = 0.0;
+    for (int e = 0; e < N; ++e) (e < nu ? tu : td) += U[(size_t)e * A3 + c];
+    double pfx = 0.0;
+    for (int e = 0; e < N; ++e) {
+      if (e == nu) pfx = 0.0;
+      const bool up = e < nu;
+      const double phi = U[(size_t)e * A3 + c];
+      U[(size_t)e * A3 + c] = up ? pfx : pfx + tu;
+      V[(size_t)e * A3 + c] = up ? (tu - pfx - phi) + td : td - pfx - phi;
+      pfx += phi;
+    }
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < N * A3; it += blockDim.x) {
+    const int e = it / A3, c = it - e * A3;
+    const double* u = U + (size_t)e * A3;
+    const double* v = V + (size_t)e * A3;
+    double acc = s.j3vec[c];
+    for (int cp = 0; cp < A3; ++cp) acc += s.j3mat[(size_t)cp * A3 + c] * u[cp] + s.j3matT[(size_t)cp * A3 + c] * v[cp];
+    h[it] = (Tab)acc;
+    if (hlo) hlo[it] = (float)(acc - (double)(Tab)acc);
+  }
+}
+
 // Walker initialisation in FP64: G, G^-1 (Gauss-Jordan, partial pivoting), T
 // tables and J3 field, written in the table type Tab.  M_up / M_dn go to the
 // double scratch (for Tab == double the T buffers themselves).
@@ -2452,34 +2504,72 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
     __syncthreads();
   }
   if constexpr (sizeof(Tab) == sizeof(float)) {
-    // mixed form: M_up / M_dn are float-float pairs from k_rebuild_m; G column j
-    // = M_up phi_dn(r_j) by compensated float-float dot products (one warp per row)
+    // mixed form: M_up / M_dn are float-float pairs from k_rebuild_m (or the
+    // tensor-core GEMM).  phi_dn(r_j) of every down electron in FP64, split into
+    // float pairs over the T buffers (hi in T_up, lo in T_dn: free until the T
+    // phase), all (electron, shell) items at once; then G[i][j] = M_up[i] .
+    // phi_dn[j] by compensated float-float dots, 2 x 4 (i, j) per warp
     const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
-    float2* vec2 = reinterpret_cast<float2*>(vec);
+    float* ph = reinterpret_cast<float*>(Tup);
+    float* pl = reinterpret_cast<float*>(Tdn);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = 0; j < s.n_dn; ++j) {
-      const int e = s.n_up + j;
-      ao_fill_block<double, double>(s.det, s.atom_pos, r[3 * e], r[3 * e + 1], r[3 * e + 2], vec);
-      __syncthreads();
-      for (int a = threadIdx.x; a < A; a += blockDim.x) {   // split in place (same slot)
-        const double v = vec[a];
-        const float hi = (float)v;
-        vec2[a] = make_float2(hi, (float)(v - (double)hi));
-      }
-      __syncthreads();
-      for (int i = wid; i < n; i += nw) {
-        F2 acc;
-        acc_zero(acc);
-        const float2* row = Mup2 + (size_t)i * A;
-        for (int a = lane; a < A; a += 32) {
-          const float2 m = row[a], p = vec2[a];
-          dot2_step(acc.s, acc.c, m.x, m.y, p.x, p.y);
+    const int nsh = s.det.nshell, nd = s.n_dn;
+    for (int it = threadIdx.x; it < nd * nsh; it += blockDim.x) {
+      const int j = it / nsh, sh = it - j * nsh, e = s.n_up + j;
+      float* hi = ph + (size_t)j * A;
+      float* lo = pl + (size_t)j * A;
+      double dx, dy, dz;
+      disp<double>(s.atom_pos, s.det.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
+      if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.det.shells[kSh * sh + kShReach])) {
+        for (int a = 0; a < s.det.shells[kSh * sh + 5]; ++a) {
+          hi[s.det.shells[kSh * sh + 4] + a] = 0.f;
+          lo[s.det.shells[kSh * sh + 4] + a] = 0.f;
         }
-        const double g = acc_out(acc);
-        if (lane == 0) Gd[i * n + j] = g;
+        continue;
       }
-      __syncthreads();
+      auto f = [&](int a, double v) {
+        const float h = (float)v;
+        hi[a] = h;
+        lo[a] = (float)(v - (double)h);
+      };
+      shell_val_d<double>(s.det, sh, dx, dy, dz, f);
     }
+    __syncthreads();
+    constexpr int BI = 2, BJ = 4;   // (i, j) block of one warp
+    const int nbi = (n + BI - 1) / BI, nbj = (nd + BJ - 1) / BJ;
+    for (int blk = wid; blk < nbi * nbj; blk += nw) {
+      const int i0 = BI * (blk / nbj), j0 = BJ * (blk % nbj);
+      F2 acc[BI][BJ];
+#pragma unroll
+      for (int u = 0; u < BI; ++u)
+#pragma unroll
+        for (int v = 0; v < BJ; ++v) acc_zero(acc[u][v]);
+      int ri[BI], rj[BJ];
+#pragma unroll
+      for (int u = 0; u < BI; ++u) ri[u] = min(i0 + u, n - 1) * A;
+#pragma unroll
+      for (int v = 0; v < BJ; ++v) rj[v] = min(j0 + v, nd - 1) * A;
+      for (int a = lane; a < A; a += 32) {
+        float2 m[BI];
+        float xh[BJ], xl[BJ];
+#pragma unroll
+        for (int u = 0; u < BI; ++u) m[u] = Mup2[ri[u] + a];
+#pragma unroll
+        for (int v = 0; v < BJ; ++v) { xh[v] = ph[rj[v] + a]; xl[v] = pl[rj[v] + a]; }
+#pragma unroll
+        for (int u = 0; u < BI; ++u)
+#pragma unroll
+          for (int v = 0; v < BJ; ++v) dot2_step(acc[u][v].s, acc[u][v].c, m[u].x, m[u].y, xh[v], xl[v]);
+      }
+#pragma unroll
+      for (int u = 0; u < BI; ++u)
+#pragma unroll
+        for (int v = 0; v < BJ; ++v) {
+          const double g = acc_out(acc[u][v]);
+          if (lane == 0 && i0 + u < n && j0 + v < nd) Gd[(i0 + u) * n + j0 + v] = g;
+        }
+    }
+    __syncthreads();
   } else {
     for (int j = 0; j < s.n_dn; ++j) {
       const int e = s.n_up + j;
@@ -2664,6 +2754,9 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
       j3_field<Tab, Tab>(s, h, r, reinterpret_cast<Tab*>(vec), j3m_of<Tab>(s), j3mT_of<Tab>(s));
       if (hlo)
         for (int c = threadIdx.x; c < N * A3; c += blockDim.x) hlo[c] = 0.f;
+    } else if (sizeof(Tab) == sizeof(float) && P.ws.scratch && (size_t)2 * N * A3 <= (size_t)2 * n * A) {
+      __syncthreads();   // the T phase has read the scratch
+      j3_field_rows<Tab>(s, h, hlo, r, P.ws.scratch + (size_t)w * 2 * n * A);
     } else {
       j3_field<double, Tab>(s, h, r, vec, s.j3mat, s.j3matT, hlo);
     }
@@ -2671,7 +2764,7 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
 }
 
 template <class Tab>
-__global__ void k_walker_init(KParams P, InitLayout IL, int mode) {
+__global__ void __launch_bounds__(128, 3) k_walker_init(KParams P, InitLayout IL, int mode) {
   extern __shared__ __align__(16) unsigned char smem[];
   walker_init_body<Tab>(P, blockIdx.x, IL, mode, smem);
 }

@@ -16,12 +16,22 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
+def _without_j3(ham):
+    """The Hamiltonian without its three-body Jastrow: M depends on the geminal
+    alone, and without J3 the build leaves M in the rebuild scratch (the J3
+    field's work space overwrites it otherwise)."""
+    from dataclasses import replace
+    wf = ham.wavefunction_data
+    jd = replace(wf.jastrow_data, jastrow_three_body_data=None)
+    return replace(ham, wavefunction_data=replace(wf, jastrow_data=jd))
+
+
 @pytest.mark.parametrize("name,walkers", [("water_like", 8), ("ring12", 40), ("chain32", 6)])
 def test_tensor_core_lambda_gemm_matches_fp64(name, walkers):
     from jqmc_gb300 import _lib, synthetic
     from jqmc_gb300.engine import GpuSystem, WalkerSet
     syn = synthetic.SYSTEMS[name]()
-    gs = GpuSystem(syn.hamiltonian)
+    gs = GpuSystem(_without_j3(syn.hamiltonian))
     assert _lib.lib().jqmc_tensor_core_rebuild(gs.handle) == 1
     n, A = gs.n_up, gs.A
     r_up, r_dn = syn.initial_electrons(walkers, seed=5)
