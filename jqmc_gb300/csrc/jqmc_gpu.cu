@@ -1394,21 +1394,16 @@ struct Terms {
   float* Rf;      // mixed form: 9 rotation + nv x (g_x, g_y, g_z, 1/|g|) rotated quadrature directions, float
   float* dA;      // mixed form: N*natom*3  float(r_e - R_a)
   float* dE;      // mixed form: N*N*3      float(r_e - r_m)
-  float* tst;     // float projection: per warp, its electron's T row and J3 field row (A + A3 floats;
-  int tst_stride; //   the same shared memory as act, which the float projection does not use)
 };
 
 // Warps per CTA of the walker kernels with FP64 mesh ratios (the only ones that
 // keep shell lists); the float projection launches without the list slots.
 constexpr int kMaxWarps = 4;
 static_assert(LrdmcShape<double, double>::threads / 32 <= kMaxWarps, "shell-list slots for every warp");
-// Warps per CTA of the float projection, each with a staging slot for its
-// electron's T row and J3 field row.
-constexpr int kStageWarps = LrdmcShape<float, float>::threads / 32;
 
 struct TermsLayout {
   int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, off_act,
-      act_warp, tst_stride, bytes;
+      act_warp, bytes;
 };
 
 // rel: reserve the float displacement caches of the mixed form in shared memory
@@ -1429,23 +1424,16 @@ TermsLayout terms_layout(const Sys& s, int base, bool rel) {
   L.off_Rf = o; o = align16(o + (9 + 4 * (s.nv > 0 ? s.nv : 1)) * 4);
   L.off_dA = o; o = align16(o + (rel ? N * s.natom * 3 * 4 : 0));
   L.off_dE = o; o = align16(o + (rel ? N * N * 3 * 4 : 0));
-  // last, shared by the shell lists of the FP64 mesh kernels and the row
-  // staging of the float projection (no kernel uses both); each kernel launches
-  // with what its warps use of it (terms_smem)
+  // last, so that a kernel of fewer warps launches with less of it
   L.act_warp = align16((s.det.nshell + (s.has_j3 ? s.j3.nshell : 0)) * 2);
-  L.tst_stride = (s.det.nao + (s.has_j3 ? s.j3.nao : 0) + 3) & ~3;
-  L.off_act = o;
-  o += std::max(kMaxWarps * L.act_warp, kStageWarps * L.tst_stride * 4);
+  L.off_act = o; o += kMaxWarps * L.act_warp;
   L.bytes = o;
   return L;
 }
 
-// Dynamic shared memory of a walker kernel with `list_threads` threads per CTA
-// running FP64 mesh ratios (shell lists) or `stage_threads` running the float
-// projection (row staging); 0 for neither.
-int terms_smem(const TermsLayout& L, int list_threads, int stage_threads) {
-  return L.off_act + std::max(list_threads / 32 * L.act_warp, stage_threads / 32 * L.tst_stride * 4);
-}
+// Dynamic shared memory of a walker kernel whose FP64 mesh ratios run in
+// `threads` threads per CTA (0: no FP64 mesh ratios, no shell lists).
+int terms_smem(const TermsLayout& L, int threads) { return L.bytes - (kMaxWarps - threads / 32) * L.act_warp; }
 
 // Displacement caches bigger than this live in global memory (per walker).
 constexpr int kDcacheSmemMax = 64 * 1024;
@@ -1466,8 +1454,6 @@ __device__ Terms make_terms(const TermsLayout& L, unsigned char* smem, float* gd
   t.V = reinterpret_cast<double*>(smem + L.off_V);
   t.vm = reinterpret_cast<float*>(smem + L.off_vm);
   t.act = reinterpret_cast<uint16_t*>(smem + L.off_act);
-  t.tst = reinterpret_cast<float*>(smem + L.off_act);
-  t.tst_stride = L.tst_stride;
   t.R = reinterpret_cast<double*>(smem + L.off_R);
   t.Rf = reinterpret_cast<float*>(smem + L.off_Rf);
   t.dA = L.off_dE > L.off_dA ? reinterpret_cast<float*>(smem + L.off_dA) : nullptr;
@@ -1726,8 +1712,7 @@ __device__ __forceinline__ R pair_delta(R d0x, R d0y, R d0z, R sx, R sy, R sz, i
 template <int P, class R, class Tab, class Acc>
 __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R* sx, const R* sy, const R* sz,
                              typename AccTraits<Acc>::out* ratio, float* mag = nullptr, const float* sl = nullptr,
-                             bool dlt = false, unsigned vneg = 0u, const ShellList* lst = nullptr, const Tab* Tov = nullptr,
-                             const Tab* hov = nullptr) {
+                             bool dlt = false, unsigned vneg = 0u, const ShellList* lst = nullptr) {
   using Out = typename AccTraits<Acc>::out;
   const Sys& s = k.s;
   const int lane = threadIdx.x & 31;
@@ -1737,8 +1722,7 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
   auto det_at = [&](int q) { return lst ? (int)lst->det[q] : q; };
   auto j3_at = [&](int q) { return lst ? (int)lst->j3[q] : q; };
   const int i = up ? e : e - s.n_up;
-  // the electron's T row (the warp's staged copy when given)
-  const Tab* Trow = Tov ? Tov : (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
+  const Tab* Trow = (up ? k.Tup : k.Tdn) + (size_t)i * k.A;
   // block energy on fresh tables (mixed form): the T row's low parts as well
   constexpr bool kMayRefine = sizeof(Tab) == sizeof(float) && !std::is_same<Acc, float>::value;
   const float* Tlo = nullptr;
@@ -1808,7 +1792,7 @@ __device__ void wf_ratio_pts(const Work<Tab>& k, const Terms& t, int e, const R*
       }
     }
     if (s.has_j3) {
-      const Tab* h = hov ? hov : k.h3 + (size_t)e * k.A3;
+      const Tab* h = k.h3 + (size_t)e * k.A3;
       for (int q = lane; q < nj3; q += 32) {
         const int sh = s.j3.shells[kSh * j3_at(q) + 7];
         R x, y, z;
@@ -1930,29 +1914,6 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
       lst = shell_list(k, t, e, margin);
     }
     const ShellList* lstp = sizeof(R) == sizeof(double) ? &lst : nullptr;
-    // the float projection: the warp's copy of the electron's T row and J3 field
-    // row in shared memory (one coalesced pass; the shells then read it there)
-    const Tab* Tst = nullptr;
-    const Tab* hst = nullptr;
-    if constexpr (sizeof(R) == sizeof(float) && !kErr && sizeof(Tab) == sizeof(float)) {
-      float* st = t.tst + (size_t)wid * t.tst_stride;
-      const float* Tg = e < s.n_up ? k.Tup + (size_t)e * k.A : k.Tdn + (size_t)(e - s.n_up) * k.A;
-      __syncwarp();   // the previous electron's rows are no longer read
-      if ((k.A & 3) == 0) {
-        const float4* T4 = reinterpret_cast<const float4*>(Tg);
-        float4* s4 = reinterpret_cast<float4*>(st);
-        for (int a = lane; a < (k.A >> 2); a += 32) s4[a] = T4[a];
-      } else {
-        for (int a = lane; a < k.A; a += 32) st[a] = Tg[a];
-      }
-      if (s.has_j3) {
-        const float* hg = k.h3 + (size_t)e * k.A3;
-        for (int a = lane; a < k.A3; a += 32) st[k.A + a] = hg[a];
-      }
-      __syncwarp();
-      Tst = st;
-      hst = s.has_j3 ? st + k.A : nullptr;
-    }
     if (e + nw < N) {   // this warp's next electron: its T row, J3 field and displacements
       const int en = e + nw;
       const Tab* Tn = (en < s.n_up ? k.Tup + (size_t)en * k.A : k.Tdn + (size_t)(en - s.n_up) * k.A);
@@ -2054,7 +2015,7 @@ __device__ Cancellation mesh_terms(const Work<Tab>& k, Terms& t, double alat, bo
         }
         wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, mag, sl, dlt, vneg, lstp);
       } else {
-        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg, lstp, Tst, hst);
+        wf_ratio_pts<P, R, Tab, Acc>(k, t, e, sx, sy, sz, ratio, nullptr, nullptr, dlt, vneg, lstp);
       }
       if (lane < np) {
         Out rr = Out(0);
@@ -3816,7 +3777,7 @@ double shell_reach2(const jqmc_basis_desc& b, int k, double C) {
 int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const double* d_draw, double alat, double E_scf,
                  double* d_w, double* d_eL, double* d_vd, void* stream, TauArgs ta = TauArgs{nullptr, nullptr, nullptr}) {
   KParams P = make_params(sys, w);
-  const int smem = terms_smem(P.ml, LrdmcShape<double, double>::threads, 0);   // 4-warp kernels
+  const int smem = terms_smem(P.ml, LrdmcShape<double, double>::threads);   // 4-warp kernels
   if (is_mixed(w->precision)) {
     // projections: float arithmetic on the float tables.  The local energy of a
     // block (K == 0): float values with compensated float-float sums, then FP64
@@ -3825,7 +3786,7 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
     // (JQMC_PREC_MIXED_FASTE)
     if (K > 0) {
       auto fn = k_lrdmc<float, float, float>;
-      const int smem_p = terms_smem(P.ml, 0, LrdmcShape<float, float>::threads);   // float mesh ratios, staged rows
+      const int smem_p = terms_smem(P.ml, 0);   // float mesh ratios only
       int rc = launch_check((const void*)fn, smem_p);
       if (rc) return rc;
       fn<<<w->nwalk, LrdmcShape<float, float>::threads, smem_p, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta, kEnergyPlain);
@@ -4241,7 +4202,7 @@ int jqmc_kinetic_mesh(const jqmc_system* sys, const jqmc_walkers* w, const doubl
                       void* stream) {
   if (!walkers_ok(sys, w) || w->precision != JQMC_PREC_FP64 || !d_angles || !d_el || !(alat > 0.0)) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
-  const int smem = terms_smem(P.ml, 128, 0);
+  const int smem = terms_smem(P.ml, 128);
   int rc = launch_check((const void*)k_kinetic_mesh, smem);
   if (rc) return rc;
   k_kinetic_mesh<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, alat, d_el);
@@ -4307,7 +4268,7 @@ int jqmc_vmc_measure(const jqmc_system* sys, const jqmc_walkers* w, const double
   if (!walkers_ok(sys, w) || !d_angles || !d_eL || !d_wL) return JQMC_E_ARG;
   if (w->precision != JQMC_PREC_FP64) return JQMC_E_ARG;
   KParams P = make_params(sys, w);
-  const int smem = terms_smem(P.ml, 128, 0);
+  const int smem = terms_smem(P.ml, 128);
   int rc = launch_check((const void*)k_vmc_measure, smem);
   if (rc) return rc;
   k_vmc_measure<<<w->nwalk, 128, smem, S(stream)>>>(P, d_angles, eps_AS, d_eL, d_wL);
