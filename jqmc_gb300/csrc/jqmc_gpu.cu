@@ -223,6 +223,7 @@ struct Sys {
   const double* j3vec;   // A3
   const float* j3matf;
   const float* j3matTf;
+  const float4* j3k4;   // (cp, c): float pairs of J[cp][c] and J[c][cp] (hi, lo, hi, lo)
   int ecp_flag;
   const int* ecp_maxl1;
   const int* ecp_chan;
@@ -2399,22 +2400,28 @@ __device__ void j3_field(const Sys& s, Tab* h, const double* r, J* buf, const J*
 }
 
 // The J3 field of the mixed rebuild with the walker's rebuild scratch (free
-// after the T phase) as work space, all electrons at once (same result as
-// j3_field up to the order of the FP64 sums):
-//   1. phi3(r_e) of every electron into U (N x A3), all (electron, shell) items;
+// after the T phase) as work space, all electrons at once (j3_field's sums in
+// another order and arithmetic):
+//   1. phi3(r_e) of every electron in FP64 into the scratch (N x A3 doubles),
+//      all (electron, shell) items;
 //   2. per column c, over the electrons in order: u_e = prefix_e (+ tot_up for a
 //      down electron), v_e = tot_same - prefix_e - phi3_e (+ tot_dn for an up
-//      electron), prefix_e the sum of phi3 over the same-spin electrons before e;
-//   3. h_e[c] = j[c] + sum_cp J[cp][c] u_e[cp] + J[c][cp] v_e[cp] for all (e, c),
-//      a warp over 32 consecutive c of one e.
+//      electron), prefix_e the sum of phi3 over the same-spin electrons before e,
+//      in FP64 and stored as float pairs (U, V: N x A3 float2 each, over the
+//      scratch);
+//   3. h_e[c] = j[c] + sum_cp J[cp][c] u_e[cp] + J[c][cp] v_e[cp] for all (e, c)
+//      by compensated float-float dots (Dot2) with the float pairs of J
+//      (s.j3k4), a warp over 32 consecutive c of one e.
 // Written in Tab with the low parts in hlo (when given).  Needs 2 N A3 doubles.
 template <class Tab>
-__device__ void j3_field_rows(const Sys& s, Tab* h, float* hlo, const double* r, double* U) {
+__device__ void j3_field_rows(const Sys& s, Tab* h, float* hlo, const double* r, double* scr) {
   const int N = s.N, A3 = s.j3.nao, nsh = s.j3.nshell, nu = s.n_up;
-  double* V = U + (size_t)N * A3;
+  double* Phi = scr + (size_t)N * A3;   // phase 1 output, read by phase 2 only
+  float2* U = reinterpret_cast<float2*>(scr);
+  float2* V = U + (size_t)N * A3;
   for (int it = threadIdx.x; it < N * nsh; it += blockDim.x) {
     const int e = it / nsh, sh = it - e * nsh;
-    double* row = U + (size_t)e * A3;
+    double* row = Phi + (size_t)e * A3;
     double dx, dy, dz;
     disp<double>(s.atom_pos, s.j3.shells[kSh * sh], r[3 * e], r[3 * e + 1], r[3 * e + 2], dx, dy, dz);
     if ((float)(dx * dx + dy * dy + dz * dz) > __int_as_float(s.j3.shells[kSh * sh + kShReach])) {
@@ -2425,26 +2432,36 @@ __device__ void j3_field_rows(const Sys& s, Tab* h, float* hlo, const double* r,
     shell_val_d<double>(s.j3, sh, dx, dy, dz, f);
   }
   __syncthreads();
+  // U (float2) takes the first N A3 doubles, V the second, over Phi: element
+  // (e, c) of V is written after Phi (e, c) is read, by the thread that owns
+  // column c
+  auto pair = [](double x) { const float hi = (float)x; return make_float2(hi, (float)(x - (double)hi)); };
   for (int c = threadIdx.x; c < A3; c += blockDim.x) {
     double tu = 0.0, td = 0.0;
-    for (int e = 0; e < N; ++e) (e < nu ? tu : td) += U[(size_t)e * A3 + c];
+    for (int e = 0; e < N; ++e) (e < nu ? tu : td) += Phi[(size_t)e * A3 + c];
     double pfx = 0.0;
     for (int e = 0; e < N; ++e) {
       if (e == nu) pfx = 0.0;
       const bool up = e < nu;
-      const double phi = U[(size_t)e * A3 + c];
-      U[(size_t)e * A3 + c] = up ? pfx : pfx + tu;
-      V[(size_t)e * A3 + c] = up ? (tu - pfx - phi) + td : td - pfx - phi;
+      const double phi = Phi[(size_t)e * A3 + c];
+      U[(size_t)e * A3 + c] = pair(up ? pfx : pfx + tu);
+      V[(size_t)e * A3 + c] = pair(up ? (tu - pfx - phi) + td : td - pfx - phi);
       pfx += phi;
     }
   }
   __syncthreads();
   for (int it = threadIdx.x; it < N * A3; it += blockDim.x) {
     const int e = it / A3, c = it - e * A3;
-    const double* u = U + (size_t)e * A3;
-    const double* v = V + (size_t)e * A3;
-    double acc = s.j3vec[c];
-    for (int cp = 0; cp < A3; ++cp) acc += s.j3mat[(size_t)cp * A3 + c] * u[cp] + s.j3matT[(size_t)cp * A3 + c] * v[cp];
+    const float2* u = U + (size_t)e * A3;
+    const float2* v = V + (size_t)e * A3;
+    float sh = 0.f, sc = 0.f;
+    for (int cp = 0; cp < A3; ++cp) {
+      const float4 k = s.j3k4[(size_t)cp * A3 + c];
+      const float2 uu = u[cp], vv = v[cp];
+      dot2_step(sh, sc, k.x, k.y, uu.x, uu.y);
+      dot2_step(sh, sc, k.z, k.w, vv.x, vv.y);
+    }
+    const double acc = s.j3vec[c] + ((double)sh + (double)sc);
     h[it] = (Tab)acc;
     if (hlo) hlo[it] = (float)(acc - (double)(Tab)acc);
   }
@@ -3879,12 +3896,13 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       lamTl[(size_t)b * A + a] = (float)(v - (double)(float)v);
     }
   std::vector<double> j3m, j3mT, j3v;
-  std::vector<float> j3mf, j3mTf;
+  std::vector<float> j3mf, j3mTf, j3k4;
   if (d->has_j3) {
     j3m.resize((size_t)A3 * A3);
     j3mT.resize((size_t)A3 * A3);
     j3mf.resize((size_t)A3 * A3);
     j3mTf.resize((size_t)A3 * A3);
+    j3k4.resize((size_t)A3 * A3 * 4);
     j3v.resize(A3);
     for (int a = 0; a < A3; ++a) {
       for (int b = 0; b < A3; ++b) {
@@ -3896,6 +3914,13 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
       }
       j3v[a] = d->j3_matrix[(size_t)a * (A3 + 1) + A3];
     }
+    for (int cp = 0; cp < A3; ++cp)
+      for (int c = 0; c < A3; ++c) {
+        const double x = d->j3_matrix[(size_t)cp * (A3 + 1) + c], y = d->j3_matrix[(size_t)c * (A3 + 1) + cp];
+        float* q = &j3k4[((size_t)cp * A3 + c) * 4];
+        q[0] = (float)x; q[1] = (float)(x - (double)q[0]);
+        q[2] = (float)y; q[3] = (float)(y - (double)q[2]);
+      }
   }
   auto to_float = [](const double* p, size_t n) { std::vector<float> v(n); for (size_t i = 0; i < n; ++i) v[i] = (float)p[i]; return v; };
   std::vector<float> dprf = to_float(d->det.prims, (size_t)d->det.nprim * 2);
@@ -3942,7 +3967,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
   const size_t o_laml = put(laml.data(), (size_t)A * A * 4);
   const size_t o_lamTl = put(lamTl.data(), (size_t)A * A * 4);
   const size_t o_j1z = put(j1cA.data(), (size_t)M * 16);
-  size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0;
+  size_t o_jsh = 0, o_jpr = 0, o_jprf = 0, o_j3m = 0, o_j3mT = 0, o_j3v = 0, o_j3mf = 0, o_j3mTf = 0, o_j3k4 = 0;
   if (d->has_j3) {
     const std::vector<int32_t> jsh_rows = with_order(d->j3);
     o_jsh = put(jsh_rows.data(), jsh_rows.size() * 4);
@@ -3953,6 +3978,7 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     o_j3v = put(j3v.data(), j3v.size() * 8);
     o_j3mf = put(j3mf.data(), j3mf.size() * 4);
     o_j3mTf = put(j3mTf.data(), j3mTf.size() * 4);
+    o_j3k4 = put(j3k4.data(), j3k4.size() * 4);
   }
   const size_t o_maxl1 = put(d->ecp_flag ? d->ecp_maxl1 : zeroi.data(), (size_t)M * 4);
   const size_t o_chan = put(d->ecp_flag ? d->ecp_chan : zeroi.data(), (size_t)M * kSlots * 8);
@@ -3985,10 +4011,12 @@ int jqmc_system_create(const jqmc_system_desc* d, jqmc_system** out) {
     s.j3.nshell = d->j3.nshell; s.j3.nao = A3; s.j3.nprim = d->j3.nprim;
     s.j3.shells = ip(o_jsh); s.j3.prims = dp(o_jpr); s.j3.primsf = fp(o_jprf);
     s.j3mat = dp(o_j3m); s.j3matT = dp(o_j3mT); s.j3vec = dp(o_j3v); s.j3matf = fp(o_j3mf); s.j3matTf = fp(o_j3mTf);
+    s.j3k4 = reinterpret_cast<const float4*>(fp(o_j3k4));
   } else {
     s.j3.nshell = 0; s.j3.nao = 0; s.j3.nprim = 0; s.j3.shells = nullptr; s.j3.prims = nullptr; s.j3.primsf = nullptr;
     s.j3mat = s.j3matT = s.j3vec = nullptr;
     s.j3matf = s.j3matTf = nullptr;
+    s.j3k4 = nullptr;
   }
   s.ecp_flag = d->ecp_flag;
   s.ecp_maxl1 = ip(o_maxl1); s.ecp_chan = ip(o_chan);
