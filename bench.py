@@ -78,37 +78,54 @@ def parse():
 
 # ----------------------------------------------------------------------------- CPU oracle arm
 def _oracle_worker(args):
-    """Project one walker with the oracle for about `budget` seconds; returns walker-steps done and seconds."""
-    workload, seed, alat, budget = args
+    """Run branching cycles of the walker-batched NumPy GFMC_n step (oracle/batched.py:
+    the oracle's algorithm with every mesh point of a walker in one array): K
+    projections, then the block energy, as the GPU cycle does (the comb over one
+    process's walkers is left out: it costs nothing next to a projection).  Whole
+    cycles until about `budget` seconds have passed, after one untimed step;
+    returns walker-steps done and seconds."""
+    workload, seed, alat, budget, walkers, K = args
     from jqmc_gb300 import synthetic
-    from oracle import drivers as D
+    from oracle.batched import BatchedGFMCn
     from oracle.wf import OracleSystem
     syn = synthetic.SYSTEMS[workload]()
     o = OracleSystem(syn.hamiltonian)
-    r_up, r_dn = syn.initial_electrons(1, seed=seed)
-    st = D.init_state(o, r_up[0], r_dn[0])
+    r_up, r_dn = syn.initial_electrons(walkers, seed=seed)
+    r = np.concatenate([r_up, r_dn], axis=1)
+    b = BatchedGFMCn(o, alat)
     rng = np.random.default_rng(seed)
-    w = 1.0
+    w = np.ones(walkers)
+
+    def draws():
+        return np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, (walkers, 3)), rng.uniform(size=(walkers, 1))], axis=1)
+
+    r, w, _, _, _ = b.step(r, w, draws(), 0.0)
     t0 = time.perf_counter()
     done = 0
     while True:
-        draw = np.concatenate([rng.uniform(-2 * np.pi, 2 * np.pi, 3), rng.uniform(size=1)])
-        w, _, _, _ = D.lrdmc_step(o, st, w, draw, alat, 0.0)
-        done += 1
+        for _ in range(K):
+            d = draws()
+            r, w, _, _, _ = b.step(r, w, d, 0.0)
+        b.energy(r, d)
+        w[:] = 1.0
+        done += walkers * K
         if time.perf_counter() - t0 >= budget:
             break
     return done, time.perf_counter() - t0
 
 
-def oracle_rate(workload: str, alat: float, procs: int, budget: float):
-    """walker-steps/s of the oracle with `procs` processes (spawned before any GPU use)."""
+def oracle_rate(workload: str, alat: float, procs: int, budget: float, K: int = 40, walkers: int = 1):
+    """walker-steps/s of the batched NumPy cycle with `procs` single-threaded
+    processes (spawned before any GPU use), each projecting its own walkers."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
     if procs == 1:
-        done, secs = _oracle_worker((workload, 0, alat, budget))
+        done, secs = _oracle_worker((workload, 0, alat, budget, walkers, K))
         return done / secs, done
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_oracle_worker, [(workload, s, alat, budget) for s in range(procs)])
+        res = pool.map(_oracle_worker, [(workload, s, alat, budget, walkers, K) for s in range(procs)])
     return sum(d / s for d, s in res), sum(d for d, _ in res)
 
 
@@ -117,16 +134,15 @@ def reference_arm(a):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
     vals = []
-    for _ in range(a.warmup):
-        pass
     budget = 15.0
     for _ in range(a.steps):
-        v, _ = oracle_rate(a.workload, a.alat, cores, budget)
+        v, _ = oracle_rate(a.workload, a.alat, cores, budget, a.nproj)
         vals.append(v)
     v = statistics.median(vals)
-    sample = f"{cores} processes x 1 walker of {a.workload}, LRDMC projections for {budget:.0f} s each, {a.steps} samples"
+    sample = (f"{cores} single-threaded processes x 1 walker of {a.workload}, branching cycles of {a.nproj} "
+              f"walker-batched NumPy GFMC_n steps and the block energy (oracle/batched.py), whole cycles for "
+              f"at least {budget:.0f} s after one untimed step, median of {a.steps} samples")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": f"lrdmc_{a.workload}", "walkers": a.walkers, "projections_per_branching": a.nproj,
@@ -551,9 +567,12 @@ def gpu_arm(a):
     cpu_base = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         budget = 12.0
-        v, done = oracle_rate(a.workload, a.alat, 1, budget)
-        cpu_base = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                    "sample": f"1 walker of {a.workload}, {done} LRDMC projections in {budget:.0f} s (NumPy oracle, 1 process)"}
+        cores = os.cpu_count() or 1
+        v, done = oracle_rate(a.workload, a.alat, cores, budget, a.nproj)
+        cpu_base = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                    "sample": f"{cores} single-threaded processes x 1 walker of {a.workload}, {done} walker-steps in "
+                              f"branching cycles of {a.nproj} walker-batched NumPy GFMC_n steps and the block energy "
+                              f"(oracle/batched.py), whole cycles for at least {budget:.0f} s"}
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
