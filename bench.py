@@ -51,7 +51,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "walker-steps/s on 1 GB300: mixed-prec+batched vs plain FP64 at |Δ<E>|≤0.1 mHa"
-NCU_TRAFFIC_PER_WALKER_STEP = {"chain32": (4.629343e9 + 0.7037056e9) / (912 * 2)}
+NCU_TRAFFIC_PER_WALKER_STEP = {"chain32": (5.096144e9 + 0.7726876e9) / (912 * 2)}
 UNIT = "walker-steps/s"
 
 
