@@ -2270,7 +2270,8 @@ __global__ void __launch_bounds__(128) k_rebuild_m(KParams P) {
 // shared-memory layout: [row tile][K chunk][slice][128 x 32 canonical block].
 // Rows at or past rows_total are written as zeros.  Shared memory: 8 x K doubles.
 __global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long long row0, long long rows_total, int nk,
-                                                   uint8_t* __restrict__ a_sl, int* __restrict__ row_exp) {
+                                                   uint8_t* __restrict__ a_sl, int* __restrict__ row_exp,
+                                                   float* __restrict__ phi_hi, float* __restrict__ phi_lo) {
   using namespace jqmc_tc;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int ex[8];
@@ -2311,6 +2312,20 @@ __global__ void __launch_bounds__(128) k_ao_slices(KParams P, int spin, long lon
     }
   }
   __syncthreads();
+  if (phi_hi) {
+    // the rows' FP64 values as float pairs (row g = walker * n + electron, A per
+    // row), which the walker initialisation reads instead of evaluating them again
+    const int A = s.det.nao;
+    for (int t = threadIdx.x; t < 8 * A; t += blockDim.x) {
+      const int rr = t / A, a = t - rr * A;
+      const long long g = g0 + rr;
+      if (g >= rows_total) continue;
+      const double v = phi[rr * K + a];
+      const float h = (float)v;
+      phi_hi[g * A + a] = h;
+      phi_lo[g * A + a] = (float)(v - (double)h);
+    }
+  }
   const int lr0 = 8 * blockIdx.x;             // first local row of this CTA
   const int tile = lr0 / kBM, rg = (lr0 % kBM) / 8;
   if (threadIdx.x < 8) row_exp[lr0 + threadIdx.x] = ex[threadIdx.x];
@@ -2479,10 +2494,13 @@ __device__ void j3_field_rows(const Sys& s, Tab* h, float* hlo, const double* r,
 // mode bit 3 (kInitJ3Table): compute the J3 field in the table type (the float
 // form's drift-control rebuild between VMC measurements; an energy is measured
 // only after a full build, whose field is FP64).
+// mode bit 4 (kInitPhiReady, mixed form): phi_dn of every down electron is
+// already in the T buffers as float pairs (k_ao_slices).
 constexpr int kInitTablesOnly = 1;
 constexpr int kInitRefine = 2;
 constexpr int kInitMReady = 4;
 constexpr int kInitJ3Table = 8;
+constexpr int kInitPhiReady = 16;
 template <class Tab>
 __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, int mode,
                                  unsigned char* smem) {
@@ -2524,14 +2542,15 @@ __device__ void walker_init_body(const KParams& P, int w, const InitLayout& IL, 
     // mixed form: M_up / M_dn are float-float pairs from k_rebuild_m (or the
     // tensor-core GEMM).  phi_dn(r_j) of every down electron in FP64, split into
     // float pairs over the T buffers (hi in T_up, lo in T_dn: free until the T
-    // phase), all (electron, shell) items at once; then G[i][j] = M_up[i] .
+    // phase), all (electron, shell) items at once (or left there by the
+    // tensor-core path's k_ao_slices: kInitPhiReady); then G[i][j] = M_up[i] .
     // phi_dn[j] by compensated float-float dots, 2 x 4 (i, j) per warp
     const float2* Mup2 = reinterpret_cast<const float2*>(Mup);
     float* ph = reinterpret_cast<float*>(Tup);
     float* pl = reinterpret_cast<float*>(Tdn);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nsh = s.det.nshell, nd = s.n_dn;
-    for (int it = threadIdx.x; it < nd * nsh; it += blockDim.x) {
+    for (int it = threadIdx.x; it < ((mode & kInitPhiReady) ? 0 : nd * nsh); it += blockDim.x) {
       const int j = it / nsh, sh = it - j * nsh, e = s.n_up + j;
       float* hi = ph + (size_t)j * A;
       float* lo = pl + (size_t)j * A;
@@ -4161,8 +4180,10 @@ static int tc_rebuild_m(const jqmc_system* csys, const jqmc_walkers* w, const KP
     for (long long r0 = 0; r0 < rows_total; r0 += sys->tc_rows_cap) {
       const long long rows = std::min(sys->tc_rows_cap, rows_total - r0);
       const int tiles = (int)((rows + kBM - 1) / kBM);
-      k_ao_slices<<<tiles * (kBM / 8), 128, smem_a, S(stream)>>>(P, spin, r0, rows_total, nk,
-                                                                 reinterpret_cast<uint8_t*>(sys->tc_a), sys->tc_row_exp);
+      // the down spin also leaves phi_dn as float pairs over T_up (hi) and T_dn (lo)
+      k_ao_slices<<<tiles * (kBM / 8), 128, smem_a, S(stream)>>>(
+          P, spin, r0, rows_total, nk, reinterpret_cast<uint8_t*>(sys->tc_a), sys->tc_row_exp,
+          spin == 1 ? static_cast<float*>(w->Tup) : nullptr, spin == 1 ? static_cast<float*>(w->Tdn) : nullptr);
       rc = ozaki_gemm(sys->tc_a, sys->tc_b + spin * b_spin, sys->tc_row_exp, sys->tc_col_exp + (size_t)spin * nct * kBN, nk,
                       nct, tiles, r0, rows_total, n, A, spin == 0 ? 1 : 0, reinterpret_cast<float2*>(w->scratch), w->status,
                       JQMC_ST_NAN, S(stream));
@@ -4194,9 +4215,10 @@ static int launch_walker_init(const jqmc_system* sys, const jqmc_walkers* w, voi
       if (rows == 8) k_rebuild_m<8><<<grid_m, 128, smem_m, S(stream)>>>(P);
       else k_rebuild_m<4><<<grid_m, 128, smem_m, S(stream)>>>(P);
     }
+    const int phi = rc == kTcUnavailable ? 0 : kInitPhiReady;
     rc = launch_check((const void*)k_walker_init<float>, smem);
     if (rc) return rc;
-    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, IL, mode | kInitMReady);
+    k_walker_init<float><<<w->nwalk, 128, smem, S(stream)>>>(P, IL, mode | kInitMReady | phi);
   } else {
     int rc = launch_check((const void*)k_walker_init<double>, smem);
     if (rc) return rc;
