@@ -797,23 +797,18 @@ __device__ __forceinline__ Tab column_dot(const Tab* __restrict__ v, size_t A, i
   return r;
 }
 
-// sum_a L[a*A + b] x[a] (column b of a row-major A x A matrix) over the nonzero
-// entries of x only (positions nz[0 .. nnz)), with kMLP independent partial sums
+// sum_a L[a*A + b] x[a] (column b of a row-major A x A matrix) with kMLP partial sums
 template <class Tab>
-__device__ __forceinline__ Tab matvec_col_nz(const Tab* __restrict__ L, int A, int b, const Tab* __restrict__ x,
-                                             const uint16_t* __restrict__ nz, int nnz) {
+__device__ __forceinline__ Tab matvec_col(const Tab* __restrict__ L, int A, int b, const Tab* __restrict__ x) {
   Tab acc[kMLP];
 #pragma unroll
   for (int u = 0; u < kMLP; ++u) acc[u] = Tab(0);
-  int q = 0;
-  for (; q + kMLP <= nnz; q += kMLP) {
+  int a = 0;
+  for (; a + kMLP <= A; a += kMLP) {
 #pragma unroll
-    for (int u = 0; u < kMLP; ++u) {
-      const int a = nz[q + u];
-      acc[u] += L[(size_t)a * A + b] * x[a];
-    }
+    for (int u = 0; u < kMLP; ++u) acc[u] += L[(size_t)(a + u) * A + b] * x[a + u];
   }
-  for (; q < nnz; ++q) acc[0] += L[(size_t)nz[q] * A + b] * x[nz[q]];
+  for (; a < A; ++a) acc[0] += L[(size_t)a * A + b] * x[a];
   Tab r = Tab(0);
 #pragma unroll
   for (int u = 0; u < kMLP; ++u) r += acc[u];
@@ -1105,14 +1100,13 @@ struct Work {
   Tab* vn3;
   double* red;   // kRed
   double* sc;    // 32 scalars
-  uint16_t* nz;  // A: positions of the nonzero entries of a move's dphi (sm_move)
   const float* tlo_up;   // mixed form: low parts of T_up / T_dn and of the J3 field
   const float* tlo_dn;   // from the last build (nullptr when the tables have moved
   const float* h3lo;     // since, or are not kept); h3lo is nullptr without J3
 };
 
 struct WorkLayout {
-  int off_r, off_G, off_Gi, off_vA, off_v3, off_vn, off_red, off_sc, off_nz, bytes;
+  int off_r, off_G, off_Gi, off_vA, off_v3, off_vn, off_red, off_sc, bytes;
 };
 
 // Shared-memory offsets of the walker (re)initialisation (after the staged tables)
@@ -1132,7 +1126,6 @@ WorkLayout work_layout(const Sys& s, int base, int tab_bytes) {
   L.off_vn = o; o = align16(o + 4 * s.n_up * tab_bytes);
   L.off_red = o; o = align16(o + kRed * 8);
   L.off_sc = o; o = align16(o + 32 * 8);
-  L.off_nz = o; o = align16(o + s.det.nao * 2);
   L.bytes = o;
   return L;
 }
@@ -1160,7 +1153,6 @@ __device__ Work<Tab> make_work(const Sys& s, const WorkLayout& L, unsigned char*
   k.vn3 = k.vn2 + k.n;
   k.red = reinterpret_cast<double*>(smem + L.off_red);
   k.sc = reinterpret_cast<double*>(smem + L.off_sc);
-  k.nz = reinterpret_cast<uint16_t*>(smem + L.off_nz);
   k.Tup = static_cast<Tab*>(ws.Tup) + (size_t)w * k.n * k.A;
   k.Tdn = static_cast<Tab*>(ws.Tdn) + (size_t)w * k.n * k.A;
   k.h3 = s.has_j3 ? static_cast<Tab*>(ws.h3) + (size_t)w * k.N * k.A3 : nullptr;
@@ -1230,28 +1222,6 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     for (int a = threadIdx.x; a < A3; a += blockDim.x) k.v31[a] = k.v30[a] - k.v31[a];
   rows_dot<Tab>(up ? k.Tup : k.Tdn, n, A, k.vA0, k.vn0);
   __syncthreads();
-  // positions of the nonzero entries of dphi, in order: the shells out of reach of
-  // both positions left exact zeros, and the lambda products skip them
-  int nnz = 0;
-  {
-    int* cnt = reinterpret_cast<int*>(k.red);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int a0 = 0; a0 < A; a0 += blockDim.x) {
-      const int a = a0 + threadIdx.x;
-      const bool nzf = a < A && k.vA1[a] != Tab(0);
-      const unsigned m = __ballot_sync(0xffffffffu, nzf);
-      if (lane == 0) cnt[wid] = __popc(m);
-      __syncthreads();
-      int off = nnz, tot = nnz;
-      for (int q = 0; q < nw; ++q) {
-        if (q < wid) off += cnt[q];
-        tot += cnt[q];
-      }
-      if (nzf) k.nz[off + __popc(m & ((1u << lane) - 1u))] = (uint16_t)a;
-      nnz = tot;
-      __syncthreads();
-    }
-  }
   const Tab ratio = k.vn0[i];
   const Tab inv = Tab(1) / ratio;
   Tab* scn = reinterpret_cast<Tab*>(k.sc);  // 32 doubles of scratch
@@ -1269,7 +1239,7 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     }
     __syncthreads();
     for (int b = threadIdx.x; b < A; b += blockDim.x) {
-      const Tab dl = matvec_col_nz<Tab>(lam, A, b, k.vA1, k.nz, nnz);
+      const Tab dl = matvec_col<Tab>(lam, A, b, k.vA1);
       const Tab mw = column_dot<Tab>(k.Tdn, A, b, n, k.vn2);
       k.vA2[b] = (dl - mw) * inv;
     }
@@ -1305,7 +1275,7 @@ __device__ double sm_move(Work<Tab>& k, int e, double px, double py, double pz) 
     }
     __syncthreads();
     for (int a = threadIdx.x; a < A; a += blockDim.x) {
-      const Tab dm = matvec_col_nz<Tab>(lamT, A, a, k.vA1, k.nz, nnz);
+      const Tab dm = matvec_col<Tab>(lamT, A, a, k.vA1);
       const Tab mq = column_dot<Tab>(k.Tup, A, a, n, k.vn2);
       k.vA2[a] = (dm - mq) * inv;
     }
