@@ -43,6 +43,7 @@ def test_fp64_batch_matches_single_molecule_sweeps():
         acc = torch.zeros(ws.nwalk, dtype=torch.int32, device=b.device)
         ws.vmc_sweep(idr.contiguous(), fdr.contiguous(), b.Dt, b.epsilon_AS, acc)
         acc_single.append(acc)
+    r0 = [b.walkers[i].r.cpu().numpy().copy() for i in bk.items]
     b.sweep(bk, idraw, fdraw, caches=True, threads=64)
     torch.cuda.synchronize()
     for j, i in enumerate(bk.items):
@@ -51,6 +52,20 @@ def test_fp64_batch_matches_single_molecule_sweeps():
     assert torch.equal(bk.accept, torch.cat(acc_single))
     for ws in b.walkers:
         assert not ws.status.any()
+    # and against the oracle (jqmc_mcmc.py:4278-4533): the first and last walker
+    # of every molecule replayed with the batch's draws
+    from jqmc_gb300 import synthetic
+    from oracle import drivers as D
+    from oracle.wf import OracleSystem
+    for j, (i, idr, fdr) in enumerate(zip(bk.items, _split(b, idraw), _split(b, fdraw))):
+        o = OracleSystem(synthetic.random_molecule(SEEDS[i]).hamiltonian)
+        n = o.n_up
+        idr, fdr = idr.cpu().numpy(), fdr.cpu().numpy()
+        for w in (0, WALKERS[i] - 1):
+            st = D.init_state(o, r0[j][w, :n], r0[j][w, n:])
+            D.vmc_block(o, st, idr[w], fdr[w], b.Dt, b.epsilon_AS)
+            got = b.walkers[i].r[w].cpu().numpy()
+            assert np.max(np.abs(got - np.vstack([st.r_up, st.r_dn]))) < 1e-12, (i, w)
     b.close()
 
 
