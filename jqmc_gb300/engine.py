@@ -216,13 +216,13 @@ class WalkerSet:
     precision "fp64": every table double (the plain drop-in);
     precision "mixed": G, G^-1, T tables and the J3 field in float, rebuilt in
     double from the positions by ``init`` / ``rebuild`` (an FP64 scratch of
-    2 n A doubles per walker is held for that rebuild); the block energy from
-    float values with compensated float-float sums, the walkers whose mesh
-    ratios cancel strongly (factor above ``_lib.FAST_ENERGY_CANCEL``, about
-    2.5 % of sampled configurations) recomputed in FP64 arithmetic on the float
-    tables;
-    precision "mixed_fast_energy": as "mixed", the compensated energy alone
-    (rare configurations carry errors of 1e-4 Ha)."""
+    2 n A doubles per walker is held for that rebuild, and every build writes
+    the tables' low float parts to ``tlo``); the block energy right after a
+    build reads the FP64-accurate tables (T_hi + T_lo, h_hi + h_lo) with the
+    electron terms and the heavy electrons' ECP elements in FP64 and the other
+    mesh ratios in compensated float, and the walkers whose mesh ratios cancel
+    strongly (factor above ``_lib.FAST_ENERGY_CANCEL``) are recomputed in FP64;
+    precision "mixed_fast_energy": as "mixed" without that recompute."""
 
     def __init__(self, system: GpuSystem, r_up, r_dn, precision: str = "fp64", scratch: torch.Tensor | None = None):
         self.sys = system
