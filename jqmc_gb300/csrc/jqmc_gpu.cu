@@ -127,6 +127,12 @@ struct F2 {
   float s, c;
   float m;   // sum of |terms| (the scale of the rounding of the float inputs)
 };
+// the block energy of the mixed form, like the float projection, at 8 warps per
+// walker and 2 CTAs per SM (11 % faster than 4 warps at 3 CTAs on the chain)
+template <>
+struct LrdmcShape<float, F2> {
+  static constexpr int threads = 256, min_ctas = 2;
+};
 __device__ __forceinline__ void acc_zero(float& a) { a = 0.f; }
 __device__ __forceinline__ void acc_zero(double& a) { a = 0.0; }
 __device__ __forceinline__ void acc_zero(F2& a) { a.s = 0.f; a.c = 0.f; a.m = 0.f; }
@@ -1398,9 +1404,11 @@ struct Terms {
 };
 
 // Warps per CTA of the walker kernels with FP64 mesh ratios (the only ones that
-// keep shell lists); the float projection launches without the list slots.
-constexpr int kMaxWarps = 4;
-static_assert(LrdmcShape<double, double>::threads / 32 <= kMaxWarps, "shell-list slots for every warp");
+// keep shell lists: the FP64 kernels and the block energy's FP64 refinement);
+// the float projection launches without the list slots.
+constexpr int kMaxWarps = 8;
+static_assert(LrdmcShape<double, double>::threads / 32 <= kMaxWarps && LrdmcShape<float, F2>::threads / 32 <= kMaxWarps,
+              "shell-list slots for every warp");
 
 struct TermsLayout {
   int off_ke, off_c3, off_ei, off_eid, off_ed, off_ea, off_el, off_V, off_vm, off_R, off_Rf, off_dA, off_dE, off_act,
@@ -3829,9 +3837,10 @@ int launch_lrdmc(const jqmc_system* sys, const jqmc_walkers* w, int K, const dou
     } else {
       const bool gate = w->precision == JQMC_PREC_MIXED;
       auto fn = k_lrdmc<float, float, F2>;
-      int rc = launch_check((const void*)fn, smem);
+      const int smem_e = terms_smem(P.ml, LrdmcShape<float, F2>::threads);
+      int rc = launch_check((const void*)fn, smem_e);
       if (rc) return rc;
-      fn<<<w->nwalk, LrdmcShape<float, F2>::threads, smem, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
+      fn<<<w->nwalk, LrdmcShape<float, F2>::threads, smem_e, S(stream)>>>(P, K, d_draw, alat, E_scf, d_w, d_eL, d_vd, ta,
                                                                          gate ? kEnergyBound : kEnergyPlain);
       if (gate) {
         auto fd = k_lrdmc<double, float, double>;
