@@ -19,7 +19,18 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-TREXIO_DIR = "/root/reference/tests/trexio_example_files"
+
+
+def _reference_trexio_dir():
+    """The reference's TREXIO example files where the fixture recipe
+    (tests/golden/make_trexio_golden.py) reads them; absent elsewhere."""
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_trexio_golden import REFERENCE
+    return os.path.join(REFERENCE, "tests", "trexio_example_files")
+
+
+TREXIO_DIR = _reference_trexio_dir()
 
 
 def trexio_case(fixture: str, case: str):
