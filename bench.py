@@ -117,15 +117,24 @@ def _oracle_worker(args):
 def oracle_rate(workload: str, alat: float, procs: int, budget: float, K: int = 40, walkers: int = 1):
     """walker-steps/s of the batched NumPy cycle with `procs` single-threaded
     processes (spawned before any GPU use), each projecting its own walkers."""
-    os.environ["OMP_NUM_THREADS"] = "1"
-    os.environ["OPENBLAS_NUM_THREADS"] = "1"
     if procs == 1:
         done, secs = _oracle_worker((workload, 0, alat, budget, walkers, K))
         return done / secs, done
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        res = pool.map(_oracle_worker, [(workload, s, alat, budget, walkers, K) for s in range(procs)])
+    keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:   # the spawned workers start with one BLAS thread each
+        os.environ[k] = "1"
+    try:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_oracle_worker, [(workload, s, alat, budget, walkers, K) for s in range(procs)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     return sum(d / s for d, s in res), sum(d for d, _ in res)
 
 
