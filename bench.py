@@ -138,6 +138,63 @@ def oracle_rate(workload: str, alat: float, procs: int, budget: float, K: int = 
     return sum(d / s for d, s in res), sum(d for d, _ in res)
 
 
+def _vmc_worker(args):
+    """VMC blocks of the walker-batched NumPy Metropolis step (oracle/batched.py
+    BatchedVMC): K proposals of every walker, then E_L and w_L, whole blocks for
+    about `budget` seconds after one untimed proposal; returns walker-steps
+    (proposals) done and seconds."""
+    workload, seed, budget, walkers, K = args
+    from jqmc_gb300 import synthetic
+    from oracle.batched import BatchedVMC
+    from oracle.wf import OracleSystem
+    syn = synthetic.SYSTEMS[workload]()
+    o = OracleSystem(syn.hamiltonian)
+    r_up, r_dn = syn.initial_electrons(walkers, seed=seed)
+    r = np.concatenate([r_up, r_dn], axis=1)
+    b = BatchedVMC(o, 0.4, 0.0)
+    G, Ginv = b.init(r)
+    rng = np.random.default_rng(seed)
+    n, nd = o.n_up, o.n_dn
+
+    def draws():
+        idraw = np.stack([rng.integers(0, n + nd, walkers), rng.integers(0, n, walkers), rng.integers(0, max(nd, 1), walkers),
+                          rng.integers(0, 3, walkers)], axis=-1)
+        return idraw, np.stack([rng.normal(size=walkers), rng.uniform(size=walkers)], axis=-1)
+
+    b.proposal(r, G, Ginv, *draws())
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        for _ in range(K):
+            b.proposal(r, G, Ginv, *draws())
+        b.measure(r, G, Ginv, rng.uniform(-np.pi, np.pi, (walkers, 3)))
+        done += walkers * K
+        if time.perf_counter() - t0 >= budget:
+            break
+    return done, time.perf_counter() - t0
+
+
+def vmc_cpu_rate(workload: str, procs: int, budget: float, K: int = 40, walkers: int = 64):
+    """walker-steps/s (proposals) of the batched NumPy VMC blocks with `procs`
+    single-threaded processes, each with its own walkers."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ[k] = "1"
+    try:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_vmc_worker, [(workload, s, budget, walkers, K) for s in range(procs)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return sum(d / s for d, s in res), sum(d for d, _ in res)
+
+
 def reference_arm(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:

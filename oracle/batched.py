@@ -217,6 +217,52 @@ class BatchedGFMCn:
             lap = lap + np.einsum("wea,wea->we", v3[4], h)
         return -0.5 * (lap + np.sum(g * g, axis=-1))
 
+    def _ecp(self, r, Rm, dnuc, Tu, Td, h, a3):
+        """(local ECP energy (W,), non-local elements V (W, N, Nv), quadrature points
+        (W, N, Nv, 3)) with the rotations Rm (coulomb_potential.py:601-661, :1478-1712
+        with NN = 1, as OracleSystem.ecp_local / ecp_nonlocal)."""
+        o = self.o
+        W, N, _ = r.shape
+        Nv = self.Nv
+        atom = np.argmin(dnuc, axis=2)                                        # (W, N), first nearest
+        loc = np.zeros(W)
+        for a in range(o.M):
+            loc += np.sum(self._V_channel(np.full((W, N), a), int(o.maxl1[a]), dnuc[:, :, a]), axis=1)
+        Ra = o.R[atom]                                                        # (W, N, 3)
+        rel = Ra - r
+        dist = np.linalg.norm(rel, axis=-1)
+        gq = np.einsum("qx,wyx->wqy", self.mesh_pts, Rm)                      # (W, Nv, 3): mesh R^T
+        pe = r[:, :, None, :] + rel[:, :, None, :] + dist[:, :, None, None] * gq[:, None]
+        cos_t = np.einsum("wex,wqx->weq", -rel / dist[..., None], gq / np.linalg.norm(gq, axis=-1)[..., None])
+        lmax = o.maxl1[atom]                                                  # (W, N)
+        wv = np.zeros((W, N, Nv))
+        for l in range(int(o.maxl1.max())):
+            Vl = self._V_channel(atom, l, dist)                               # (W, N)
+            act = (l < lmax)[..., None]
+            wv = wv + np.where(act, Vl[..., None] * (2 * l + 1) * legendre(l, cos_t) * self.mesh_w, 0.0)
+        ratio_e = self._det_ratio(pe, Tu, Td) * self._jastrow_ratio(r, pe, np.arange(N), h, a3)
+        return loc, wv * ratio_e, pe
+
+    def tables(self, r, Ginv=None):
+        """(Pu, Pdn, B, G, Ginv, Tu, Td, a3, h) at positions r; G^-1 from the positions
+        unless given."""
+        o = self.o
+        W, N, _ = r.shape
+        n, nd = self.n, self.nd
+        Pu = self._orb(o.tab_up, o.mo_up, r[:, :n].reshape(-1, 3)).reshape(W, n, -1)
+        Pdn = self._orb(o.tab_dn, o.mo_dn, r[:, n:].reshape(-1, 3)).reshape(W, nd, -1)
+        B = np.einsum("ab,wjb->waj", o.lam_p, Pdn)                             # (W, A, nd)
+        if n > nd:
+            B = np.concatenate([B, np.broadcast_to(o.lam_u, (W,) + o.lam_u.shape)], axis=2)
+        G = np.einsum("wia,waj->wij", Pu, B)
+        if Ginv is None:
+            Ginv = np.linalg.inv(G)
+        Tu = B @ Ginv                                                          # (W, A, n)
+        Td = np.einsum("wjk,wkb->wjb", Ginv[:, :nd, :], np.einsum("wia,ab->wib", Pu, o.lam_p))
+        a3 = ao_value(o.tab_j3, r.reshape(-1, 3)).T.reshape(W, N, -1) if o.j3 is not None else None
+        h = self._j3_fields(a3) if o.j3 is not None else None
+        return Pu, Pdn, B, G, Ginv, Tu, Td, a3, h
+
     # ------------------------------------------------------------------ the step
     def step(self, r: np.ndarray, w: np.ndarray, draws: np.ndarray, E_scf: float):
         """One projection of every walker: r (W, N, 3), w (W,), draws (W, 4) = (alpha,
@@ -256,17 +302,7 @@ class BatchedGFMCn:
         alat = self.alat
         Rm = np.stack([rotation_matrix(*d[:3]) for d in draws])               # (W, 3, 3)
         # geminal, inverse and the ratio tables
-        Pu = self._orb(o.tab_up, o.mo_up, r[:, :n].reshape(-1, 3)).reshape(W, n, -1)
-        Pdn = self._orb(o.tab_dn, o.mo_dn, r[:, n:].reshape(-1, 3)).reshape(W, nd, -1)
-        B = np.einsum("ab,wjb->waj", o.lam_p, Pdn)                             # (W, A, nd)
-        if n > nd:
-            B = np.concatenate([B, np.broadcast_to(o.lam_u, (W,) + o.lam_u.shape)], axis=2)
-        G = np.einsum("wia,waj->wij", Pu, B)
-        Ginv = np.linalg.inv(G)
-        Tu = B @ Ginv                                                          # (W, A, n)
-        Td = np.einsum("wjk,wkb->wjb", Ginv[:, :nd, :], np.einsum("wia,ab->wib", Pu, o.lam_p))
-        a3 = ao_value(o.tab_j3, r.reshape(-1, 3)).T.reshape(W, N, -1) if o.j3 is not None else None
-        h = self._j3_fields(a3) if o.j3 is not None else None
+        _, _, _, _, Ginv, Tu, Td, a3, h = self.tables(r)
         ke = self._kinetic(r, Ginv, h)                                        # (W, N)
         allE = np.arange(N)
         # lattice elements
@@ -291,24 +327,7 @@ class BatchedGFMCn:
         diag_kin = 3.0 / (2.0 * alat**2) * N
         Nv = self.Nv
         if o.ecp:
-            atom = np.argmin(dnuc, axis=2)                                    # (W, N), first nearest
-            loc = np.zeros(W)
-            for a in range(o.M):
-                loc += np.sum(self._V_channel(np.full((W, N), a), int(o.maxl1[a]), dnuc[:, :, a]), axis=1)
-            Ra = o.R[atom]                                                    # (W, N, 3)
-            rel = Ra - r
-            dist = np.linalg.norm(rel, axis=-1)
-            gq = np.einsum("qx,wyx->wqy", self.mesh_pts, Rm)                  # (W, Nv, 3): mesh R^T
-            pe = r[:, :, None, :] + rel[:, :, None, :] + dist[:, :, None, None] * gq[:, None]
-            cos_t = np.einsum("wex,wqx->weq", -rel / dist[..., None], gq / np.linalg.norm(gq, axis=-1)[..., None])
-            lmax = o.maxl1[atom]                                              # (W, N)
-            wv = np.zeros((W, N, Nv))
-            for l in range(int(o.maxl1.max())):
-                Vl = self._V_channel(atom, l, dist)                           # (W, N)
-                act = (l < lmax)[..., None]
-                wv = wv + np.where(act, Vl[..., None] * (2 * l + 1) * legendre(l, cos_t) * self.mesh_w, 0.0)
-            ratio_e = self._det_ratio(pe, Tu, Td) * self._jastrow_ratio(r, pe, allE, h, a3)
-            V = wv * ratio_e                                                  # (W, N, Nv)
+            loc, V, pe = self._ecp(r, Rm, dnuc, Tu, Td, h, a3)
             vfn = np.minimum(V, 0.0)
             sp_ecp = np.maximum(V, 0.0).sum(axis=(1, 2))
             nondiag = nondiag + vfn.sum(axis=(1, 2))
@@ -319,3 +338,130 @@ class BatchedGFMCn:
             p = fn.reshape(W, -1)
             pe = None
         return diag, nondiag, p, pl, pe
+
+
+class BatchedVMC:
+    """Metropolis proposals and VMC measurements of a batch of walkers, as
+    ``oracle.drivers.vmc_proposal`` / ``vmc_measure`` (jqmc_mcmc.py:4278-4533,
+    E_L and w_L of :725-747): one proposal of every walker at once, G and G^-1
+    carried by the same Sherman-Morrison updates, the Jastrow ratio from
+    pair-function differences and the J3 field."""
+
+    def __init__(self, o: OracleSystem, Dt: float, eps_AS: float, Nv: int = 6):
+        self.o = o
+        self.Dt, self.eps_AS = float(Dt), float(eps_AS)
+        self.g = BatchedGFMCn(o, 0.2, Nv)   # shared pieces (orbitals, Jastrow, ECP)
+
+    def init(self, r):
+        """(G, G^-1) from the positions (W, N, 3)."""
+        _, _, _, G, Ginv, _, _, _, _ = self.g.tables(r)
+        return G, Ginv
+
+    def _step_scale(self, p):
+        """f(r) of the proposal width at points p (W, 3) (jqmc_mcmc.py:4355-4361)."""
+        o = self.o
+        d = np.linalg.norm(p[:, None, :] - o.R, axis=-1)
+        a = np.argmin(d, axis=1)
+        Z = o.Zeff[a]
+        dd = d[np.arange(len(a)), a]
+        return 1.0 / Z**2 * (1.0 + Z**2 * dd) / (1.0 + dd)
+
+    @staticmethod
+    def _as_factor(G, Ginv):
+        F = np.sum(Ginv**2, axis=(1, 2))
+        S = np.minimum(np.min(np.sum(G**2, axis=2), axis=1), np.min(np.sum(G**2, axis=1), axis=1))
+        SF = S * F
+        with np.errstate(divide="ignore"):
+            return np.where(SF > 0.0, SF ** (-3.0 / 8.0), 0.0)
+
+    def proposal(self, r, G, Ginv, idraw, fdraw):
+        """One proposal of every walker in place: idraw (W, 4) = (sel, up index, down
+        index, axis), fdraw (W, 2) = (gauss, uniform).  Returns the accepted mask."""
+        o, gf = self.o, self.g
+        W, N, _ = r.shape
+        n, nd = o.n_up, o.n_dn
+        ws = np.arange(W)
+        sel, up_i, dn_i, axis = (idraw[:, k].astype(int) for k in range(4))
+        gauss, u = fdraw[:, 0], fdraw[:, 1]
+        is_up = sel < n
+        idx = np.where(is_up, up_i, dn_i)
+        e = np.where(is_up, idx, n + idx)
+        old = r[ws, e].copy()
+        f_l = self._step_scale(old)
+        new = old.copy()
+        new[ws, axis] += gauss * (f_l * self.Dt)
+        f_p = self._step_scale(new)
+        dist2 = np.sum((new - old) ** 2, axis=1)
+        T_ratio = (f_l / f_p) * np.exp(-dist2 * (1.0 / (2.0 * f_p**2 * self.Dt**2) - 1.0 / (2.0 * f_l**2 * self.Dt**2)))
+        # Jastrow ratio of the move
+        dJ = np.zeros(W)
+        if o.j1 is not None:
+            dJ += gf._j1(new) - gf._j1(old)
+        if o.j2 is not None:
+            mask = np.ones((W, N))
+            mask[ws, e] = 0.0
+            dJ += np.sum((gf._j2f(np.linalg.norm(new[:, None, :] - r, axis=-1))
+                          - gf._j2f(np.linalg.norm(old[:, None, :] - r, axis=-1))) * mask, axis=1)
+        if o.j3 is not None:
+            a3 = ao_value(o.tab_j3, r.reshape(-1, 3)).T.reshape(W, N, -1)
+            h = gf._j3_fields(a3)
+            p3 = ao_value(o.tab_j3, new).T
+            dJ += np.einsum("wa,wa->w", p3 - a3[ws, e], h[ws, e])
+        J_ratio = np.exp(dJ)
+        # geminal row (up) or column (down) at the new position, Sherman-Morrison
+        Pu = gf._orb(o.tab_up, o.mo_up, r[:, :n].reshape(-1, 3)).reshape(W, n, -1)
+        Pdn = gf._orb(o.tab_dn, o.mo_dn, r[:, n:].reshape(-1, 3)).reshape(W, nd, -1)
+        pu_new = gf._orb(o.tab_up, o.mo_up, new)                             # (W, A)
+        pd_new = gf._orb(o.tab_dn, o.mo_dn, new)
+        row = np.einsum("wa,ab,wjb->wj", pu_new, o.lam_p, Pdn)
+        if n > nd:
+            row = np.concatenate([row, pu_new @ o.lam_u], axis=1)
+        col = np.einsum("wia,ab,wb->wi", Pu, o.lam_p, pd_new)
+        G_new, Ginv_new = G.copy(), Ginv.copy()
+        det_ratio = np.empty(W)
+        for w in range(W):
+            i = idx[w]
+            if is_up[w]:
+                v = row[w] - G[w, i]
+                Ainv_u = Ginv[w][:, i]
+                vT_Ainv = v @ Ginv[w]
+                det_ratio[w] = 1.0 + v @ Ainv_u
+                G_new[w, i, :] += v
+            else:
+                u_vec = col[w] - G[w][:, i]
+                Ainv_u = Ginv[w] @ u_vec
+                vT_Ainv = Ginv[w][i, :]
+                det_ratio[w] = 1.0 + Ainv_u[i]
+                G_new[w][:, i] += u_vec
+            Ginv_new[w] = Ginv[w] - np.outer(Ainv_u, vT_Ainv) / det_ratio[w]
+        Rp = self._as_factor(G_new, Ginv_new)
+        Ro = self._as_factor(G, Ginv)
+        eps = self.eps_AS
+        R_AS_ratio = (np.maximum(Rp, eps) / Rp) / (np.maximum(Ro, eps) / Ro)
+        R_ratio = (R_AS_ratio * J_ratio * det_ratio) ** 2.0
+        p = np.minimum(1.0, R_ratio * T_ratio)
+        acc = u < p
+        r[ws[acc], e[acc]] = new[acc]
+        G[acc] = G_new[acc]
+        Ginv[acc] = Ginv_new[acc]
+        return acc
+
+    def measure(self, r, G, Ginv, angles):
+        """(e_L, w_L) of every walker with RT = R(angles).T (jqmc_mcmc.py:725-747)."""
+        o, gf = self.o, self.g
+        W, N, _ = r.shape
+        n = o.n_up
+        Rm = np.stack([rotation_matrix(*a) for a in angles])
+        _, _, _, _, _, Tu, Td, a3, h = gf.tables(r, Ginv)
+        ke = gf._kinetic(r, Ginv, h)
+        dnuc = np.linalg.norm(r[:, :, None, :] - o.R, axis=-1)
+        iu, ju = np.triu_indices(N, k=1)
+        V = (o.coulomb_ion_ion() + np.sum(-o.Zeff / dnuc, axis=(1, 2))
+             + np.sum(1.0 / np.linalg.norm(r[:, iu] - r[:, ju], axis=-1), axis=1))
+        if o.ecp:
+            loc, Vnl, _ = gf._ecp(r, Rm, dnuc, Tu, Td, h, a3)
+            V = V + loc + Vnl.sum(axis=(1, 2))
+        e = ke[:, :n].sum(axis=1) + ke[:, n:].sum(axis=1) + V
+        R = self._as_factor(G, Ginv)
+        w = (R / np.maximum(R, self.eps_AS)) ** 2
+        return e, w

@@ -39,3 +39,38 @@ def test_batched_gfmc_n_matches_oracle(name):
     for i in range(W):
         e, v = D.lrdmc_energy(o, states[i], draws[-1][i], alat)
         np.testing.assert_allclose([eb[i], vb[i]], [e, v], rtol=1e-10)
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12"])
+def test_batched_vmc_matches_oracle(name):
+    """oracle/batched.py BatchedVMC against oracle/drivers.py vmc_proposal /
+    vmc_measure on the same draws: the same acceptances, positions, and
+    e_L, w_L to 1e-10."""
+    from jqmc_gb300 import synthetic
+    from oracle import drivers as D
+    from oracle.batched import BatchedVMC
+    from oracle.wf import OracleSystem
+    syn = synthetic.SYSTEMS[name]()
+    o = OracleSystem(syn.hamiltonian)
+    W, K, Dt, eps = 3, 12, 0.4, 0.0
+    r_up, r_dn = syn.initial_electrons(W, seed=23)
+    r = np.concatenate([r_up, r_dn], axis=1)
+    rng = np.random.default_rng(6)
+    n, nd = o.n_up, o.n_dn
+    idraw = np.stack([rng.integers(0, n + nd, (W, K)), rng.integers(0, n, (W, K)), rng.integers(0, max(nd, 1), (W, K)),
+                      rng.integers(0, 3, (W, K))], axis=-1)
+    fdraw = np.stack([rng.normal(size=(W, K)), rng.uniform(size=(W, K))], axis=-1)
+    angles = rng.uniform(-np.pi, np.pi, (W, 3))
+    b = BatchedVMC(o, Dt, eps)
+    G, Ginv = b.init(r)
+    states = [D.init_state(o, r_up[i], r_dn[i]) for i in range(W)]
+    for k in range(K):
+        acc = b.proposal(r, G, Ginv, idraw[:, k], fdraw[:, k])
+        for i in range(W):
+            assert D.vmc_proposal(o, states[i], idraw[i, k], fdraw[i, k], Dt, eps) == bool(acc[i])
+    ro = np.stack([np.vstack([s.r_up, s.r_dn]) for s in states])
+    np.testing.assert_allclose(r, ro, rtol=0, atol=1e-12)
+    e, w = b.measure(r, G, Ginv, angles)
+    for i in range(W):
+        eo, wo = D.vmc_measure(o, states[i], angles[i], eps)
+        np.testing.assert_allclose([e[i], w[i]], [eo, wo], rtol=1e-10)
