@@ -33,6 +33,69 @@ from .wf import OracleSystem, _meshes, legendre, rotation_matrix
 _E6 = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], dtype=np.float64)
 
 
+def _solid_values(l: int, d: np.ndarray) -> np.ndarray:
+    """The real solid harmonics of oracle.ao.solid_harmonics (same closed form,
+    same row order m + l), values only: (2l+1, ...)."""
+    from math import sqrt
+
+    from .ao import _pi_terms
+    x, y, z = d[..., 0], d[..., 1], d[..., 2]
+    r2 = x * x + y * y + z * z
+    S = np.zeros((2 * l + 1,) + x.shape)
+    w = x + 1j * y
+    for m in range(0, l + 1):
+        P = np.zeros_like(x)
+        for c, k, zp in _pi_terms(l, m):
+            P = P + c * r2**k * z**zp
+        if m == 0:
+            S[l] = P
+            continue
+        wm = w**m
+        S[l + m] = sqrt(2.0) * P * wm.real
+        S[l - m] = sqrt(2.0) * P * wm.imag
+    return S
+
+
+class ShellAO:
+    """AO values of a spherical AOTable evaluated shell by shell: the AOs of one
+    shell (same centre, l and primitives) share their radial part and one set
+    of 2l+1 solid harmonics, which oracle.ao.ao_value evaluates once per AO.
+    Same values (tests/test_oracle_batched.py holds them to ao_value)."""
+
+    def __init__(self, tab):
+        self.A = tab.num_ao
+        groups = {}
+        for a in range(tab.num_ao):
+            key = (tuple(np.round(tab.centers[a], 14)), int(tab.l[a]), tuple(tab.Z[a]), tuple(tab.cN[a]))
+            groups.setdefault(key, []).append(a)
+        self.by_l = {}
+        for (c, l, Z, cN), aos in groups.items():
+            self.by_l.setdefault(l, []).append((c, Z, cN, aos))
+        self.tables = {}
+        for l, shells in self.by_l.items():
+            C = np.array([sh[0] for sh in shells])
+            Zs = np.array([sh[1] for sh in shells])
+            cNs = np.array([sh[2] for sh in shells])
+            idx = -np.ones((len(shells), 2 * l + 1), dtype=int)
+            for j, sh in enumerate(shells):
+                for a in sh[3]:
+                    idx[j, tab.m[a] + l] = a
+            self.tables[l] = (C, Zs, cNs, idx)
+
+    def values(self, pts: np.ndarray) -> np.ndarray:
+        """(P, A) AO values at points (P, 3)."""
+        out = np.zeros((pts.shape[0], self.A))
+        for l, (C, Zs, cNs, idx) in self.tables.items():
+            d = pts[:, None, :] - C[None]                                     # (P, S, 3)
+            r2 = np.sum(d * d, axis=-1)
+            rad = np.einsum("psk,sk->ps", np.exp(-Zs[None] * r2[:, :, None]), cNs)
+            Sv = _solid_values(l, d)                                           # (2l+1, P, S)
+            for j in range(2 * l + 1):
+                ok = idx[:, j] >= 0
+                out[:, idx[ok, j]] = (Sv[j] * rad)[:, ok]
+        return out
+
+
 class BatchedGFMCn:
     """GFMC_n projection of a batch of walkers (positions (W, N, 3), up first)."""
 
@@ -43,6 +106,7 @@ class BatchedGFMCn:
         self.n, self.nd = o.n_up, o.n_dn
         self.N = o.n_up + o.n_dn
         self.mesh_w, self.mesh_pts = _meshes()[Nv]
+        self._shell_ao = {}
         if o.ecp:
             # per (atom, l): arrays of the channel's (exponent, coefficient, power)
             self.chan = {}
@@ -51,10 +115,19 @@ class BatchedGFMCn:
             self.chan = {k: np.array(v) for k, v in self.chan.items()}
 
     # ------------------------------------------------------------------ pieces
+    def _ao(self, tab, pts):
+        """(P, A) AO values: shell by shell for spherical tables, else oracle.ao.ao_value."""
+        if tab.cart:
+            return ao_value(tab, pts).T
+        ev = self._shell_ao.get(id(tab))
+        if ev is None:
+            ev = self._shell_ao[id(tab)] = ShellAO(tab)
+        return ev.values(pts)
+
     def _orb(self, tab, mo, pts):
         """Orbital values at points (P, 3) -> (P, A)."""
-        v = ao_value(tab, pts)
-        return (v if mo is None else mo @ v).T
+        v = self._ao(tab, pts)
+        return v if mo is None else v @ mo.T
 
     def _V_channel(self, atom: np.ndarray, l: int, dist: np.ndarray) -> np.ndarray:
         """r^-2 sum_k c_k r^n_k exp(-alpha_k r^2) of channel l at each atom (elementwise)."""
@@ -126,7 +199,7 @@ class BatchedGFMCn:
             mask[np.arange(len(e_of)), e_of] = 0.0
             dJ += np.einsum("wekn,en->wek", f_new, mask) - np.einsum("wen,en->we", f_old, mask)[:, :, None]
         if o.j3 is not None:
-            p3 = ao_value(o.tab_j3, pts.reshape(-1, 3)).T.reshape(W, len(e_of), pts.shape[2], -1)
+            p3 = self._ao(o.tab_j3, pts.reshape(-1, 3)).reshape(W, len(e_of), pts.shape[2], -1)
             he = h[:, e_of]
             dJ += np.einsum("weka,wea->wek", p3, he) - np.einsum("wea,wea->we", a3[:, e_of], he)[:, :, None]
         return np.exp(dJ)
@@ -259,7 +332,7 @@ class BatchedGFMCn:
             Ginv = np.linalg.inv(G)
         Tu = B @ Ginv                                                          # (W, A, n)
         Td = np.einsum("wjk,wkb->wjb", Ginv[:, :nd, :], np.einsum("wia,ab->wib", Pu, o.lam_p))
-        a3 = ao_value(o.tab_j3, r.reshape(-1, 3)).T.reshape(W, N, -1) if o.j3 is not None else None
+        a3 = self._ao(o.tab_j3, r.reshape(-1, 3)).reshape(W, N, -1) if o.j3 is not None else None
         h = self._j3_fields(a3) if o.j3 is not None else None
         return Pu, Pdn, B, G, Ginv, Tu, Td, a3, h
 
@@ -403,9 +476,9 @@ class BatchedVMC:
             dJ += np.sum((gf._j2f(np.linalg.norm(new[:, None, :] - r, axis=-1))
                           - gf._j2f(np.linalg.norm(old[:, None, :] - r, axis=-1))) * mask, axis=1)
         if o.j3 is not None:
-            a3 = ao_value(o.tab_j3, r.reshape(-1, 3)).T.reshape(W, N, -1)
+            a3 = gf._ao(o.tab_j3, r.reshape(-1, 3)).reshape(W, N, -1)
             h = gf._j3_fields(a3)
-            p3 = ao_value(o.tab_j3, new).T
+            p3 = gf._ao(o.tab_j3, new)
             dJ += np.einsum("wa,wa->w", p3 - a3[ws, e], h[ws, e])
         J_ratio = np.exp(dJ)
         # geminal row (up) or column (down) at the new position, Sherman-Morrison

@@ -74,3 +74,18 @@ def test_batched_vmc_matches_oracle(name):
     for i in range(W):
         eo, wo = D.vmc_measure(o, states[i], angles[i], eps)
         np.testing.assert_allclose([e[i], w[i]], [eo, wo], rtol=1e-10)
+
+
+@pytest.mark.parametrize("name", ["water_like", "ring12", "chain32"])
+def test_shell_ao_values_match_oracle(name):
+    """oracle/batched.py's shell-by-shell AO values equal oracle.ao.ao_value."""
+    from jqmc_gb300 import synthetic
+    from oracle.ao import ao_value
+    from oracle.batched import ShellAO
+    from oracle.wf import OracleSystem
+    o = OracleSystem(synthetic.SYSTEMS[name]().hamiltonian)
+    pts = np.random.default_rng(8).normal(scale=3.0, size=(300, 3)) + o.R.mean(axis=0)
+    for tab in [o.tab_up] + ([o.tab_j3] if o.j3 is not None else []):
+        ref = ao_value(tab, pts).T
+        got = ShellAO(tab).values(pts)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
